@@ -1,0 +1,402 @@
+#!/usr/bin/env python
+"""Powder-averaged muon polarisation throughput on one GB300.
+
+Workload (the 24-dimensional powder configuration): spins mu, e, 1H, 14N
+(Hilbert dimension 24) with seeded random anisotropic hyperfine, dipolar and
+quadrupolar couplings, 10,000 ZCW-style orientations, 4096 times on
+0-20 us, B = 0.01 T, T = inf, muon polarised along z -- the muon-first
+fast path.  Synthetic inputs stand in for a real material; see
+muspinsim_gb300/workloads.py.
+
+Metric: P(t) samples/s, one sample = one (orientation, time) value before the
+orientation average.  ``value`` is the mixed-precision pipeline (FP32 Jacobi +
+double-word refinement + FP32 phase sum) with inputs resident in HBM; the
+all-FP64 pipeline is timed beside it (``fp64``) and the max |dP| between the
+two is reported.  ``e2e`` runs the public ``powder_average`` call on host
+inputs (host->device copies and the device->host result inside the timed
+region).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "powder-avg P(t) samples/s, mixed-prec vs FP64 GPU at max|ΔP|≤1e-6, 1×GB300"
+WORKLOAD = "mu_e_1H_14N_dim24_powder_10k_orient_4096_t"
+L2_BYTES = 129 * 1024 * 1024
+# FP32 FMA lanes per SM on GB300 (152 SMs); the FP32 SIMT roofline is
+# 152 * 128 * 2 flop * SM clock.  MEASURED_PEAKS.json carries HBM and bf16
+# tensor figures only.
+SMS, FP32_FMA_PER_SM = 152, 128
+# dram bytes per launch of the dominant kernel from the committed ncu capture
+# (profiles/); None until captured
+DOMINANT_TRAFFIC_BYTES = None
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--orientations", type=int, default=10000)
+    p.add_argument("--times", type=int, default=4096)
+    p.add_argument("--fp64-steps", type=int, default=3)
+    p.add_argument("--cpu-orientations", type=int, default=2500,
+                   help="orientations in the bounded CPU-baseline sample (~10 s)")
+    p.add_argument("--ref-orientations", type=int, default=400,
+                   help="orientations per step of the --impl reference arm")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------- distributed
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "gb300" and torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- workload
+
+def build_workload(args):
+    from muspinsim_gb300 import quaternion as Q
+    from muspinsim_gb300 import workloads
+    from muspinsim_gb300.orientations import orientation_rows_to_quats
+
+    wl = workloads.config2(n_orient=args.orientations, n_times=args.times)
+    sy = wl.system()
+    qs, ws = orientation_rows_to_quats(wl.orientations)
+    N = len(qs)
+    ws = ws * (N / ws.sum())
+    p = wl.polarization / np.linalg.norm(wl.polarization)
+    B_lab = Q.rotate(qs, wl.fields[0])
+    p_lab = Q.rotate(qs, p)
+    return wl, sy, B_lab, p_lab, ws / N
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU reference
+
+def cpu_reference_rate(sy, B_lab, p_lab, times, n_orient, threads):
+    """Samples/s of the reference's fast path on the host: per orientation
+    H = Hsys + b.Z, numpy eigh, A = |U^dag (sigma (x) 1) U|^2, W, and the
+    reference's own Cython cosine sum compiled from its sources
+    (oracle/_ref), with all host threads; the C restatement
+    (oracle/fast_cos_sum.c) when the reference kernel is absent."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import build as obuild
+    from oracle import port
+
+    kind = "port"
+    kernel = None
+    try:
+        path = obuild.build_ref()
+        if path:
+            import importlib.util
+
+            spec = importlib.util.spec_from_file_location(obuild.REF_MODULE, path)
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            kernel = mod.parallel_fast_time_evolve
+            kind = "reference"
+    except Exception:
+        kernel = None
+    obuild.build_port()
+    Hsys = sy.hamiltonian_matrix()
+    Z = sy.zeeman_operators()
+    d = Hsys.shape[0] // 2
+    t = np.ascontiguousarray(times, dtype=np.float64)
+    t0 = time.perf_counter()
+    acc = np.zeros(len(t))
+    for k in range(n_orient):
+        H = Hsys + np.einsum("a,aij->ij", B_lab[k], Z)
+        A, W, _ = port.fast_amplitudes(H, port.sigma_mu(p_lab[k]), d)
+        if kernel is not None:
+            r = np.asarray(kernel(t, d, np.ascontiguousarray(A), np.ascontiguousarray(W)))
+        else:
+            r = port.fast_cos_sum(t, d, A, W, threads)
+        acc += 0.5 * r
+    dt = time.perf_counter() - t0
+    return n_orient * len(t) / dt, dt, kind
+
+
+# ---------------------------------------------------------------- main arms
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    wl, sy, B_lab, p_lab, _ = build_workload(args)
+    threads = os.cpu_count() or 1
+    n = min(args.ref_orientations, len(B_lab))
+    rates = []
+    for step in range(args.warmup + args.steps):
+        rate, dt, kind = cpu_reference_rate(sy, B_lab, p_lab, wl.times, n, threads)
+        if step >= args.warmup:
+            rates.append((rate, dt))
+    value = statistics.median([r for r, _ in rates])
+    ms = statistics.median([d for _, d in rates]) * 1e3
+    sample = f"{n} of {len(B_lab)} orientations x {len(wl.times)} times per step"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "orientations": len(B_lab), "times": len(wl.times),
+                   "dim": 24, "l2": "n/a (host)"},
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+
+    from muspinsim_gb300 import _lib, kernels
+    from muspinsim_gb300.powder import powder_average
+
+    torch.cuda.set_device(local)
+    wl, sy, B_lab, p_lab, wscale = build_workload(args)
+    S, T = len(B_lab), len(wl.times)
+    Hsys, Z = sy.hamiltonian_matrix(), sy.zeeman_operators()
+    n = Hsys.shape[0]
+    slot = np.zeros(S, dtype=np.int32)
+
+    def plan(prec):
+        return kernels.PowderPlan(n, Hsys, Z, B_lab, p_lab, wscale, slot, 1, wl.times,
+                                  mode=_lib.MODE_FAST, precision=prec, dims=list(sy.dimension),
+                                  mu_index=sy.muon_index, gammas=sy.gammas)
+
+    mixed, fp64 = plan(_lib.PREC_MIXED), plan(_lib.PREC_FP64)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed(pl, steps, timer=None):
+        times_ms = []
+        for _ in range(steps):
+            flush.fill_(1.0)  # evict L2 between iterations (outside the events)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            pl.run(timer)
+            ev1.record(stream)
+            ev1.synchronize()
+            times_ms.append(ev0.elapsed_time(ev1))
+        return times_ms
+
+    # warm-up
+    for _ in range(args.warmup):
+        mixed.run()
+    fp64.run()
+    torch.cuda.synchronize()
+
+    timer = kernels.StageTimer()
+    timer.read()
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    ms_mixed = timed(mixed, args.steps, timer)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    stages, runs = timer.read()
+    res_mixed = mixed.out.clone()
+    st_mixed = int(mixed.status[:S].max().item())
+
+    ms_fp64 = timed(fp64, max(1, args.fp64_steps))
+    res_fp64 = fp64.out.clone()
+    st_fp64 = int(fp64.status[:S].max().item())
+    dP = float((res_mixed - res_fp64).abs().max().item())
+
+    # e2e through the public API, host inputs
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = powder_average(sy, wl.orientations, wl.fields[0], wl.polarization, wl.times,
+                           precision="mixed")
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_ms.append((t1 - t0) * 1e3)
+    dP_e2e = float(np.abs(r - res_fp64[0].cpu().numpy()).max())
+    h2d = (Hsys.size + Z.size) * 16 + S * (3 + 3 + 1 + 1) * 8 + S * 4 + T * 8
+    d2h = T * 8 + S * 4
+
+    t_mixed = statistics.median(ms_mixed)
+    t_fp64 = statistics.median(ms_fp64)
+    t_e2e = statistics.median(e2e_ms)
+    t_mixed_max = max_over_ranks(world, t_mixed)
+    samples = S * T
+    value = world * samples / (t_mixed_max * 1e-3)
+
+    # roofline of the dominant kernel (live CUDA-event stage times)
+    per_run = {k: v / max(runs, 1) for k, v in stages.items()}
+    dom = max(per_run, key=per_run.get)
+    flops = {"snapshots": 68.0 * n**3 * S, "phase": (4.0 * n * n + 2.0) * samples,
+             "schedule": 0.0, "reduce": 2.0 * samples}
+    kname = {"snapshots": "msp_snap_fast_kernel<float,true>",
+             "phase": "msp_phase_uniform_kernel<float>",
+             "schedule": "msp_schedule_kernel", "reduce": "msp_reduce_kernel"}[dom]
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    fp32_peak = SMS * FP32_FMA_PER_SM * 2 * 2070e6 / 1e12
+    achieved = flops[dom] / (per_run[dom] * 1e-3) / 1e12
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    line = {
+        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed_max,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (Jacobi, phase sum) + df32/f64 (refinement, phase reduction, accumulation)",
+        "data": "synthetic (seeded couplings, ZCW-style grid)",
+        "config": {"workload": WORKLOAD, "orientations": S, "times": T, "dim": n,
+                   "precision": "mixed", "l2": "flushed between timed steps (258 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "max_abs_dP_mixed_vs_fp64": dP,
+        "fp64": {"value": world * samples / (max_over_ranks(world, t_fp64) * 1e-3),
+                 "unit": "samples/s", "ms_per_step": t_fp64, "steps": len(ms_fp64)},
+        "mixed_over_fp64": t_fp64 / t_mixed,
+        "status_max": {"mixed": st_mixed, "fp64": st_fp64},
+        "e2e": {"value": world * samples / (max_over_ranks(world, t_e2e) * 1e-3),
+                "unit": "samples/s", "ms_per_step": t_e2e, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "api": "muspinsim_gb300.powder_average",
+                "max_abs_dP_vs_fp64": dP_e2e},
+        "stage_ms_per_step": per_run,
+        "roofline": {
+            "bound": "fp32-pipe", "kernel": kname, "achieved": achieved,
+            "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+            "traffic": DOMINANT_TRAFFIC_BYTES,
+            "algorithmic": f"{'68 n^3 per snapshot' if dom == 'snapshots' else '(4 n^2 + 2) per sample'}",
+            "peak_source": "nominal FP32 FMA pipe at sm_max_mhz (152 x 128 x 2 x 2070 MHz)",
+            "tensor_frac_of_measured_bf16": achieved / peaks["bf16_tflops"] if peaks else None,
+        },
+        "clocks": clk,
+        "gpu_launches": 4 * args.steps,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        nc = min(args.cpu_orientations, S)
+        rate, dt, kind = cpu_reference_rate(sy, B_lab, p_lab, wl.times, nc, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": "samples/s", "cores": threads,
+                                "kind": kind, "seconds": dt,
+                                "sample": f"{nc} of {S} orientations x {T} times"}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank)
+    else:
+        rc = run_gb300(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

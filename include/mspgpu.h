@@ -1,0 +1,194 @@
+/*
+ * mspgpu.h -- C ABI of the GB300 muon-polarisation library (libmspgpu.so).
+ *
+ * Drop-in replacement for the numerical core of MuSpinSim's polarisation
+ * path.  Every entry point:
+ *   - takes DEVICE pointers (CUDA global memory) unless stated otherwise;
+ *   - stores complex numbers as interleaved (re, im) doubles, matrices
+ *     row-major, batches back to back;
+ *   - runs asynchronously on the given CUDA stream (NULL = legacy default
+ *     stream) and allocates nothing: scratch memory comes from the caller,
+ *     sized by the matching *_workspace query;
+ *   - returns an msp status code; MSP_OK means the work was enqueued.
+ *     Data-dependent outcomes (an eigensolve that hit its sweep cap, an
+ *     out-of-range slot index) are written to the caller's per-item
+ *     `status` array, read after the stream has been synchronised.
+ *
+ * Units follow the reference: Hamiltonians in MHz, fields in T, times in
+ * microseconds, phases 2 pi * MHz * us.
+ */
+#ifndef MSPGPU_H
+#define MSPGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define MSP_OK 0
+#define MSP_ERR_ARG 1         /* invalid argument (see msp_last_error) */
+#define MSP_ERR_CUDA 2        /* a CUDA runtime call or launch failed */
+#define MSP_ERR_WORKSPACE 3   /* caller workspace too small */
+#define MSP_ERR_UNSUPPORTED 4 /* size outside the supported range */
+
+/* per-item status values written by the kernels */
+#define MSP_ITEM_OK 0
+#define MSP_ITEM_NOT_CONVERGED 1 /* Jacobi reached max_sweeps */
+#define MSP_ITEM_BAD_SLOT 2      /* slot index out of range / not sorted */
+
+/* precision of the eigensolve and phase sum */
+#define MSP_PREC_FP64 0  /* all-FP64: bit-faithful drop-in (max|dP| <= 1e-10) */
+#define MSP_PREC_MIXED 1 /* FP32 Jacobi + FP64 Rayleigh-quotient eigenvalues,
+                            FP32 phase sum with FP64 phase reduction and
+                            FP64 cross-block accumulation */
+
+/* evolution algorithm of a snapshot batch */
+#define MSP_MODE_FAST 0     /* muon-first, T = inf cosine sum */
+#define MSP_MODE_EVOLVE 1   /* general <O>(t) from rho0 */
+#define MSP_MODE_INTEGRAL 2 /* exponentially weighted time integral */
+
+#define MSP_MAX_DIM 64   /* largest Hilbert dimension of the Jacobi kernels */
+#define MSP_MAX_SPINS 16
+
+/* ---- library information ---------------------------------------------- */
+int msp_version(void);
+/* Copies the message of the last MSP_ERR_* in this thread into buf. */
+int msp_last_error(char *buf, size_t len);
+
+/* ---- building blocks ---------------------------------------------------- */
+
+/* H[b] = Hsys + sum_a fields[b][a] * Z[a]  (n x n complex128, batch b).
+ * Replaces ExperimentRunner.Hz / Htot (muspinsim/experiment.py:239-250,
+ * 332-341).  fields: batch*3 doubles. */
+int msp_assemble(const double *Hsys, const double *Z, const double *fields, int n,
+                 int batch, double *H, void *stream);
+
+/* Batched Hermitian eigensolve, 1 <= n <= MSP_MAX_DIM: cyclic Jacobi, one CTA
+ * per matrix.  evals: batch*n ascending; evecs: batch*n*n complex128 with the
+ * eigenvectors as COLUMNS (numpy.linalg.eigh layout); status: batch ints.
+ * precision MSP_PREC_MIXED runs the sweeps in FP32 and refines the eigenvalues
+ * with FP64 Rayleigh quotients.  Replaces Hermitian.diag / numpy.linalg.eigh
+ * (muspinsim/spinop.py:51-82). */
+int msp_eigh_batched(const double *H, int n, int batch, int precision, int max_sweeps,
+                     double *evals, double *evecs, int *status, void *stream);
+
+/* out[b] = U[b]^dag M[b] U[b]  (adjoint = 0)  or  U[b] M[b] U[b]^dag
+ * (adjoint = 1).  m_stride = complex elements between consecutive M
+ * matrices (0 broadcasts one M), u_stride likewise for U.  Replaces
+ * Operator.basis_change (muspinsim/spinop.py:330-355). */
+int msp_basis_change(const double *U, long long u_stride, const double *M,
+                     long long m_stride, int n, int batch, int adjoint, double *out,
+                     void *stream);
+
+/* out[i] = (1/d) sum_j [ 0.5 A[j,j] + sum_{k<j} A[j,k] cos(W[j,k] t_i) ]
+ * A, W: n x n doubles.  Same arithmetic as parallel_fast_time_evolve
+ * (muspinsim/cython/parallel.pyx:16-69). */
+int msp_fast_cos_sum(const double *times, int num_times, int other_dimension,
+                     const double *A, const double *W, int n, double *out, void *stream);
+
+/* A = |U^dag (sigma (x) 1_d) U|^2, W = 2 pi (l_j - l_k); sigma: 2x2
+ * complex128 (muon first).  Replaces muspinsim/hamiltonian.py:204-211. */
+int msp_fast_amplitudes(const double *evals, const double *evecs, const double *sigma,
+                        int n, int other_dimension, double *A, double *W, void *stream);
+
+/* out[t][o] = sum_ij rho[i][j] op_o[j][i] exp(-2 pi i (l_i - l_j) t_t), with
+ * rho and ops already in the eigenbasis; out: num_times*num_ops complex128.
+ * Replaces the time loop of Hamiltonian.evolve (muspinsim/hamiltonian.py:86-107). */
+int msp_evolve_expect(const double *evals, const double *rho, const double *ops, int n,
+                      int num_ops, const double *times, int num_times, double *out,
+                      void *stream);
+
+/* out[t] = exp(-2 pi i (l_i - l_j) t) * rho[i][j] for every time: the
+ * eigenbasis density matrices of Hamiltonian.evolve without operators
+ * (muspinsim/hamiltonian.py:89-90, 108-116); out: num_times*n*n complex128. */
+int msp_evolve_phases(const double *evals, const double *rho, int n, const double *times,
+                      int num_times, double *out, void *stream);
+
+/* out[o] = sum_ij rho[i][j] * (-op_o[j][i] / (2 pi i (l_j - l_i) - 1/tau)),
+ * rho and ops in the eigenbasis; out: num_ops complex128.  Replaces
+ * Hamiltonian.integrate_decaying (muspinsim/hamiltonian.py:150-164). */
+int msp_integrate_decaying(const double *evals, const double *rho, const double *ops,
+                           int n, int num_ops, double tau, double *out, void *stream);
+
+/* ---- stage timer ---------------------------------------------------------- */
+
+/* Opaque set of CUDA events that msp_powder_run records around its stages
+ * when msp_powder_args.timer is set: snapshots (assembly, eigensolve,
+ * eigenbasis amplitudes), schedule, phase sum, reduction.  No counterpart in
+ * the reference, which has no timing beyond wall-clock logging
+ * (muspinsim/__main__.py:124, 163-165). */
+typedef struct msp_timer msp_timer;
+#define MSP_TIMER_STAGES 4
+#define MSP_TIMER_CAPACITY 512 /* runs recorded between two reads */
+
+int msp_timer_create(msp_timer **timer);
+int msp_timer_destroy(msp_timer *timer);
+/* Waits for the recorded runs, writes the summed milliseconds of each stage
+ * into ms[MSP_TIMER_STAGES] and the number of runs into *runs, and empties
+ * the timer. */
+int msp_timer_read(msp_timer *timer, double *ms, int *runs);
+
+/* ---- fused powder pipeline ---------------------------------------------- */
+
+/* One batch of configuration snapshots of one spin system, reduced on the
+ * device into output rows ("slots"): the loop of ExperimentRunner.run /
+ * run_single plus MuSpinConfig.store_time_slice (muspinsim/experiment.py:
+ * 358-382, 434-498; muspinsim/simconfig.py:347-368).  All pointers are
+ * device pointers except where noted. */
+typedef struct msp_powder_args {
+    int n;                    /* Hilbert dimension, 2 .. MSP_MAX_DIM */
+    int num_spins;            /* spins in the system, <= MSP_MAX_SPINS */
+    int mu_index;             /* position of the muon in the spin order */
+    int dims[MSP_MAX_SPINS];  /* per-spin multiplicity 2I+1 (host values) */
+    const double *Hsys;       /* n*n complex128, field-independent part (MHz) */
+    const double *Z;          /* 3*n*n complex128, Z_a = sum_i gamma_i S^a_i */
+    int num_snap;             /* snapshots in the batch */
+    const double *field;      /* num_snap*3 lab-frame field incl. intrinsic (T) */
+    const double *pol;        /* num_snap*3 lab-frame muon polarisation */
+    const double *wscale;     /* num_snap: orientation weight / averaged count */
+    const int *slot;          /* num_snap output rows, non-decreasing, < num_slots */
+    const double *temperature;/* EVOLVE/INTEGRAL: num_snap temperatures (K) of the
+                                 initial state; NULL means T = inf for all */
+    double gammas[MSP_MAX_SPINS]; /* per-spin gyromagnetic ratio, MHz/T (host) */
+    const double *rho_fac;    /* EVOLVE/INTEGRAL, optional: per snapshot, the
+                                 Kronecker factors of rho0 (dims[s]^2 complex128
+                                 per spin, spin order), back to back.  NULL:
+                                 the kernel builds them from field, pol,
+                                 temperature and gammas: muon pure along pol,
+                                 other spins thermal in their own Zeeman
+                                 field (muspinsim/experiment.py:170-236) */
+    int num_slots;            /* output rows */
+    const double *times;      /* num_times (ignored when uniform = 1) */
+    int num_times;            /* FAST/EVOLVE time samples; 1 for INTEGRAL */
+    int uniform;              /* 1: t_k = t0 + k dt */
+    double t0, dt;
+    double tau;               /* INTEGRAL: decay time (us) */
+    int mode;                 /* MSP_MODE_* */
+    int precision;            /* MSP_PREC_* */
+    int max_sweeps;           /* Jacobi sweep cap, <= 0 selects 40 */
+    double *out;              /* num_slots*num_times (FAST/EVOLVE) or num_slots */
+    int *status;              /* num_snap per-snapshot status (MSP_ITEM_*) */
+    void *workspace;          /* caller scratch, >= msp_powder_workspace bytes,
+                                 256-byte aligned */
+    size_t workspace_bytes;
+    void *stream;             /* cudaStream_t */
+    msp_timer *timer;         /* optional stage timer (NULL: none) */
+} msp_powder_args;
+
+/* Scratch bytes msp_powder_run needs for these arguments (no pointer is
+ * dereferenced). */
+int msp_powder_workspace(const msp_powder_args *args, size_t *bytes);
+
+/* Runs the batch: Hamiltonian assembly, batched eigensolve, eigenbasis
+ * amplitudes, phase sum over time, weighted reduction into args->out
+ * (overwritten).  Kernels launched: msp_snap_* (one CTA per snapshot),
+ * msp_schedule, msp_phase_* (time tiles x pair chunks), msp_reduce. */
+int msp_powder_run(const msp_powder_args *args);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSPGPU_H */

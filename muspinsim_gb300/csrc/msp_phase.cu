@@ -1,0 +1,535 @@
+// Time-domain kernels: the phase sum over eigenvalue pairs, its work
+// schedule and its deterministic reduction into output rows, plus the small
+// single-Hamiltonian building blocks of the C ABI.
+//
+// The phase sum replaces the per-snapshot time loops of the reference --
+// the Cython cosine sum (muspinsim/cython/parallel.pyx:59-67) and the
+// evolve loop (muspinsim/hamiltonian.py:95-107) -- and the accumulation of
+// MuSpinConfig.store_time_slice (muspinsim/simconfig.py:347-368): all pairs
+// of all snapshots that feed one output row are summed on the device.
+//
+// Uniform grids t_k = t0 + k dt use a blocked form.  A time tile of
+// 64 x 64 samples, k = 64 k1 + k0, factorises every term:
+//   Re[(a_c - i a_s) e^{i w t_k}] = Re[X_m(k1) Y_m(k0)],
+//   X_m(k1) = (a_c - i a_s) e^{i w (t_tile + 64 k1 dt)},  Y_m(k0) = e^{i w k0 dt},
+// so each tile is a sum of outer products -- 2 FMAs per (pair, sample) in
+// register tiles, with no per-sample sin/cos.  X and Y come from a phase
+// recurrence: five exactly reduced phases per pair (w dt, 8 w dt, 64 w dt,
+// 512 w dt, w t_tile, reduced modulo 2 pi in FP64), their sin/cos, then
+// products of short power tables -- at most 16 rounding steps from an exact
+// value, which is the periodic resync.
+#include "msp_internal.cuh"
+
+namespace msp {
+
+template <typename T>
+struct PhaseCfg;
+template <>
+struct PhaseCfg<float> {
+    enum { TM = 8, TN = 8, PS = 32 };
+};
+template <>
+struct PhaseCfg<double> {
+    enum { TM = 4, TN = 8, PS = 16 };
+};
+
+__device__ __forceinline__ void sincos_t(double x, double *s, double *c) { sincos(x, s, c); }
+__device__ __forceinline__ void sincos_t(double x, float *s, float *c) {
+    sincosf((float)x, s, c);
+}
+
+// Pair range [begin, end) of work item `item`; begin = -1 when the item does
+// not exist.  item_first / slot_first are num_slots + 1 prefix arrays.
+__device__ __forceinline__ void item_range(const PhaseArgs &a, int item, int *b, int *e) {
+    const int total = a.item_first[a.num_slots];
+    if (item >= total) {
+        *b = -1;
+        *e = -1;
+        return;
+    }
+    int lo = 0, hi = a.num_slots - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.item_first[mid] <= item)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const int sb = a.slot_first[lo] + (item - a.item_first[lo]) * a.SB;
+    int se = sb + a.SB;
+    if (se > a.slot_first[lo + 1]) se = a.slot_first[lo + 1];
+    *b = sb * a.P;
+    *e = se * a.P;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) msp_phase_uniform_kernel(PhaseArgs a) {
+    constexpr int K = 64, TM = PhaseCfg<T>::TM, TN = PhaseCfg<T>::TN, PS = PhaseCfg<T>::PS;
+    constexpr int TY = K / TM, TX = K / TN, TPG = TY * TX, GROUPS = 128 / TPG;
+    typedef typename PairCoef<T>::type coef_t;
+    typedef cx<T> C;
+    __shared__ __align__(16) C Xs[PS][K];
+    __shared__ __align__(16) C Ys[PS][K];
+    __shared__ __align__(16) C pw[4][8][PS];  // pair index last: conflict-free stores
+    __shared__ int s_range[2];
+
+    const int tid = threadIdx.x;
+    if (tid == 0) item_range(a, blockIdx.x, &s_range[0], &s_range[1]);
+    __syncthreads();
+    const int pbeg = s_range[0], pend = s_range[1];
+    if (pbeg < 0) return;
+
+    const int g = tid / TPG, lt = tid - (tid / TPG) * TPG;
+    const int ty = lt / TX, tx = lt - (lt / TX) * TX;
+    const double dt = a.dt;
+    const long long tile_base = (long long)blockIdx.y * (K * K);
+    const double tb = a.t0 + (double)tile_base * dt;
+    const coef_t *coef = reinterpret_cast<const coef_t *>(a.pair_coef);
+
+    T acc[TM][TN];
+#pragma unroll
+    for (int r = 0; r < TM; ++r)
+#pragma unroll
+        for (int c = 0; c < TN; ++c) acc[r][c] = T(0);
+
+    for (int pb = pbeg; pb < pend; pb += PS) {
+        const int np = (pend - pb) < PS ? (pend - pb) : PS;
+        if (tid < np) {
+            const int i = tid;
+            const coef_t cf = coef[pb + i];
+            const double w = a.pair_omega[pb + i];
+            const double psi = reduce_2pi(w * dt);
+            const double psi8 = reduce_2pi(8.0 * psi);
+            const double psi64 = reduce_2pi(8.0 * psi8);
+            const double psi512 = reduce_2pi(8.0 * psi64);
+            const double ph0 = reduce_2pi(w * tb);
+            C e1, e8, e64, e512, e0;
+            sincos_t(psi, &e1.im, &e1.re);
+            sincos_t(psi8, &e8.im, &e8.re);
+            sincos_t(psi64, &e64.im, &e64.re);
+            sincos_t(psi512, &e512.im, &e512.re);
+            sincos_t(ph0, &e0.im, &e0.re);
+            const C cc = cmul(mk<T>((T)cf.x, (T)(-cf.y)), e0);
+            C p0 = mk<T>(T(1), T(0)), p1 = p0, p2 = p0, p3 = cc;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                pw[0][r][i] = p0;
+                pw[1][r][i] = p1;
+                pw[2][r][i] = p2;
+                pw[3][r][i] = p3;
+                p0 = cmul(p0, e1);
+                p1 = cmul(p1, e8);
+                p2 = cmul(p2, e64);
+                p3 = cmul(p3, e512);
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < np * 2 * K; e += 128) {
+            const int i = e / (2 * K), k = e - (e / (2 * K)) * (2 * K);
+            if (k < K) {
+                Ys[i][k] = cmul(pw[1][k >> 3][i], pw[0][k & 7][i]);
+            } else {
+                const int kk = k - K;
+                Xs[i][kk] = cmul(pw[3][kk >> 3][i], pw[2][kk & 7][i]);
+            }
+        }
+        __syncthreads();
+        for (int i = g; i < np; i += GROUPS) {
+            C xv[TM], yv[TN];
+#pragma unroll
+            for (int r = 0; r < TM; ++r) xv[r] = Xs[i][ty + TY * r];
+#pragma unroll
+            for (int c = 0; c < TN; ++c) yv[c] = Ys[i][tx + TX * c];
+#pragma unroll
+            for (int r = 0; r < TM; ++r)
+#pragma unroll
+                for (int c = 0; c < TN; ++c) {
+                    acc[r][c] = fma(xv[r].re, yv[c].re, acc[r][c]);
+                    acc[r][c] = fma(-xv[r].im, yv[c].im, acc[r][c]);
+                }
+        }
+        __syncthreads();
+    }
+
+    // combine the groups (they summed disjoint pairs of the same tile)
+    T *red = reinterpret_cast<T *>(&Xs[0][0]);  // K*K values fit in Xs+Ys
+    if (GROUPS > 1) {
+        for (int gg = 1; gg < GROUPS; ++gg) {
+            if (g == gg) {
+#pragma unroll
+                for (int r = 0; r < TM; ++r)
+#pragma unroll
+                    for (int c = 0; c < TN; ++c) {
+                        const int k = (ty + TY * r) * K + tx + TX * c;
+                        red[k] = (gg == 1) ? acc[r][c] : red[k] + acc[r][c];
+                    }
+            }
+            __syncthreads();
+        }
+    }
+    if (g == 0) {
+        double *out = a.partial + (size_t)blockIdx.x * a.num_times;
+#pragma unroll
+        for (int r = 0; r < TM; ++r)
+#pragma unroll
+            for (int c = 0; c < TN; ++c) {
+                const int k = (ty + TY * r) * K + tx + TX * c;
+                const long long t = tile_base + k;
+                double v = (double)acc[r][c];
+                if (GROUPS > 1) v += (double)red[k];
+                if (t < a.num_times) out[t] = v;
+            }
+    }
+}
+
+// Arbitrary time grids: one thread per sample, every pair's phase reduced in
+// FP64 and evaluated with sincos.
+template <typename T>
+__global__ void __launch_bounds__(256) msp_phase_direct_kernel(PhaseArgs a) {
+    typedef typename PairCoef<T>::type coef_t;
+    __shared__ coef_t sc[256];
+    __shared__ double sw[256];
+    __shared__ int s_range[2];
+    const int tid = threadIdx.x;
+    if (tid == 0) item_range(a, blockIdx.x, &s_range[0], &s_range[1]);
+    __syncthreads();
+    const int pbeg = s_range[0], pend = s_range[1];
+    if (pbeg < 0) return;
+    const coef_t *coef = reinterpret_cast<const coef_t *>(a.pair_coef);
+    const int t = blockIdx.y * 256 + tid;
+    const bool valid = t < a.num_times;
+    const double tt = valid ? a.times[t] : 0.0;
+    double acc = 0.0;
+    for (int pb = pbeg; pb < pend; pb += 256) {
+        const int np = (pend - pb) < 256 ? (pend - pb) : 256;
+        if (tid < np) {
+            sc[tid] = coef[pb + tid];
+            sw[tid] = a.pair_omega[pb + tid];
+        }
+        __syncthreads();
+        T part = T(0);
+        for (int i = 0; i < np; ++i) {
+            T s, c;
+            sincos_t(reduce_2pi(sw[i] * tt), &s, &c);
+            part = fma((T)sc[i].x, c, part);
+            part = fma((T)sc[i].y, s, part);
+        }
+        acc += (double)part;
+        __syncthreads();
+    }
+    if (valid) a.partial[(size_t)blockIdx.x * a.num_times + t] = acc;
+}
+
+// Slot bookkeeping: first snapshot of every output row, and the prefix of
+// work items (chunks of SB snapshots, never straddling two rows).  A slot
+// index out of range or out of order marks the snapshot MSP_ITEM_BAD_SLOT
+// and empties the whole schedule.
+__global__ void msp_schedule_kernel(const int *__restrict__ slot, int S, int num_slots, int SB,
+                                    int count_items, int *__restrict__ slot_first,
+                                    int *__restrict__ item_first, int *__restrict__ status) {
+    __shared__ int bad;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (tid == 0) bad = 0;
+    __syncthreads();
+    for (int s = tid; s < S; s += nt) {
+        const int sl = slot[s];
+        const bool ok = sl >= 0 && sl < num_slots && (s == 0 || sl >= slot[s - 1]);
+        if (!ok) {
+            status[s] |= MSP_ITEM_BAD_SLOT;
+            atomicOr(&bad, 1);
+        }
+    }
+    __syncthreads();
+    if (bad) {
+        for (int x = tid; x <= num_slots; x += nt) {
+            slot_first[x] = 0;
+            item_first[x] = 0;
+        }
+        return;
+    }
+    for (int s = tid; s < S; s += nt) {
+        const int sl = slot[s];
+        const int prev = s == 0 ? -1 : slot[s - 1];
+        for (int x = prev + 1; x <= sl; ++x) slot_first[x] = s;
+    }
+    const int last = S > 0 ? slot[S - 1] : -1;
+    for (int x = last + 1 + tid; x <= num_slots; x += nt) slot_first[x] = S;
+    __syncthreads();
+    if (tid == 0) {
+        int acc = 0;
+        for (int x = 0; x < num_slots; ++x) {
+            item_first[x] = acc;
+            if (count_items) {
+                const int len = slot_first[x + 1] - slot_first[x];
+                acc += (len + SB - 1) / SB;
+            }
+        }
+        item_first[num_slots] = acc;
+    }
+}
+
+// out[slot][t] = sum of the slot's snapshot constants + its items' partials,
+// in a fixed order (deterministic).
+__global__ void __launch_bounds__(256) msp_reduce_kernel(PhaseArgs a,
+                                                         const double *__restrict__ snap_const,
+                                                         double *__restrict__ out, int T) {
+    __shared__ double red[16];
+    const int sl = blockIdx.y;
+    const int tid = threadIdx.x;
+    const int s0 = a.slot_first[sl], s1 = a.slot_first[sl + 1];
+    double c = 0.0;
+    for (int s = s0 + tid; s < s1; s += blockDim.x) c += snap_const[s];
+    // block reduction (fixed tree: deterministic)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((tid & 31) == 0) red[tid >> 5] = c;
+    __syncthreads();
+    c = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) c += red[w];
+    const int t = blockIdx.x * blockDim.x + tid;
+    if (t < T) {
+        double v = c;
+        const int i0 = a.item_first[sl], i1 = a.item_first[sl + 1];
+        for (int it = i0; it < i1; ++it) v += a.partial[(size_t)it * T + t];
+        out[(size_t)sl * T + t] = v;
+    }
+}
+
+int phase_snaps_per_item(int num_snap, int P, int precision) {
+    if (P <= 0) return 1;
+    // about 1500 items for load balance; FP32 accumulates at most ~8k pairs
+    const int cap = (precision == MSP_PREC_MIXED ? 8192 : 65536) / P;
+    int sb = (num_snap + 1499) / 1500;
+    if (sb > cap) sb = cap;
+    if (sb < 1) sb = 1;
+    return sb;
+}
+
+int phase_max_items(int num_snap, int num_slots, int SB) {
+    return (num_snap + SB - 1) / SB + num_slots;
+}
+
+cudaError_t launch_schedule(const int *slot, int num_snap, int num_slots, int SB,
+                            int count_items, int *slot_first, int *item_first, int *status,
+                            cudaStream_t st) {
+    msp_schedule_kernel<<<1, 1024, 0, st>>>(slot, num_snap, num_slots, SB, count_items,
+                                            slot_first, item_first, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phase(const PhaseArgs &a, int precision, int max_items, int uniform,
+                         cudaStream_t st) {
+    if (max_items <= 0 || a.num_times <= 0) return cudaSuccess;
+    if (uniform) {
+        dim3 grid(max_items, (a.num_times + 4095) / 4096);
+        if (precision == MSP_PREC_MIXED)
+            msp_phase_uniform_kernel<float><<<grid, 128, 0, st>>>(a);
+        else
+            msp_phase_uniform_kernel<double><<<grid, 128, 0, st>>>(a);
+    } else {
+        dim3 grid(max_items, (a.num_times + 255) / 256);
+        if (precision == MSP_PREC_MIXED)
+            msp_phase_direct_kernel<float><<<grid, 256, 0, st>>>(a);
+        else
+            msp_phase_direct_kernel<double><<<grid, 256, 0, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce(const PhaseArgs &a, const double *snap_const, double *out,
+                          int num_times, cudaStream_t st) {
+    if (a.num_slots <= 0) return cudaSuccess;
+    dim3 grid((num_times + 255) / 256, a.num_slots);
+    msp_reduce_kernel<<<grid, 256, 0, st>>>(a, snap_const, out, num_times);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ building blocks
+
+// The reference's cosine sum, same summation order per time
+// (muspinsim/cython/parallel.pyx:59-67).
+__global__ void msp_fast_cos_sum_kernel(const double *__restrict__ times, int T, int d,
+                                        const double *__restrict__ A,
+                                        const double *__restrict__ W, int n,
+                                        double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= T) return;
+    const double t = times[i];
+    double acc = 0.0;
+    for (int j = 0; j < n; ++j) {
+        acc += 0.5 * A[(size_t)j * n + j];
+        for (int k = 0; k < j; ++k) acc += A[(size_t)j * n + k] * cos(W[(size_t)j * n + k] * t);
+    }
+    out[i] = acc * (1.0 / (double)d);
+}
+
+cudaError_t launch_fast_cos_sum(const double *times, int num_times, int d, const double *A,
+                                const double *W, int n, double *out, cudaStream_t st) {
+    if (num_times <= 0) return cudaSuccess;
+    msp_fast_cos_sum_kernel<<<(num_times + 127) / 128, 128, 0, st>>>(times, num_times, d, A, W,
+                                                                      n, out);
+    return cudaGetLastError();
+}
+
+// A = |U^dag (sigma (x) 1_d) U|^2, W = 2 pi (l_j - l_k) (muspinsim/hamiltonian.py:204-211)
+__global__ void msp_fast_amplitudes_kernel(const double *__restrict__ evals,
+                                           const cx<double> *__restrict__ U,
+                                           const cx<double> *__restrict__ sig, int n, int d,
+                                           double *__restrict__ A, double *__restrict__ W) {
+    extern __shared__ __align__(16) char smem[];
+    cx<double> *sU = reinterpret_cast<cx<double> *>(smem);
+    cx<double> *sM = sU + n * n;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int e = tid; e < n * n; e += nt) sU[e] = U[e];
+    __syncthreads();
+    const cx<double> s00 = sig[0], s01 = sig[1], s10 = sig[2], s11 = sig[3];
+    for (int e = tid; e < n * n; e += nt) {
+        const int i = e / n, k = e - (e / n) * n;
+        cx<double> v;
+        if (i < d)
+            v = cadd(cmul(s00, sU[i * n + k]), cmul(s01, sU[(i + d) * n + k]));
+        else
+            v = cadd(cmul(s10, sU[(i - d) * n + k]), cmul(s11, sU[i * n + k]));
+        sM[e] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {
+        const int j = e / n, k = e - (e / n) * n;
+        double gr = 0, gi = 0;
+        for (int i = 0; i < n; ++i) {
+            const cx<double> u = sU[i * n + j], mm = sM[i * n + k];
+            gr += u.re * mm.re + u.im * mm.im;
+            gi += u.re * mm.im - u.im * mm.re;
+        }
+        A[e] = gr * gr + gi * gi;
+        W[e] = 6.283185307179586476925 * (evals[j] - evals[k]);
+    }
+}
+
+cudaError_t launch_fast_amplitudes(const double *evals, const double *evecs,
+                                   const double *sigma, int n, int d, double *A, double *W,
+                                   cudaStream_t st) {
+    const size_t smem = (size_t)2 * n * n * sizeof(cx<double>);
+    cudaError_t e = cudaFuncSetAttribute(msp_fast_amplitudes_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    msp_fast_amplitudes_kernel<<<1, 256, smem, st>>>(
+        evals, reinterpret_cast<const cx<double> *>(evecs),
+        reinterpret_cast<const cx<double> *>(sigma), n, d, A, W);
+    return cudaGetLastError();
+}
+
+// out[t][o] = sum_ij rho_ij op_o[j][i] exp(-i w_ij t), w_ij = 2 pi (l_i - l_j):
+// the general (not necessarily Hermitian operator) expectation series of
+// Hamiltonian.evolve (muspinsim/hamiltonian.py:86-107).  One thread per time.
+__global__ void __launch_bounds__(256) msp_evolve_expect_kernel(
+    const double *__restrict__ evals, const cx<double> *__restrict__ rho,
+    const cx<double> *__restrict__ ops, int n, int num_ops, const double *__restrict__ times,
+    int T, cx<double> *__restrict__ out) {
+    __shared__ cx<double> sc[256];
+    __shared__ double sw[256];
+    const int o = blockIdx.y;
+    const cx<double> *op = ops + (size_t)o * n * n;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = t < T;
+    const double tt = valid ? times[t] : 0.0;
+    double ar = 0.0, ai = 0.0;
+    const int nn = n * n;
+    for (int b = 0; b < nn; b += 256) {
+        const int e = b + threadIdx.x;
+        if (e < nn) {
+            const int i = e / n, j = e - (e / n) * n;
+            sc[threadIdx.x] = cmul(rho[(size_t)i * n + j], op[(size_t)j * n + i]);
+            sw[threadIdx.x] = 6.283185307179586476925 * (evals[i] - evals[j]);
+        }
+        __syncthreads();
+        const int cnt = (nn - b) < 256 ? (nn - b) : 256;
+        for (int q = 0; q < cnt; ++q) {
+            double s, c;
+            sincos(reduce_2pi(sw[q] * tt), &s, &c);
+            // C (cos - i sin)
+            ar += sc[q].re * c + sc[q].im * s;
+            ai += sc[q].im * c - sc[q].re * s;
+        }
+        __syncthreads();
+    }
+    if (valid) out[(size_t)t * num_ops + o] = mk<double>(ar, ai);
+}
+
+cudaError_t launch_evolve_expect(const double *evals, const double *rho, const double *ops,
+                                 int n, int num_ops, const double *times, int num_times,
+                                 double *out, cudaStream_t st) {
+    if (num_times <= 0 || num_ops <= 0) return cudaSuccess;
+    dim3 grid((num_times + 255) / 256, num_ops);
+    msp_evolve_expect_kernel<<<grid, 256, 0, st>>>(
+        evals, reinterpret_cast<const cx<double> *>(rho),
+        reinterpret_cast<const cx<double> *>(ops), n, num_ops, times, num_times,
+        reinterpret_cast<cx<double> *>(out));
+    return cudaGetLastError();
+}
+
+__global__ void msp_evolve_phases_kernel(const double *__restrict__ evals,
+                                         const cx<double> *__restrict__ rho, int n,
+                                         const double *__restrict__ times, int T,
+                                         cx<double> *__restrict__ out) {
+    const size_t nn = (size_t)n * n, total = nn * T;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t t = e / nn, o = e - t * nn;
+        const int i = (int)(o / n), j = (int)(o - (o / n) * n);
+        double s, c;
+        sincos(reduce_2pi(6.283185307179586476925 * (evals[i] - evals[j]) * times[t]), &s, &c);
+        // exp(-i w t) * rho_ij
+        out[e] = cmul(mk<double>(c, -s), rho[o]);
+    }
+}
+
+cudaError_t launch_evolve_phases(const double *evals, const double *rho, int n,
+                                 const double *times, int num_times, double *out,
+                                 cudaStream_t st) {
+    const size_t total = (size_t)n * n * num_times;
+    if (total == 0) return cudaSuccess;
+    int grid = (int)((total + 255) / 256);
+    if (grid > 152 * 16) grid = 152 * 16;
+    msp_evolve_phases_kernel<<<grid, 256, 0, st>>>(evals,
+                                                   reinterpret_cast<const cx<double> *>(rho), n,
+                                                   times, num_times,
+                                                   reinterpret_cast<cx<double> *>(out));
+    return cudaGetLastError();
+}
+
+// out[o] = sum_ij rho_ij (-op_o[j][i]) / (2 pi i (l_j - l_i) - 1/tau)
+// (muspinsim/hamiltonian.py:155-164).  One CTA per operator.
+__global__ void __launch_bounds__(256) msp_integrate_kernel(const double *__restrict__ evals,
+                                                            const cx<double> *__restrict__ rho,
+                                                            const cx<double> *__restrict__ ops,
+                                                            int n, double tau,
+                                                            cx<double> *__restrict__ out) {
+    __shared__ double red[16];
+    const int o = blockIdx.x;
+    const cx<double> *op = ops + (size_t)o * n * n;
+    double ar = 0.0, ai = 0.0;
+    const double inv_tau = 1.0 / tau;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e - (e / n) * n;
+        const cx<double> c = cmul(rho[(size_t)i * n + j], op[(size_t)j * n + i]);
+        const double x = 6.283185307179586476925 * (evals[j] - evals[i]);
+        // -c / (-1/tau + i x) = c (1/tau + i x) / (1/tau^2 + x^2)
+        const double den = inv_tau * inv_tau + x * x;
+        ar += (c.re * inv_tau - c.im * x) / den;
+        ai += (c.im * inv_tau + c.re * x) / den;
+    }
+    block_sum2(ar, ai, red);
+    if (threadIdx.x == 0) out[o] = mk<double>(ar, ai);
+}
+
+cudaError_t launch_integrate(const double *evals, const double *rho, const double *ops, int n,
+                             int num_ops, double tau, double *out, cudaStream_t st) {
+    if (num_ops <= 0) return cudaSuccess;
+    msp_integrate_kernel<<<num_ops, 256, 0, st>>>(evals, reinterpret_cast<const cx<double> *>(rho),
+                                                  reinterpret_cast<const cx<double> *>(ops), n,
+                                                  tau, reinterpret_cast<cx<double> *>(out));
+    return cudaGetLastError();
+}
+
+}  // namespace msp

@@ -1,0 +1,851 @@
+// Per-snapshot kernels: one CTA diagonalises one Hamiltonian in shared
+// memory and turns its eigenbasis into the quantities the time evolution
+// needs.  Replaces, per configuration snapshot, ExperimentRunner.Htot
+// (muspinsim/experiment.py:332-341), Hermitian.diag (muspinsim/spinop.py:
+// 51-82) and the eigenbasis part of Hamiltonian.fast_evolve / evolve /
+// integrate_decaying (muspinsim/hamiltonian.py:76-87, 149-160, 195-211).
+//
+// Precision modes:
+//   FP64  -- Jacobi sweeps, eigenvalues and eigenbasis products in FP64.
+//   MIXED -- Jacobi sweeps in FP32, then one Ogita-Aishima refinement step
+//            evaluated in double-word FP32 arithmetic (dw_acc): residual
+//            products H X, X^H H X and X^H X to ~2^-44, eigenvalues to FP64
+//            accuracy (Rayleigh quotient plus the second-order term), the
+//            eigenvectors corrected to FP32 rounding.  GB300 runs FP32 at
+//            ~60x its FP64 rate, so this costs about as much as the FP32
+//            sweeps themselves instead of dominating as FP64 would.
+#include "msp_internal.cuh"
+#include "msp_jacobi.cuh"
+
+#include <math_constants.h>
+
+namespace msp {
+
+// ------------------------------------------------------------------ smem layout
+
+struct SnapLayout {
+    size_t H, U, sn, cs, da, db, red, pp, pq;  // Jacobi work
+    size_t lam, acc, rank;                     // eigenvalues, reductions, sort
+    size_t Hh, Hl, Yl, SR, sd, corr, rd;       // refinement (MIXED)
+    size_t fac, B2;                            // general path
+    size_t total;
+};
+
+__host__ __device__ inline size_t lay_take(size_t &off, size_t bytes) {
+    off = (off + 15) & ~size_t(15);
+    const size_t o = off;
+    off += bytes;
+    return o;
+}
+
+// Byte offsets of every shared-memory buffer of a snapshot kernel.  The
+// same function sizes the launch (host) and carves the buffers (device).
+__host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine, bool rho,
+                                                  int fac_len, int nwarps) {
+    SnapLayout L;
+    const size_t m = (size_t)(n + (n & 1));
+    const size_t mm = m * (m + 1);  // leading dimension m + 1 (odd): no bank conflicts
+    size_t off = 0;
+    L.H = lay_take(off, mm * 2 * esize);
+    L.U = lay_take(off, mm * 2 * esize);
+    L.sn = lay_take(off, (m / 2) * 2 * esize);
+    L.cs = lay_take(off, (m / 2) * esize);
+    L.da = lay_take(off, (m / 2) * esize);
+    L.db = lay_take(off, (m / 2) * esize);
+    L.red = lay_take(off, 2 * (size_t)nwarps * esize);
+    L.pp = lay_take(off, (m / 2) * 4);
+    L.pq = lay_take(off, (m / 2) * 4);
+    L.lam = lay_take(off, m * 8);
+    L.acc = lay_take(off, 2 * m * 8);
+    L.rank = lay_take(off, m * 4);
+    L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = 0;
+    if (refine) {
+        L.Hh = lay_take(off, mm * 8);
+        L.Hl = lay_take(off, mm * 8);
+        L.Yl = lay_take(off, mm * 8);
+        L.SR = lay_take(off, mm * 8);
+        L.sd = lay_take(off, m * 8);
+        L.corr = lay_take(off, m * 8);
+        L.rd = lay_take(off, m * 4);
+    }
+    L.fac = L.B2 = 0;
+    if (rho) {
+        L.fac = lay_take(off, (size_t)fac_len * 16);
+        // MIXED: the second basis buffer reuses Hh (free after refinement)
+        L.B2 = refine ? L.Hh : lay_take(off, mm * 2 * esize);
+    }
+    L.total = (off + 15) & ~size_t(15);
+    return L;
+}
+
+static int jacobi_threads(int m) {
+    if (m <= 8) return 32;
+    if (m <= 16) return 64;
+    if (m <= 32) return 128;
+    return 256;
+}
+
+size_t snap_smem_bytes(int n, int mode, int precision, int fac_len) {
+    const int m = n + (n & 1);
+    const bool mixed = precision == MSP_PREC_MIXED;
+    return snap_layout(n, mixed ? 4 : 8, mixed, mode != MSP_MODE_FAST, fac_len,
+                       jacobi_threads(m) / 32)
+        .total;
+}
+
+template <typename T>
+struct SnapSmem {
+    JacobiWork<T> w;
+    double *lam, *acc;
+    int *rank;
+    cx<float> *Hh, *Hl, *Yl, *SR;
+    double *sd, *corr;
+    float *rd;
+    cx<double> *fac;
+    cx<T> *B2;
+};
+
+template <typename T, bool REFINE>
+__device__ __forceinline__ SnapSmem<T> snap_carve(char *base, int n, bool rho, int fac_len) {
+    const SnapLayout L =
+        snap_layout(n, sizeof(T), REFINE, rho, fac_len, (blockDim.x + 31) >> 5);
+    SnapSmem<T> s;
+    s.w.H = reinterpret_cast<cx<T> *>(base + L.H);
+    s.w.U = reinterpret_cast<cx<T> *>(base + L.U);
+    s.w.sn = reinterpret_cast<cx<T> *>(base + L.sn);
+    s.w.cs = reinterpret_cast<T *>(base + L.cs);
+    s.w.da = reinterpret_cast<T *>(base + L.da);
+    s.w.db = reinterpret_cast<T *>(base + L.db);
+    s.w.red = reinterpret_cast<T *>(base + L.red);
+    s.w.pp = reinterpret_cast<int *>(base + L.pp);
+    s.w.pq = reinterpret_cast<int *>(base + L.pq);
+    s.lam = reinterpret_cast<double *>(base + L.lam);
+    s.acc = reinterpret_cast<double *>(base + L.acc);
+    s.rank = reinterpret_cast<int *>(base + L.rank);
+    s.Hh = REFINE ? reinterpret_cast<cx<float> *>(base + L.Hh) : nullptr;
+    s.Hl = REFINE ? reinterpret_cast<cx<float> *>(base + L.Hl) : nullptr;
+    s.Yl = REFINE ? reinterpret_cast<cx<float> *>(base + L.Yl) : nullptr;
+    s.SR = REFINE ? reinterpret_cast<cx<float> *>(base + L.SR) : nullptr;
+    s.sd = REFINE ? reinterpret_cast<double *>(base + L.sd) : nullptr;
+    s.corr = REFINE ? reinterpret_cast<double *>(base + L.corr) : nullptr;
+    s.rd = REFINE ? reinterpret_cast<float *>(base + L.rd) : nullptr;
+    s.fac = rho ? reinterpret_cast<cx<double> *>(base + L.fac) : nullptr;
+    s.B2 = rho ? reinterpret_cast<cx<T> *>(base + L.B2) : nullptr;
+    return s;
+}
+
+// ------------------------------------------------------------------ helpers
+
+__device__ __forceinline__ void tri_index(int e, int &j, int &k) {
+    // e -> (j, k) with j >= k, e = j (j + 1) / 2 + k
+    j = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+    while ((j + 1) * (j + 2) / 2 <= e) ++j;
+    while (j * (j + 1) / 2 > e) --j;
+    k = e - j * (j + 1) / 2;
+}
+
+__device__ __forceinline__ int pair_index(int j, int k) { return j * (j - 1) / 2 + k; }
+
+// H = Hsys + b . Z (FP64) into the Jacobi buffer (precision T, padded to m);
+// in MIXED mode also its exact split H = Hh + Hl into two FP32 matrices.
+template <typename T, bool REFINE>
+__device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
+                                 const double *b, int n, int m, SnapSmem<T> &s) {
+    const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1;
+    const double bx = b[0], by = b[1], bz = b[2];
+    const size_t nn = (size_t)n * n;
+    for (int e = tid; e < m * m; e += nt) {
+        const int i = e / m, j = e - (e / m) * m;
+        cx<double> h = mk<double>(0.0, 0.0);
+        if (i < n && j < n) {
+            const size_t o = (size_t)i * n + j;
+            const cx<double> hs = Hsys[o], z0 = Z[o], z1 = Z[nn + o], z2 = Z[2 * nn + o];
+            h.re = hs.re + bx * z0.re + by * z1.re + bz * z2.re;
+            h.im = hs.im + bx * z0.im + by * z1.im + bz * z2.im;
+        }
+        s.w.H[i * ld + j] = mk<T>((T)h.re, (T)h.im);
+        if (REFINE) {
+            const float hr = (float)h.re, hi = (float)h.im;
+            s.Hh[i * ld + j] = mk<float>(hr, hi);
+            s.Hl[i * ld + j] = mk<float>((float)(h.re - (double)hr), (float)(h.im - (double)hi));
+        }
+    }
+    __syncthreads();
+}
+
+// One Ogita-Aishima refinement step of the FP32 eigenvector matrix X
+// (columns) against H = Hh + Hl (Ogita & Aishima, Japan J. Indust. Appl.
+// Math. 35 (2018) 1007, Algorithm 1, Hermitian form):
+//   R = I - X^H X,  S = X^H H X,  l_i = S_ii / (1 - R_ii),
+//   E_ij = (S_ij + l_j R_ij) / (l_j - l_i)  (i != j, separated pair),
+//   E_ij = R_ij / 2  (i != j, |l_j - l_i| below the FP32 resolution),
+//   E_ii = R_ii / 2,   X <- X + X E.
+// H X, X^H H X and X^H X use double-word FP32 accumulation; X E is plain
+// FP32 (E is O(1e-6)).  Eigenvalues: l_i plus the second-order term
+// sum_j |S_ij + l_i R_ij|^2 / (l_i - l_j), in FP64.
+// Returns the largest |E_ij| of a separated pair (the size of the
+// first-order correction); s.rank[0] is its scratch.
+__device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
+    const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1;
+    cx<float> *X = s.w.U;
+    cx<float> *Yh = s.w.H;  // Jacobi work matrix is free now
+    if (tid == 0) s.rank[0] = 0;
+    // Y = H X
+    for (int e = tid; e < n * n; e += nt) {
+        const int i = e / n, j = e - (e / n) * n;
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+        for (int k = 0; k < n; ++k) {
+            const cx<float> h = s.Hh[i * ld + k], hl = s.Hl[i * ld + k], x = X[k * ld + j];
+            dw_acc(rh, rl, h.re, x.re);
+            dw_acc(rh, rl, -h.im, x.im);
+            dw_acc(ih, il, h.re, x.im);
+            dw_acc(ih, il, h.im, x.re);
+            rl = fmaf(hl.re, x.re, rl);
+            rl = fmaf(-hl.im, x.im, rl);
+            il = fmaf(hl.re, x.im, il);
+            il = fmaf(hl.im, x.re, il);
+        }
+        Yh[i * ld + j] = mk<float>(rh, ih);
+        s.Yl[i * ld + j] = mk<float>(rl, il);
+    }
+    __syncthreads();
+    // S_ij (i <= j) into SR upper triangle / sd; R_ij (i < j) into SR lower
+    // triangle at (j, i); R_ii into rd
+    const int ntri = n * (n + 1) / 2;
+    for (int e = tid; e < ntri; e += nt) {
+        int j, i;
+        tri_index(e, j, i);  // j >= i
+        float sr = 0.f, srl = 0.f, si = 0.f, sil = 0.f;
+        float gr = 0.f, grl = 0.f, gi = 0.f, gil = 0.f;
+        for (int k = 0; k < n; ++k) {
+            const cx<float> xi = X[k * ld + i], xj = X[k * ld + j];
+            const cx<float> yh = Yh[k * ld + j], yl = s.Yl[k * ld + j];
+            // conj(xi) * (yh + yl)
+            dw_acc(sr, srl, xi.re, yh.re);
+            dw_acc(sr, srl, xi.im, yh.im);
+            dw_acc(si, sil, xi.re, yh.im);
+            dw_acc(si, sil, -xi.im, yh.re);
+            srl = fmaf(xi.re, yl.re, fmaf(xi.im, yl.im, srl));
+            sil = fmaf(xi.re, yl.im, fmaf(-xi.im, yl.re, sil));
+            // conj(xi) * xj
+            dw_acc(gr, grl, xi.re, xj.re);
+            dw_acc(gr, grl, xi.im, xj.im);
+            dw_acc(gi, gil, xi.re, xj.im);
+            dw_acc(gi, gil, -xi.im, xj.re);
+        }
+        if (i == j) {
+            s.sd[i] = (double)sr + (double)srl;
+            s.rd[i] = __fsub_rn(__fsub_rn(1.0f, gr), grl);  // 1 - G_ii, exact first step
+        } else {
+            s.SR[i * ld + j] = mk<float>(sr + srl, si + sil);
+            s.SR[j * ld + i] = mk<float>(-(gr + grl), -(gi + gil));  // R_ij = -G_ij
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+        s.lam[i] = s.sd[i] / (1.0 - (double)s.rd[i]);
+        s.corr[i] = 0.0;
+    }
+    __syncthreads();
+    double lmax = 0.0;
+    for (int i = 0; i < n; ++i) lmax = fmax(lmax, fabs(s.lam[i]));
+    const double deg = 1e-7 * (lmax + 1e-300);
+    // E in place of S/R; second-order eigenvalue terms
+    const int nup = n * (n - 1) / 2;
+    for (int e = tid; e < nup; e += nt) {
+        // strict upper pairs (i < j): j = row of the packed strict triangle
+        int j = (int)((sqrtf(8.0f * (float)e + 1.0f) + 1.0f) * 0.5f);
+        while (j * (j - 1) / 2 > e) --j;
+        while ((j + 1) * j / 2 <= e) ++j;
+        const int i = e - j * (j - 1) / 2;  // 0 <= i < j
+        const cx<float> S = s.SR[i * ld + j], R = s.SR[j * ld + i];
+        const double li = s.lam[i], lj = s.lam[j];
+        const double dl = lj - li;
+        cx<float> Eij, Eji;
+        if (fabs(dl) > deg) {
+            // E_ij = (S_ij + l_j R_ij) / (l_j - l_i); E_ji = (S_ji + l_i R_ji) / (l_i - l_j)
+            const float inv = (float)(1.0 / dl);
+            const float lj_f = (float)lj, li_f = (float)li;
+            Eij = mk<float>((S.re + lj_f * R.re) * inv, (S.im + lj_f * R.im) * inv);
+            Eji = mk<float>(-(S.re + li_f * R.re) * inv, (S.im + li_f * R.im) * inv);
+            // second order: |S_ij + l_i R_ij|^2 / (l_i - l_j) for l_i, and the mirror
+            const double ar = (double)S.re + li * (double)R.re, ai = (double)S.im + li * (double)R.im;
+            const double br = (double)S.re + lj * (double)R.re, bi = (double)S.im + lj * (double)R.im;
+            atomicAdd(&s.corr[i], -(ar * ar + ai * ai) / dl);
+            atomicAdd(&s.corr[j], (br * br + bi * bi) / dl);
+            const float mag = fmaxf(fmaxf(fabsf(Eij.re), fabsf(Eij.im)),
+                                    fmaxf(fabsf(Eji.re), fabsf(Eji.im)));
+            atomicMax(&s.rank[0], __float_as_int(mag));  // non-negative: int order = float order
+        } else {
+            Eij = mk<float>(0.5f * R.re, 0.5f * R.im);
+            Eji = mk<float>(0.5f * R.re, -0.5f * R.im);
+        }
+        s.SR[i * ld + j] = Eij;
+        s.SR[j * ld + i] = Eji;
+    }
+    __syncthreads();
+    // X' = X + X E  (into Yh), E_ii = R_ii / 2
+    for (int e = tid; e < n * n; e += nt) {
+        const int k = e / n, j = e - (e / n) * n;
+        const cx<float> xkj = X[k * ld + j];
+        const float hr = 0.5f * s.rd[j];
+        float ar = xkj.re + hr * xkj.re, ai = xkj.im + hr * xkj.im;
+        for (int i = 0; i < n; ++i) {
+            if (i == j) continue;
+            const cx<float> x = X[k * ld + i], E = s.SR[i * ld + j];
+            ar = fmaf(x.re, E.re, fmaf(-x.im, E.im, ar));
+            ai = fmaf(x.re, E.im, fmaf(x.im, E.re, ai));
+        }
+        Yh[k * ld + j] = mk<float>(ar, ai);
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {
+        const int k = e / n, j = e - (e / n) * n;
+        X[k * ld + j] = Yh[k * ld + j];
+    }
+    for (int i = tid; i < n; i += nt) s.lam[i] += s.corr[i];
+    __syncthreads();
+    const float emax = __int_as_float(s.rank[0]);
+    __syncthreads();
+    return emax;
+}
+
+// Eigenvalues into lam[0..n): the Jacobi diagonal (FP64), or the refined
+// values (MIXED; also refines the eigenvectors in place).
+template <typename T, bool REFINE>
+__device__ void eigenpairs(SnapSmem<T> &s, int n, int m);
+
+template <>
+__device__ void eigenpairs<double, false>(SnapSmem<double> &s, int n, int m) {
+    const int ld = m + 1;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) s.lam[j] = s.w.H[j * ld + j].re;
+    __syncthreads();
+}
+
+// One refinement step leaves an error of order E^2; a step whose largest
+// correction exceeds 2e-4 (a pair within ~1e3 FP32 resolutions, as at a
+// level anticrossing) is followed by another, at most three in all.
+template <>
+__device__ void eigenpairs<float, true>(SnapSmem<float> &s, int n, int m) {
+    for (int it = 0; it < 3; ++it)
+        if (oa_refine(s, n, m) <= 2e-4f) break;
+}
+
+// ------------------------------------------------------------------ eigh
+
+template <typename T, bool REFINE>
+__global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int batch,
+                                int max_sweeps, double *__restrict__ evals,
+                                cx<double> *__restrict__ evecs, int *__restrict__ status) {
+    extern __shared__ __align__(16) char smem[];
+    const int m = n + (n & 1), ld = m + 1;
+    SnapSmem<T> s = snap_carve<T, REFINE>(smem, n, false, 0);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int bidx = blockIdx.x; bidx < batch; bidx += gridDim.x) {
+        const cx<double> *Hb = Hin + (size_t)bidx * n * n;
+        for (int e = tid; e < m * m; e += nt) {
+            const int i = e / m, j = e - (e / m) * m;
+            cx<double> h = mk<double>(0.0, 0.0);
+            if (i < n && j < n) h = Hb[(size_t)i * n + j];
+            s.w.H[i * ld + j] = mk<T>((T)h.re, (T)h.im);
+            if (REFINE) {
+                const float hr = (float)h.re, hi = (float)h.im;
+                s.Hh[i * ld + j] = mk<float>(hr, hi);
+                s.Hl[i * ld + j] = mk<float>((float)(h.re - (double)hr), (float)(h.im - (double)hi));
+            }
+        }
+        __syncthreads();
+        const int st = jacobi_sweeps<T>(s.w, m, max_sweeps);
+        eigenpairs<T, REFINE>(s, n, m);
+        // ascending order, ties by index (stable)
+        for (int j = tid; j < n; j += nt) {
+            int r = 0;
+            const double lj = s.lam[j];
+            for (int k = 0; k < n; ++k) {
+                const double lk = s.lam[k];
+                r += (lk < lj) || (lk == lj && k < j);
+            }
+            s.rank[j] = r;
+            evals[(size_t)bidx * n + r] = lj;
+        }
+        __syncthreads();
+        cx<double> *Vb = evecs + (size_t)bidx * n * n;
+        for (int e = tid; e < n * n; e += nt) {
+            const int i = e / n, j = e - (e / n) * n;
+            const cx<T> u = s.w.U[i * ld + j];
+            Vb[(size_t)i * n + s.rank[j]] = mk<double>((double)u.re, (double)u.im);
+        }
+        if (tid == 0) status[bidx] = st;
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ fast path
+
+// One snapshot of the muon-first T = inf shortcut (muspinsim/hamiltonian.py:
+// 166-217): A = |U^dag (sigma_p (x) 1_d) U|^2 and omega_jk = 2 pi (l_j - l_k)
+// for j > k, scaled by 0.5 * w / (d * N_avg), plus the constant
+// 0.5 * sum_j A_jj part.
+template <typename T, bool REFINE>
+__global__ void msp_snap_fast_kernel(SnapArgs a) {
+    extern __shared__ __align__(16) char smem[];
+    const int n = a.n, m = n + (n & 1), ld = m + 1, d = n / 2;
+    SnapSmem<T> s = snap_carve<T, REFINE>(smem, n, false, 0);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int P = n * (n - 1) / 2;
+    typedef typename PairCoef<T>::type coef_t;
+    coef_t *coef = reinterpret_cast<coef_t *>(a.pair_coef);
+
+    for (int sn = blockIdx.x; sn < a.num_snap; sn += gridDim.x) {
+        load_hamiltonian<T, REFINE>(a.Hsys, a.Z, a.field + 3 * (size_t)sn, n, m, s);
+        const int st = jacobi_sweeps<T>(s.w, m, a.max_sweeps);
+        eigenpairs<T, REFINE>(s, n, m);
+
+        // sigma_p = p . sigma (Pauli), applied on the muon (slowest) digit
+        const double px = a.pol[3 * (size_t)sn], py = a.pol[3 * (size_t)sn + 1],
+                     pz = a.pol[3 * (size_t)sn + 2];
+        const cx<T> s00 = mk<T>((T)pz, T(0)), s01 = mk<T>((T)px, (T)(-py));
+        const cx<T> s10 = mk<T>((T)px, (T)py), s11 = mk<T>((T)(-pz), T(0));
+        cx<T> *M = s.w.H;  // free buffer
+        const cx<T> *U = s.w.U;
+        for (int e = tid; e < n * n; e += nt) {
+            const int i = e / n, k = e - (e / n) * n;
+            cx<T> v;
+            if (i < d)
+                v = cadd(cmul(s00, U[i * ld + k]), cmul(s01, U[(i + d) * ld + k]));
+            else
+                v = cadd(cmul(s10, U[(i - d) * ld + k]), cmul(s11, U[i * ld + k]));
+            M[i * ld + k] = v;
+        }
+        if (tid == 0) s.acc[0] = 0.0;
+        __syncthreads();
+        const double scale = 0.5 * a.wscale[sn] / (double)d;
+        const int ntri = n * (n + 1) / 2;
+        double diag_local = 0.0;
+        for (int e = tid; e < ntri; e += nt) {
+            int j, k;
+            tri_index(e, j, k);
+            T gr = 0, gi = 0;
+            for (int i = 0; i < n; ++i) {
+                const cx<T> u = U[i * ld + j], mm = M[i * ld + k];
+                gr += u.re * mm.re + u.im * mm.im;
+                gi += u.re * mm.im - u.im * mm.re;
+            }
+            const double A = (double)(gr * gr + gi * gi);
+            if (j == k) {
+                diag_local += A;
+            } else {
+                const size_t o = (size_t)sn * P + pair_index(j, k);
+                coef[o] = PairCoef<T>::make(scale * A, 0.0);
+                a.pair_omega[o] = 6.283185307179586476925 * (s.lam[j] - s.lam[k]);
+            }
+        }
+        atomicAdd(&s.acc[0], diag_local);
+        __syncthreads();
+        if (tid == 0) {
+            a.snap_const[sn] = scale * 0.5 * s.acc[0];
+            a.status[sn] = st;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ general path
+
+#define MSP_FACTOR_MAXD 10
+
+// Kronecker factors of rho0 for snapshot s (muspinsim/experiment.py:170-236):
+// the muon in the pure +1/2 state along its polarisation, every other spin
+// thermal in its own Zeeman field gamma_i B (uniform at T = inf, ground
+// state at T <= 0).  Each factor is sum_k w_k P_k with P_k the spectral
+// projectors of n.S, written exactly by Lagrange interpolation over the
+// eigenvalues m = I .. -I -- the reference's 2x2/3x3 eigh in closed form.
+// One thread per spin; spins up to I = 9/2.
+__device__ void build_rho_factors(const SnapArgs &a, int s, cx<double> *fac) {
+    const int i = threadIdx.x;
+    if (i >= a.num_spins) return;
+    int off = 0;
+    for (int k = 0; k < i; ++k) off += a.dims[k] * a.dims[k];
+    const int d = a.dims[i];
+    cx<double> *R = fac + off;
+    for (int e = 0; e < d * d; ++e) R[e] = mk<double>(0.0, 0.0);
+    if (d > MSP_FACTOR_MAXD) return;  // rejected on the host
+    const double I = 0.5 * (d - 1);
+    const bool is_mu = i == a.mu_index;
+    const double *v = is_mu ? a.pol + 3 * (size_t)s : a.field + 3 * (size_t)s;
+    const double vn = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    double nx = 0.0, ny = 0.0, nz = 1.0;
+    if (vn > 0.0) {
+        nx = v[0] / vn;
+        ny = v[1] / vn;
+        nz = v[2] / vn;
+    }
+    double w[MSP_FACTOR_MAXD];
+    if (is_mu) {
+        for (int k = 0; k < d; ++k) w[k] = k == 0 ? 1.0 : 0.0;
+    } else {
+        const double T = a.temperature ? a.temperature[s] : CUDART_INF;
+        const double h = 6.62607015e-34, kB = 1.380649e-23;
+        double E[MSP_FACTOR_MAXD];
+        for (int k = 0; k < d; ++k) E[k] = (I - k) * vn * 1e6 * a.gammas[i];
+        double sum = 0.0;
+        if (T > 0.0) {
+            double xmax = -CUDART_INF;
+            for (int k = 0; k < d; ++k) {
+                w[k] = -h * E[k] / (kB * T);
+                xmax = fmax(xmax, w[k]);
+            }
+            for (int k = 0; k < d; ++k) {
+                w[k] = exp(w[k] - xmax);
+                sum += w[k];
+            }
+        } else {
+            double emin = E[0];
+            for (int k = 1; k < d; ++k) emin = fmin(emin, E[k]);
+            for (int k = 0; k < d; ++k) {
+                w[k] = E[k] == emin ? 1.0 : 0.0;
+                sum += w[k];
+            }
+        }
+        for (int k = 0; k < d; ++k) w[k] = sum > 0.0 ? w[k] / sum : 1.0 / d;
+    }
+    // n.S: diagonal n_z m_k, off-diagonal (n_x -/+ i n_y)/2 c_k,
+    // c_k = sqrt((k+1)(2I-k)) = <m+1|S+|m>
+    cx<double> nS[MSP_FACTOR_MAXD * MSP_FACTOR_MAXD];
+    for (int e = 0; e < d * d; ++e) nS[e] = mk<double>(0.0, 0.0);
+    for (int k = 0; k < d; ++k) nS[k * d + k] = mk<double>(nz * (I - k), 0.0);
+    for (int k = 0; k + 1 < d; ++k) {
+        const double c = sqrt((double)(k + 1) * (2.0 * I - k));
+        nS[k * d + k + 1] = mk<double>(0.5 * nx * c, -0.5 * ny * c);
+        nS[(k + 1) * d + k] = mk<double>(0.5 * nx * c, 0.5 * ny * c);
+    }
+    cx<double> P[MSP_FACTOR_MAXD * MSP_FACTOR_MAXD], Tm[MSP_FACTOR_MAXD * MSP_FACTOR_MAXD];
+    for (int k = 0; k < d; ++k) {
+        if (w[k] == 0.0) continue;
+        const double mk_ = I - k;
+        for (int e = 0; e < d * d; ++e) P[e] = mk<double>((e / d) == (e % d) ? 1.0 : 0.0, 0.0);
+        for (int k2 = 0; k2 < d; ++k2) {
+            if (k2 == k) continue;
+            const double m2 = I - k2, inv = 1.0 / (mk_ - m2);
+            // Tm = P (nS - m2) / (mk - m2)
+            for (int r = 0; r < d; ++r)
+                for (int c = 0; c < d; ++c) {
+                    double tr = 0.0, ti = 0.0;
+                    for (int l = 0; l < d; ++l) {
+                        cx<double> x = nS[l * d + c];
+                        if (l == c) x.re -= m2;
+                        const cx<double> p = P[r * d + l];
+                        tr += p.re * x.re - p.im * x.im;
+                        ti += p.re * x.im + p.im * x.re;
+                    }
+                    Tm[r * d + c] = mk<double>(tr * inv, ti * inv);
+                }
+            for (int e = 0; e < d * d; ++e) P[e] = Tm[e];
+        }
+        for (int e = 0; e < d * d; ++e) {
+            R[e].re += w[k] * P[e].re;
+            R[e].im += w[k] * P[e].im;
+        }
+    }
+    double tr = 0.0;
+    for (int k = 0; k < d; ++k) tr += R[k * d + k].re;
+    for (int e = 0; e < d * d; ++e) {
+        R[e].re /= tr;
+        R[e].im /= tr;
+    }
+}
+
+// Applies the single-spin matrix F (dim x dim, complex128) on digit `stride`
+// of the row index of X (n x n, leading dim m) into Y: Y = (1 (x) F (x) 1) X.
+template <typename T>
+__device__ void apply_digit(const cx<double> *F, int dim, int stride, const cx<T> *X,
+                            cx<T> *Y, int n, int m) {
+    const int ld = m + 1;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e / n, k = e - (e / n) * n;
+        const int di = (i / stride) % dim;
+        const int base = i - di * stride;
+        T yr = 0, yi = 0;
+        for (int l = 0; l < dim; ++l) {
+            const cx<double> f = F[di * dim + l];
+            const cx<T> x = X[(base + l * stride) * ld + k];
+            yr += (T)f.re * x.re - (T)f.im * x.im;
+            yi += (T)f.re * x.im + (T)f.im * x.re;
+        }
+        Y[i * ld + k] = mk<T>(yr, yi);
+    }
+    __syncthreads();
+}
+
+// One snapshot of the general path: rho' = U^dag rho0 U, O' = U^dag O U with
+// rho0 = (x)_s rho_s (Kronecker factors) and O = p . S_mu.  EVOLVE writes the
+// pair coefficients of <O>(t) = sum_ij rho'_ij O'_ji exp(-i w_ij t)
+// (muspinsim/hamiltonian.py:80-107); INTEGRAL writes the decaying integral
+// divided by tau (muspinsim/hamiltonian.py:150-164, experiment.py:492-496).
+template <typename T, bool REFINE, bool INTEGRAL>
+__global__ void msp_snap_rho_kernel(SnapArgs a) {
+    extern __shared__ __align__(16) char smem[];
+    const int n = a.n, m = n + (n & 1), ld = m + 1;
+    SnapSmem<T> s = snap_carve<T, REFINE>(smem, n, true, a.fac_len);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int P = n * (n - 1) / 2;
+    typedef typename PairCoef<T>::type coef_t;
+    coef_t *coef = reinterpret_cast<coef_t *>(a.pair_coef);
+    const double twopi = 6.283185307179586476925;
+
+    for (int sn = blockIdx.x; sn < a.num_snap; sn += gridDim.x) {
+        if (a.rho_fac) {
+            for (int e = tid; e < a.fac_len; e += nt)
+                s.fac[e] = a.rho_fac[(size_t)sn * a.fac_len + e];
+        } else {
+            build_rho_factors(a, sn, s.fac);
+        }
+        load_hamiltonian<T, REFINE>(a.Hsys, a.Z, a.field + 3 * (size_t)sn, n, m, s);
+        const int st = jacobi_sweeps<T>(s.w, m, a.max_sweeps);
+        eigenpairs<T, REFINE>(s, n, m);
+        const cx<T> *U = s.w.U;
+
+        // T1 = rho0 U by Kronecker factors: X ping-pongs between H and B2
+        const cx<T> *X = U;
+        cx<T> *Y = s.w.H;
+        {
+            int off = 0;
+            for (int sp = 0; sp < a.num_spins; ++sp) {
+                const int dim = a.dims[sp];
+                apply_digit<T>(s.fac + off, dim, a.strides[sp], X, Y, n, m);
+                off += dim * dim;
+                X = Y;
+                Y = (Y == s.w.H) ? s.B2 : s.w.H;
+            }
+        }
+        // X holds rho0 U.  rho'_jk (j >= k) -> Y (the other buffer).
+        const int ntri = n * (n + 1) / 2;
+        for (int e = tid; e < ntri; e += nt) {
+            int j, k;
+            tri_index(e, j, k);
+            T gr = 0, gi = 0;
+            for (int i = 0; i < n; ++i) {
+                const cx<T> u = U[i * ld + j], x = X[i * ld + k];
+                gr += u.re * x.re + u.im * x.im;
+                gi += u.re * x.im - u.im * x.re;
+            }
+            Y[j * ld + k] = mk<T>(gr, gi);
+        }
+        __syncthreads();
+        // O U into the buffer X (free now): O = sum_a p_a S^a on the muon digit
+        cx<T> *OU = const_cast<cx<T> *>(X);
+        const double px = a.pol[3 * (size_t)sn], py = a.pol[3 * (size_t)sn + 1],
+                     pz = a.pol[3 * (size_t)sn + 2];
+        {
+            const int stride = a.strides[a.mu_index];
+            const cx<T> o00 = mk<T>((T)(0.5 * pz), T(0));
+            const cx<T> o01 = mk<T>((T)(0.5 * px), (T)(-0.5 * py));
+            const cx<T> o10 = mk<T>((T)(0.5 * px), (T)(0.5 * py));
+            const cx<T> o11 = mk<T>((T)(-0.5 * pz), T(0));
+            for (int e = tid; e < n * n; e += nt) {
+                const int i = e / n, k = e - (e / n) * n;
+                const int di = (i / stride) & 1;
+                const int base = i - di * stride;
+                const cx<T> x0 = U[base * ld + k], x1 = U[(base + stride) * ld + k];
+                OU[i * ld + k] = di == 0 ? cadd(cmul(o00, x0), cmul(o01, x1))
+                                        : cadd(cmul(o10, x0), cmul(o11, x1));
+            }
+        }
+        if (tid == 0) s.acc[0] = 0.0;
+        __syncthreads();
+        const double scale = a.wscale[sn];
+        double local = 0.0;
+        for (int e = tid; e < ntri; e += nt) {
+            int j, k;
+            tri_index(e, j, k);
+            // O'_kj = sum_i conj(U_ik) (O U)_ij
+            T orr = 0, oii = 0;
+            for (int i = 0; i < n; ++i) {
+                const cx<T> u = U[i * ld + k], x = OU[i * ld + j];
+                orr += u.re * x.re + u.im * x.im;
+                oii += u.re * x.im - u.im * x.re;
+            }
+            const cx<T> r = Y[j * ld + k];
+            // C_jk = rho'_jk O'_kj
+            const double cr = (double)r.re * (double)orr - (double)r.im * (double)oii;
+            const double ci = (double)r.re * (double)oii + (double)r.im * (double)orr;
+            if (INTEGRAL) {
+                // term = C_jk * (-1) / (2 pi i (l_k - l_j) - 1/tau); pairs count twice
+                const double inv_tau = 1.0 / a.tau;
+                if (j == k) {
+                    local += cr * a.tau;
+                } else {
+                    const double x = twopi * (s.lam[k] - s.lam[j]);
+                    // -C / (-1/tau + i x) = C (1/tau + i x) / (1/tau^2 + x^2)
+                    const double den = inv_tau * inv_tau + x * x;
+                    local += 2.0 * (cr * inv_tau - ci * x) / den;
+                }
+            } else {
+                if (j == k) {
+                    local += cr;
+                } else {
+                    const size_t o = (size_t)sn * P + pair_index(j, k);
+                    coef[o] = PairCoef<T>::make(2.0 * scale * cr, 2.0 * scale * ci);
+                    a.pair_omega[o] = twopi * (s.lam[j] - s.lam[k]);
+                }
+            }
+        }
+        atomicAdd(&s.acc[0], local);
+        __syncthreads();
+        if (tid == 0) {
+            a.snap_const[sn] = INTEGRAL ? scale * s.acc[0] / a.tau : scale * s.acc[0];
+            a.status[sn] = st;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+
+template <typename K>
+static cudaError_t launch_snap(K kernel, const SnapArgs &a, int grid, size_t smem,
+                               cudaStream_t st) {
+    const int m = a.n + (a.n & 1);
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    kernel<<<grid, jacobi_threads(m), smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStream_t st) {
+    if (a.num_snap <= 0) return cudaSuccess;
+    const size_t smem = snap_smem_bytes(a.n, mode, precision, a.fac_len);
+    const int grid = a.num_snap;
+    const bool mixed = precision == MSP_PREC_MIXED;
+    if (mode == MSP_MODE_FAST) {
+        return mixed ? launch_snap(msp_snap_fast_kernel<float, true>, a, grid, smem, st)
+                     : launch_snap(msp_snap_fast_kernel<double, false>, a, grid, smem, st);
+    } else if (mode == MSP_MODE_EVOLVE) {
+        return mixed ? launch_snap(msp_snap_rho_kernel<float, true, false>, a, grid, smem, st)
+                     : launch_snap(msp_snap_rho_kernel<double, false, false>, a, grid, smem, st);
+    }
+    return mixed ? launch_snap(msp_snap_rho_kernel<float, true, true>, a, grid, smem, st)
+                 : launch_snap(msp_snap_rho_kernel<double, false, true>, a, grid, smem, st);
+}
+
+cudaError_t launch_eigh(const double *H, int n, int batch, int precision, int max_sweeps,
+                        double *evals, double *evecs, int *status, cudaStream_t st) {
+    const int m = n + (n & 1);
+    const size_t smem = snap_smem_bytes(n, MSP_MODE_FAST, precision, 0);
+    const int grid = batch;
+    const cx<double> *Hc = reinterpret_cast<const cx<double> *>(H);
+    cx<double> *Vc = reinterpret_cast<cx<double> *>(evecs);
+    cudaError_t e;
+    if (precision == MSP_PREC_MIXED) {
+        e = cudaFuncSetAttribute(msp_eigh_kernel<float, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        msp_eigh_kernel<float, true><<<grid, jacobi_threads(m), smem, st>>>(
+            Hc, n, batch, max_sweeps, evals, Vc, status);
+    } else {
+        e = cudaFuncSetAttribute(msp_eigh_kernel<double, false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        msp_eigh_kernel<double, false><<<grid, jacobi_threads(m), smem, st>>>(
+            Hc, n, batch, max_sweeps, evals, Vc, status);
+    }
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ assemble / basis change
+
+__global__ void msp_assemble_kernel(const cx<double> *__restrict__ Hsys,
+                                    const cx<double> *__restrict__ Z,
+                                    const double *__restrict__ fields, int n, int batch,
+                                    cx<double> *__restrict__ H) {
+    const size_t nn = (size_t)n * n;
+    const size_t total = nn * batch;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t b = e / nn, o = e - b * nn;
+        const double bx = fields[3 * b], by = fields[3 * b + 1], bz = fields[3 * b + 2];
+        const cx<double> hs = Hsys[o], z0 = Z[o], z1 = Z[nn + o], z2 = Z[2 * nn + o];
+        H[e] = mk<double>(hs.re + bx * z0.re + by * z1.re + bz * z2.re,
+                          hs.im + bx * z0.im + by * z1.im + bz * z2.im);
+    }
+}
+
+cudaError_t launch_assemble(const double *Hsys, const double *Z, const double *fields, int n,
+                            int batch, double *H, cudaStream_t st) {
+    const size_t total = (size_t)n * n * batch;
+    int grid = (int)((total + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    if (grid < 1) grid = 1;
+    msp_assemble_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const cx<double> *>(Hsys),
+                                              reinterpret_cast<const cx<double> *>(Z), fields, n,
+                                              batch, reinterpret_cast<cx<double> *>(H));
+    return cudaGetLastError();
+}
+
+// out = U^dag M U (adjoint = 0) or U M U^dag (adjoint = 1), FP64, one CTA per
+// matrix, n <= 64: U and M staged in shared memory, T = M U (or M U^dag)
+// kept in shared memory, then out = U^dag T (or U T) written to global.
+__global__ void msp_basis_change_kernel(const cx<double> *__restrict__ U, long long u_stride,
+                                        const cx<double> *__restrict__ M, long long m_stride,
+                                        int n, int batch, int adjoint,
+                                        cx<double> *__restrict__ out) {
+    extern __shared__ __align__(16) char smem[];
+    cx<double> *sU = reinterpret_cast<cx<double> *>(smem);
+    cx<double> *sM = sU + n * n;
+    cx<double> *sT = sM + n * n;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int b = blockIdx.x; b < batch; b += gridDim.x) {
+        const cx<double> *Ub = U + (size_t)b * u_stride;
+        const cx<double> *Mb = M + (size_t)b * m_stride;
+        for (int e = tid; e < n * n; e += nt) {
+            sU[e] = Ub[e];
+            sM[e] = Mb[e];
+        }
+        __syncthreads();
+        for (int e = tid; e < n * n; e += nt) {
+            const int i = e / n, k = e - (e / n) * n;
+            double tr = 0, ti = 0;
+            for (int l = 0; l < n; ++l) {
+                const cx<double> mv = sM[i * n + l];
+                // adjoint: (U^dag)_lk = conj(U_kl)
+                const cx<double> uv = adjoint ? conj(sU[k * n + l]) : sU[l * n + k];
+                tr += mv.re * uv.re - mv.im * uv.im;
+                ti += mv.re * uv.im + mv.im * uv.re;
+            }
+            sT[e] = mk<double>(tr, ti);
+        }
+        __syncthreads();
+        cx<double> *Ob = out + (size_t)b * n * n;
+        for (int e = tid; e < n * n; e += nt) {
+            const int j = e / n, k = e - (e / n) * n;
+            double tr = 0, ti = 0;
+            for (int i = 0; i < n; ++i) {
+                // row j of U^dag = conj(U_ij); row j of U = U_ji
+                const cx<double> uv = adjoint ? sU[j * n + i] : conj(sU[i * n + j]);
+                const cx<double> tv = sT[i * n + k];
+                tr += uv.re * tv.re - uv.im * tv.im;
+                ti += uv.re * tv.im + uv.im * tv.re;
+            }
+            Ob[e] = mk<double>(tr, ti);
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_basis_change(const double *U, long long u_stride, const double *M,
+                                long long m_stride, int n, int batch, int adjoint, double *out,
+                                cudaStream_t st) {
+    const size_t smem = (size_t)3 * n * n * sizeof(cx<double>);
+    cudaError_t e = cudaFuncSetAttribute(msp_basis_change_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int grid = batch < 152 * 8 ? batch : 152 * 8;
+    msp_basis_change_kernel<<<grid, n <= 16 ? 64 : 256, smem, st>>>(
+        reinterpret_cast<const cx<double> *>(U), u_stride,
+        reinterpret_cast<const cx<double> *>(M), m_stride, n, batch, adjoint,
+        reinterpret_cast<cx<double> *>(out));
+    return cudaGetLastError();
+}
+
+}  // namespace msp

@@ -1,0 +1,276 @@
+"""Thin Python layer over the C ABI: torch CUDA tensors in, torch tensors out.
+
+Each function here launches one entry point of ``libmspgpu.so`` on the
+current torch CUDA stream.  Inputs may be numpy arrays (copied to the
+device) or CUDA tensors (used in place).  Nothing here computes on the CPU.
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from muspinsim_gb300 import _lib
+
+def device():
+    """The CUDA device the library runs on; raises when there is none."""
+    if not torch.cuda.is_available():
+        raise RuntimeError(
+            "muspinsim_gb300 needs a CUDA device: the polarisation kernels have no CPU path"
+        )
+    _lib.load()
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def dev(a, dtype):
+    """Contiguous device tensor of `dtype` from a numpy array or tensor."""
+    d = device()
+    if isinstance(a, torch.Tensor):
+        return a.to(device=d, dtype=dtype).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).to(d)
+
+
+def eigh(H, precision=_lib.PREC_FP64, max_sweeps=0):
+    """Batched Hermitian eigensolve of (batch, n, n) complex matrices.
+
+    Returns (evals (batch, n) float64 ascending, evecs (batch, n, n)
+    complex128 with eigenvectors as columns, status (batch,) int32)."""
+    Hd = dev(H, torch.complex128)
+    if Hd.dim() == 2:
+        Hd = Hd[None]
+    b, n, _ = Hd.shape
+    evals = torch.empty((b, n), dtype=torch.float64, device=Hd.device)
+    evecs = torch.empty((b, n, n), dtype=torch.complex128, device=Hd.device)
+    status = torch.empty((b,), dtype=torch.int32, device=Hd.device)
+    _lib.call("msp_eigh_batched", ptr(Hd), n, b, int(precision), int(max_sweeps), ptr(evals),
+              ptr(evecs), ptr(status), stream())
+    return evals, evecs, status
+
+
+def assemble(Hsys, Z, fields):
+    """H[b] = Hsys + sum_a fields[b, a] Z[a]."""
+    Hs = dev(Hsys, torch.complex128)
+    Zd = dev(Z, torch.complex128)
+    F = dev(fields, torch.float64).reshape(-1, 3)
+    n = Hs.shape[-1]
+    out = torch.empty((F.shape[0], n, n), dtype=torch.complex128, device=Hs.device)
+    _lib.call("msp_assemble", ptr(Hs), ptr(Zd), ptr(F), n, F.shape[0], ptr(out), stream())
+    return out
+
+
+def basis_change(U, M, adjoint=False):
+    """U^dag M U (or U M U^dag when adjoint) for batched or single matrices."""
+    Ud = dev(U, torch.complex128)
+    Md = dev(M, torch.complex128)
+    n = Ud.shape[-1]
+    ub = Ud.reshape(-1, n, n).shape[0]
+    mb = Md.reshape(-1, n, n).shape[0]
+    batch = max(ub, mb)
+    if ub not in (1, batch) or mb not in (1, batch):
+        raise ValueError("basis_change: incompatible batch sizes")
+    out = torch.empty((batch, n, n), dtype=torch.complex128, device=Ud.device)
+    _lib.call("msp_basis_change", ptr(Ud), 0 if ub == 1 else n * n, ptr(Md),
+              0 if mb == 1 else n * n, n, batch, 1 if adjoint else 0, ptr(out), stream())
+    return out
+
+
+def fast_cos_sum(times, d, A, W):
+    t = dev(times, torch.float64)
+    Ad = dev(A, torch.float64)
+    Wd = dev(W, torch.float64)
+    out = torch.empty(t.shape[0], dtype=torch.float64, device=t.device)
+    _lib.call("msp_fast_cos_sum", ptr(t), t.shape[0], int(d), ptr(Ad), ptr(Wd), Ad.shape[0],
+              ptr(out), stream())
+    return out
+
+
+def fast_amplitudes(evals, evecs, sigma, d):
+    ev = dev(evals, torch.float64)
+    U = dev(evecs, torch.complex128)
+    s = dev(sigma, torch.complex128)
+    n = ev.shape[-1]
+    A = torch.empty((n, n), dtype=torch.float64, device=ev.device)
+    W = torch.empty((n, n), dtype=torch.float64, device=ev.device)
+    _lib.call("msp_fast_amplitudes", ptr(ev), ptr(U), ptr(s), n, int(d), ptr(A), ptr(W), stream())
+    return A, W
+
+
+def evolve_expect(evals, rho, ops, times):
+    ev = dev(evals, torch.float64)
+    r = dev(rho, torch.complex128)
+    o = dev(ops, torch.complex128)
+    t = dev(times, torch.float64)
+    n = ev.shape[-1]
+    nops = o.reshape(-1, n, n).shape[0]
+    out = torch.empty((t.shape[0], nops), dtype=torch.complex128, device=ev.device)
+    _lib.call("msp_evolve_expect", ptr(ev), ptr(r), ptr(o), n, nops, ptr(t), t.shape[0],
+              ptr(out), stream())
+    return out
+
+
+def evolve_phases(evals, rho, times):
+    ev = dev(evals, torch.float64)
+    r = dev(rho, torch.complex128)
+    t = dev(times, torch.float64)
+    n = ev.shape[-1]
+    out = torch.empty((t.shape[0], n, n), dtype=torch.complex128, device=ev.device)
+    _lib.call("msp_evolve_phases", ptr(ev), ptr(r), n, ptr(t), t.shape[0], ptr(out), stream())
+    return out
+
+
+def integrate_decaying(evals, rho, ops, tau):
+    ev = dev(evals, torch.float64)
+    r = dev(rho, torch.complex128)
+    o = dev(ops, torch.complex128)
+    n = ev.shape[-1]
+    nops = o.reshape(-1, n, n).shape[0]
+    out = torch.empty((nops,), dtype=torch.complex128, device=ev.device)
+    _lib.call("msp_integrate_decaying", ptr(ev), ptr(r), ptr(o), n, nops, float(tau), ptr(out),
+              stream())
+    return out
+
+
+def uniform_grid(times, rtol=1e-12):
+    """(is_uniform, t0, dt) for a 1-D time array."""
+    t = np.asarray(times, dtype=np.float64)
+    if t.size == 0:
+        return False, 0.0, 0.0
+    if t.size == 1:
+        return True, float(t[0]), 0.0
+    dt = (t[-1] - t[0]) / (t.size - 1)
+    grid = t[0] + dt * np.arange(t.size)
+    scale = max(np.abs(t).max(), 1e-300)
+    ok = bool(np.all(np.abs(grid - t) <= rtol * scale)) and dt != 0.0
+    return ok, float(t[0]), float(dt)
+
+
+class StageTimer:
+    """CUDA-event timer that msp_powder_run fills per stage (snapshots,
+    schedule, phase sum, reduction), recorded on the launch stream."""
+
+    def __init__(self):
+        lib = _lib.load()
+        h = ctypes.c_void_p(0)
+        _lib.check(lib.msp_timer_create(ctypes.byref(h)), "msp_timer_create")
+        self.handle = h
+
+    def read(self):
+        """Summed milliseconds per stage since the last read, and the run count."""
+        ms = (ctypes.c_double * _lib.TIMER_STAGES)()
+        runs = ctypes.c_int(0)
+        _lib.check(_lib.load().msp_timer_read(self.handle, ms, ctypes.byref(runs)), "msp_timer_read")
+        return dict(zip(_lib.TIMER_STAGE_NAMES, list(ms))), runs.value
+
+    def close(self):
+        if self.handle:
+            _lib.load().msp_timer_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PowderPlan:
+    """Device-resident inputs, outputs and scratch of one msp_powder_run
+    batch, reusable for repeated runs (benchmarks, fits).
+
+    field, pol: (S, 3); wscale: (S,); slot: (S,) non-decreasing; times: 1-D.
+    ``out`` has shape (num_slots,) for MODE_INTEGRAL, else
+    (num_slots, len(times)).
+    """
+
+    def __init__(self, n, Hsys, Z, field, pol, wscale, slot, num_slots, times,
+                 mode=_lib.MODE_FAST, precision=_lib.PREC_FP64, dims=None, mu_index=0,
+                 gammas=None, temperature=None, rho_fac=None, tau=1.0, max_sweeps=0):
+        d = device()
+        a = _lib.PowderArgs()
+        a.n = int(n)
+        if dims is not None:
+            a.num_spins = len(dims)
+            for i, x in enumerate(dims):
+                a.dims[i] = int(x)
+        a.mu_index = int(mu_index)
+        if gammas is not None:
+            for i, g in enumerate(gammas):
+                a.gammas[i] = float(g)
+        self.Hs = dev(Hsys, torch.complex128)
+        self.Zd = dev(Z, torch.complex128)
+        self.F = dev(field, torch.float64).reshape(-1, 3)
+        self.Pl = dev(pol, torch.float64).reshape(-1, 3)
+        self.W = dev(wscale, torch.float64).reshape(-1)
+        self.Sl = dev(slot, torch.int32).reshape(-1)
+        S = self.F.shape[0]
+        self.num_snap = S
+        a.Hsys, a.Z = self.Hs.data_ptr(), self.Zd.data_ptr()
+        a.num_snap = S
+        a.field, a.pol = self.F.data_ptr(), self.Pl.data_ptr()
+        a.wscale, a.slot = self.W.data_ptr(), self.Sl.data_ptr()
+        self.R = None
+        if rho_fac is not None:
+            self.R = dev(rho_fac, torch.complex128)
+            a.rho_fac = self.R.data_ptr()
+        self.Tp = None
+        if temperature is not None:
+            tarr = np.broadcast_to(np.asarray(temperature, dtype=np.float64), (S,))
+            self.Tp = dev(np.ascontiguousarray(tarr), torch.float64)
+            a.temperature = self.Tp.data_ptr()
+        a.num_slots = int(num_slots)
+        self.T = None
+        if mode == _lib.MODE_INTEGRAL:
+            a.num_times = 1
+            a.uniform = 1
+            shape = (int(num_slots),)
+        else:
+            th = times.detach().cpu().numpy() if isinstance(times, torch.Tensor) else np.asarray(times)
+            uni, t0, dt = uniform_grid(th)
+            self.T = dev(times, torch.float64).reshape(-1)
+            a.times = self.T.data_ptr()
+            a.num_times = self.T.shape[0]
+            a.uniform = 1 if uni else 0
+            a.t0, a.dt = t0, dt
+            shape = (int(num_slots), self.T.shape[0])
+        a.tau = float(tau)
+        a.mode = int(mode)
+        a.precision = int(precision)
+        a.max_sweeps = int(max_sweeps)
+        self.out = torch.empty(shape, dtype=torch.float64, device=d)
+        self.status = torch.zeros((max(S, 1),), dtype=torch.int32, device=d)
+        a.out = self.out.data_ptr()
+        a.status = self.status.data_ptr()
+        nbytes = ctypes.c_size_t(0)
+        _lib.check(_lib.load().msp_powder_workspace(ctypes.byref(a), ctypes.byref(nbytes)),
+                   "msp_powder_workspace")
+        self.ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device=d)
+        off = (-self.ws.data_ptr()) % 256
+        a.workspace = self.ws.data_ptr() + off
+        a.workspace_bytes = int(nbytes.value)
+        self.workspace_bytes = int(nbytes.value)
+        self.args = a
+
+    def run(self, timer=None):
+        """Enqueue the batch on the current stream; returns the output tensor."""
+        self.args.stream = torch.cuda.current_stream().cuda_stream
+        self.args.timer = timer.handle.value if timer is not None else None
+        _lib.check(_lib.load().msp_powder_run(ctypes.byref(self.args)), "msp_powder_run")
+        return self.out
+
+
+def powder_run(n, Hsys, Z, field, pol, wscale, slot, num_slots, times, mode=_lib.MODE_FAST,
+               precision=_lib.PREC_FP64, dims=None, mu_index=0, gammas=None, temperature=None,
+               rho_fac=None, tau=1.0, max_sweeps=0):
+    """One msp_powder_run on fresh device buffers; returns (out, status)."""
+    plan = PowderPlan(n, Hsys, Z, field, pol, wscale, slot, num_slots, times, mode, precision,
+                      dims, mu_index, gammas, temperature, rho_fac, tau, max_sweeps)
+    out = plan.run()
+    return out, plan.status[:plan.num_snap]

@@ -1,0 +1,384 @@
+"""CPU oracle for the polarisation path -- TEST INFRASTRUCTURE ONLY.
+
+A plain numpy restatement of the reference's algorithm, used by ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg as the checker.
+Nothing in ``muspinsim_gb300`` imports it; the product path runs on the GPU
+and fails loudly without its CUDA library.
+
+Every function cites the reference lines it restates.  The oracle is pinned
+against golden vectors produced by running the reference itself
+(``tests/golden/make_golden.py``) and against the analytic known-answer tests
+of the reference suite (``muspinsim/tests/test_hamiltonian.py``,
+``test_experiment.py``, ``test_spinsys.py``).  Matrices are dense complex128;
+the reference keeps them in scipy CSR, which changes storage, not values.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+import scipy.constants as cnst
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+ELEC_GAMMA = -28024.9514242  # muspinsim/constants.py:12
+MU_GAMMA = -(ELEC_GAMMA / 206.7669883)  # muspinsim/constants.py:13
+MU_TAU = 2.19703  # muspinsim/constants.py:14
+EFG_2_MHZ = (  # muspinsim/constants.py:20-25
+    cnst.physical_constants["atomic unit of electric field gradient"][0] * cnst.e * 1e-37 / cnst.h
+)
+
+
+# ---------------------------------------------------------------- spin matrices
+def mvals(I):
+    """m = +I ... -I (muspinsim/spinop.py:14-15)."""
+    return np.linspace(I, -I, int(2 * I + 1))
+
+
+def spin_matrix(I, axis):
+    """Single-spin operator for axis in 'xyz+-0' (muspinsim/spinop.py:18-41)."""
+    m = mvals(I)
+    sp = 2 * np.diag(0.5 * (np.cumsum(2 * m)[:-1] ** 0.5), k=1) + 0.0j
+    if axis == "+":
+        return sp
+    if axis == "-":
+        return sp.T
+    if axis == "x":
+        return 0.5 * (sp + sp.T)
+    if axis == "y":
+        return 0.5j * (sp.T - sp)
+    if axis == "z":
+        return np.diag(m) + 0.0j
+    if axis == "0":
+        return np.eye(len(m)) + 0.0j
+    raise ValueError(axis)
+
+
+def embed(Is, ops):
+    """Kronecker embedding of per-spin operators, identity elsewhere; spin 0
+    is the slowest index (muspinsim/spinsys.py:545-592).  ``ops`` maps a spin
+    index to an axis letter or a list of letters (multiplied in order)."""
+    M = None
+    for i, I in enumerate(Is):
+        o = ops.get(i, "0")
+        if isinstance(o, (list, tuple)):
+            m = spin_matrix(I, o[0])
+            for a in o[1:]:
+                m = m @ spin_matrix(I, a)
+        else:
+            m = spin_matrix(I, o)
+        M = m if M is None else np.kron(M, m)
+    return M
+
+
+# ---------------------------------------------------------------- spin systems
+class System:
+    """Spins plus interaction terms (muspinsim/spinsys.py:161-216, 640-705).
+
+    ``terms`` holds ``(indices, tensor)`` with tensors already in MHz, as the
+    reference's ``InteractionTerm`` stores them."""
+
+    def __init__(self, spins, gammas, Is, Qs):
+        self.spins = list(spins)
+        self.gammas = np.array(gammas, dtype=float)
+        self.Is = np.array(Is, dtype=float)
+        self.Qs = np.array(Qs, dtype=float)
+        self.dims = tuple(int(2 * I + 1) for I in self.Is)
+        self.terms = []
+        self.mu_i = self.spins.index("mu") if "mu" in self.spins else None
+
+    @property
+    def n(self):
+        return int(np.prod(self.dims))
+
+    def add_term(self, indices, tensor):
+        self.terms.append((tuple(indices), np.array(tensor, dtype=float)))
+
+    def add_zeeman(self, i, B):
+        """(muspinsim/spinsys.py:354-375)"""
+        if np.isscalar(B):
+            B = [0, 0, B]
+        self.add_term([i], np.array(B, dtype=float) * self.gammas[i])
+
+    def add_hyperfine(self, i, A, j):
+        """(muspinsim/spinsys.py:664-705); j is the electron index."""
+        self.add_term([i, j], A)
+
+    def add_dipolar(self, i, j, r):
+        """(muspinsim/spinsys.py:377-413), r in Angstrom."""
+        r = np.array(r, dtype=float)
+        rnorm = np.linalg.norm(r)
+        D = -(np.eye(3) - 3.0 / rnorm**2.0 * r[:, None] * r[None, :])
+        dij = -(cnst.mu_0 * cnst.hbar * (self.gammas[i] * self.gammas[j] * 1e6)) / (
+            2 * (rnorm * 1e-10) ** 3
+        )
+        self.add_term([i, j], D * dij)
+
+    def add_quadrupolar(self, i, EFG):
+        """(muspinsim/spinsys.py:415-442)"""
+        I = self.Is[i]
+        Qtens = EFG_2_MHZ * self.Qs[i] / (2 * I * (2 * I - 1)) * np.array(EFG, dtype=float)
+        self.add_term([i, i], Qtens)
+
+    def term_matrix(self, indices, tensor):
+        """sum over tensor index tuples of T_ab S^a_i S^b_j; a same-spin pair
+        uses the matrix product S^a_i S^b_i (muspinsim/spinsys.py:34-69)."""
+        n = self.n
+        total = np.zeros((n, n), dtype=complex)
+        if len(indices) == 0:
+            return total + tensor * np.eye(n)
+        for ii in np.ndindex(*tensor.shape):
+            if len(indices) == 2 and indices[0] == indices[1]:
+                ops = {indices[0]: ["xyz"[ii[0]], "xyz"[ii[1]]]}
+            else:
+                ops = {ind: "xyz"[ii[k]] for k, ind in enumerate(indices)}
+            total += embed(self.Is, ops) * tensor[ii]
+        return total
+
+    def hamiltonian(self):
+        """Hsys = sum of the term matrices (muspinsim/spinsys.py:613-626)."""
+        H = np.zeros((self.n, self.n), dtype=complex)
+        for ind, T in self.terms:
+            H += self.term_matrix(ind, T)
+        return H
+
+    def zeeman_operators(self):
+        """Z_a = sum_i gamma_i S^a_i, so that Hz(B) = sum_a B_a Z_a
+        (muspinsim/experiment.py:105-111, 239-250)."""
+        Z = np.zeros((3, self.n, self.n), dtype=complex)
+        for i, g in enumerate(self.gammas):
+            for a, ax in enumerate("xyz"):
+                Z[a] += g * embed(self.Is, {i: ax})
+        return Z
+
+    def muon_operator(self, v):
+        """O = sum_a v_a S^a_mu (muspinsim/spinsys.py:707-732)."""
+        return sum(v[a] * embed(self.Is, {self.mu_i: ax}) for a, ax in enumerate("xyz"))
+
+
+def sigma_mu(v):
+    """sum_a v_a sigma_a, 2x2 Pauli combination (muspinsim/spinsys.py:734-760)."""
+    sx = np.array([[0, 1], [1, 0]], dtype=complex)
+    sy = np.array([[0, -1j], [1j, 0]], dtype=complex)
+    sz = np.array([[1, 0], [0, -1]], dtype=complex)
+    return v[0] * sx + v[1] * sy + v[2] * sz
+
+
+# ---------------------------------------------------------------- orientations
+def quat_mul(a, b):
+    w1, x1, y1, z1 = a
+    w2, x2, y2, z2 = b
+    return np.array(
+        [
+            w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2,
+            w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2,
+            w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2,
+            w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2,
+        ]
+    )
+
+
+def quat_axis(axis, angle):
+    axis = np.asarray(axis, dtype=float)
+    return np.concatenate([[np.cos(angle / 2)], np.sin(angle / 2) * axis])
+
+
+def orientation_quat(row, mode="zyz"):
+    """Stored (conjugated) orientation quaternion and weight for an input row:
+    (theta, phi) polar, (a, b, c) or (a, b, c, w) Euler
+    (muspinsim/simconfig.py:596-613; muspinsim/utils.py:53-68; Euler
+    composition q_c q_b q_a pinned by muspinsim/tests/test_config.py:233-285)."""
+    row = list(row)
+    w = 1.0
+    if len(row) == 2:
+        theta, phi = row
+        a, b, c, mode = phi, theta, phi, "zyz"
+    else:
+        a, b, c = row[:3]
+        if len(row) == 4:
+            w = row[3]
+    bax = [0, 1, 0] if mode == "zyz" else [1, 0, 0]
+    q = quat_mul(quat_mul(quat_axis([0, 0, 1], c), quat_axis(bax, b)), quat_axis([0, 0, 1], a))
+    return q * np.array([1.0, -1, -1, -1]), w
+
+
+def quat_rotate(q, v):
+    """q v q* (muspinsim/experiment.py:405-406)."""
+    qv = np.concatenate([[0.0], np.asarray(v, dtype=float)])
+    return quat_mul(quat_mul(q, qv), q * np.array([1.0, -1, -1, -1]))[1:]
+
+
+# ---------------------------------------------------------------- states
+def density_from_vector(I, vec):
+    """Pure state along vec (muspinsim/spinop.py:455-530, gamma = 0)."""
+    S = [spin_matrix(I, a) for a in "xyz"]
+    o = sum(S[i] * vec[i] for i in range(3))
+    evals, evecs = np.linalg.eigh(o)
+    psi = evecs[:, np.argmax(evals)]
+    m = psi[:, None] * psi[None, :].conj()
+    return m / np.trace(m)
+
+
+def rho0(system, B, p, T):
+    """Initial state: muon along p, other spins thermal in their own Zeeman
+    field, uniform at T = inf (muspinsim/experiment.py:170-236)."""
+    rhos = []
+    for i, I in enumerate(system.Is):
+        if i == system.mu_i:
+            r = density_from_vector(I, p)
+        else:
+            Hz = sum(B[j] * spin_matrix(I, e) for j, e in enumerate("xyz"))
+            evals, evecs = np.linalg.eigh(Hz)
+            E = evals * 1e6 * system.gammas[i]
+            if T > 0:
+                Z = np.exp(-cnst.h * E / (cnst.k * T))
+            else:
+                Z = np.where(E == np.amin(E), 1.0, 0.0)
+            if np.sum(Z) > 0:
+                Z /= np.sum(Z)
+            else:
+                Z = np.ones(len(E)) / len(E)
+            r = np.sum(evecs[:, None, :] * evecs[None, :, :].conj() * Z[None, None, :], axis=-1)
+            r = r / np.trace(r)
+        rhos.append(r)
+    M = rhos[0]
+    for r in rhos[1:]:
+        M = np.kron(M, r)
+    return M
+
+
+# ---------------------------------------------------------------- propagation
+def evolve(H, rho, times, operators):
+    """<O>(t) = sum_ij rho'_ij O'_ji exp(-2 pi i (l_i - l_j) t) in the
+    eigenbasis; complex [T, n_ops] (muspinsim/hamiltonian.py:40-117)."""
+    evals, evecs = np.linalg.eigh(H)
+    U = evecs
+    rp = U.conj().T @ rho @ U
+    ll = -2.0j * np.pi * (evals[:, None] - evals[None, :])
+    times = np.asarray(times, dtype=float)
+    out = np.empty((len(times), len(operators)), dtype=complex)
+    for k, O in enumerate(operators):
+        Op = U.conj().T @ O @ U
+        c = (rp * Op.T).reshape(-1)
+        ph = np.exp(ll.reshape(-1)[None, :] * times[:, None])
+        out[:, k] = ph @ c
+    return out
+
+
+def integrate_decaying(H, rho, tau, operators):
+    """int_0^inf <O>(t) exp(-t/tau) dt = sum_ij rho'_ij [-O'/(2 pi i (l_i -
+    l_j) - 1/tau)]^T_ij (muspinsim/hamiltonian.py:119-164)."""
+    evals, evecs = np.linalg.eigh(H)
+    U = evecs
+    rp = U.conj().T @ rho @ U
+    ll = 2.0j * np.pi * (evals[:, None] - evals[None, :])
+    res = []
+    for O in operators:
+        Op = U.conj().T @ O @ U
+        intop = (-Op / (ll - 1.0 / tau)).T
+        res.append(np.sum(rp * intop))
+    return np.array(res)
+
+
+_LIB = None
+
+
+def _oracle_lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "_build", "liboracle.so")
+        if not os.path.exists(path):
+            import importlib.util
+
+            spec = importlib.util.spec_from_file_location("oracle_build", os.path.join(HERE, "build.py"))
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            path = mod.build_port()
+        lib = ctypes.CDLL(path)
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib.oracle_fast_cos_sum.argtypes = [dp, ctypes.c_long, ctypes.c_long, dp, dp,
+                                            ctypes.c_long, dp, ctypes.c_int]
+        lib.oracle_fast_cos_powder.argtypes = [dp, ctypes.c_long, ctypes.c_long, dp, dp,
+                                               ctypes.c_long, ctypes.c_long, dp, dp, ctypes.c_int]
+        _LIB = lib
+    return _LIB
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def fast_cos_sum(times, d, A, W, nthreads=0):
+    """The reference's cosine phase sum (muspinsim/cython/parallel.pyx:16-69),
+    through the C restatement in oracle/fast_cos_sum.c."""
+    times = np.ascontiguousarray(times, dtype=np.float64)
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    out = np.zeros(len(times))
+    _oracle_lib().oracle_fast_cos_sum(_dp(times), len(times), int(d), _dp(A), _dp(W),
+                                      A.shape[0], _dp(out), int(nthreads))
+    return out
+
+
+def fast_amplitudes(H, sig, d):
+    """A = |U^dag (sigma (x) 1_d) U|^2 and W = 2 pi (l_j - l_k)
+    (muspinsim/hamiltonian.py:196-211)."""
+    evals, U = np.linalg.eigh(H)
+    S = np.kron(sig, np.eye(d))
+    A = np.abs(U.conj().T @ S @ U) ** 2
+    W = 2 * np.pi * np.subtract.outer(evals, evals)
+    return A, W, evals
+
+
+def fast_evolve(H, sig, times, d, nthreads=0):
+    """Muon-first, T = inf shortcut, x 0.5 (muspinsim/hamiltonian.py:166-217)."""
+    A, W, _ = fast_amplitudes(H, sig, d)
+    return fast_cos_sum(times, d, A, W, nthreads) * 0.5
+
+
+# ---------------------------------------------------------------- driver
+def t_inf_speedup(B, T, mu_i):
+    """Fast-path selection rule (muspinsim/experiment.py:413-430)."""
+    Bn = np.linalg.norm(B)
+    check = (cnst.e * (cnst.hbar**2) * Bn) / (2 * cnst.m_p * cnst.k * T)
+    return bool(check == 0) and mu_i == 0
+
+
+def snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y="asymmetry", nthreads=0):
+    """One configuration: rotate B and p by q, add the intrinsic field, pick
+    the path, return real(data) * w (muspinsim/experiment.py:384-498)."""
+    Bl = quat_rotate(q, B) + np.asarray(intrinsic_B, dtype=float)
+    pl = quat_rotate(q, p)
+    H = Hsys + np.einsum("a,aij->ij", Bl, Z)
+    if y == "integral":
+        rho = rho0(system, Bl, pl, T)
+        O = system.muon_operator(pl)
+        data = integrate_decaying(H, rho, MU_TAU, [O])[0] / MU_TAU
+    elif t_inf_speedup(Bl, T, system.mu_i):
+        d = system.n // system.dims[system.mu_i]
+        data = fast_evolve(H, sigma_mu(pl), times, d, nthreads)
+    else:
+        rho = rho0(system, Bl, pl, T)
+        O = system.muon_operator(pl)
+        data = evolve(H, rho, times, [O])[:, 0]
+    return np.real(data) * w
+
+
+def powder_average(system, orientations, B, p, T, times, intrinsic_B=(0, 0, 0),
+                   y="asymmetry", nthreads=0):
+    """Orientation average: weights normalised to sum to N, result = sum_k
+    w_k P_k / N (muspinsim/simconfig.py:152-159, 347-368)."""
+    Hsys = system.hamiltonian()
+    Z = system.zeeman_operators()
+    qs = [orientation_quat(o) for o in orientations]
+    N = len(qs)
+    if N > 1:
+        norm = N / np.sum([w for _, w in qs])
+        qs = [(q, w * norm) for q, w in qs]
+    else:
+        qs = [(q, 1.0) for q, _ in qs]
+    acc = None
+    for q, w in qs:
+        r = snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y, nthreads)
+        acc = r / N if acc is None else acc + r / N
+    return acc

@@ -1,0 +1,53 @@
+"""Shared test helpers: oracle systems built from the same inputs the GPU
+library receives, and random Hermitian matrices."""
+
+import numpy as np
+
+from muspinsim_gb300 import constants as C
+from oracle import port
+
+
+def oracle_system(spins, couplings):
+    """oracle.port.System for a spin list and input-file style couplings."""
+    gam, Is, Qs = [], [], []
+    for s in spins:
+        el, iso = s if isinstance(s, tuple) else (s, None)
+        gam.append(C.gyromagnetic_ratio(el, iso))
+        Is.append(C.spin(el, iso))
+        Qs.append(C.quadrupole_moment(el, iso))
+    sy = port.System(spins, gam, Is, Qs)
+    for kind, args, val in couplings:
+        i = args["i"] - 1
+        j = args.get("j")
+        j = None if j is None else j - 1
+        if kind == "hyperfine":
+            if j is None:
+                j = spins.index("e")
+            sy.add_hyperfine(i, val, j)
+        elif kind == "dipolar":
+            sy.add_dipolar(i, j, val)
+        elif kind == "quadrupolar":
+            sy.add_quadrupolar(i, val)
+        elif kind == "zeeman":
+            sy.add_zeeman(i, val)
+        else:
+            raise ValueError(kind)
+    return sy
+
+
+def oracle_powder(wl, orientations=None, times=None, field=None, temperature=None,
+                  y_axis=None):
+    """Oracle powder average of a muspinsim_gb300.workloads.Workload."""
+    sy = oracle_system(wl.spins, wl.couplings)
+    o = wl.orientations if orientations is None else orientations
+    t = wl.times if times is None else times
+    B = wl.fields[0] if field is None else field
+    T = wl.temperature if temperature is None else temperature
+    y = wl.y_axis if y_axis is None else y_axis
+    p = wl.polarization / np.linalg.norm(wl.polarization)
+    return port.powder_average(sy, o, np.asarray(B, float), p, T, t, y=y)
+
+
+def random_hermitian(rng, n, scale=100.0):
+    A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    return scale * (A + A.conj().T) / 2.0

@@ -1,0 +1,195 @@
+"""GPU parity of the CUDA kernels against the CPU oracle (oracle/port.py).
+
+Tolerances: FP64 path max|dP| <= 1e-10 and eigenvalues <= 1e-12 relative
+to max|lambda|; mixed path max|dP| <= 1e-6 on powder averages.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import port
+from tests.helpers import oracle_powder, oracle_system, random_hermitian
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+MIXED_TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def K():
+    from muspinsim_gb300 import kernels
+
+    kernels.device()
+    return kernels
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 8, 12, 16, 24, 31, 32, 48, 64])
+def test_eigh_fp64_random(K, n):
+    rng = np.random.default_rng(100 + n)
+    H = np.stack([random_hermitian(rng, n) for _ in range(6)])
+    ev, U, st = K.eigh(H)
+    ev, U, st = ev.cpu().numpy(), U.cpu().numpy(), st.cpu().numpy()
+    assert np.all(st == 0)
+    for b in range(H.shape[0]):
+        ref = np.linalg.eigvalsh(H[b])
+        scale = np.abs(ref).max()
+        assert np.abs(ev[b] - ref).max() <= 1e-12 * scale
+        assert np.all(np.diff(ev[b]) >= 0)
+        rec = (U[b] * ev[b][None, :]) @ U[b].conj().T
+        assert np.abs(rec - H[b]).max() <= 1e-12 * scale
+        assert np.abs(U[b].conj().T @ U[b] - np.eye(n)).max() <= 1e-12
+
+
+@pytest.mark.parametrize("n", [4, 8, 24, 32, 64])
+def test_eigh_mixed_random(K, n):
+    from muspinsim_gb300 import _lib
+
+    rng = np.random.default_rng(200 + n)
+    H = np.stack([random_hermitian(rng, n) for _ in range(6)])
+    ev, U, st = K.eigh(H, precision=_lib.PREC_MIXED)
+    ev, U, st = ev.cpu().numpy(), U.cpu().numpy(), st.cpu().numpy()
+    assert np.all(st == 0)
+    for b in range(H.shape[0]):
+        ref = np.linalg.eigvalsh(H[b])
+        scale = np.abs(ref).max()
+        # refined eigenvalues: FP64-level; eigenvectors stored in FP32
+        assert np.abs(ev[b] - ref).max() <= 1e-11 * scale
+        assert np.abs(U[b].conj().T @ U[b] - np.eye(n)).max() <= 2e-6
+
+
+def test_eigh_degenerate_and_trivial(K):
+    rng = np.random.default_rng(7)
+    n = 24
+    Qm, _ = np.linalg.qr(rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))
+    lam = np.repeat([-3.0, 0.5, 0.5 + 1e-9, 2.0], 6)
+    H = np.stack([(Qm * lam) @ Qm.conj().T, np.zeros((n, n)), np.eye(n) * 5.0,
+                  np.diag(np.arange(n, dtype=float))])
+    ev, U, st = K.eigh(H)
+    ev, U = ev.cpu().numpy(), U.cpu().numpy()
+    assert np.all(st.cpu().numpy() == 0)
+    for b in range(H.shape[0]):
+        ref = np.linalg.eigvalsh(H[b])
+        assert np.abs(ev[b] - ref).max() <= 1e-12 * max(np.abs(ref).max(), 1.0)
+        rec = (U[b] * ev[b][None, :]) @ U[b].conj().T
+        assert np.abs(rec - H[b]).max() <= 1e-12 * max(np.abs(ref).max(), 1.0)
+
+
+def test_fast_cos_sum_matches_oracle(K):
+    rng = np.random.default_rng(3)
+    n = 24
+    H = random_hermitian(rng, n)
+    A, W, _ = port.fast_amplitudes(H, port.sigma_mu([0, 0, 1.0]), n // 2)
+    t = np.linspace(0, 20, 777)
+    ref = port.fast_cos_sum(t, n // 2, A, W)
+    got = K.fast_cos_sum(t, n // 2, A, W).cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-13
+
+
+def _workload2(n_orient=24, n_times=640):
+    from muspinsim_gb300 import workloads
+
+    return workloads.config2(n_orient=n_orient, n_times=n_times)
+
+
+def _gpu_powder(wl, precision="fp64", **kw):
+    from muspinsim_gb300.powder import powder_average
+
+    sy = wl.system()
+    args = dict(orientations=wl.orientations, field=wl.fields[0], polarization=wl.polarization,
+                times=wl.times, temperature=wl.temperature, y_axis=wl.y_axis)
+    args.update(kw)
+    return powder_average(sy, precision=precision, **args)
+
+
+def test_powder_fast_fp64_vs_oracle():
+    wl = _workload2()
+    ref = oracle_powder(wl)
+    got = _gpu_powder(wl)
+    assert np.abs(got - ref).max() <= FP64_TOL
+
+
+def test_powder_fast_mixed_vs_oracle():
+    wl = _workload2()
+    ref = oracle_powder(wl)
+    got = _gpu_powder(wl, "mixed")
+    assert np.abs(got - ref).max() <= MIXED_TOL
+
+
+def test_powder_fast_nonuniform_times():
+    wl = _workload2(n_orient=8, n_times=300)
+    rng = np.random.default_rng(11)
+    t = np.sort(rng.uniform(0, 20, 300))
+    ref = oracle_powder(wl, times=t)
+    got = _gpu_powder(wl, times=t)
+    assert np.abs(got - ref).max() <= FP64_TOL
+    got_m = _gpu_powder(wl, "mixed", times=t)
+    assert np.abs(got_m - ref).max() <= MIXED_TOL
+
+
+def test_powder_multi_tile_times():
+    # more than one 4096-sample tile, with a ragged last tile
+    wl = _workload2(n_orient=4, n_times=9000)
+    ref = oracle_powder(wl)
+    got = _gpu_powder(wl)
+    assert np.abs(got - ref).max() <= FP64_TOL
+
+
+def test_powder_evolve_finite_temperature():
+    wl = _workload2(n_orient=10, n_times=400)
+    ref = oracle_powder(wl, temperature=5.0)
+    got = _gpu_powder(wl, temperature=5.0)
+    assert np.abs(got - ref).max() <= FP64_TOL
+    got_m = _gpu_powder(wl, "mixed", temperature=5.0)
+    assert np.abs(got_m - ref).max() <= MIXED_TOL
+
+
+def test_powder_evolve_muon_not_first():
+    from muspinsim_gb300.spinsys import MuonSpinSystem
+    from muspinsim_gb300.powder import powder_average
+
+    rng = np.random.default_rng(21)
+    spins = ["e", "mu", "H"]
+    A1 = rng.normal(0, 50, (3, 3))
+    A1 = A1 + A1.T
+    A2 = rng.normal(0, 5, (3, 3))
+    A2 = A2 + A2.T
+    coup = [("hyperfine", {"i": 2, "j": 1}, A1), ("hyperfine", {"i": 3, "j": 1}, A2)]
+    sy = MuonSpinSystem(spins)
+    sy.add_hyperfine_term(1, A1, 0)
+    sy.add_hyperfine_term(2, A2, 0)
+    orients = [(0.1, 0.2, 0.3), (1.0, 2.0, 0.5, 2.0), (0.7, 1.1)]
+    t = np.linspace(0, 5, 333)
+    B = np.array([0.0, 0.01, 0.02])
+    p = np.array([1.0, 0.0, 0.0])
+    ref = port.powder_average(oracle_system(spins, coup), orients, B, p, np.inf, t)
+    got = powder_average(sy, orients, B, p, t)
+    assert np.abs(got - ref).max() <= FP64_TOL
+
+
+def test_powder_integral_vs_oracle():
+    from muspinsim_gb300 import workloads
+
+    wl = workloads.config3(n_fields=4, n_orient=6)
+    e64, emx = [], []
+    for B in wl.fields:
+        ref = oracle_powder(wl, field=B)
+        e64.append(abs(_gpu_powder(wl, field=B) - ref))
+        emx.append(abs(_gpu_powder(wl, "mixed", field=B) - ref))
+    print("integral |dP| fp64:", e64, "mixed:", emx)
+    assert max(e64) <= FP64_TOL
+    assert max(emx) <= MIXED_TOL
+
+
+def test_mixed_single_orientations():
+    """Mixed precision per crystallite (no powder averaging to hide errors)."""
+    from muspinsim_gb300 import workloads
+
+    wl = workloads.config2(n_orient=12, n_times=1024)
+    errs = []
+    for o in wl.orientations:
+        ref = oracle_powder(wl, orientations=[o])
+        got = _gpu_powder(wl, "mixed", orientations=[o])
+        errs.append(np.abs(got - ref).max())
+    print("mixed per-orientation max|dP|:", max(errs))
+    assert max(errs) <= 5e-7
