@@ -63,6 +63,18 @@ __device__ __forceinline__ double reduce_2pi(double x) {
     return fma(-k, twopi_lo, r);
 }
 
+// x / d by multiply and shift with c = ceil(2^20 / d): exact whenever
+// 0 <= x < 2^20 / d (x * c then fits 32 bits and the rounding excess stays
+// below 1/d), which covers every index of an m x m matrix with m <= 64.
+struct FastDiv {
+    unsigned int c;
+    __device__ __forceinline__ explicit FastDiv(int d)
+        : c(((1u << 20) + (unsigned)d - 1u) / (unsigned)d) {}
+    __device__ __forceinline__ int div(int x) const {
+        return (int)(((unsigned)x * c) >> 20);
+    }
+};
+
 // Double-word ("df32") accumulation on the FP32 pipe: (hi, lo) += a * b with
 // the product split exactly (TwoProduct via FMA) and the running sum kept by
 // TwoSum (Knuth), the low words summed plainly.  About 2^-44 relative

@@ -34,6 +34,7 @@ struct JacobiWork {
     int *pp;    // m/2 pair first index
     int *pq;    // m/2 pair second index
     T *red;     // 2 * warps scratch
+    unsigned *tab;  // (m/2)(m/2+1)/2 block tasks: k1 | k2 << 16, k1 <= k2
 };
 
 template <typename T>
@@ -64,10 +65,19 @@ __device__ int jacobi_sweeps(const JacobiWork<T> &w, int m, int max_sweeps) {
     const int ntask = nblk + half * m;
     const T tol = JacobiConst<T>::tol;
     const int ld = m + 1;  // padded row stride of H and U
+    const FastDiv fdm(m);
 
     for (int e = tid; e < m * m; e += nt) {
-        const int i = e / m, j = e - (e / m) * m;
+        const int i = fdm.div(e), j = e - i * m;
         w.U[i * ld + j] = mk<T>(i == j ? T(1) : T(0), T(0));
+    }
+    // block task table, decoded once instead of at every step
+    for (int task = tid; task < nblk; task += nt) {
+        int k2 = (int)((sqrtf(8.0f * (float)task + 1.0f) - 1.0f) * 0.5f);
+        while ((k2 + 1) * (k2 + 2) / 2 <= task) ++k2;
+        while (k2 * (k2 + 1) / 2 > task) --k2;
+        const int k1 = task - k2 * (k2 + 1) / 2;
+        w.tab[task] = (unsigned)k1 | ((unsigned)k2 << 16);
     }
 
     int status = MSP_ITEM_NOT_CONVERGED;
@@ -75,7 +85,7 @@ __device__ int jacobi_sweeps(const JacobiWork<T> &w, int m, int max_sweeps) {
     for (int sweep = 0;; ++sweep) {
         T off = 0, fro = 0;
         for (int e = tid; e < m * m; e += nt) {
-            const int i = e / m, j = e - (e / m) * m;
+            const int i = fdm.div(e), j = e - i * m;
             const T v = cabs2(w.H[i * ld + j]);
             fro += v;
             if (i != j) off += v;
@@ -138,10 +148,8 @@ __device__ int jacobi_sweeps(const JacobiWork<T> &w, int m, int max_sweeps) {
             // phase 2: H <- G^dag H G (2x2 blocks), U <- U G
             for (int task = tid; task < ntask; task += nt) {
                 if (task < nblk) {
-                    int k2 = (int)((sqrtf(8.0f * (float)task + 1.0f) - 1.0f) * 0.5f);
-                    while ((k2 + 1) * (k2 + 2) / 2 <= task) ++k2;
-                    while (k2 * (k2 + 1) / 2 > task) --k2;
-                    const int k1 = task - k2 * (k2 + 1) / 2;
+                    const unsigned kk = w.tab[task];
+                    const int k1 = (int)(kk & 0xffffu), k2 = (int)(kk >> 16);
                     const int p = w.pp[k1], q = w.pq[k1];
                     if (k1 == k2) {
                         w.H[p * ld + p] = mk<T>(w.da[k1], T(0));
@@ -175,7 +183,7 @@ __device__ int jacobi_sweeps(const JacobiWork<T> &w, int m, int max_sweeps) {
                     }
                 } else {
                     const int t2 = task - nblk;
-                    const int k = t2 / m, row = t2 - (t2 / m) * m;
+                    const int k = fdm.div(t2), row = t2 - k * m;
                     const int p = w.pp[k], q = w.pq[k];
                     const T c = w.cs[k];
                     const cx<T> s = w.sn[k];

@@ -70,7 +70,11 @@ __global__ void __launch_bounds__(128) msp_phase_uniform_kernel(PhaseArgs a) {
     typedef cx<T> C;
     __shared__ __align__(16) C Xs[PS][K];
     __shared__ __align__(16) C Ys[PS][K];
-    __shared__ __align__(16) C pw[4][8][PS];  // pair index last: conflict-free stores
+    // power tables, pair index last with a padded stride: the chain writes
+    // (consecutive pairs) and the table-fill reads (8 powers of one pair)
+    // both hit distinct banks
+    __shared__ __align__(16) C pw[4][8][PS + 1];
+    __shared__ __align__(16) C pc[PS];  // (a_c - i a_s) e^{i w t_tile}
     __shared__ int s_range[2];
 
     const int tid = threadIdx.x;
@@ -94,43 +98,40 @@ __global__ void __launch_bounds__(128) msp_phase_uniform_kernel(PhaseArgs a) {
 
     for (int pb = pbeg; pb < pend; pb += PS) {
         const int np = (pend - pb) < PS ? (pend - pb) : PS;
-        if (tid < np) {
-            const int i = tid;
-            const coef_t cf = coef[pb + i];
-            const double w = a.pair_omega[pb + i];
-            const double psi = reduce_2pi(w * dt);
-            const double psi8 = reduce_2pi(8.0 * psi);
-            const double psi64 = reduce_2pi(8.0 * psi8);
-            const double psi512 = reduce_2pi(8.0 * psi64);
-            const double ph0 = reduce_2pi(w * tb);
-            C e1, e8, e64, e512, e0;
-            sincos_t(psi, &e1.im, &e1.re);
-            sincos_t(psi8, &e8.im, &e8.re);
-            sincos_t(psi64, &e64.im, &e64.re);
-            sincos_t(psi512, &e512.im, &e512.re);
-            sincos_t(ph0, &e0.im, &e0.re);
-            const C cc = cmul(mk<T>((T)cf.x, (T)(-cf.y)), e0);
-            C p0 = mk<T>(T(1), T(0)), p1 = p0, p2 = p0, p3 = cc;
+        // setup, spread over the CTA: thread (chain c, pair i) reduces the
+        // phase 8^c w dt exactly in FP64 and builds that chain's 8 powers;
+        // chain 0 also forms the tile-start coefficient
+        for (int e = tid; e < 4 * PS; e += 128) {
+            const int c = e / PS, i = e - (e / PS) * PS;
+            if (i < np) {
+                const double w = a.pair_omega[pb + i];
+                double ph = reduce_2pi(w * dt);
+                for (int q = 0; q < c; ++q) ph = reduce_2pi(8.0 * ph);
+                C base;
+                sincos_t(ph, &base.im, &base.re);
+                C p = mk<T>(T(1), T(0));
 #pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                pw[0][r][i] = p0;
-                pw[1][r][i] = p1;
-                pw[2][r][i] = p2;
-                pw[3][r][i] = p3;
-                p0 = cmul(p0, e1);
-                p1 = cmul(p1, e8);
-                p2 = cmul(p2, e64);
-                p3 = cmul(p3, e512);
+                for (int r = 0; r < 8; ++r) {
+                    pw[c][r][i] = p;
+                    p = cmul(p, base);
+                }
+                if (c == 0) {
+                    const coef_t cf = coef[pb + i];
+                    C e0;
+                    sincos_t(reduce_2pi(w * tb), &e0.im, &e0.re);
+                    pc[i] = cmul(mk<T>((T)cf.x, (T)(-cf.y)), e0);
+                }
             }
         }
         __syncthreads();
+        // Y[k0] = e^{i w dt k0}, X[k1] = coef e^{i w (t_tile + 64 dt k1)}
         for (int e = tid; e < np * 2 * K; e += 128) {
             const int i = e / (2 * K), k = e - (e / (2 * K)) * (2 * K);
             if (k < K) {
                 Ys[i][k] = cmul(pw[1][k >> 3][i], pw[0][k & 7][i]);
             } else {
                 const int kk = k - K;
-                Xs[i][kk] = cmul(pw[3][kk >> 3][i], pw[2][kk & 7][i]);
+                Xs[i][kk] = cmul(pc[i], cmul(pw[3][kk >> 3][i], pw[2][kk & 7][i]));
             }
         }
         __syncthreads();

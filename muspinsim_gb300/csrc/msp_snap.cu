@@ -24,9 +24,9 @@ namespace msp {
 // ------------------------------------------------------------------ smem layout
 
 struct SnapLayout {
-    size_t H, U, sn, cs, da, db, red, pp, pq;  // Jacobi work
+    size_t H, U, sn, cs, da, db, red, pp, pq, tab;  // Jacobi work
     size_t lam, acc, rank;                     // eigenvalues, reductions, sort
-    size_t Hh, Hl, Yl, SR, sd, corr, rd;       // refinement (MIXED)
+    size_t Hh, Hl, Yl, SR, sd, corr, rd, lamf;  // refinement (MIXED)
     size_t fac, B2;                            // general path
     size_t total;
 };
@@ -55,18 +55,20 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
     L.red = lay_take(off, 2 * (size_t)nwarps * esize);
     L.pp = lay_take(off, (m / 2) * 4);
     L.pq = lay_take(off, (m / 2) * 4);
+    L.tab = lay_take(off, (m / 2) * (m / 2 + 1) / 2 * 4);
     L.lam = lay_take(off, m * 8);
     L.acc = lay_take(off, 2 * m * 8);
     L.rank = lay_take(off, m * 4);
-    L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = 0;
+    L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = L.lamf = 0;
     if (refine) {
         L.Hh = lay_take(off, mm * 8);
         L.Hl = lay_take(off, mm * 8);
         L.Yl = lay_take(off, mm * 8);
         L.SR = lay_take(off, mm * 8);
         L.sd = lay_take(off, m * 8);
-        L.corr = lay_take(off, m * 8);
+        L.corr = lay_take(off, m * 4);
         L.rd = lay_take(off, m * 4);
+        L.lamf = lay_take(off, m * 4);
     }
     L.fac = L.B2 = 0;
     if (rho) {
@@ -99,8 +101,8 @@ struct SnapSmem {
     double *lam, *acc;
     int *rank;
     cx<float> *Hh, *Hl, *Yl, *SR;
-    double *sd, *corr;
-    float *rd;
+    double *sd;
+    float *corr, *rd, *lamf;
     cx<double> *fac;
     cx<T> *B2;
 };
@@ -119,6 +121,7 @@ __device__ __forceinline__ SnapSmem<T> snap_carve(char *base, int n, bool rho, i
     s.w.red = reinterpret_cast<T *>(base + L.red);
     s.w.pp = reinterpret_cast<int *>(base + L.pp);
     s.w.pq = reinterpret_cast<int *>(base + L.pq);
+    s.w.tab = reinterpret_cast<unsigned *>(base + L.tab);
     s.lam = reinterpret_cast<double *>(base + L.lam);
     s.acc = reinterpret_cast<double *>(base + L.acc);
     s.rank = reinterpret_cast<int *>(base + L.rank);
@@ -127,8 +130,9 @@ __device__ __forceinline__ SnapSmem<T> snap_carve(char *base, int n, bool rho, i
     s.Yl = REFINE ? reinterpret_cast<cx<float> *>(base + L.Yl) : nullptr;
     s.SR = REFINE ? reinterpret_cast<cx<float> *>(base + L.SR) : nullptr;
     s.sd = REFINE ? reinterpret_cast<double *>(base + L.sd) : nullptr;
-    s.corr = REFINE ? reinterpret_cast<double *>(base + L.corr) : nullptr;
+    s.corr = REFINE ? reinterpret_cast<float *>(base + L.corr) : nullptr;
     s.rd = REFINE ? reinterpret_cast<float *>(base + L.rd) : nullptr;
+    s.lamf = REFINE ? reinterpret_cast<float *>(base + L.lamf) : nullptr;
     s.fac = rho ? reinterpret_cast<cx<double> *>(base + L.fac) : nullptr;
     s.B2 = rho ? reinterpret_cast<cx<T> *>(base + L.B2) : nullptr;
     return s;
@@ -155,7 +159,7 @@ __device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
     const double bx = b[0], by = b[1], bz = b[2];
     const size_t nn = (size_t)n * n;
     for (int e = tid; e < m * m; e += nt) {
-        const int i = e / m, j = e - (e / m) * m;
+        const int i = FastDiv(m).div(e), j = e - i * m;
         cx<double> h = mk<double>(0.0, 0.0);
         if (i < n && j < n) {
             const size_t o = (size_t)i * n + j;
@@ -192,7 +196,7 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     if (tid == 0) s.rank[0] = 0;
     // Y = H X
     for (int e = tid; e < n * n; e += nt) {
-        const int i = e / n, j = e - (e / n) * n;
+        const int i = FastDiv(n).div(e), j = e - i * n;
         float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
         for (int k = 0; k < n; ++k) {
             const cx<float> h = s.Hh[i * ld + k], hl = s.Hl[i * ld + k], x = X[k * ld + j];
@@ -243,14 +247,19 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     }
     __syncthreads();
     for (int i = tid; i < n; i += nt) {
-        s.lam[i] = s.sd[i] / (1.0 - (double)s.rd[i]);
-        s.corr[i] = 0.0;
+        const double l = s.sd[i] / (1.0 - (double)s.rd[i]);
+        s.lam[i] = l;
+        s.lamf[i] = (float)l;
+        s.corr[i] = 0.f;
     }
     __syncthreads();
-    double lmax = 0.0;
-    for (int i = 0; i < n; ++i) lmax = fmax(lmax, fabs(s.lam[i]));
-    const double deg = 1e-7 * (lmax + 1e-300);
-    // E in place of S/R; second-order eigenvalue terms
+    float lmax = 0.f;
+    for (int i = 0; i < n; ++i) lmax = fmaxf(lmax, fabsf(s.lamf[i]));
+    const float deg = 1e-7f * lmax + 1e-30f;
+    // E in place of S/R; second-order eigenvalue terms.  Only the gap
+    // l_j - l_i needs FP64 (a difference of nearly equal large numbers);
+    // E, S, R and the second-order terms are small corrections, FP32 is
+    // ample for them.
     const int nup = n * (n - 1) / 2;
     for (int e = tid; e < nup; e += nt) {
         // strict upper pairs (i < j): j = row of the packed strict triangle
@@ -259,20 +268,19 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         while ((j + 1) * j / 2 <= e) ++j;
         const int i = e - j * (j - 1) / 2;  // 0 <= i < j
         const cx<float> S = s.SR[i * ld + j], R = s.SR[j * ld + i];
-        const double li = s.lam[i], lj = s.lam[j];
-        const double dl = lj - li;
+        const float dl = (float)(s.lam[j] - s.lam[i]);
         cx<float> Eij, Eji;
-        if (fabs(dl) > deg) {
+        if (fabsf(dl) > deg) {
             // E_ij = (S_ij + l_j R_ij) / (l_j - l_i); E_ji = (S_ji + l_i R_ji) / (l_i - l_j)
-            const float inv = (float)(1.0 / dl);
-            const float lj_f = (float)lj, li_f = (float)li;
-            Eij = mk<float>((S.re + lj_f * R.re) * inv, (S.im + lj_f * R.im) * inv);
-            Eji = mk<float>(-(S.re + li_f * R.re) * inv, (S.im + li_f * R.im) * inv);
+            const float inv = 1.0f / dl;
+            const float lj_f = s.lamf[j], li_f = s.lamf[i];
+            const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;
+            const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;
+            Eij = mk<float>(br * inv, bi * inv);
+            Eji = mk<float>(-ar * inv, ai * inv);
             // second order: |S_ij + l_i R_ij|^2 / (l_i - l_j) for l_i, and the mirror
-            const double ar = (double)S.re + li * (double)R.re, ai = (double)S.im + li * (double)R.im;
-            const double br = (double)S.re + lj * (double)R.re, bi = (double)S.im + lj * (double)R.im;
-            atomicAdd(&s.corr[i], -(ar * ar + ai * ai) / dl);
-            atomicAdd(&s.corr[j], (br * br + bi * bi) / dl);
+            atomicAdd(&s.corr[i], -(ar * ar + ai * ai) * inv);
+            atomicAdd(&s.corr[j], (br * br + bi * bi) * inv);
             const float mag = fmaxf(fmaxf(fabsf(Eij.re), fabsf(Eij.im)),
                                     fmaxf(fabsf(Eji.re), fabsf(Eji.im)));
             atomicMax(&s.rank[0], __float_as_int(mag));  // non-negative: int order = float order
@@ -286,7 +294,7 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     __syncthreads();
     // X' = X + X E  (into Yh), E_ii = R_ii / 2
     for (int e = tid; e < n * n; e += nt) {
-        const int k = e / n, j = e - (e / n) * n;
+        const int k = FastDiv(n).div(e), j = e - k * n;
         const cx<float> xkj = X[k * ld + j];
         const float hr = 0.5f * s.rd[j];
         float ar = xkj.re + hr * xkj.re, ai = xkj.im + hr * xkj.im;
@@ -300,10 +308,10 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     }
     __syncthreads();
     for (int e = tid; e < n * n; e += nt) {
-        const int k = e / n, j = e - (e / n) * n;
+        const int k = FastDiv(n).div(e), j = e - k * n;
         X[k * ld + j] = Yh[k * ld + j];
     }
-    for (int i = tid; i < n; i += nt) s.lam[i] += s.corr[i];
+    for (int i = tid; i < n; i += nt) s.lam[i] += (double)s.corr[i];
     __syncthreads();
     const float emax = __int_as_float(s.rank[0]);
     __syncthreads();
@@ -344,7 +352,7 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
     for (int bidx = blockIdx.x; bidx < batch; bidx += gridDim.x) {
         const cx<double> *Hb = Hin + (size_t)bidx * n * n;
         for (int e = tid; e < m * m; e += nt) {
-            const int i = e / m, j = e - (e / m) * m;
+            const int i = FastDiv(m).div(e), j = e - i * m;
             cx<double> h = mk<double>(0.0, 0.0);
             if (i < n && j < n) h = Hb[(size_t)i * n + j];
             s.w.H[i * ld + j] = mk<T>((T)h.re, (T)h.im);
@@ -371,7 +379,7 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
         __syncthreads();
         cx<double> *Vb = evecs + (size_t)bidx * n * n;
         for (int e = tid; e < n * n; e += nt) {
-            const int i = e / n, j = e - (e / n) * n;
+            const int i = FastDiv(n).div(e), j = e - i * n;
             const cx<T> u = s.w.U[i * ld + j];
             Vb[(size_t)i * n + s.rank[j]] = mk<double>((double)u.re, (double)u.im);
         }
@@ -409,7 +417,7 @@ __global__ void msp_snap_fast_kernel(SnapArgs a) {
         cx<T> *M = s.w.H;  // free buffer
         const cx<T> *U = s.w.U;
         for (int e = tid; e < n * n; e += nt) {
-            const int i = e / n, k = e - (e / n) * n;
+            const int i = FastDiv(n).div(e), k = e - i * n;
             cx<T> v;
             if (i < d)
                 v = cadd(cmul(s00, U[i * ld + k]), cmul(s01, U[(i + d) * ld + k]));
@@ -562,7 +570,7 @@ __device__ void apply_digit(const cx<double> *F, int dim, int stride, const cx<T
                             cx<T> *Y, int n, int m) {
     const int ld = m + 1;
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        const int i = e / n, k = e - (e / n) * n;
+        const int i = FastDiv(n).div(e), k = e - i * n;
         const int di = (i / stride) % dim;
         const int base = i - di * stride;
         T yr = 0, yi = 0;
@@ -643,7 +651,7 @@ __global__ void msp_snap_rho_kernel(SnapArgs a) {
             const cx<T> o10 = mk<T>((T)(0.5 * px), (T)(0.5 * py));
             const cx<T> o11 = mk<T>((T)(-0.5 * pz), T(0));
             for (int e = tid; e < n * n; e += nt) {
-                const int i = e / n, k = e - (e / n) * n;
+                const int i = FastDiv(n).div(e), k = e - i * n;
                 const int di = (i / stride) & 1;
                 const int base = i - di * stride;
                 const cx<T> x0 = U[base * ld + k], x1 = U[(base + stride) * ld + k];
@@ -804,7 +812,7 @@ __global__ void msp_basis_change_kernel(const cx<double> *__restrict__ U, long l
         }
         __syncthreads();
         for (int e = tid; e < n * n; e += nt) {
-            const int i = e / n, k = e - (e / n) * n;
+            const int i = FastDiv(n).div(e), k = e - i * n;
             double tr = 0, ti = 0;
             for (int l = 0; l < n; ++l) {
                 const cx<double> mv = sM[i * n + l];
@@ -818,7 +826,7 @@ __global__ void msp_basis_change_kernel(const cx<double> *__restrict__ U, long l
         __syncthreads();
         cx<double> *Ob = out + (size_t)b * n * n;
         for (int e = tid; e < n * n; e += nt) {
-            const int j = e / n, k = e - (e / n) * n;
+            const int j = FastDiv(n).div(e), k = e - j * n;
             double tr = 0, ti = 0;
             for (int i = 0; i < n; ++i) {
                 // row j of U^dag = conj(U_ij); row j of U = U_ji

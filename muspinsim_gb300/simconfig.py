@@ -1,0 +1,451 @@
+"""Simulation configuration: evaluated input parameters expanded into
+snapshots, API-compatible with ``muspinsim/simconfig.py``.
+
+Each input keyword holds one value or a range.  A range is the x axis, an
+averaged axis or a file range (``muspinsim/simconfig.py:112-171``);
+snapshots are the Cartesian product file x average x x-axis
+(``:299-321``); a snapshot's result is added to
+results[file idx + x idx] divided by the number of averaged configurations
+(``store_time_slice``, ``:347-368``).  Orientation weights are normalised to
+sum to N when orientations are averaged, else ignored (``:152-159``).
+
+The text input language (a lark grammar in the reference) is not part of
+this library: parameters come as the dictionary ``MuSpinInput.evaluate``
+returns, which ``make_params`` builds from Python values.
+"""
+
+import datetime
+import logging
+import os
+import re
+from collections import OrderedDict, namedtuple
+from collections.abc import Iterable
+from itertools import product
+
+import numpy as np
+
+from muspinsim_gb300.orientations import orientation_rows_to_quats
+from muspinsim_gb300.quaternion import Quaternion
+from muspinsim_gb300.spinsys import MuonSpinSystem
+
+__version__ = "2.3.1"  # reference version whose output format is written
+
+_CDICT = {
+    "polarization": "mupol",
+    "field": "B",
+    "intrinsic_field": "intrinsic_B",
+    "time": "t",
+    "orientation": "orient",
+    "temperature": "T",
+}
+_CSDICT = {
+    "zeeman": "zmn",
+    "dipolar": "dip",
+    "quadrupolar": "quad",
+    "hyperfine": "hfc",
+    "dissipation": "dsp",
+}
+
+ConfigSnapshot = namedtuple("ConfigSnapshot", ["id", "y"] + list(_CDICT.values()))
+MuSpinInputValue = namedtuple("MuSpinInputValue", ["name", "args", "value"])
+
+
+class MuSpinConfigError(Exception):
+    pass
+
+
+class _Identity:
+    def evaluate(self, **kw):
+        return kw["y"]
+
+
+class CallableResults:
+    """Wraps f(x, y, **variables) as a results_function."""
+
+    def __init__(self, fn):
+        self.fn = fn
+
+    def evaluate(self, **kw):
+        return self.fn(**kw)
+
+
+def make_params(spins=("mu", "e"), couplings=(), time=None, orientation=((0.0, 0.0, 0.0),),
+                field=(0.0,), intrinsic_field=(0.0,), polarization=((1.0, 0.0, 0.0),),
+                temperature=(np.inf,), y_axis="asymmetry", x_axis="time",
+                average_axes=("orientation",), name="muspinsim", orientation_mode="zyz",
+                results_function=None, celio=(0, 0)):
+    """The evaluated-parameter dictionary for MuSpinConfig / ExperimentRunner.
+
+    Every axis keyword takes a list of rows (one value: a constant; several:
+    a range), with the reference's defaults (``muspinsim/input/keyword.py:
+    364-485``): time = linspace(0, 10, 101), polarization transverse (x),
+    orientation (0, 0, 0), temperature inf, field 0.  ``couplings`` is a list
+    of ``(kind, {"i": 1-based, ["j": 1-based]}, value)``.
+    """
+    if time is None:
+        time = np.linspace(0, 10, 101)
+
+    def rows(v):
+        return np.array([np.atleast_1d(np.asarray(r, dtype=float)) for r in v], dtype=float)
+
+    p = {
+        "name": MuSpinInputValue("name", {}, np.array([[name]])),
+        "spins": MuSpinInputValue("spins", {}, np.array([list(spins)], dtype=object)),
+        "celio": MuSpinInputValue("celio", {}, np.array([[str(c) for c in celio]])),
+        "y_axis": MuSpinInputValue("y_axis", {}, np.array([[y_axis]])),
+        "x_axis": MuSpinInputValue("x_axis", {}, np.array([[x_axis]])),
+        "average_axes": MuSpinInputValue("average_axes", {}, np.array([list(average_axes)])),
+        "polarization": MuSpinInputValue("polarization", {}, rows(polarization)),
+        "field": MuSpinInputValue("field", {}, rows(field)),
+        "intrinsic_field": MuSpinInputValue("intrinsic_field", {}, rows(intrinsic_field)),
+        "time": MuSpinInputValue("time", {}, np.asarray(time, dtype=float).reshape(-1, 1)),
+        "orientation": MuSpinInputValue("orientation", {"mode": orientation_mode},
+                                        np.array([np.asarray(o, float) for o in orientation],
+                                                 dtype=object if len({len(o) for o in orientation}) > 1 else float)),
+        "temperature": MuSpinInputValue("temperature", {},
+                                        np.asarray(temperature, dtype=float).reshape(-1, 1)),
+        "results_function": results_function if results_function is not None else _Identity(),
+        "fitting_info": {"fit": False},
+        "couplings": {},
+    }
+    for k, (kind, args, value) in enumerate(couplings):
+        p["couplings"][f"{kind}_{k}"] = MuSpinInputValue(kind, dict(args),
+                                                          [np.asarray(value, dtype=float)])
+    return p
+
+
+class ParamsInput:
+    """Minimal stand-in for MuSpinInput: ``evaluate()`` returns the params."""
+
+    def __init__(self, params):
+        self._params = params
+
+    def evaluate(self, **variables):
+        return dict(self._params)
+
+
+class MuSpinConfig:
+    """Ranges, snapshots and result accumulation of one simulation
+    (muspinsim/simconfig.py:78-647)."""
+
+    def __init__(self, params={}, use_experimental_x_axis=True):
+        self._constants = {}
+        self._file_ranges = OrderedDict()
+        self._avg_ranges = OrderedDict()
+        self._x_range = OrderedDict()
+        if len(params) == 0:
+            return
+        self._name = self.validate("name", params["name"].value)[0]
+        self._spins = self.validate("spins", params["spins"].value[0])
+        self._celio = self._validate_celio(params["celio"].value[0])
+        self._y_axis = self.validate("y", params["y_axis"].value[0])[0]
+        self._results_function = params["results_function"]
+        try:
+            x = _CDICT[params["x_axis"].value[0][0]]
+        except KeyError as exc:
+            raise MuSpinConfigError("Invalid x axis name in input file") from exc
+        self._x_range[x] = None
+        for a in np.asarray(params["average_axes"].value).reshape((-1,)):
+            if str(a).lower() == "none":
+                continue
+            try:
+                self._avg_ranges[_CDICT[a]] = None
+            except KeyError as exc:
+                raise MuSpinConfigError("Invalid average axis name in input file") from exc
+        self._time_N = 0
+        self._time_isavg = "t" in self._avg_ranges
+        for iname, cname in _CDICT.items():
+            try:
+                p = params[iname]
+            except KeyError as exc:
+                raise MuSpinConfigError(
+                    f"Invalid params object passed to MuSpinConfig: missing {iname}") from exc
+            v = self.validate(cname, p.value, p.args)
+            if cname == "t":
+                if self._y_axis == "integral":
+                    logging.warning("Ignoring time axis since Y = integral")
+                    v = [np.inf]
+                self._time_N = len(v)
+            elif cname == "orient":
+                if cname in self._avg_ranges:
+                    norm = len(v) / np.sum(np.array([w for (q, w) in v]))
+                    v = [(q, w * norm) for (q, w) in v]
+                else:
+                    v = [(q, 1.0) for (q, w) in v]
+            if len(v) > 1:
+                if cname in self._x_range:
+                    self._x_range[cname] = v
+                elif cname in self._avg_ranges:
+                    self._avg_ranges[cname] = v
+                else:
+                    self._file_ranges[cname] = v
+            else:
+                self._constants[cname] = v[0]
+        if self._y_axis == "integral" and "t" in self._x_range:
+            raise MuSpinConfigError("Can not use time as X axis when evaluating integral of signal")
+        if params["fitting_info"].get("fit"):
+            raise MuSpinConfigError("Fitting configurations are not supported by muspinsim_gb300")
+        if list(self._x_range.values())[0] is None:
+            raise MuSpinConfigError("Specified x axis is not a range")
+        self._avg_ranges = OrderedDict((k, v) for k, v in self._avg_ranges.items() if v is not None)
+
+        self._system = MuonSpinSystem(self._spins, self.celio_k)
+        self._dissip_terms = {}
+        for iid, idata in params["couplings"].items():
+            try:
+                cname = _CSDICT[idata.name]
+            except KeyError as exc:
+                raise MuSpinConfigError(
+                    f"Invalid params object passed to MuSpinConfig: unknown {idata.name} coupling"
+                ) from exc
+            args = idata.args
+            ij = np.array([v for v in args.values() if v is not None])
+            if (ij < 1).any() or (ij > len(self._spins)).any():
+                raise MuSpinConfigError("Out of range indices for coupling")
+            cval = np.asarray(idata.value[0], dtype=float)
+            shape = {"zmn": (3,), "dip": (3,), "hfc": (3, 3), "quad": (3, 3), "dsp": (1,)}[cname]
+            if cval.shape != shape:
+                raise MuSpinConfigError(f"Invalid shape for {idata.name} coupling term")
+            i = args.get("i")
+            j = args.get("j")
+            i = i - 1 if i is not None else None
+            j = j - 1 if j is not None else None
+            if cname == "zmn":
+                self._system.add_zeeman_term(i, cval)
+            elif cname == "dip":
+                self._system.add_dipolar_term(i, j, cval)
+            elif cname == "hfc":
+                self._system.add_hyperfine_term(i, cval, j)
+            elif cname == "quad":
+                self._system.add_quadrupolar_term(i, cval)
+            elif cname == "dsp":
+                self._dissip_terms[i] = cval[0]
+
+        res_shape = [len(v) for v in self._file_ranges.values()]
+        res_shape += [len(v) for v in self._x_range.values()]
+        self._results = np.zeros(res_shape)
+
+        def make_configs(od):
+            cfg = []
+            for k, v in od.items():
+                cfg.append([slice(None)] if k == "t" else np.arange(len(v)))
+            return list(product(*cfg))
+
+        fconfigs = make_configs(self._file_ranges)
+        aconfigs = make_configs(self._avg_ranges)
+        xconfigs = make_configs(self._x_range)
+        self._configurations = list(product(*[fconfigs, aconfigs, xconfigs]))
+        self._avg_N = len(aconfigs)
+
+    # -------------------------------------------------------------- validators
+    def validate(self, name, value, args=None):
+        args = {} if args is None else args
+        fn = getattr(self, f"_validate_{name}", None)
+        if fn is not None:
+            value = [fn(v, **args) for v in value]
+        return value
+
+    def _validate_name(self, v):
+        if len(v) > 1:
+            raise MuSpinConfigError("Name must be a word without spaces")
+        return v[0]
+
+    def _validate_spins(self, v):
+        m = re.compile("([0-9]+)([A-Z][a-z]*|e)").match(v)
+        if m is None:
+            return v
+        A, el = m.groups()
+        return (el, int(A))
+
+    def _validate_celio(self, v):
+        try:
+            k = int(v[0])
+        except ValueError as exc:
+            raise MuSpinConfigError("Value of k for Celio's method must be an integer") from exc
+        if k < 0:
+            raise MuSpinConfigError("Value of k for Celio's method must a postive integer or 0")
+        avg = int(v[1]) if len(v) == 2 else 0
+        if avg < 0:
+            raise MuSpinConfigError(
+                "Value of averages for Celio's method must a postive integer or 0")
+        return (k, avg)
+
+    def _validate_t(self, v):
+        if len(v) != 1:
+            raise MuSpinConfigError("Invalid line in time range")
+        return v[0]
+
+    def _validate_B(self, v):
+        v = np.atleast_1d(np.asarray(v, dtype=float))
+        if len(v) == 1:
+            return np.array([0, 0, v[0]])
+        if len(v) != 3:
+            raise MuSpinConfigError("Invalid magnetic field value")
+        return v
+
+    def _validate_intrinsic_B(self, v):
+        v = np.atleast_1d(np.asarray(v, dtype=float))
+        if len(v) == 1:
+            return np.array([0, 0, v[0]])
+        if len(v) != 3:
+            raise MuSpinConfigError("Invalid intrinsic magnetic field value")
+        return v
+
+    def _validate_mupol(self, v):
+        v = np.array(v, dtype=float)
+        if len(v) != 3:
+            raise MuSpinConfigError("Invalid muon polarization direction")
+        return v / np.linalg.norm(v)
+
+    def _validate_orient(self, v, mode="zyz"):
+        qs, ws = orientation_rows_to_quats([np.asarray(v, dtype=float)], mode)
+        return (Quaternion(qs[0]), float(ws[0]))
+
+    def _validate_T(self, v):
+        return np.atleast_1d(v)[0]
+
+    # -------------------------------------------------------------- results
+    def store_time_slice(self, config_id, tslice):
+        if isinstance(tslice, Iterable) and len(tslice) != self._time_N:
+            raise ValueError("Time slice has invalid length")
+        if self._time_isavg:
+            tslice = np.average(tslice)
+        ii = tuple(list(config_id[0]) + list(config_id[2]))
+        self._results[ii] += tslice / self._avg_N
+
+    def save_output(self, name=None, path=".", extension=".dat"):
+        """Write one two-column .dat file per file-range combination
+        (muspinsim/simconfig.py:370-429)."""
+        if name is None:
+            name = self.name
+        header = ("MUSPINSIM v.{version}\nOutput file written on {date}\nParameters used:\n"
+                  .format(version=__version__, date=datetime.datetime.now().ctime()))
+        for fn in self._file_ranges:
+            header += "\t{0:<20} = {{{0}}}\n".format(fn)
+        x = self.x_axis_values
+        if "B" in self._x_range or "intrinsic_B" in self._x_range:
+            x = np.linalg.norm(x, axis=-1)
+        for inds in product(*[range(len(r)) for r in self._file_ranges.values()]):
+            fid = "".join(f"_{i}" for i in inds)
+            vdict = {}
+            for i, (key, val) in enumerate(self._file_ranges.items()):
+                v = val[inds[i]]
+                pf = getattr(self, f"_print_{key}", None)
+                vdict[key] = pf(v) if pf else v
+            data = np.zeros((len(x), 2))
+            data[:, 0] = x
+            data[:, 1] = self._results[inds]
+            np.savetxt(os.path.join(path, f"{name}{fid}{extension}"), data,
+                       header=header.format(**vdict))
+
+    def _print_B(self, v):
+        return "{0} T".format(v)
+
+    def _print_orient(self, v):
+        o, w = v
+        abc = o.euler_angles("zyz") * 180 / np.pi
+        return "[ZYZ] a = {0:.1f} deg, b = {1:.1f} deg, c = {2:.1f} deg, weight = {3}".format(*abc, w)
+
+    # -------------------------------------------------------------- properties
+    @property
+    def name(self):
+        return self._name
+
+    @property
+    def spins(self):
+        return list(self._spins)
+
+    @property
+    def celio_k(self):
+        return self._celio[0]
+
+    @property
+    def celio_averages(self):
+        return self._celio[1]
+
+    @property
+    def system(self):
+        return self._system.clone()
+
+    @property
+    def constants(self):
+        return {**self._constants}
+
+    @property
+    def dissipation_terms(self):
+        return {**self._dissip_terms}
+
+    @property
+    def results(self):
+        return np.array(self._results)
+
+    @results.setter
+    def results(self, r):
+        r = np.array(r)
+        if r.shape != self._results.shape:
+            raise ValueError("Trying to set an invalid results array")
+        self._results = r
+
+    @property
+    def x_axis(self):
+        return [*self._x_range.keys()][0]
+
+    @property
+    def x_axis_values(self):
+        return np.array([*self._x_range.values()][0])
+
+    @property
+    def y_axis(self):
+        return self._y_axis
+
+    @property
+    def results_function(self):
+        return self._results_function
+
+    @property
+    def file_ranges(self):
+        return OrderedDict(self._file_ranges)
+
+    @property
+    def avg_ranges(self):
+        return OrderedDict(self._avg_ranges)
+
+    @property
+    def x_range(self):
+        return OrderedDict(self._x_range)
+
+    @property
+    def avg_N(self):
+        return self._avg_N
+
+    @property
+    def time_N(self):
+        return self._time_N
+
+    @property
+    def time_is_averaged(self):
+        return self._time_isavg
+
+    @property
+    def configurations(self):
+        return list(self._configurations)
+
+    def __len__(self):
+        return len(self._configurations)
+
+    def __getitem__(self, i):
+        isint = isinstance(i, int)
+        if isint:
+            i = slice(i, i + 1)
+        elif not isinstance(i, slice):
+            raise TypeError(f"Indices must be integer or slices, not {type(i)}")
+
+        def pick(inds, od):
+            return {k: v[inds[n]] for n, (k, v) in enumerate(od.items())}
+
+        ans = []
+        for fc, ac, xc in self._configurations[i]:
+            ans.append(ConfigSnapshot(id=(fc, ac, xc), y=self._y_axis, **self._constants,
+                                      **pick(fc, self._file_ranges), **pick(ac, self._avg_ranges),
+                                      **pick(xc, self._x_range)))
+        return ans[0] if isint else ans

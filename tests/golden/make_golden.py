@@ -1,0 +1,142 @@
+"""Generate the golden fixtures of tests/golden/ by running the REFERENCE.
+
+Needs the reference tree (imported through tests/golden/refshim.py) and its
+Cython kernel built by oracle/build.py; run it only where the reference is
+present:
+
+    python tests/golden/make_golden.py
+
+Each fixture is a small .npz with the inputs (spins, couplings as JSON,
+orientations, fields, times, polarisation, temperature, axes) and the
+reference's output of ExperimentRunner.run() -- or of Hamiltonian.diag /
+evolve / fast_evolve / integrate_decaying for the direct-API cases.  The
+synthetic systems come from muspinsim_gb300.workloads (seeded), reduced in
+size so that the CPU oracle and the reference finish in seconds.
+"""
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, HERE)
+
+import refshim  # noqa: E402
+
+
+def _jsonable_couplings(couplings):
+    return [[k, dict(a), np.asarray(v, dtype=float).tolist()] for k, a, v in couplings]
+
+
+def _run_reference(spins, couplings, times, orientations, fields, pol, temps, y_axis,
+                   x_axis, intrinsic=((0.0, 0.0, 0.0),), average_axes=("orientation",)):
+    from muspinsim.experiment import ExperimentRunner
+
+    p = refshim.make_params(spins, couplings, times, orientations, field=fields,
+                            intrinsic_field=intrinsic, polarization=pol, temperature=temps,
+                            y_axis=y_axis, x_axis=x_axis, average_axes=average_axes)
+    er = ExperimentRunner(refshim.ParamsInput(p))
+    return np.array(er.run())
+
+
+def save_experiment(name, spins, couplings, times, orientations, fields=((0.0, 0.0, 0.0),),
+                    pol=(1.0, 0.0, 0.0), temps=(np.inf,), y_axis="asymmetry", x_axis="time",
+                    intrinsic=((0.0, 0.0, 0.0),), average_axes=("orientation",)):
+    out = _run_reference(spins, couplings, times, orientations, fields, pol, temps, y_axis,
+                         x_axis, intrinsic, average_axes)
+    meta = {"spins": list(spins), "couplings": _jsonable_couplings(couplings),
+            "y_axis": y_axis, "x_axis": x_axis, "average_axes": list(average_axes)}
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        meta=np.array(json.dumps(meta)),
+        times=np.asarray(times, dtype=float),
+        orientations=np.asarray(orientations, dtype=float),
+        fields=np.asarray([np.atleast_1d(f) for f in fields], dtype=float),
+        intrinsic=np.asarray([np.atleast_1d(f) for f in intrinsic], dtype=float),
+        polarization=np.asarray(pol, dtype=float),
+        temperatures=np.asarray(temps, dtype=float),
+        result=out,
+    )
+    print(f"{name}: result shape {out.shape}")
+
+
+def save_direct(name):
+    """Direct-API goldens: diag, evolve (with and without operators),
+    fast_evolve, integrate_decaying of one random dim-24 Hamiltonian."""
+    from muspinsim.spinop import DensityOperator
+    from muspinsim.spinsys import MuonSpinSystem
+
+    from muspinsim_gb300 import workloads
+
+    wl = workloads.config2(n_orient=1, n_times=64)
+    sy = MuonSpinSystem(list(wl.spins))
+    for kind, args, val in wl.couplings:
+        i, j = args["i"] - 1, args.get("j")
+        j = None if j is None else j - 1
+        {"hyperfine": lambda: sy.add_hyperfine_term(i, val, j),
+         "dipolar": lambda: sy.add_dipolar_term(i, j, val),
+         "quadrupolar": lambda: sy.add_quadrupolar_term(i, val)}[kind]()
+    sy.add_zeeman_term(0, [0.001, 0.002, 0.01])
+    sy.add_zeeman_term(1, [0.001, 0.002, 0.01])
+    # a fresh Hamiltonian per call: the reference's diag() cache-hit branch
+    # fails under scipy >= 1.15 (muspinsim/spinop.py:61-66)
+    evals, evecs = sy.hamiltonian.diag()
+    Hm = sy.hamiltonian.matrix.toarray()
+    t = np.linspace(0, 2.0, 64)
+    rho0 = DensityOperator.from_vectors([0.5, 0.5, 0.5, 1.0], [[0, 0, 1], [1, 0, 0], [0, 1, 0],
+                                                             [0, 0, 1]], [0, 0, 0, 0.5])
+    ops = [sy.operator({0: "x"}), sy.operator({0: "z"}), sy.operator({2: "+"})]
+    ev = sy.hamiltonian.evolve(rho0, t, ops)
+    dens = sy.hamiltonian.evolve(rho0, t[:4])
+    dens = np.array([d.matrix.toarray() for d in dens])
+    fast = sy.hamiltonian.fast_evolve(sy.sigma_mu([0.3, 0.4, 0.5]), t, 12)
+    integ = sy.hamiltonian.integrate_decaying(rho0, 2.19703, ops)
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        H=Hm, evals=evals, times=t, rho0=rho0.matrix.toarray(),
+        ops=np.array([o.matrix.toarray() for o in ops]), evolve=ev, density=dens,
+        sigma=sy.sigma_mu([0.3, 0.4, 0.5]).toarray(), fast=fast, integral=integ)
+    print(f"{name}: dim {Hm.shape[0]}")
+
+
+def main():
+    refshim.install()
+    from muspinsim_gb300 import workloads
+
+    w1 = workloads.config1()
+    save_experiment("config1_fast", w1.spins, w1.couplings, w1.times, w1.orientations,
+                    w1.fields, w1.polarization)
+    w2 = workloads.config2(n_orient=16, n_times=512)
+    save_experiment("config2_powder16", w2.spins, w2.couplings, w2.times, w2.orientations,
+                    w2.fields, w2.polarization)
+    save_experiment("config2_powder8_T10K", w2.spins, w2.couplings, w2.times[:300],
+                    w2.orientations[:8], w2.fields, (1.0, 0.0, 0.0), temps=(10.0,))
+    w3 = workloads.config3(n_fields=6, n_orient=5)
+    save_experiment("config3_alc", w3.spins, w3.couplings, [0.0], w3.orientations,
+                    [tuple(f) for f in w3.fields], w3.polarization, y_axis="integral",
+                    x_axis="field")
+    w5 = workloads.config5(n_orient=24, n_times=300)
+    save_experiment("config5_fmuf", w5.spins, w5.couplings, w5.times, w5.orientations,
+                    w5.fields, w5.polarization)
+    # muon not first (general evolve path), Euler rows with weights, intrinsic field
+    rng = np.random.default_rng(77)
+    A1 = workloads.random_hyperfine(rng)
+    A2 = workloads.random_hyperfine(rng, 5.0)
+    save_experiment("e_mu_H_weighted", ["e", "mu", "H"],
+                    [("hyperfine", {"i": 2, "j": 1}, A1), ("hyperfine", {"i": 3, "j": 1}, A2)],
+                    np.linspace(0, 5, 200),
+                    [(0.1, 0.2, 0.3, 1.0), (1.0, 2.0, 0.5, 2.0), (2.5, 0.4, 1.5, 0.5)],
+                    [(0.0, 0.01, 0.02)], (1.0, 1.0, 0.0), intrinsic=[(0.0, 0.0, 0.005)])
+    # file ranges: field x temperature, time axis (muspinsim/tests/test_experiment.py:269)
+    save_experiment("file_ranges", ["e", "mu"], [("zeeman", {"i": 2}, [0, 0, 1.0 / 135.53880943285955])],
+                    np.linspace(0, 10, 100), [(0.0, 0.0, 0.0)],
+                    [(0.0, 0.0, 0.0), (0.0, 0.0, 10.0)], (1.0, 0.0, 0.0), temps=(np.inf, 0.0))
+    save_direct("direct_dim24")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,6 +1,9 @@
 """Shared test helpers: oracle systems built from the same inputs the GPU
 library receives, and random Hermitian matrices."""
 
+import json
+import os
+
 import numpy as np
 
 from muspinsim_gb300 import constants as C
@@ -46,6 +49,37 @@ def oracle_powder(wl, orientations=None, times=None, field=None, temperature=Non
     y = wl.y_axis if y_axis is None else y_axis
     p = wl.polarization / np.linalg.norm(wl.polarization)
     return port.powder_average(sy, o, np.asarray(B, float), p, T, t, y=y)
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_golden(name):
+    """A fixture written by tests/golden/make_golden.py: the meta JSON
+    unpacked (spins, couplings with numpy tensors, axes) plus the arrays."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    out = {k: z[k] for k in z.files if k != "meta"}
+    if "meta" in z.files:
+        meta = json.loads(str(z["meta"]))
+        meta["couplings"] = [(k, {kk: int(vv) for kk, vv in a.items()}, np.array(v))
+                             for k, a, v in meta["couplings"]]
+        out.update(meta)
+    return out
+
+
+def golden_oracle(g, field_index=0, temp_index=0):
+    """Oracle evaluation of one (field, temperature) row of a golden fixture."""
+    sy = oracle_system(g["spins"], g["couplings"])
+    p = g["polarization"] / np.linalg.norm(g["polarization"])
+    B = g["fields"][field_index]
+    if B.size == 1:
+        B = np.array([0.0, 0.0, B[0]])
+    intr = g["intrinsic"][0]
+    if intr.size == 1:
+        intr = np.array([0.0, 0.0, intr[0]])
+    y = "integral" if g["y_axis"] == "integral" else "asymmetry"
+    return port.powder_average(sy, list(g["orientations"]), B, p, g["temperatures"][temp_index],
+                               g["times"], intrinsic_B=intr, y=y)
 
 
 def random_hermitian(rng, n, scale=100.0):
