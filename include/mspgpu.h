@@ -187,6 +187,23 @@ int msp_powder_workspace(const msp_powder_args *args, size_t *bytes);
  * msp_schedule, msp_phase_* (time tiles x pair chunks), msp_reduce. */
 int msp_powder_run(const msp_powder_args *args);
 
+/* Bytes of scratch built into the library for msp_powder_run_static. */
+#define MSP_STATIC_SCRATCH_BYTES (32u << 20)
+
+/* msp_powder_run for callers that cannot allocate device memory (a host
+ * whose GPU memory belongs to another runtime, a binding with no route to
+ * cudaMalloc, a loop that must not let an allocation synchronise the
+ * device).  No counterpart in the reference.  args->workspace and
+ * args->workspace_bytes are ignored: the scratch is a file-scope device
+ * array of MSP_STATIC_SCRATCH_BYTES that every GPU loading the library keeps
+ * until exit, and a batch needing more returns MSP_ERR_WORKSPACE with the
+ * sizes in msp_last_error.  Nothing is allocated.  The first call on each
+ * device (with it current) looks up the array's device address; make that
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.  Same
+ * results as msp_powder_run. */
+int msp_powder_run_static(const msp_powder_args *args);
+
 #ifdef __cplusplus
 }
 #endif

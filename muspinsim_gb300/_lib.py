@@ -30,6 +30,7 @@ MODE_EVOLVE = 1
 MODE_INTEGRAL = 2
 
 MAX_DIM = 64
+STATIC_SCRATCH_BYTES = 32 << 20  # MSP_STATIC_SCRATCH_BYTES
 MAX_SPINS = 16
 
 _c_dp = ctypes.c_void_p  # device pointers travel as void*
@@ -115,6 +116,7 @@ _SIGNATURES = {
         [ctypes.POINTER(PowderArgs), ctypes.POINTER(ctypes.c_size_t)],
     ),
     "msp_powder_run": (ctypes.c_int, [ctypes.POINTER(PowderArgs)]),
+    "msp_powder_run_static": (ctypes.c_int, [ctypes.POINTER(PowderArgs)]),
     "msp_timer_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
     "msp_timer_destroy": (ctypes.c_int, [_c_dp]),
     "msp_timer_read": (

@@ -26,6 +26,11 @@ static int cuda_check(cudaError_t e, const char *what) {
     return MSP_OK;
 }
 
+namespace msp {
+// Records an error message for msp_last_error from another translation unit.
+int record_error(int code, const char *msg) { return fail(code, "%s", msg); }
+}  // namespace msp
+
 #define MSP_CHECK_PTR(p)                                    \
     do {                                                    \
         if ((p) == NULL) return fail(MSP_ERR_ARG, "%s is NULL", #p); \
