@@ -234,6 +234,7 @@ static cudaEvent_t *timer_slot(msp_timer *t) {
 struct Layout {
     size_t coef, omega, snap_const, slot_first, item_first, partial, total;
     int P, SB, max_items, T;
+    bool phase_records;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -294,7 +295,10 @@ static Layout powder_layout(const msp_powder_args *a) {
     L.coef = off;
     off += align256(has_pairs ? S * L.P * ce : 0);
     L.omega = off;
-    off += align256(has_pairs ? S * L.P * 8 : 0);
+    // mixed precision on a uniform grid stores double-word phases (16 B)
+    // instead of FP64 frequencies (8 B)
+    L.phase_records = has_pairs && a->precision == MSP_PREC_MIXED && a->uniform;
+    off += align256(has_pairs ? S * L.P * (L.phase_records ? 16 : 8) : 0);
     L.snap_const = off;
     off += align256(S * 8);
     L.slot_first = off;
@@ -302,7 +306,7 @@ static Layout powder_layout(const msp_powder_args *a) {
     L.item_first = off;
     off += align256((size_t)(a->num_slots + 1) * 4);
     L.partial = off;
-    off += align256((size_t)L.max_items * L.T * 8);
+    off += align256((size_t)L.max_items * L.T * (L.phase_records ? 4 : 8));
     L.total = off;
     return L;
 }
@@ -366,7 +370,10 @@ int msp_powder_run(const msp_powder_args *a) {
         sa.fac_len = fac;
     }
     sa.pair_coef = ws + L.coef;
-    sa.pair_omega = reinterpret_cast<double *>(ws + L.omega);
+    sa.pair_omega = L.phase_records ? NULL : reinterpret_cast<double *>(ws + L.omega);
+    sa.pair_phase = L.phase_records ? reinterpret_cast<float4 *>(ws + L.omega) : NULL;
+    sa.t0 = a->t0;
+    sa.dt = a->dt;
     sa.snap_const = reinterpret_cast<double *>(ws + L.snap_const);
     sa.status = a->status;
 
@@ -383,7 +390,8 @@ int msp_powder_run(const msp_powder_args *a) {
     PhaseArgs pa;
     memset(&pa, 0, sizeof(pa));
     pa.pair_coef = ws + L.coef;
-    pa.pair_omega = reinterpret_cast<const double *>(ws + L.omega);
+    pa.pair_omega = L.phase_records ? NULL : reinterpret_cast<const double *>(ws + L.omega);
+    pa.pair_phase = L.phase_records ? reinterpret_cast<const float4 *>(ws + L.omega) : NULL;
     pa.P = L.P;
     pa.SB = L.SB;
     pa.slot_first = reinterpret_cast<int *>(ws + L.slot_first);
@@ -393,7 +401,8 @@ int msp_powder_run(const msp_powder_args *a) {
     pa.dt = a->dt;
     pa.num_times = L.T;
     pa.times = a->times;
-    pa.partial = reinterpret_cast<double *>(ws + L.partial);
+    pa.partial = L.phase_records ? NULL : reinterpret_cast<double *>(ws + L.partial);
+    pa.partial_f32 = L.phase_records ? reinterpret_cast<float *>(ws + L.partial) : NULL;
 
     rc = cuda_check(launch_schedule(a->slot, a->num_snap, a->num_slots, L.SB,
                                     a->mode != MSP_MODE_INTEGRAL,

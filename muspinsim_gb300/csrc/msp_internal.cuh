@@ -42,9 +42,14 @@ struct SnapArgs {
     double gammas[MSP_MAX_SPINS];
     int fac_len;
     double tau;
+    // time grid (uniform grids: t_k = t0 + k dt)
+    double t0, dt;
     // outputs
     void *pair_coef;     // num_snap * P of float2 / double2: (a_c, a_s)
-    double *pair_omega;  // num_snap * P
+    double *pair_omega;  // num_snap * P angular frequencies (FP64 path, arbitrary grids)
+    float4 *pair_phase;  // mixed path on a uniform grid instead of pair_omega:
+                         // (psi_hi, psi_lo, phi0_hi, phi0_lo), psi = w dt and
+                         // phi0 = w t0 reduced modulo 2 pi, as double-word floats
     double *snap_const;  // num_snap
     int *status;         // num_snap
 };
@@ -53,6 +58,7 @@ struct SnapArgs {
 struct PhaseArgs {
     const void *pair_coef;
     const double *pair_omega;
+    const float4 *pair_phase;  // see SnapArgs::pair_phase
     int P;             // pairs per snapshot
     int SB;            // snapshots per work item
     const int *slot_first;
@@ -62,6 +68,7 @@ struct PhaseArgs {
     int num_times;
     const double *times;  // NULL for uniform grids
     double *partial;      // max_items * num_times
+    float *partial_f32;   // mixed path on a uniform grid: FP32 partials instead
 };
 
 size_t snap_smem_bytes(int n, int mode, int precision, int fac_len);

@@ -183,6 +183,194 @@ __global__ void __launch_bounds__(128) msp_phase_uniform_kernel(PhaseArgs a) {
     }
 }
 
+// ---------------------------------------------------------------- FP32 path
+//
+// Mixed precision on a uniform grid.  Same tiling as above, two changes:
+//  * no FP64 on the GPU's slow FP64 pipe: the snapshot kernel stored each
+//    pair's phases psi = w dt and phi0 = w t0 already reduced modulo 2 pi as
+//    double-word floats (hi + lo); the chain phases 8^c psi are exact float
+//    scalings, reduced again in double-word arithmetic, then evaluated as
+//    sincosf(hi) turned by the small angle lo;
+//  * the outer products use the packed FP32x2 FMA of sm_100-class GPUs
+//    (fma.rn.f32x2): two accumulators of adjacent time columns per
+//    instruction, half the issue slots of scalar FMAs.
+
+#define MSP_TWOPI_HI 6.28318548202514648f      // fl32(2 pi)
+#define MSP_TWOPI_LO (-1.7484555314695172e-07f)  // 2 pi - MSP_TWOPI_HI
+
+// (h, l) <- (h + l) reduced modulo 2 pi, then renormalised (|l| <= half an
+// ulp of h).  k * MSP_TWOPI_HI is split exactly by an FMA and h - p is
+// exact (Sterbenz), so only the low-word sum rounds; the _rn intrinsics keep
+// the compiler from contracting the split.
+__device__ __forceinline__ void dw_reduce_2pi(float &h, float &l) {
+    const float k = rintf(h * 0.15915494309189535f);
+    const float p = __fmul_rn(k, MSP_TWOPI_HI);
+    const float e = fmaf(k, MSP_TWOPI_HI, -p);
+    const float t = __fsub_rn(h, p);
+    const float lo = (l - e) - k * MSP_TWOPI_LO;
+    const float s = __fadd_rn(t, lo);
+    const float bb = __fsub_rn(s, t);
+    l = __fadd_rn(__fsub_rn(t, __fsub_rn(s, bb)), __fsub_rn(lo, bb));
+    h = s;
+}
+
+// (h, l) += (h2, l2), the high sum split exactly (TwoSum).
+__device__ __forceinline__ void dw_add(float &h, float &l, float h2, float l2) {
+    const float s = __fadd_rn(h, h2);
+    const float bb = __fsub_rn(s, h);
+    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+    h = s;
+    l = l + l2 + err;
+}
+
+// e^{i (h + l)} for |l| <~ 1e-3: sincosf(h) turned by l, second order in l.
+__device__ __forceinline__ cx<float> dw_expi(float h, float l) {
+    float s, c;
+    sincosf(h, &s, &c);
+    const float cl = 1.0f - 0.5f * l * l;
+    return mk<float>(c * cl - s * l, s * cl + c * l);
+}
+
+__device__ __forceinline__ unsigned long long pk2(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+__device__ __forceinline__ void ffma2(unsigned long long &acc, unsigned long long a,
+                                      unsigned long long b) {
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(a), "l"(b));
+}
+
+__global__ void __launch_bounds__(128, 4) msp_phase_uniform_f32_kernel(PhaseArgs a) {
+    constexpr int K = 64, PS = 32;
+    __shared__ __align__(16) cx<float> Xs[PS][K];  // (x_re, -x_im)
+    __shared__ __align__(16) float Yr[PS][K];
+    __shared__ __align__(16) float Yi[PS][K];
+    __shared__ __align__(16) cx<float> pw[4][8][PS + 1];
+    __shared__ int s_range[2];
+
+    const int tid = threadIdx.x;
+    if (tid == 0) item_range(a, blockIdx.x, &s_range[0], &s_range[1]);
+    __syncthreads();
+    const int pbeg = s_range[0], pend = s_range[1];
+    if (pbeg < 0) return;
+
+    const int g = tid >> 6, lt = tid & 63;
+    const int ty = lt >> 3, tx = lt & 7;
+    const long long tile_base = (long long)blockIdx.y * (K * K);
+    const float tile_steps = (float)tile_base;  // exact: < 2^24
+    const float2 *coef = reinterpret_cast<const float2 *>(a.pair_coef);
+
+    unsigned long long acc[8][4];
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[r][j] = 0ull;
+
+    for (int pb = pbeg; pb < pend; pb += PS) {
+        const int np = (pend - pb) < PS ? (pend - pb) : PS;
+        {
+            // thread (chain c, pair i): e^{i 8^c psi} and its powers 0..7;
+            // chain 3 starts from the tile-start coefficient
+            // (a_c - i a_s) e^{i (phi0 + tile_base psi)}, so that X needs one
+            // product per entry
+            const int c = tid >> 5, i = tid & 31;
+            if (i < np) {
+                const float4 rec = a.pair_phase[pb + i];
+                const float sc = c == 0 ? 1.f : c == 1 ? 8.f : c == 2 ? 64.f : 512.f;
+                float h = rec.x * sc, l = rec.y * sc;  // exact power-of-two scaling
+                dw_reduce_2pi(h, l);
+                const cx<float> base = dw_expi(h, l);
+                cx<float> p = mk<float>(1.f, 0.f);
+                if (c == 3) {
+                    float th = rec.z, tl = rec.w;
+                    if (tile_base > 0) {
+                        const float ph = rec.x * tile_steps;
+                        float bh = ph, bl = fmaf(rec.x, tile_steps, -ph) + rec.y * tile_steps;
+                        dw_reduce_2pi(bh, bl);
+                        dw_add(th, tl, bh, bl);
+                        dw_reduce_2pi(th, tl);
+                    }
+                    const float2 cf = coef[pb + i];
+                    p = mk<float>(cf.x, -cf.y);
+                    if (th != 0.f || tl != 0.f) p = cmul(p, dw_expi(th, tl));
+                }
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    pw[c][r][i] = p;
+                    p = cmul(p, base);
+                }
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < np * 2 * K; e += 128) {
+            const int i = e >> 7, k = e & 127;
+            if (k < K) {
+                const cx<float> y = cmul(pw[1][k >> 3][i], pw[0][k & 7][i]);
+                Yr[i][k] = y.re;
+                Yi[i][k] = y.im;
+            } else {
+                const int kk = k - K;
+                const cx<float> x = cmul(pw[3][kk >> 3][i], pw[2][kk & 7][i]);
+                Xs[i][kk] = mk<float>(x.re, -x.im);
+            }
+        }
+        __syncthreads();
+        for (int i = g; i < np; i += 2) {
+            unsigned long long yr[4], yi[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                yr[j] = *reinterpret_cast<const unsigned long long *>(&Yr[i][2 * tx + 16 * j]);
+                yi[j] = *reinterpret_cast<const unsigned long long *>(&Yi[i][2 * tx + 16 * j]);
+            }
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const cx<float> x = Xs[i][ty + 8 * r];
+                const unsigned long long xr = pk2(x.re, x.re), xi = pk2(x.im, x.im);
+                // real-part products for the four column pairs first, so that
+                // no FMA waits on the one just issued
+#pragma unroll
+                for (int j = 0; j < 4; ++j) ffma2(acc[r][j], xr, yr[j]);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) ffma2(acc[r][j], xi, yi[j]);
+            }
+        }
+        __syncthreads();
+    }
+
+    // combine the two groups, then write FP32 partials (the cross-item sum
+    // in msp_reduce_kernel is FP64)
+    float *red = reinterpret_cast<float *>(&Xs[0][0]);  // K*K floats
+    if (g == 1) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float v0, v1;
+                asm("mov.b64 {%0, %1}, %2;" : "=f"(v0), "=f"(v1) : "l"(acc[r][j]));
+                const int k = (ty + 8 * r) * K + 2 * tx + 16 * j;
+                red[k] = v0;
+                red[k + 1] = v1;
+            }
+    }
+    __syncthreads();
+    if (g == 0) {
+        float *out = a.partial_f32 + (size_t)blockIdx.x * a.num_times;
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float v0, v1;
+                asm("mov.b64 {%0, %1}, %2;" : "=f"(v0), "=f"(v1) : "l"(acc[r][j]));
+                const int k = (ty + 8 * r) * K + 2 * tx + 16 * j;
+                const long long t = tile_base + k;
+                if (t < a.num_times) out[t] = v0 + red[k];
+                if (t + 1 < a.num_times) out[t + 1] = v1 + red[k + 1];
+            }
+    }
+}
+
 // Arbitrary time grids: one thread per sample, every pair's phase reduced in
 // FP64 and evaluated with sincos.
 template <typename T>
@@ -291,7 +479,10 @@ __global__ void __launch_bounds__(256) msp_reduce_kernel(PhaseArgs a,
     if (t < T) {
         double v = c;
         const int i0 = a.item_first[sl], i1 = a.item_first[sl + 1];
-        for (int it = i0; it < i1; ++it) v += a.partial[(size_t)it * T + t];
+        if (a.partial_f32)
+            for (int it = i0; it < i1; ++it) v += (double)a.partial_f32[(size_t)it * T + t];
+        else
+            for (int it = i0; it < i1; ++it) v += a.partial[(size_t)it * T + t];
         out[(size_t)sl * T + t] = v;
     }
 }
@@ -324,7 +515,7 @@ cudaError_t launch_phase(const PhaseArgs &a, int precision, int max_items, int u
     if (uniform) {
         dim3 grid(max_items, (a.num_times + 4095) / 4096);
         if (precision == MSP_PREC_MIXED)
-            msp_phase_uniform_kernel<float><<<grid, 128, 0, st>>>(a);
+            msp_phase_uniform_f32_kernel<<<grid, 128, 0, st>>>(a);
         else
             msp_phase_uniform_kernel<double><<<grid, 128, 0, st>>>(a);
     } else {

@@ -150,6 +150,22 @@ __device__ __forceinline__ void tri_index(int e, int &j, int &k) {
 
 __device__ __forceinline__ int pair_index(int j, int k) { return j * (j - 1) / 2 + k; }
 
+// Frequency record of pair o: the FP64 angular frequency w, or -- for the
+// mixed-precision phase kernel on a uniform grid -- the phases w dt and
+// w t0 reduced modulo 2 pi here in FP64 and stored as double-word floats,
+// so that the phase kernel needs no FP64 arithmetic.
+__device__ __forceinline__ void store_frequency(const SnapArgs &a, size_t o, double w) {
+    if (a.pair_phase) {
+        const double psi = reduce_2pi(w * a.dt);
+        const double ph0 = a.t0 == 0.0 ? 0.0 : reduce_2pi(w * a.t0);
+        const float psh = (float)psi, p0h = (float)ph0;
+        a.pair_phase[o] = make_float4(psh, (float)(psi - (double)psh), p0h,
+                                      (float)(ph0 - (double)p0h));
+    } else {
+        a.pair_omega[o] = w;
+    }
+}
+
 // H = Hsys + b . Z (FP64) into the Jacobi buffer (precision T, padded to m);
 // in MIXED mode also its exact split H = Hh + Hl into two FP32 matrices.
 template <typename T, bool REFINE>
@@ -445,7 +461,7 @@ __global__ void msp_snap_fast_kernel(SnapArgs a) {
             } else {
                 const size_t o = (size_t)sn * P + pair_index(j, k);
                 coef[o] = PairCoef<T>::make(scale * A, 0.0);
-                a.pair_omega[o] = 6.283185307179586476925 * (s.lam[j] - s.lam[k]);
+                store_frequency(a, o, 6.283185307179586476925 * (s.lam[j] - s.lam[k]));
             }
         }
         atomicAdd(&s.acc[0], diag_local);
@@ -694,7 +710,7 @@ __global__ void msp_snap_rho_kernel(SnapArgs a) {
                 } else {
                     const size_t o = (size_t)sn * P + pair_index(j, k);
                     coef[o] = PairCoef<T>::make(2.0 * scale * cr, 2.0 * scale * ci);
-                    a.pair_omega[o] = twopi * (s.lam[j] - s.lam[k]);
+                    store_frequency(a, o, twopi * (s.lam[j] - s.lam[k]));
                 }
             }
         }
