@@ -26,7 +26,7 @@ namespace msp {
 struct SnapLayout {
     size_t H, U, sn, cs, da, db, red, pp, pq, tab;  // Jacobi work
     size_t lam, acc, rank;                     // eigenvalues, reductions, sort
-    size_t Hh, Hl, Yl, SR, sd, corr, rd, lamf;  // refinement (MIXED)
+    size_t Hh, Hl, Yl, SR, sd, corr, rd, ed, lamf;  // refinement (MIXED)
     size_t fac, B2;                            // general path
     size_t total;
 };
@@ -59,7 +59,7 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
     L.lam = lay_take(off, m * 8);
     L.acc = lay_take(off, 2 * m * 8);
     L.rank = lay_take(off, m * 4);
-    L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = L.lamf = 0;
+    L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = L.ed = L.lamf = 0;
     if (refine) {
         L.Hh = lay_take(off, mm * 8);
         L.Hl = lay_take(off, mm * 8);
@@ -67,7 +67,8 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
         L.SR = lay_take(off, mm * 8);
         L.sd = lay_take(off, m * 8);
         L.corr = lay_take(off, m * 4);
-        L.rd = lay_take(off, m * 4);
+        L.rd = lay_take(off, m * 8);
+        L.ed = lay_take(off, m * 4);
         L.lamf = lay_take(off, m * 4);
     }
     L.fac = L.B2 = 0;
@@ -101,8 +102,8 @@ struct SnapSmem {
     double *lam, *acc;
     int *rank;
     cx<float> *Hh, *Hl, *Yl, *SR;
-    double *sd;
-    float *corr, *rd, *lamf;
+    double *sd, *rd;
+    float *corr, *ed, *lamf;
     cx<double> *fac;
     cx<T> *B2;
 };
@@ -131,7 +132,8 @@ __device__ __forceinline__ SnapSmem<T> snap_carve(char *base, int n, bool rho, i
     s.SR = REFINE ? reinterpret_cast<cx<float> *>(base + L.SR) : nullptr;
     s.sd = REFINE ? reinterpret_cast<double *>(base + L.sd) : nullptr;
     s.corr = REFINE ? reinterpret_cast<float *>(base + L.corr) : nullptr;
-    s.rd = REFINE ? reinterpret_cast<float *>(base + L.rd) : nullptr;
+    s.rd = REFINE ? reinterpret_cast<double *>(base + L.rd) : nullptr;
+    s.ed = REFINE ? reinterpret_cast<float *>(base + L.ed) : nullptr;
     s.lamf = REFINE ? reinterpret_cast<float *>(base + L.lamf) : nullptr;
     s.fac = rho ? reinterpret_cast<cx<double> *>(base + L.fac) : nullptr;
     s.B2 = rho ? reinterpret_cast<cx<T> *>(base + L.B2) : nullptr;
@@ -197,14 +199,25 @@ __device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
 // (columns) against H = Hh + Hl (Ogita & Aishima, Japan J. Indust. Appl.
 // Math. 35 (2018) 1007, Algorithm 1, Hermitian form):
 //   R = I - X^H X,  S = X^H H X,  l_i = S_ii / (1 - R_ii),
-//   E_ij = (S_ij + l_j R_ij) / (l_j - l_i)  (i != j, separated pair),
-//   E_ij = R_ij / 2  (i != j, |l_j - l_i| below the FP32 resolution),
-//   E_ii = R_ii / 2,   X <- X + X E.
-// H X, X^H H X and X^H X use double-word FP32 accumulation; X E is plain
-// FP32 (E is O(1e-6)).  Eigenvalues: l_i plus the second-order term
-// sum_j |S_ij + l_i R_ij|^2 / (l_i - l_j), in FP64.
-// Returns the largest |E_ij| of a separated pair (the size of the
-// first-order correction); s.rank[0] is its scratch.
+//   E_ij = (S_ij + l_j R_ij) / (l_j - l_i)  (i != j),
+//   E_ii = R_ii / 2,   X <- X + X E,
+// with eigenvalues l_i plus the second-order term
+// sum_j |S_ij + l_i R_ij|^2 / (l_i - l_j).  H X, X^H H X and X^H X use
+// double-word FP32 accumulation, 1 - R_ii and l_i are FP64; E, the
+// second-order terms and X E are FP32 (they are small corrections).
+//
+// Near-degenerate pairs: FP32 Jacobi leaves levels whose gap is within a
+// few FP32 resolutions of |H| mixed by angles up to ~0.5, where the
+// first-order E is no longer accurate and the iteration stalls or
+// diverges.  A pair whose first-order |E_ij| would exceed 1e-2 is instead
+// rotated exactly: the 2x2 Hermitian block [[l_i, c], [conj(c), l_j]],
+// c = S_ij + (l_i + l_j) / 2 R_ij (the coupling after first-order
+// orthonormalisation), is diagonalised by the Jacobi rotation
+// [[k, s], [-conj(s), k]], which enters E as E_ij = s + R_ij / 2,
+// E_ji = -conj(s) + conj(R_ij) / 2 and k - 1 on both diagonal entries;
+// the eigenvalues move by -/+ t |c|.
+// Returns the largest first-order |E_ij| or rotation |s| (the size of the
+// correction just applied); s.rank[0] is its scratch.
 __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1;
     cx<float> *X = s.w.U;
@@ -255,7 +268,7 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         }
         if (i == j) {
             s.sd[i] = (double)sr + (double)srl;
-            s.rd[i] = __fsub_rn(__fsub_rn(1.0f, gr), grl);  // 1 - G_ii, exact first step
+            s.rd[i] = (1.0 - (double)gr) - (double)grl;  // R_ii = 1 - G_ii
         } else {
             s.SR[i * ld + j] = mk<float>(sr + srl, si + sil);
             s.SR[j * ld + i] = mk<float>(-(gr + grl), -(gi + gil));  // R_ij = -G_ij
@@ -263,20 +276,19 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     }
     __syncthreads();
     for (int i = tid; i < n; i += nt) {
-        const double l = s.sd[i] / (1.0 - (double)s.rd[i]);
+        const double l = s.sd[i] / (1.0 - s.rd[i]);
         s.lam[i] = l;
         s.lamf[i] = (float)l;
         s.corr[i] = 0.f;
+        s.ed[i] = 0.f;
     }
     __syncthreads();
-    float lmax = 0.f;
-    for (int i = 0; i < n; ++i) lmax = fmaxf(lmax, fabsf(s.lamf[i]));
-    const float deg = 1e-7f * lmax + 1e-30f;
     // E in place of S/R; second-order eigenvalue terms.  Only the gap
     // l_j - l_i needs FP64 (a difference of nearly equal large numbers);
     // E, S, R and the second-order terms are small corrections, FP32 is
     // ample for them.
     const int nup = n * (n - 1) / 2;
+    float emax = 0.f;
     for (int e = tid; e < nup; e += nt) {
         // strict upper pairs (i < j): j = row of the packed strict triangle
         int j = (int)((sqrtf(8.0f * (float)e + 1.0f) + 1.0f) * 0.5f);
@@ -284,35 +296,57 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         while ((j + 1) * j / 2 <= e) ++j;
         const int i = e - j * (j - 1) / 2;  // 0 <= i < j
         const cx<float> S = s.SR[i * ld + j], R = s.SR[j * ld + i];
+        // only the gap needs FP64 (a difference of nearly equal large numbers)
         const float dl = (float)(s.lam[j] - s.lam[i]);
+        const float lj_f = s.lamf[j], li_f = s.lamf[i];
+        const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;  // S_ij + l_j R_ij
+        const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;  // S_ij + l_i R_ij
         cx<float> Eij, Eji;
-        if (fabsf(dl) > deg) {
-            // E_ij = (S_ij + l_j R_ij) / (l_j - l_i); E_ji = (S_ji + l_i R_ji) / (l_i - l_j)
+        if (fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) < 1e-2f * fabsf(dl)) {
+            // separated pair: E_ij = (S_ij + l_j R_ij) / (l_j - l_i),
+            // E_ji = (S_ji + l_i R_ji) / (l_i - l_j)
             const float inv = 1.0f / dl;
-            const float lj_f = s.lamf[j], li_f = s.lamf[i];
-            const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;
-            const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;
             Eij = mk<float>(br * inv, bi * inv);
             Eji = mk<float>(-ar * inv, ai * inv);
             // second order: |S_ij + l_i R_ij|^2 / (l_i - l_j) for l_i, and the mirror
             atomicAdd(&s.corr[i], -(ar * ar + ai * ai) * inv);
             atomicAdd(&s.corr[j], (br * br + bi * bi) * inv);
-            const float mag = fmaxf(fmaxf(fabsf(Eij.re), fabsf(Eij.im)),
-                                    fmaxf(fabsf(Eji.re), fabsf(Eji.im)));
-            atomicMax(&s.rank[0], __float_as_int(mag));  // non-negative: int order = float order
+            emax = fmaxf(emax, fmaxf(fmaxf(fabsf(Eij.re), fabsf(Eij.im)),
+                                     fmaxf(fabsf(Eji.re), fabsf(Eji.im))));
         } else {
-            Eij = mk<float>(0.5f * R.re, 0.5f * R.im);
-            Eji = mk<float>(0.5f * R.re, -0.5f * R.im);
+            // near-degenerate pair: exact rotation of the orthonormalised 2x2 block
+            const float cr = 0.5f * (ar + br), ci = 0.5f * (ai + bi);
+            const float mag = sqrtf(cr * cr + ci * ci);
+            float sr = 0.f, si = 0.f;
+            if (mag > 0.f) {
+                const float zeta = dl / (2.0f * mag);
+                const float t = fabsf(zeta) > 1e18f
+                                    ? 0.5f / zeta
+                                    : copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                const float q = sqrtf(1.0f + t * t);  // 1 / k
+                const float f = t / (q * mag);
+                sr = f * cr;
+                si = f * ci;
+                atomicAdd(&s.corr[i], -t * mag);
+                atomicAdd(&s.corr[j], t * mag);
+                const float km1 = -t * t / (q * (1.0f + q));  // k - 1 without cancellation
+                atomicAdd(&s.ed[i], km1);
+                atomicAdd(&s.ed[j], km1);
+            }
+            Eij = mk<float>(sr + 0.5f * R.re, si + 0.5f * R.im);
+            Eji = mk<float>(-sr + 0.5f * R.re, si - 0.5f * R.im);
+            emax = fmaxf(emax, fmaxf(fabsf(sr), fabsf(si)));
         }
         s.SR[i * ld + j] = Eij;
         s.SR[j * ld + i] = Eji;
     }
+    atomicMax(&s.rank[0], __float_as_int(emax));  // non-negative: int order = float order
     __syncthreads();
-    // X' = X + X E  (into Yh), E_ii = R_ii / 2
+    // X' = X + X E  (into Yh), E_ii = R_ii / 2 plus the rotations' k - 1
     for (int e = tid; e < n * n; e += nt) {
         const int k = FastDiv(n).div(e), j = e - k * n;
         const cx<float> xkj = X[k * ld + j];
-        const float hr = 0.5f * s.rd[j];
+        const float hr = (float)(0.5 * s.rd[j]) + s.ed[j];
         float ar = xkj.re + hr * xkj.re, ai = xkj.im + hr * xkj.im;
         for (int i = 0; i < n; ++i) {
             if (i == j) continue;
@@ -329,9 +363,9 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     }
     for (int i = tid; i < n; i += nt) s.lam[i] += (double)s.corr[i];
     __syncthreads();
-    const float emax = __int_as_float(s.rank[0]);
+    const float step = __int_as_float(s.rank[0]);
     __syncthreads();
-    return emax;
+    return step;
 }
 
 // Eigenvalues into lam[0..n): the Jacobi diagonal (FP64), or the refined
@@ -348,10 +382,10 @@ __device__ void eigenpairs<double, false>(SnapSmem<double> &s, int n, int m) {
 
 // One refinement step leaves an error of order E^2; a step whose largest
 // correction exceeds 2e-4 (a pair within ~1e3 FP32 resolutions, as at a
-// level anticrossing) is followed by another, at most three in all.
+// level anticrossing) is followed by another, at most four in all.
 template <>
 __device__ void eigenpairs<float, true>(SnapSmem<float> &s, int n, int m) {
-    for (int it = 0; it < 3; ++it)
+    for (int it = 0; it < 4; ++it)
         if (oa_refine(s, n, m) <= 2e-4f) break;
 }
 

@@ -193,3 +193,71 @@ def test_mixed_single_orientations():
         errs.append(np.abs(got - ref).max())
     print("mixed per-orientation max|dP|:", max(errs))
     assert max(errs) <= 5e-7
+
+
+# Snapshots of a dense ALC scan (dim 32, fields linspace(0, 1, 500) T along
+# z, 24 ZCW-style orientations) whose Hamiltonians have level pairs within
+# a few FP32 resolutions of |H| (gap / max|lambda| ~ 2e-7 .. 6e-7): FP32
+# Jacobi leaves them mixed by angles up to ~0.5.  (field index, orientation)
+NEAR_DEGENERATE = [(352, 21), (447, 20), (199, 12), (107, 17)]
+
+
+def _alc_scan():
+    from muspinsim_gb300 import quaternion as Q
+    from muspinsim_gb300 import workloads
+    from muspinsim_gb300.orientations import orientation_rows_to_quats
+
+    wl = workloads.config3(n_fields=500, n_orient=24)
+    qs, ws = orientation_rows_to_quats(wl.orientations)
+    return wl, qs, ws, Q
+
+
+def test_eigh_mixed_near_degenerate(K):
+    from muspinsim_gb300 import _lib
+
+    wl, qs, _, Q = _alc_scan()
+    sy = wl.system()
+    Hs, Z = sy.hamiltonian_matrix(), sy.zeeman_operators()
+    H = np.stack([Hs + np.einsum("a,aij->ij", Q.rotate(qs[o:o + 1], wl.fields[f])[0], Z)
+                  for f, o in NEAR_DEGENERATE])
+    ev, U, st = K.eigh(H, precision=_lib.PREC_MIXED)
+    ev, U, st = ev.cpu().numpy(), U.cpu().numpy(), st.cpu().numpy()
+    assert np.all(st == 0)
+    n = H.shape[1]
+    for b in range(H.shape[0]):
+        ref = np.linalg.eigvalsh(H[b])
+        scale = np.abs(ref).max()
+        assert np.diff(ref).min() < 1e-6 * scale  # the case is what it claims to be
+        assert np.abs(ev[b] - ref).max() <= 1e-12 * scale
+        assert np.abs(U[b].conj().T @ U[b] - np.eye(n)).max() <= 1e-6
+        assert np.abs(H[b] @ U[b] - U[b] * ev[b][None, :]).max() <= 1e-6 * scale
+
+
+def test_alc_integral_mixed_near_degenerate():
+    """Orientation-averaged ALC integrals at the fields of the near-degenerate
+    snapshots: mixed against FP64 and against the oracle."""
+    from muspinsim_gb300 import _lib, constants, kernels
+
+    wl, qs, ws, Q = _alc_scan()
+    sy = wl.system()
+    Hs, Z = sy.hamiltonian_matrix(), sy.zeeman_operators()
+    fields = sorted({f for f, _ in NEAR_DEGENERATE})
+    N = len(qs)
+    w = ws * (N / ws.sum()) / N
+    B = np.concatenate([Q.rotate(qs, wl.fields[f]) for f in fields])
+    P = np.tile(Q.rotate(qs, wl.polarization), (len(fields), 1))
+    W = np.tile(w, len(fields))
+    slot = np.repeat(np.arange(len(fields)), N).astype(np.int32)
+    out = {}
+    for prec in (_lib.PREC_MIXED, _lib.PREC_FP64):
+        out[prec], st = kernels.powder_run(
+            Hs.shape[0], Hs, Z, B, P, W, slot, len(fields), None, mode=_lib.MODE_INTEGRAL,
+            precision=prec, dims=list(sy.dimension), mu_index=sy.muon_index, gammas=sy.gammas,
+            tau=constants.MU_TAU)
+        assert int(st.max()) == 0
+    mixed = out[_lib.PREC_MIXED].cpu().numpy()
+    fp64 = out[_lib.PREC_FP64].cpu().numpy()
+    ref = np.array([oracle_powder(wl, field=wl.fields[f]) for f in fields])
+    print("near-degenerate ALC |mixed - fp64|:", np.abs(mixed - fp64))
+    assert np.abs(fp64 - ref).max() <= FP64_TOL
+    assert np.abs(mixed - ref).max() <= MIXED_TOL
