@@ -90,6 +90,28 @@ __device__ __forceinline__ void dw_acc(float &hi, float &lo, float a, float b) {
     lo = __fadd_rn(lo, __fadd_rn(err, e));
 }
 
+// Packed FP32 pairs (Blackwell f32x2 instructions): two lanes in one 64-bit
+// register, one instruction for both.
+__device__ __forceinline__ unsigned long long f32x2(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void split_f32x2(unsigned long long v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long fma_f32x2(unsigned long long a, unsigned long long b,
+                                                        unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ unsigned long long mul_f32x2(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 // Block-wide sum of two values; every thread receives the totals.  `red`
 // needs 2 * (blockDim.x / 32) entries of shared memory.
 template <typename T>

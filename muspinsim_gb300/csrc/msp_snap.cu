@@ -21,10 +21,12 @@
 
 namespace msp {
 
+static_assert(sizeof(JRot<float>) == 16 && sizeof(JRot<double>) == 32, "JRot layout");
+
 // ------------------------------------------------------------------ smem layout
 
 struct SnapLayout {
-    size_t H, U, sn, cs, da, db, red, pp, pq, tab;  // Jacobi work
+    size_t H, U, rot, dia, red, tab, diag;     // Jacobi work
     size_t lam, acc, rank;                     // eigenvalues, reductions, sort
     size_t Hh, Hl, Yl, SR, sd, corr, rd, ed, lamf;  // refinement (MIXED)
     size_t fac, B2;                            // general path
@@ -45,19 +47,19 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
     SnapLayout L;
     const size_t m = (size_t)(n + (n & 1));
     const size_t mm = m * (m + 1);  // leading dimension m + 1 (odd): no bank conflicts
+    // the two Jacobi buffers hold either a matrix with row stride m + 1 or
+    // the eigenvector planes with column stride jacobi_ldu(m)
+    const size_t mj = (size_t)jacobi_buffer((int)m);
     size_t off = 0;
-    L.H = lay_take(off, mm * 2 * esize);
-    L.U = lay_take(off, mm * 2 * esize);
-    L.sn = lay_take(off, (m / 2) * 2 * esize);
-    L.cs = lay_take(off, (m / 2) * esize);
-    L.da = lay_take(off, (m / 2) * esize);
-    L.db = lay_take(off, (m / 2) * esize);
+    L.H = lay_take(off, mj * 2 * esize);
+    L.U = lay_take(off, mj * 2 * esize);
+    L.rot = lay_take(off, 2 * (m / 2) * (esize == 4 ? 16 : 32));  // sizeof(JRot<T>)
+    L.dia = lay_take(off, 2 * m * esize);
     L.red = lay_take(off, 2 * (size_t)nwarps * esize);
-    L.pp = lay_take(off, (m / 2) * 4);
-    L.pq = lay_take(off, (m / 2) * 4);
-    L.tab = lay_take(off, (m / 2) * (m / 2 + 1) / 2 * 4);
+    L.tab = lay_take(off, (m / 2) * (m / 2 + 1) / 2 * 8);
+    L.diag = lay_take(off, m * esize);
     L.lam = lay_take(off, m * 8);
-    L.acc = lay_take(off, 2 * m * 8);
+    L.acc = lay_take(off, 2 * 8);
     L.rank = lay_take(off, m * 4);
     L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = L.ed = L.lamf = 0;
     if (refine) {
@@ -115,14 +117,11 @@ __device__ __forceinline__ SnapSmem<T> snap_carve(char *base, int n, bool rho, i
     SnapSmem<T> s;
     s.w.H = reinterpret_cast<cx<T> *>(base + L.H);
     s.w.U = reinterpret_cast<cx<T> *>(base + L.U);
-    s.w.sn = reinterpret_cast<cx<T> *>(base + L.sn);
-    s.w.cs = reinterpret_cast<T *>(base + L.cs);
-    s.w.da = reinterpret_cast<T *>(base + L.da);
-    s.w.db = reinterpret_cast<T *>(base + L.db);
+    s.w.rot = reinterpret_cast<JRot<T> *>(base + L.rot);
+    s.w.dia = reinterpret_cast<T *>(base + L.dia);
     s.w.red = reinterpret_cast<T *>(base + L.red);
-    s.w.pp = reinterpret_cast<int *>(base + L.pp);
-    s.w.pq = reinterpret_cast<int *>(base + L.pq);
-    s.w.tab = reinterpret_cast<unsigned *>(base + L.tab);
+    s.w.tab = reinterpret_cast<uint2 *>(base + L.tab);
+    s.w.diag = reinterpret_cast<T *>(base + L.diag);
     s.lam = reinterpret_cast<double *>(base + L.lam);
     s.acc = reinterpret_cast<double *>(base + L.acc);
     s.rank = reinterpret_cast<int *>(base + L.rank);
@@ -173,7 +172,7 @@ __device__ __forceinline__ void store_frequency(const SnapArgs &a, size_t o, dou
 template <typename T, bool REFINE>
 __device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
                                  const double *b, int n, int m, SnapSmem<T> &s) {
-    const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1;
+    const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1, ldh = jacobi_ldh(m);
     const double bx = b[0], by = b[1], bz = b[2];
     const size_t nn = (size_t)n * n;
     for (int e = tid; e < m * m; e += nt) {
@@ -185,7 +184,7 @@ __device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
             h.re = hs.re + bx * z0.re + by * z1.re + bz * z2.re;
             h.im = hs.im + bx * z0.im + by * z1.im + bz * z2.im;
         }
-        s.w.H[i * ld + j] = mk<T>((T)h.re, (T)h.im);
+        s.w.H[i * ldh + j] = mk<T>((T)h.re, (T)h.im);
         if (REFINE) {
             const float hr = (float)h.re, hi = (float)h.im;
             s.Hh[i * ld + j] = mk<float>(hr, hi);
@@ -375,8 +374,7 @@ __device__ void eigenpairs(SnapSmem<T> &s, int n, int m);
 
 template <>
 __device__ void eigenpairs<double, false>(SnapSmem<double> &s, int n, int m) {
-    const int ld = m + 1;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) s.lam[j] = s.w.H[j * ld + j].re;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) s.lam[j] = s.w.diag[j];
     __syncthreads();
 }
 
@@ -396,7 +394,7 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
                                 int max_sweeps, double *__restrict__ evals,
                                 cx<double> *__restrict__ evecs, int *__restrict__ status) {
     extern __shared__ __align__(16) char smem[];
-    const int m = n + (n & 1), ld = m + 1;
+    const int m = n + (n & 1), ld = m + 1, ldh = jacobi_ldh(m);
     SnapSmem<T> s = snap_carve<T, REFINE>(smem, n, false, 0);
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int bidx = blockIdx.x; bidx < batch; bidx += gridDim.x) {
@@ -405,7 +403,7 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
             const int i = FastDiv(m).div(e), j = e - i * m;
             cx<double> h = mk<double>(0.0, 0.0);
             if (i < n && j < n) h = Hb[(size_t)i * n + j];
-            s.w.H[i * ld + j] = mk<T>((T)h.re, (T)h.im);
+            s.w.H[i * ldh + j] = mk<T>((T)h.re, (T)h.im);
             if (REFINE) {
                 const float hr = (float)h.re, hi = (float)h.im;
                 s.Hh[i * ld + j] = mk<float>(hr, hi);
