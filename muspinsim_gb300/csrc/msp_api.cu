@@ -247,6 +247,8 @@ static int check_powder(const msp_powder_args *a) {
     if (a->num_snap < 0 || a->num_slots < 1)
         return fail(MSP_ERR_ARG, "msp_powder: num_snap=%d num_slots=%d", a->num_snap,
                     a->num_slots);
+    if (a->num_slots > 65535)
+        return fail(MSP_ERR_UNSUPPORTED, "msp_powder: num_slots=%d exceeds 65535", a->num_slots);
     if (a->mode != MSP_MODE_FAST && a->mode != MSP_MODE_EVOLVE && a->mode != MSP_MODE_INTEGRAL)
         return fail(MSP_ERR_ARG, "msp_powder: mode=%d", a->mode);
     if (a->precision != MSP_PREC_FP64 && a->precision != MSP_PREC_MIXED)

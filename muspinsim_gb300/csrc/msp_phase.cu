@@ -458,32 +458,46 @@ __global__ void msp_schedule_kernel(const int *__restrict__ slot, int S, int num
 }
 
 // out[slot][t] = sum of the slot's snapshot constants + its items' partials,
-// in a fixed order (deterministic).
-__global__ void __launch_bounds__(256) msp_reduce_kernel(PhaseArgs a,
-                                                         const double *__restrict__ snap_const,
-                                                         double *__restrict__ out, int T) {
-    __shared__ double red[16];
+// in a fixed order (deterministic).  A block covers 32 times of one slot:
+// warp w sums items w, w + 8, w + 16, ... (several loads in flight per
+// thread), then the 8 warp sums are added in warp order.
+#define MSP_REDUCE_WARPS 8
+__global__ void __launch_bounds__(32 * MSP_REDUCE_WARPS)
+    msp_reduce_kernel(PhaseArgs a, const double *__restrict__ snap_const,
+                      double *__restrict__ out, int T) {
+    __shared__ double red[MSP_REDUCE_WARPS][33];
     const int sl = blockIdx.y;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int s0 = a.slot_first[sl], s1 = a.slot_first[sl + 1];
     double c = 0.0;
     for (int s = s0 + tid; s < s1; s += blockDim.x) c += snap_const[s];
-    // block reduction (fixed tree: deterministic)
+    // block reduction of the constants (fixed tree: deterministic)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if ((tid & 31) == 0) red[tid >> 5] = c;
-    __syncthreads();
-    c = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) c += red[w];
-    const int t = blockIdx.x * blockDim.x + tid;
+    if (lane == 0) red[warp][32] = c;
+    const int t = blockIdx.x * 32 + lane;
+    double v = 0.0;
     if (t < T) {
-        double v = c;
         const int i0 = a.item_first[sl], i1 = a.item_first[sl + 1];
-        if (a.partial_f32)
-            for (int it = i0; it < i1; ++it) v += (double)a.partial_f32[(size_t)it * T + t];
-        else
-            for (int it = i0; it < i1; ++it) v += a.partial[(size_t)it * T + t];
-        out[(size_t)sl * T + t] = v;
+        if (a.partial_f32) {
+            const float *p = a.partial_f32 + t;
+#pragma unroll 4
+            for (int it = i0 + warp; it < i1; it += MSP_REDUCE_WARPS)
+                v += (double)p[(size_t)it * T];
+        } else {
+            const double *p = a.partial + t;
+#pragma unroll 4
+            for (int it = i0 + warp; it < i1; it += MSP_REDUCE_WARPS) v += p[(size_t)it * T];
+        }
+    }
+    red[warp][lane] = v;
+    __syncthreads();
+    if (warp == 0 && t < T) {
+        double cs = 0.0;
+        for (int w = 0; w < MSP_REDUCE_WARPS; ++w) cs += red[w][32];
+        double s = cs;
+        for (int w = 0; w < MSP_REDUCE_WARPS; ++w) s += red[w][lane];
+        out[(size_t)sl * T + t] = s;
     }
 }
 
@@ -531,8 +545,8 @@ cudaError_t launch_phase(const PhaseArgs &a, int precision, int max_items, int u
 cudaError_t launch_reduce(const PhaseArgs &a, const double *snap_const, double *out,
                           int num_times, cudaStream_t st) {
     if (a.num_slots <= 0) return cudaSuccess;
-    dim3 grid((num_times + 255) / 256, a.num_slots);
-    msp_reduce_kernel<<<grid, 256, 0, st>>>(a, snap_const, out, num_times);
+    dim3 grid((num_times + 31) / 32, a.num_slots);
+    msp_reduce_kernel<<<grid, 32 * MSP_REDUCE_WARPS, 0, st>>>(a, snap_const, out, num_times);
     return cudaGetLastError();
 }
 
