@@ -204,6 +204,54 @@ int msp_powder_run(const msp_powder_args *args);
  * results as msp_powder_run. */
 int msp_powder_run_static(const msp_powder_args *args);
 
+/* ---------------------------------------------------------------- adjoint
+ * Gradient of a scalar loss L through the fast-path powder average
+ * (K6).  The reference has no gradient: its fitting
+ * (muspinsim/fitting.py:67-179) re-runs ExperimentRunner per objective
+ * evaluation and differentiates by finite differences; this entry point
+ * returns dL/dHsys and dL/dB_lab for one upstream gradient dL/dP(t) of
+ * the msp_powder_run output (MSP_MODE_FAST arguments: muon first, T = inf).
+ *
+ * Per snapshot, P_s(t) = kappa_s Tr(S e^{2 pi i H t} S e^{-2 pi i H t}) with
+ * S = (p . sigma) (x) 1_d and kappa_s = wscale_s / (4 d).  Its derivative
+ * uses the Frechet derivative of the matrix exponential in the FP64
+ * eigenbasis (divided differences of e^{2 pi i lambda t}, their derivative
+ * for (near-)degenerate levels), so degenerate spectra need no special
+ * handling by the caller.  Gradients use the convention
+ * dL = Re sum_ij conj(G_ij) dH_ij (the PyTorch complex-gradient convention). */
+typedef struct msp_adjoint_args {
+    int n;                    /* Hilbert dimension, even, 2 .. MSP_MAX_DIM */
+    const double *Hsys;       /* n*n complex128 (MHz) */
+    const double *Z;          /* 3*n*n complex128 */
+    int num_snap;
+    const double *field;      /* num_snap*3 lab-frame field (T) */
+    const double *pol;        /* num_snap*3 lab-frame muon polarisation */
+    const double *wscale;     /* num_snap weights, as msp_powder_args */
+    const int *slot;          /* num_snap rows of grad_out, non-decreasing */
+    int num_slots;
+    const double *times;      /* num_times (ignored when uniform = 1) */
+    int num_times;
+    int uniform;              /* 1: t_k = t0 + k dt */
+    double t0, dt;
+    const double *grad_out;   /* num_slots*num_times: dL/dP */
+    double *grad_hsys;        /* out: n*n complex128, sum over snapshots of dL/dH_s */
+    double *grad_field;       /* out, optional (NULL): num_snap*3 dL/dfield */
+    int *status;              /* num_snap per-snapshot eigensolve status */
+    int max_sweeps;           /* Jacobi sweep cap, <= 0 selects 40 */
+    void *workspace;          /* >= msp_adjoint_workspace bytes, 256-byte aligned */
+    size_t workspace_bytes;
+    void *stream;             /* cudaStream_t */
+} msp_adjoint_args;
+
+/* Scratch bytes msp_adjoint_fast needs (no pointer is dereferenced). */
+int msp_adjoint_workspace(const msp_adjoint_args *args, size_t *bytes);
+
+/* Kernels: msp_assemble, msp_eigh (FP64), msp_adjoint_transform (per level
+ * pair: sum_t g(t) e^{2 pi i nu t} and its t-weighted form, FP64),
+ * msp_adjoint_snap (one CTA per snapshot: dL/dH_s, dL/db_s),
+ * msp_adjoint_sum (deterministic sum over snapshots). */
+int msp_adjoint_fast(const msp_adjoint_args *args);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,6 +73,35 @@ class PowderArgs(ctypes.Structure):
     ]
 
 
+class AdjointArgs(ctypes.Structure):
+    """Mirror of ``msp_adjoint_args`` (include/mspgpu.h)."""
+
+    _fields_ = [
+        ("n", ctypes.c_int),
+        ("Hsys", _c_dp),
+        ("Z", _c_dp),
+        ("num_snap", ctypes.c_int),
+        ("field", _c_dp),
+        ("pol", _c_dp),
+        ("wscale", _c_dp),
+        ("slot", _c_dp),
+        ("num_slots", ctypes.c_int),
+        ("times", _c_dp),
+        ("num_times", ctypes.c_int),
+        ("uniform", ctypes.c_int),
+        ("t0", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("grad_out", _c_dp),
+        ("grad_hsys", _c_dp),
+        ("grad_field", _c_dp),
+        ("status", _c_dp),
+        ("max_sweeps", ctypes.c_int),
+        ("workspace", _c_dp),
+        ("workspace_bytes", ctypes.c_size_t),
+        ("stream", _c_dp),
+    ]
+
+
 TIMER_STAGES = 4
 TIMER_STAGE_NAMES = ("snapshots", "schedule", "phase", "reduce")
 
@@ -117,6 +146,11 @@ _SIGNATURES = {
     ),
     "msp_powder_run": (ctypes.c_int, [ctypes.POINTER(PowderArgs)]),
     "msp_powder_run_static": (ctypes.c_int, [ctypes.POINTER(PowderArgs)]),
+    "msp_adjoint_workspace": (
+        ctypes.c_int,
+        [ctypes.POINTER(AdjointArgs), ctypes.POINTER(ctypes.c_size_t)],
+    ),
+    "msp_adjoint_fast": (ctypes.c_int, [ctypes.POINTER(AdjointArgs)]),
     "msp_timer_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
     "msp_timer_destroy": (ctypes.c_int, [_c_dp]),
     "msp_timer_read": (

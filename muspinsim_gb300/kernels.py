@@ -274,3 +274,53 @@ def powder_run(n, Hsys, Z, field, pol, wscale, slot, num_slots, times, mode=_lib
                       dims, mu_index, gammas, temperature, rho_fac, tau, max_sweeps)
     out = plan.run()
     return out, plan.status[:plan.num_snap]
+
+
+def adjoint_fast(n, Hsys, Z, field, pol, wscale, slot, num_slots, times, grad_out, max_sweeps=0,
+                 want_field=True):
+    """Gradient of L through the fast-path powder average (msp_adjoint_fast).
+
+    ``grad_out``: dL/dP, shape (num_slots, len(times)) (or (len(times),) for
+    one slot).  Returns (dL/dHsys (n, n) complex128, dL/dfield (S, 3) float64
+    or None, status (S,) int32), gradients in PyTorch's complex convention
+    dL = Re sum conj(G) dH."""
+    d = device()
+    a = _lib.AdjointArgs()
+    a.n = int(n)
+    Hs = dev(Hsys, torch.complex128)
+    Zd = dev(Z, torch.complex128)
+    F = dev(field, torch.float64).reshape(-1, 3)
+    Pl = dev(pol, torch.float64).reshape(-1, 3)
+    W = dev(wscale, torch.float64).reshape(-1)
+    Sl = dev(slot, torch.int32).reshape(-1)
+    S = F.shape[0]
+    th = times.detach().cpu().numpy() if isinstance(times, torch.Tensor) else np.asarray(times)
+    uni, t0, dt = uniform_grid(th)
+    Td = dev(th, torch.float64).reshape(-1)
+    g = dev(grad_out, torch.float64).reshape(int(num_slots), -1)
+    if g.shape[1] != Td.shape[0]:
+        raise ValueError("grad_out must have one row of len(times) values per slot")
+    gH = torch.empty((a.n, a.n), dtype=torch.complex128, device=d)
+    gF = torch.empty((S, 3), dtype=torch.float64, device=d) if want_field else None
+    status = torch.zeros((max(S, 1),), dtype=torch.int32, device=d)
+    a.Hsys, a.Z = Hs.data_ptr(), Zd.data_ptr()
+    a.num_snap = S
+    a.field, a.pol, a.wscale, a.slot = F.data_ptr(), Pl.data_ptr(), W.data_ptr(), Sl.data_ptr()
+    a.num_slots = int(num_slots)
+    a.times, a.num_times = Td.data_ptr(), Td.shape[0]
+    a.uniform, a.t0, a.dt = 1 if uni else 0, t0, dt
+    a.grad_out = g.data_ptr()
+    a.grad_hsys = gH.data_ptr()
+    a.grad_field = gF.data_ptr() if gF is not None else None
+    a.status = status.data_ptr()
+    a.max_sweeps = int(max_sweeps)
+    nbytes = ctypes.c_size_t(0)
+    lib = _lib.load()
+    _lib.check(lib.msp_adjoint_workspace(ctypes.byref(a), ctypes.byref(nbytes)),
+               "msp_adjoint_workspace")
+    ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device=d)
+    a.workspace = ws.data_ptr() + ((-ws.data_ptr()) % 256)
+    a.workspace_bytes = int(nbytes.value)
+    a.stream = torch.cuda.current_stream().cuda_stream
+    _lib.check(lib.msp_adjoint_fast(ctypes.byref(a)), "msp_adjoint_fast")
+    return gH, gF, status[:S]

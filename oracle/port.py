@@ -382,3 +382,63 @@ def powder_average(system, orientations, B, p, T, times, intrinsic_B=(0, 0, 0),
         r = snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y, nthreads)
         acc = r / N if acc is None else acc + r / N
     return acc
+
+
+# ---------------------------------------------------------------- gradient checker
+def fast_snapshot_grad(H, sig, d, times, g, w):
+    """dL/dH of L = sum_t g(t) * w * fast_evolve(H, sig, times, d)(t).
+
+    The reference has no gradient (its fits difference the simulation
+    numerically, muspinsim/fitting.py:67-179); this restates the derivative
+    of the fast-path formula (muspinsim/hamiltonian.py:166-217) written as
+    P(t) = kappa Tr(S V S V^H), V = exp(2 pi i H t), kappa = w / (4 d), via
+    the Frechet derivative of the exponential in the eigenbasis (divided
+    differences of exp(2 pi i l t); their derivative for equal levels).  It
+    is the checker of the CUDA adjoint and is itself pinned against central
+    finite differences of fast_evolve in the CPU tests.  Returns G with
+    dL = Re sum conj(G) dH."""
+    n = H.shape[0]
+    lam, U = np.linalg.eigh(H)
+    S = np.kron(sig, np.eye(d))
+    M = U.conj().T @ S @ U
+    t = np.asarray(times, dtype=float)
+    nu = np.subtract.outer(lam, lam).T                      # nu[a, b] = l_b - l_a
+    E = np.exp(2j * np.pi * nu[:, :, None] * t[None, None, :])
+    Gh = E @ g
+    Gd = (E * (2j * np.pi * t)[None, None, :]) @ g
+    tmax = np.abs(t).max()
+    gap = np.subtract.outer(lam, lam)                       # gap[b, c] = l_b - l_c
+    dd = np.abs(2 * np.pi * tmax * gap) > 1e-5
+    inv = np.where(dd, 1.0 / np.where(dd, gap, 1.0), 0.0)
+    # D[a, b, c]
+    D = np.where(dd[None], (Gh[:, :, None] - Gh[:, None, :]) * inv[None],
+                 0.5 * (Gd[:, :, None] + Gd[:, None, :]))
+    K = np.einsum("ca,ab,abc->bc", M, M, D)
+    kappa = w / (4.0 * d)
+    Gp = kappa * (np.conj(K) + K.T)
+    return U @ Gp @ U.conj().T
+
+
+def fast_powder_grad(system, orientations, B, p, times, g):
+    """dL/dHsys and dL/dB_lab (per orientation) of L = sum_t g(t) P(t) for
+    the fast-path powder_average (muon first, T = inf)."""
+    Hsys = system.hamiltonian()
+    Z = system.zeeman_operators()
+    qs = [orientation_quat(o) for o in orientations]
+    N = len(qs)
+    if N > 1:
+        norm = N / np.sum([w for _, w in qs])
+        qs = [(q, w * norm) for q, w in qs]
+    else:
+        qs = [(q, 1.0) for q, _ in qs]
+    d = system.n // system.dims[system.mu_i]
+    GH = np.zeros_like(Hsys)
+    GB = []
+    for q, w in qs:
+        Bl = quat_rotate(q, B)
+        pl = quat_rotate(q, p)
+        H = Hsys + np.einsum("a,aij->ij", Bl, Z)
+        G = fast_snapshot_grad(H, sigma_mu(pl), d, times, g, w / N)
+        GH += G
+        GB.append([np.real(np.sum(np.conj(G) * Z[a])) for a in range(3)])
+    return GH, np.array(GB)
