@@ -50,6 +50,7 @@ extern "C" {
 #define MSP_MODE_INTEGRAL 2 /* exponentially weighted time integral */
 
 #define MSP_MAX_DIM 64   /* largest Hilbert dimension of the Jacobi kernels */
+#define MSP_MAX_DIM_LARGE 1024 /* largest n of the Householder + QL path (FP64) */
 #define MSP_MAX_SPINS 16
 
 /* ---- library information ---------------------------------------------- */
@@ -73,6 +74,21 @@ int msp_assemble(const double *Hsys, const double *Z, const double *fields, int 
  * (muspinsim/spinop.py:51-82). */
 int msp_eigh_batched(const double *H, int n, int batch, int precision, int max_sweeps,
                      double *evals, double *evecs, int *status, void *stream);
+
+/* Scratch bytes msp_eigh_batched_ws needs for (n, batch): 0 for
+ * n <= MSP_MAX_DIM, else one working set per CTA of the large-n solver. */
+int msp_eigh_workspace(int n, int batch, size_t *bytes);
+
+/* msp_eigh_batched for 1 <= n <= MSP_MAX_DIM_LARGE.  n <= MSP_MAX_DIM runs
+ * the Jacobi kernels (workspace unused); larger n runs, in FP64 for both
+ * precisions, Householder tridiagonalisation + implicit-shift QL with
+ * eigenvector accumulation + back-transformation, one CTA per matrix with
+ * its working matrices in `workspace` (>= msp_eigh_workspace bytes,
+ * 256-byte aligned).  Same outputs and replaced reference code as
+ * msp_eigh_batched. */
+int msp_eigh_batched_ws(const double *H, int n, int batch, int precision, int max_sweeps,
+                        double *evals, double *evecs, int *status, void *workspace,
+                        size_t workspace_bytes, void *stream);
 
 /* out[b] = U[b]^dag M[b] U[b]  (adjoint = 0)  or  U[b] M[b] U[b]^dag
  * (adjoint = 1).  m_stride = complex elements between consecutive M

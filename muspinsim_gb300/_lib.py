@@ -30,6 +30,7 @@ MODE_EVOLVE = 1
 MODE_INTEGRAL = 2
 
 MAX_DIM = 64
+MAX_DIM_LARGE = 1024  # MSP_MAX_DIM_LARGE: Householder + QL path (FP64)
 STATIC_SCRATCH_BYTES = 32 << 20  # MSP_STATIC_SCRATCH_BYTES
 MAX_SPINS = 16
 
@@ -114,6 +115,13 @@ _SIGNATURES = {
     "msp_eigh_batched": (
         ctypes.c_int,
         [_c_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp, _c_dp, _c_dp, _c_dp],
+    ),
+    "msp_eigh_workspace": (
+        ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    "msp_eigh_batched_ws": (
+        ctypes.c_int,
+        [_c_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp, _c_dp, _c_dp, _c_dp,
+         ctypes.c_size_t, _c_dp],
     ),
     "msp_basis_change": (
         ctypes.c_int,

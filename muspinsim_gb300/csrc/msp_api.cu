@@ -78,6 +78,44 @@ int msp_eigh_batched(const double *H, int n, int batch, int precision, int max_s
                       "msp_eigh_batched");
 }
 
+int msp_eigh_workspace(int n, int batch, size_t *bytes) {
+    if (n < 1 || batch < 0 || bytes == NULL)
+        return fail(MSP_ERR_ARG, "msp_eigh_workspace: n=%d batch=%d", n, batch);
+    if (n > MSP_MAX_DIM_LARGE)
+        return fail(MSP_ERR_UNSUPPORTED, "msp_eigh_workspace: n=%d exceeds %d", n,
+                    MSP_MAX_DIM_LARGE);
+    *bytes = n <= MSP_MAX_DIM ? 0 : large_scratch_bytes(n, large_grid(batch));
+    return MSP_OK;
+}
+
+int msp_eigh_batched_ws(const double *H, int n, int batch, int precision, int max_sweeps,
+                        double *evals, double *evecs, int *status, void *workspace,
+                        size_t workspace_bytes, void *stream) {
+    if (n <= MSP_MAX_DIM)
+        return msp_eigh_batched(H, n, batch, precision, max_sweeps, evals, evecs, status, stream);
+    if (n > MSP_MAX_DIM_LARGE || batch < 0)
+        return fail(n > MSP_MAX_DIM_LARGE ? MSP_ERR_UNSUPPORTED : MSP_ERR_ARG,
+                    "msp_eigh_batched_ws: n=%d batch=%d", n, batch);
+    if (precision != MSP_PREC_FP64 && precision != MSP_PREC_MIXED)
+        return fail(MSP_ERR_ARG, "msp_eigh_batched_ws: precision=%d", precision);
+    if (batch == 0) return MSP_OK;
+    MSP_CHECK_PTR(H);
+    MSP_CHECK_PTR(evals);
+    MSP_CHECK_PTR(evecs);
+    MSP_CHECK_PTR(status);
+    const int grid = large_grid(batch);
+    const size_t need = large_scratch_bytes(n, grid);
+    if (workspace == NULL || workspace_bytes < need)
+        return fail(MSP_ERR_WORKSPACE, "msp_eigh_batched_ws: workspace %zu < %zu bytes",
+                    workspace_bytes, need);
+    if (reinterpret_cast<uintptr_t>(workspace) & 255)
+        return fail(MSP_ERR_ARG, "msp_eigh_batched_ws: workspace not 256-byte aligned");
+    return cuda_check(launch_eigh_large(H, n, batch, evals, evecs, status,
+                                        reinterpret_cast<double *>(workspace), grid,
+                                        (cudaStream_t)stream),
+                      "msp_eigh_batched_ws");
+}
+
 int msp_basis_change(const double *U, long long u_stride, const double *M, long long m_stride,
                      int n, int batch, int adjoint, double *out, void *stream) {
     if (n < 1 || batch < 0 || u_stride < 0 || m_stride < 0)
@@ -232,7 +270,7 @@ static cudaEvent_t *timer_slot(msp_timer *t) {
 // ---------------------------------------------------------------- powder pipeline
 
 struct Layout {
-    size_t coef, omega, snap_const, slot_first, item_first, partial, total;
+    size_t coef, omega, snap_const, slot_first, item_first, partial, large, total;
     int P, SB, max_items, T;
     bool phase_records;
 };
@@ -242,8 +280,12 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 static int check_powder(const msp_powder_args *a) {
     if (a == NULL) return fail(MSP_ERR_ARG, "msp_powder: args is NULL");
     if (a->n < 2) return fail(MSP_ERR_ARG, "msp_powder: n=%d", a->n);
-    if (a->n > MSP_MAX_DIM)
-        return fail(MSP_ERR_UNSUPPORTED, "msp_powder: n=%d exceeds %d", a->n, MSP_MAX_DIM);
+    if (a->n > MSP_MAX_DIM_LARGE)
+        return fail(MSP_ERR_UNSUPPORTED, "msp_powder: n=%d exceeds %d", a->n, MSP_MAX_DIM_LARGE);
+    if (a->n > MSP_MAX_DIM && a->mode != MSP_MODE_FAST)
+        return fail(MSP_ERR_UNSUPPORTED,
+                    "msp_powder: n=%d > %d runs the fast path only (muon first, T = inf)", a->n,
+                    MSP_MAX_DIM);
     if (a->num_snap < 0 || a->num_slots < 1)
         return fail(MSP_ERR_ARG, "msp_powder: num_snap=%d num_slots=%d", a->num_snap,
                     a->num_slots);
@@ -309,6 +351,8 @@ static Layout powder_layout(const msp_powder_args *a) {
     off += align256((size_t)(a->num_slots + 1) * 4);
     L.partial = off;
     off += align256((size_t)L.max_items * L.T * (L.phase_records ? 4 : 8));
+    L.large = off;
+    if (a->n > MSP_MAX_DIM) off += align256(large_scratch_bytes(a->n, large_grid(a->num_snap)));
     L.total = off;
     return L;
 }
@@ -378,14 +422,24 @@ int msp_powder_run(const msp_powder_args *a) {
     sa.dt = a->dt;
     sa.snap_const = reinterpret_cast<double *>(ws + L.snap_const);
     sa.status = a->status;
+    sa.coef_f32 = a->precision == MSP_PREC_MIXED;
 
-    const size_t smem = snap_smem_bytes(a->n, a->mode, a->precision, sa.fac_len);
-    if (smem > 227 * 1024)
-        return fail(MSP_ERR_UNSUPPORTED, "msp_powder_run: %zu bytes of shared memory needed", smem);
+    const bool large = a->n > MSP_MAX_DIM;
+    if (!large) {
+        const size_t smem = snap_smem_bytes(a->n, a->mode, a->precision, sa.fac_len);
+        if (smem > 227 * 1024)
+            return fail(MSP_ERR_UNSUPPORTED, "msp_powder_run: %zu bytes of shared memory needed",
+                        smem);
+    }
 
     cudaEvent_t *ev = timer_slot(a->timer);
     if (ev) cudaEventRecord(ev[0], st);
-    rc = cuda_check(launch_snapshots(sa, a->mode, a->precision, st), "msp_snap");
+    if (large && a->num_snap > 0)
+        rc = cuda_check(launch_large_fast(sa, reinterpret_cast<double *>(ws + L.large),
+                                          large_grid(a->num_snap), st),
+                        "msp_large_fast");
+    else
+        rc = cuda_check(launch_snapshots(sa, a->mode, a->precision, st), "msp_snap");
     if (rc != MSP_OK) return rc;
     if (ev) cudaEventRecord(ev[1], st);
 

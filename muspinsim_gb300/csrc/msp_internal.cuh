@@ -52,6 +52,7 @@ struct SnapArgs {
                          // phi0 = w t0 reduced modulo 2 pi, as double-word floats
     double *snap_const;  // num_snap
     int *status;         // num_snap
+    int coef_f32;        // n > 64 kernels: pair_coef holds float2 (MIXED) instead of double2
 };
 
 // Everything the phase-sum and reduction kernels read and write.
@@ -102,6 +103,14 @@ cudaError_t launch_evolve_phases(const double *evals, const double *rho, int n,
                                  cudaStream_t st);
 cudaError_t launch_integrate(const double *evals, const double *rho, const double *ops, int n,
                              int num_ops, double tau, double *out, cudaStream_t st);
+
+// n > 64 (msp_large.cu): FP64 Householder + QL eigensolver, one CTA per
+// matrix with `grid` CTAs, each owning large_scratch_bytes(n, 1) of scratch.
+cudaError_t launch_eigh_large(const double *H, int n, int batch, double *evals, double *evecs,
+                              int *status, double *scratch, int grid, cudaStream_t st);
+cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cudaStream_t st);
+size_t large_scratch_bytes(int n, int grid);
+int large_grid(int batch);
 
 // Work decomposition of the phase sum (host side).
 int phase_snaps_per_item(int num_snap, int P, int precision);

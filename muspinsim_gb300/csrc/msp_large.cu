@@ -1,0 +1,437 @@
+// Hermitian eigensolver for 64 < n <= MSP_MAX_DIM_LARGE (FP64), one CTA per
+// matrix, working matrices in global memory (one CTA per SM keeps them in
+// L2).  Replaces numpy.linalg.eigh in Hermitian.diag (muspinsim/spinop.py:
+// 51-82) where the shared-memory Jacobi does not fit:
+//   1. Householder tridiagonalisation of the lower triangle (H = Q T Q^H,
+//      T real symmetric tridiagonal, Q = H_0 H_1 ... H_{n-2},
+//      H_k = I - tau_k v_k v_k^H), LAPACK zhetd2 order;
+//   2. implicit-shift QL on T with the rotations accumulated into Z
+//      (T = Z diag(l) Z^T; the EISPACK tql2 iteration): robust for
+//      degenerate and clustered levels, orthogonal to working precision;
+//   3. back-transformation U = Q Z and ascending sort.
+// Parallelisation: warp-per-row matrix-vector products and elementwise
+// rank-2 updates (1), the QL rotations computed by one thread and applied to
+// all rows of Z by all threads (2), one column of U per thread (3).
+#include <math_constants.h>
+#include <stdio.h>
+
+#include "msp_internal.cuh"
+
+#define MSP_DBL_EPS 2.220446049250313080847e-16  // 2^-52
+
+namespace msp {
+
+int record_error(int code, const char *msg);
+
+// Per-CTA global scratch (doubles): A (2n^2), U (2n^2), Zt (n^2), d, e,
+// lam (n each), tau (2n).
+__host__ __device__ inline size_t large_scratch_doubles(int n) {
+    return (size_t)5 * n * n + 5 * (size_t)n + 64;
+}
+
+struct LargeScratch {
+    cx<double> *A, *U;
+    double *Zt, *d, *e, *lam;
+    cx<double> *tau;
+};
+
+__device__ __forceinline__ LargeScratch large_carve(double *base, int n) {
+    LargeScratch s;
+    s.A = reinterpret_cast<cx<double> *>(base);
+    s.U = s.A + (size_t)n * n;
+    s.Zt = reinterpret_cast<double *>(s.U + (size_t)n * n);
+    s.d = s.Zt + (size_t)n * n;
+    s.e = s.d + n;
+    s.lam = s.e + n;
+    s.tau = reinterpret_cast<cx<double> *>(s.lam + n);
+    return s;
+}
+
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    T t = 0;
+    for (int w = 0; w < nw; ++w) t += red[w];
+    __syncthreads();
+    return t;
+}
+
+// Shared memory: v, p (n complex each), qc, qs (n doubles each), red.
+__host__ __device__ inline size_t large_smem_bytes(int n, int threads) {
+    return (size_t)n * 16 * 2 + (size_t)n * 8 * 2 + (size_t)(threads / 32) * 16 + 64;
+}
+
+// Eigenpairs of the Hermitian matrix already in s.A (full, row-major):
+// ascending eigenvalues into s.lam, eigenvectors (columns) into s.U.
+// Returns MSP_ITEM_OK or MSP_ITEM_NOT_CONVERGED (QL iteration cap).
+__device__ int large_eigh(LargeScratch s, int n, char *smem) {
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const int nw = nt >> 5;
+    cx<double> *v = reinterpret_cast<cx<double> *>(smem);
+    cx<double> *p = v + n;
+    double *qc = reinterpret_cast<double *>(p + n);
+    double *qs = qc + n;
+    double *red = qs + n;
+    cx<double> *A = s.A;
+
+    // ---- 1. tridiagonalisation
+    for (int k = 0; k + 1 < n; ++k) {
+        const int m = n - k - 1;  // length of x = A[k+1.., k]
+        double xn2 = 0.0;
+        for (int i = 1 + tid; i < m; i += nt) xn2 += cabs2(A[(size_t)(k + 1 + i) * n + k]);
+        xn2 = block_sum(xn2, red);
+        const cx<double> alpha = A[(size_t)(k + 1) * n + k];
+        cx<double> tau = mk<double>(0.0, 0.0);
+        double beta = alpha.re;
+        const bool reflect = !(xn2 == 0.0 && alpha.im == 0.0);
+        if (reflect) {
+            beta = -copysign(sqrt(alpha.re * alpha.re + alpha.im * alpha.im + xn2), alpha.re);
+            tau = mk<double>((beta - alpha.re) / beta, -alpha.im / beta);
+            // v = x / (alpha - beta), v_0 = 1
+            const cx<double> den = mk<double>(alpha.re - beta, alpha.im);
+            const double dd = 1.0 / cabs2(den);
+            const cx<double> sc = mk<double>(den.re * dd, -den.im * dd);
+            for (int i = tid; i < m; i += nt)
+                v[i] = i == 0 ? mk<double>(1.0, 0.0) : cmul(A[(size_t)(k + 1 + i) * n + k], sc);
+        }
+        if (tid == 0) {
+            s.d[k] = A[(size_t)k * n + k].re;
+            s.e[k] = beta;
+            s.tau[k] = tau;
+        }
+        __syncthreads();
+        if (!reflect) continue;
+        // p = tau * A22 v  (warp per row)
+        for (int i = warp; i < m; i += nw) {
+            const cx<double> *row = A + (size_t)(k + 1 + i) * n + (k + 1);
+            double pr = 0.0, pi = 0.0;
+            for (int j = lane; j < m; j += 32) {
+                const cx<double> a = row[j], x = v[j];
+                pr += a.re * x.re - a.im * x.im;
+                pi += a.re * x.im + a.im * x.re;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                pr += __shfl_xor_sync(0xffffffffu, pr, o);
+                pi += __shfl_xor_sync(0xffffffffu, pi, o);
+            }
+            if (lane == 0) p[i] = cmul(tau, mk<double>(pr, pi));
+        }
+        __syncthreads();
+        // alpha2 = -1/2 tau (p^H v); w = p + alpha2 v (in p)
+        double hr = 0.0, hi = 0.0;
+        for (int i = tid; i < m; i += nt) {
+            const cx<double> c = cmulc(p[i], v[i]);  // conj(p_i) v_i
+            hr += c.re;
+            hi += c.im;
+        }
+        hr = block_sum(hr, red);
+        hi = block_sum(hi, red);
+        const cx<double> a2 = cscale(-0.5, cmul(tau, mk<double>(hr, hi)));
+        for (int i = tid; i < m; i += nt) p[i] = cadd(p[i], cmul(a2, v[i]));
+        __syncthreads();
+        // A22 -= v w^H + w v^H
+        for (int e = tid; e < m * m; e += nt) {
+            const int i = e / m, j = e - i * m;  // FastDiv is exact only for m^3 < 2^20
+            const cx<double> vi = v[i], wi = p[i], vj = v[j], wj = p[j];
+            cx<double> &a = A[(size_t)(k + 1 + i) * n + (k + 1 + j)];
+            const cx<double> t1 = cmul(vi, conj(wj)), t2 = cmul(wi, conj(vj));
+            a = mk<double>(a.re - t1.re - t2.re, a.im - t1.im - t2.im);
+        }
+        // keep v for the back-transformation (column k below the subdiagonal)
+        for (int i = 1 + tid; i < m; i += nt) A[(size_t)(k + 1 + i) * n + k] = v[i];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        s.d[n - 1] = A[(size_t)(n - 1) * n + (n - 1)].re;
+        s.e[n - 1] = 0.0;
+    }
+    // Z = I (column-major: Zt[col * n + row])
+    for (size_t e = tid; e < (size_t)n * n; e += nt) {
+        const int c = (int)(e / n), r = (int)(e - (size_t)c * n);
+        s.Zt[e] = r == c ? 1.0 : 0.0;
+    }
+    __syncthreads();
+
+    // ---- 2. QL with implicit shifts; e[i] couples d[i], d[i+1]
+    int status = MSP_ITEM_OK;
+    __shared__ int s_ctl[4];  // m, iteration flag, rotation count, status
+    __shared__ double s_f, s_tst;
+    if (tid == 0) {
+        s_f = 0.0;
+        s_tst = 0.0;
+        s_ctl[3] = MSP_ITEM_OK;
+    }
+    __syncthreads();
+    double *d = s.d, *e = s.e;
+    for (int l = 0; l < n; ++l) {
+        for (int iter = 0;; ++iter) {
+            if (tid == 0) {
+                if (iter == 0) s_tst = fmax(s_tst, fabs(d[l]) + fabs(e[l]));
+                int m = l;
+                while (m < n - 1 && fabs(e[m]) > MSP_DBL_EPS * s_tst) ++m;
+                s_ctl[0] = m;
+                s_ctl[1] = 0;
+                s_ctl[2] = 0;
+                if (m > l && iter < 60) {
+                    // one QL step on rows l..m; rotations (c, s) for i = m-1 .. l
+                    double g = d[l];
+                    double pp = (d[l + 1] - g) / (2.0 * e[l]);
+                    double r = hypot(pp, 1.0);
+                    d[l] = e[l] / (pp + copysign(r, pp));
+                    d[l + 1] = e[l] * (pp + copysign(r, pp));
+                    const double dl1 = d[l + 1];
+                    double h = g - d[l];
+                    for (int i = l + 2; i < n; ++i) d[i] -= h;
+                    s_f += h;
+                    pp = d[m];
+                    double c = 1.0, c2 = 1.0, c3 = 1.0, sn = 0.0, s2 = 0.0;
+                    const double el1 = e[l + 1];
+                    int cnt = 0;
+                    for (int i = m - 1; i >= l; --i) {
+                        c3 = c2;
+                        c2 = c;
+                        s2 = sn;
+                        g = c * e[i];
+                        h = c * pp;
+                        r = hypot(pp, e[i]);
+                        e[i + 1] = sn * r;
+                        sn = e[i] / r;
+                        c = pp / r;
+                        pp = c * d[i] - sn * g;
+                        d[i + 1] = h + sn * (c * g + sn * d[i]);
+                        qc[cnt] = c;
+                        qs[cnt] = sn;
+                        ++cnt;
+                    }
+                    pp = -sn * s2 * c3 * el1 * e[l] / dl1;
+                    e[l] = sn * pp;
+                    d[l] = c * pp;
+                    s_ctl[1] = 1;
+                    s_ctl[2] = cnt;
+                } else if (m > l) {
+                    s_ctl[3] = MSP_ITEM_NOT_CONVERGED;
+                }
+            }
+            __syncthreads();
+            if (!s_ctl[1]) break;
+            // apply the rotations to every row of Z: columns (i, i+1), i = m-1 .. l
+            {
+                const int m = s_ctl[0], cnt = s_ctl[2];
+                for (int row = tid; row < n; row += nt) {
+                    double hcarry = s.Zt[(size_t)m * n + row];  // Z[row][i+1] for i = m-1
+                    for (int q = 0; q < cnt; ++q) {
+                        const int i = m - 1 - q;
+                        const double zi = s.Zt[(size_t)i * n + row];
+                        const double c = qc[q], sn = qs[q];
+                        s.Zt[(size_t)(i + 1) * n + row] = sn * zi + c * hcarry;
+                        hcarry = c * zi - sn * hcarry;
+                    }
+                    s.Zt[(size_t)l * n + row] = hcarry;
+                }
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            d[l] += s_f;
+            e[l] = 0.0;
+        }
+        __syncthreads();
+    }
+    status = s_ctl[3];
+
+    // ---- 3. U = Q Z (complex), reflectors applied last to first; one column per thread
+    for (size_t x = tid; x < (size_t)n * n; x += nt) {
+        const int i = (int)(x / n), j = (int)(x - (size_t)i * n);
+        s.U[x] = mk<double>(s.Zt[(size_t)j * n + i], 0.0);
+    }
+    __syncthreads();
+    for (int k = n - 2; k >= 0; --k) {
+        const cx<double> tau = s.tau[k];
+        if (tau.re == 0.0 && tau.im == 0.0) continue;
+        const int m = n - k - 1;
+        for (int j = tid; j < n; j += nt) {
+            // s_j = v^H U[k+1.., j]; U[k+1.., j] -= tau v s_j
+            double sr = 0.0, si = 0.0;
+            for (int i = 0; i < m; ++i) {
+                const cx<double> vi = i == 0 ? mk<double>(1.0, 0.0) : A[(size_t)(k + 1 + i) * n + k];
+                const cx<double> u = s.U[(size_t)(k + 1 + i) * n + j];
+                sr += vi.re * u.re + vi.im * u.im;
+                si += vi.re * u.im - vi.im * u.re;
+            }
+            const cx<double> ts = cmul(tau, mk<double>(sr, si));
+            for (int i = 0; i < m; ++i) {
+                const cx<double> vi = i == 0 ? mk<double>(1.0, 0.0) : A[(size_t)(k + 1 + i) * n + k];
+                cx<double> &u = s.U[(size_t)(k + 1 + i) * n + j];
+                const cx<double> t = cmul(vi, ts);
+                u = mk<double>(u.re - t.re, u.im - t.im);
+            }
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < n; i += nt) s.lam[i] = d[i];
+    __syncthreads();
+    return status;
+}
+
+// ascending order of s.lam (ties by index): rank[j]
+__device__ __forceinline__ int large_rank(const double *lam, int n, int j) {
+    const double lj = lam[j];
+    int r = 0;
+    for (int k = 0; k < n; ++k) {
+        const double lk = lam[k];
+        r += (lk < lj) || (lk == lj && k < j);
+    }
+    return r;
+}
+
+__global__ void msp_eigh_large_kernel(const cx<double> *__restrict__ Hin, int n, int batch,
+                                      double *__restrict__ evals, cx<double> *__restrict__ evecs,
+                                      int *__restrict__ status, double *__restrict__ scratch) {
+    extern __shared__ __align__(16) char smem[];
+    LargeScratch s = large_carve(scratch + (size_t)blockIdx.x * large_scratch_doubles(n), n);
+    for (int b = blockIdx.x; b < batch; b += gridDim.x) {
+        const cx<double> *Hb = Hin + (size_t)b * n * n;
+        for (size_t x = threadIdx.x; x < (size_t)n * n; x += blockDim.x) s.A[x] = Hb[x];
+        __syncthreads();
+        const int st = large_eigh(s, n, smem);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const int r = large_rank(s.lam, n, j);
+            evals[(size_t)b * n + r] = s.lam[j];
+            cx<double> *V = evecs + (size_t)b * n * n;
+            for (int i = 0; i < n; ++i) V[(size_t)i * n + r] = s.U[(size_t)i * n + j];
+        }
+        if (threadIdx.x == 0) status[b] = st;
+        __syncthreads();
+    }
+}
+
+// Fast path per snapshot for n > 64 (muspinsim/hamiltonian.py:166-217), the
+// large-n counterpart of msp_snap_fast_kernel: H = Hsys + b . Z, eigenpairs,
+// M = U^H (sigma_p (x) 1_d) U, pair records and the constant part.
+__global__ void msp_large_fast_kernel(SnapArgs a, double *__restrict__ scratch) {
+    extern __shared__ __align__(16) char smem[];
+    const int n = a.n, d = n / 2, P = n * (n - 1) / 2;
+    LargeScratch s = large_carve(scratch + (size_t)blockIdx.x * large_scratch_doubles(n), n);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    __shared__ double red[32];
+    const size_t nn = (size_t)n * n;
+    for (int sn = blockIdx.x; sn < a.num_snap; sn += gridDim.x) {
+        const double bx = a.field[3 * (size_t)sn], by = a.field[3 * (size_t)sn + 1],
+                     bz = a.field[3 * (size_t)sn + 2];
+        for (size_t x = tid; x < nn; x += nt) {
+            const cx<double> hs = a.Hsys[x], z0 = a.Z[x], z1 = a.Z[nn + x], z2 = a.Z[2 * nn + x];
+            s.A[x] = mk<double>(hs.re + bx * z0.re + by * z1.re + bz * z2.re,
+                                hs.im + bx * z0.im + by * z1.im + bz * z2.im);
+        }
+        __syncthreads();
+        const int st = large_eigh(s, n, smem);
+        // W = (sigma_p (x) 1_d) U into A (free now)
+        const double px = a.pol[3 * (size_t)sn], py = a.pol[3 * (size_t)sn + 1],
+                     pz = a.pol[3 * (size_t)sn + 2];
+        for (size_t x = tid; x < nn; x += nt) {
+            const int i = (int)(x / n);
+            cx<double> val;
+            if (i < d) {
+                const cx<double> u0 = s.U[x], u1 = s.U[x + (size_t)d * n];
+                val = mk<double>(pz * u0.re + px * u1.re + py * u1.im,
+                                 pz * u0.im + px * u1.im - py * u1.re);
+            } else {
+                const cx<double> u0 = s.U[x - (size_t)d * n], u1 = s.U[x];
+                val = mk<double>(px * u0.re - py * u0.im - pz * u1.re,
+                                 px * u0.im + py * u0.re - pz * u1.im);
+            }
+            s.A[x] = val;
+        }
+        __syncthreads();
+        const double scale = 0.5 * a.wscale[sn] / (double)d;
+        double diag = 0.0;
+        // pairs j >= k: G = sum_i conj(U_ij) W_ik, A = |G|^2
+        const size_t ntri = (size_t)n * (n + 1) / 2;
+        for (size_t x = tid; x < ntri; x += nt) {
+            int j = (int)((sqrt(8.0 * (double)x + 1.0) - 1.0) * 0.5);
+            while ((size_t)(j + 1) * (j + 2) / 2 <= x) ++j;
+            while ((size_t)j * (j + 1) / 2 > x) --j;
+            const int k = (int)(x - (size_t)j * (j + 1) / 2);
+            double gr = 0.0, gi = 0.0;
+            for (int i = 0; i < n; ++i) {
+                const cx<double> u = s.U[(size_t)i * n + j], w = s.A[(size_t)i * n + k];
+                gr += u.re * w.re + u.im * w.im;
+                gi += u.re * w.im - u.im * w.re;
+            }
+            const double Am = gr * gr + gi * gi;
+            if (j == k) {
+                diag += Am;
+            } else {
+                const size_t o = (size_t)sn * P + (size_t)j * (j - 1) / 2 + k;
+                const double w = 6.283185307179586476925 * (s.lam[j] - s.lam[k]);
+                if (a.pair_phase) {
+                    reinterpret_cast<float2 *>(a.pair_coef)[o] = make_float2((float)(scale * Am), 0.f);
+                    const double psi = reduce_2pi(w * a.dt);
+                    const double ph0 = a.t0 == 0.0 ? 0.0 : reduce_2pi(w * a.t0);
+                    const float psh = (float)psi, p0h = (float)ph0;
+                    a.pair_phase[o] = make_float4(psh, (float)(psi - (double)psh), p0h,
+                                                  (float)(ph0 - (double)p0h));
+                } else {
+                    if (a.coef_f32)
+                        reinterpret_cast<float2 *>(a.pair_coef)[o] = make_float2((float)(scale * Am), 0.f);
+                    else
+                        reinterpret_cast<double2 *>(a.pair_coef)[o] = make_double2(scale * Am, 0.0);
+                    a.pair_omega[o] = w;
+                }
+            }
+        }
+        diag = block_sum(diag, red);
+        if (tid == 0) {
+            a.snap_const[sn] = scale * 0.5 * diag;
+            a.status[sn] = st;
+        }
+        __syncthreads();
+    }
+}
+
+int large_threads(int n) { return n <= 128 ? 256 : 512; }
+
+cudaError_t launch_eigh_large(const double *H, int n, int batch, double *evals, double *evecs,
+                              int *status, double *scratch, int grid, cudaStream_t st) {
+    const int threads = large_threads(n);
+    const size_t smem = large_smem_bytes(n, threads);
+    cudaError_t e = cudaFuncSetAttribute(msp_eigh_large_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    msp_eigh_large_kernel<<<grid, threads, smem, st>>>(
+        reinterpret_cast<const cx<double> *>(H), n, batch, evals,
+        reinterpret_cast<cx<double> *>(evecs), status, scratch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cudaStream_t st) {
+    const int threads = large_threads(a.n);
+    const size_t smem = large_smem_bytes(a.n, threads);
+    cudaError_t e = cudaFuncSetAttribute(msp_large_fast_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    msp_large_fast_kernel<<<grid, threads, smem, st>>>(a, scratch);
+    return cudaGetLastError();
+}
+
+size_t large_scratch_bytes(int n, int grid) { return large_scratch_doubles(n) * 8 * (size_t)grid; }
+
+// One CTA per SM (the working matrices of all CTAs then fit in L2), at most
+// one per matrix.
+int large_grid(int batch) {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    return batch < sms ? (batch > 0 ? batch : 1) : sms;
+}
+
+}  // namespace msp

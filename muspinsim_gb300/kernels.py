@@ -50,8 +50,17 @@ def eigh(H, precision=_lib.PREC_FP64, max_sweeps=0):
     evals = torch.empty((b, n), dtype=torch.float64, device=Hd.device)
     evecs = torch.empty((b, n, n), dtype=torch.complex128, device=Hd.device)
     status = torch.empty((b,), dtype=torch.int32, device=Hd.device)
-    _lib.call("msp_eigh_batched", ptr(Hd), n, b, int(precision), int(max_sweeps), ptr(evals),
-              ptr(evecs), ptr(status), stream())
+    if n <= _lib.MAX_DIM:
+        _lib.call("msp_eigh_batched", ptr(Hd), n, b, int(precision), int(max_sweeps), ptr(evals),
+                  ptr(evecs), ptr(status), stream())
+        return evals, evecs, status
+    # n > 64: Householder + QL in FP64 with caller scratch
+    nbytes = ctypes.c_size_t(0)
+    _lib.call("msp_eigh_workspace", n, b, ctypes.byref(nbytes))
+    ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device=Hd.device)
+    wp = ws.data_ptr() + ((-ws.data_ptr()) % 256)
+    _lib.call("msp_eigh_batched_ws", ptr(Hd), n, b, int(precision), int(max_sweeps), ptr(evals),
+              ptr(evecs), ptr(status), ctypes.c_void_p(wp), int(nbytes.value), stream())
     return evals, evecs, status
 
 

@@ -261,3 +261,67 @@ def test_alc_integral_mixed_near_degenerate():
     print("near-degenerate ALC |mixed - fp64|:", np.abs(mixed - fp64))
     assert np.abs(fp64 - ref).max() <= FP64_TOL
     assert np.abs(mixed - ref).max() <= MIXED_TOL
+
+
+@pytest.mark.parametrize("n", [65, 96, 128, 192])
+def test_eigh_large_random(K, n):
+    """n > 64: Householder + QL (FP64) for both precisions."""
+    from muspinsim_gb300 import _lib
+
+    rng = np.random.default_rng(300 + n)
+    H = np.stack([random_hermitian(rng, n) for _ in range(3)])
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):
+        ev, U, st = K.eigh(H, precision=prec)
+        ev, U, st = ev.cpu().numpy(), U.cpu().numpy(), st.cpu().numpy()
+        assert np.all(st == 0)
+        for b in range(H.shape[0]):
+            ref = np.linalg.eigvalsh(H[b])
+            scale = np.abs(ref).max()
+            assert np.abs(ev[b] - ref).max() <= 1e-12 * scale
+            rec = (U[b] * ev[b][None, :]) @ U[b].conj().T
+            assert np.abs(rec - H[b]).max() <= 1e-12 * scale
+            assert np.abs(U[b].conj().T @ U[b] - np.eye(n)).max() <= 1e-12
+
+
+def test_eigh_large_degenerate(K):
+    """Exactly repeated eigenvalues (clusters up to 40 levels)."""
+    rng = np.random.default_rng(77)
+    n = 96
+    lam = np.concatenate([np.full(40, -2.0), np.full(20, 0.5), rng.normal(size=36)])
+    Q, _ = np.linalg.qr(rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))
+    H = Q @ np.diag(lam) @ Q.conj().T
+    H = 0.5 * (H + H.conj().T)
+    ev, U, st = K.eigh(H[None])
+    ev, U = ev[0].cpu().numpy(), U[0].cpu().numpy()
+    assert int(st.max()) == 0
+    assert np.abs(ev - np.sort(lam)).max() <= 1e-12 * np.abs(lam).max()
+    assert np.abs(U.conj().T @ U - np.eye(n)).max() <= 1e-12
+    assert np.abs((U * ev) @ U.conj().T - H).max() <= 1e-12 * np.abs(lam).max()
+
+
+def _large_workload(n_orient=4, n_times=256):
+    """mu, e, 3 x 1H, 14N: dim 96, random anisotropic hyperfine, 14N EFG."""
+    from muspinsim_gb300 import workloads
+
+    rng = np.random.default_rng(96)
+    coup = [("hyperfine", {"i": 1}, workloads.random_hyperfine(rng))]
+    for i in (3, 4, 5, 6):
+        coup.append(("hyperfine", {"i": i}, workloads.random_hyperfine(rng)))
+    V = rng.normal(size=(3, 3))
+    V = 0.5 * (V + V.T)
+    coup.append(("quadrupolar", {"i": 6}, V - np.trace(V) / 3 * np.eye(3)))
+    return workloads.Workload(
+        name="mu_e_3H_N_dim96", spins=["mu", "e", "H", "H", "H", "N"], couplings=coup,
+        orientations=workloads.zcw_gen(n_orient),
+        fields=np.array([[0.0, 0.0, 0.01]]), polarization=np.array([0.0, 0.0, 1.0]),
+        times=np.linspace(0, 10, n_times))
+
+
+def test_powder_fast_large_vs_oracle():
+    wl = _large_workload()
+    assert int(np.prod(wl.system().dimension)) == 96
+    ref = oracle_powder(wl)
+    got = _gpu_powder(wl)
+    assert np.abs(got - ref).max() <= FP64_TOL
+    got = _gpu_powder(wl, "mixed")
+    assert np.abs(got - ref).max() <= MIXED_TOL

@@ -293,8 +293,13 @@ def test_capi_library_exports_header():
     assert lib.msp_version() >= 10000
     # argument validation needs no device
     a = _lib.PowderArgs()
-    a.n = 200
+    a.n = 2000
     nbytes = ctypes.c_size_t(0)
     assert lib.msp_powder_workspace(ctypes.byref(a), ctypes.byref(nbytes)) == _lib.MSP_ERR_UNSUPPORTED
     assert "exceeds" in _lib.last_error()
+    # n > 64 runs the fast path only
+    a.n = 200
+    a.mode = _lib.MODE_EVOLVE
+    assert lib.msp_powder_workspace(ctypes.byref(a), ctypes.byref(nbytes)) == _lib.MSP_ERR_UNSUPPORTED
+    assert "fast path only" in _lib.last_error()
     assert ctypes.sizeof(_lib.PowderArgs) > 0
