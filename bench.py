@@ -41,15 +41,18 @@ L2_BYTES = 129 * 1024 * 1024
 # 152 * 128 * 2 flop * SM clock.  MEASURED_PEAKS.json carries HBM and bf16
 # tensor figures only.
 SMS, FP32_FMA_PER_SM = 152, 128
-# dram bytes per launch of the dominant kernel from the committed ncu capture
-# (profiles/); None until captured
-DOMINANT_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) per snapshot of each stage's kernel, from an ncu
+# capture of the 10,000-orientation run (dram__bytes_read.sum +
+# dram__bytes_write.sum): 8.06 MB and 68.45 MB per launch over 10,000
+# snapshots.  Traffic scales with the
+# snapshot count (pair records and constants are per snapshot).
+TRAFFIC_PER_SNAPSHOT = {"snapshots": 8.06e6 / 1e4, "phase": 68.45e6 / 1e4}
 
 
 def parse_args():
     p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=60)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--orientations", type=int, default=10000)
@@ -120,25 +123,92 @@ def build_workload(args):
 # ---------------------------------------------------------------- clocks
 
 class ClockSampler:
-    """nvidia-smi samples during the timed region (read-only queries)."""
+    """SM clock and clock-event reasons sampled during the timed region.
 
+    Polls NVML (read-only queries through ctypes: no Python NVML package is
+    needed) every 5 ms from a thread; falls back to ``nvidia-smi -lms 200``
+    when NVML cannot be loaded."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index):
+        self.samples, self.max_mhz, self.reasons = [], None, set()
+        self.proc = self.thread = None
+        self.source = "none"
+        if self._start_nvml(gpu_index):
+            return
         self.path = tempfile.mktemp(suffix=".csv")
-        self.proc = None
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
                  "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=self.fh, stderr=subprocess.DEVNULL)
+            self.source = "nvidia-smi"
         except (OSError, FileNotFoundError):
             self.proc = None
 
+    def _start_nvml(self, gpu_index):
+        import ctypes
+        import threading
+
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return False
+            h = ctypes.c_void_p()
+            uuid = None
+            try:
+                import torch
+
+                uuid = str(getattr(torch.cuda.get_device_properties(gpu_index), "uuid", "") or "")
+            except Exception:
+                uuid = None
+            ok = False
+            if uuid:
+                key = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+                ok = lib.nvmlDeviceGetHandleByUUID(key.encode(), ctypes.byref(h)) == 0
+            if not ok and lib.nvmlDeviceGetHandleByIndex_v2(gpu_index, ctypes.byref(h)) != 0:
+                return False
+            mx = ctypes.c_uint(0)
+            if lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        except (OSError, AttributeError):
+            return False
+        self._stop = threading.Event()
+
+        def poll():
+            clk, rs = ctypes.c_uint(0), ctypes.c_ulonglong(0)
+            while not self._stop.is_set():
+                if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0:
+                    self.samples.append(float(clk.value))
+                if get_reasons(h, ctypes.byref(rs)) == 0:
+                    for bit, name in self.REASONS.items():
+                        if rs.value & bit:
+                            self.reasons.add(name)
+                self._stop.wait(0.005)
+
+        self.thread = threading.Thread(target=poll, daemon=True)
+        self.thread.start()
+        self.source = "nvml"
+        return True
+
     def stop(self):
+        if self.thread is not None:
+            self._stop.set()
+            self.thread.join(timeout=5)
+            if not self.samples:
+                return None
+            return {"sm_mhz": statistics.median(self.samples),
+                    "sm_max_mhz": self.max_mhz or max(self.samples),
+                    "reasons": sorted(self.reasons), "samples": len(self.samples),
+                    "source": self.source}
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -166,7 +236,7 @@ class ClockSampler:
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": self.source}
 
 
 # ---------------------------------------------------------------- CPU reference
@@ -364,7 +434,8 @@ def run_gb300(args, world, rank, local):
         "roofline": {
             "bound": "fp32-pipe", "kernel": kname, "achieved": achieved,
             "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-            "traffic": DOMINANT_TRAFFIC_BYTES,
+            "traffic": TRAFFIC_PER_SNAPSHOT.get(dom, 0.0) * S or None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, scaled per snapshot",
             "algorithmic": f"{'68 n^3 per snapshot' if dom == 'snapshots' else '(4 n^2 + 2) per sample'}",
             "peak_source": "nominal FP32 FMA pipe at sm_max_mhz (152 x 128 x 2 x 2070 MHz)",
             "tensor_frac_of_measured_bf16": achieved / peaks["bf16_tflops"] if peaks else None,
