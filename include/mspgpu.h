@@ -220,6 +220,100 @@ int msp_powder_run(const msp_powder_args *args);
  * results as msp_powder_run. */
 int msp_powder_run_static(const msp_powder_args *args);
 
+/* ---- heterogeneous batch: many spin systems of uneven dimension ----------
+ * The loop of ExperimentRunner.run / run_single with store_time_slice
+ * (muspinsim/experiment.py:358-498, muspinsim/simconfig.py:347-368) run for
+ * many spin systems at once, each reduced into its own output row, on the
+ * muon-first T = inf path (Hamiltonian.fast_evolve, muspinsim/hamiltonian.py:
+ * 166-217).  The reference runs one ExperimentRunner per system.
+ *
+ * Systems are grouped into size buckets (one per distinct n).  A bucket is
+ * one persistent snapshot launch over all its snapshots, the phase sum and a
+ * reduction; buckets run concurrently on plan-owned streams forked from and
+ * joined to the caller's stream.  n <= MSP_MAX_DIM runs the Jacobi kernels
+ * (both precisions), larger n the FP64 Householder + QL kernel. */
+
+/* Launch parameters for the systems of one dimension (e.g. an autotuner's
+ * choice).  Zero fields keep the library's default. */
+typedef struct msp_multi_tuning {
+    int n;              /* Hilbert dimension the entry applies to */
+    int snap_threads;   /* threads per snapshot CTA: multiple of 32, <= 512 */
+    int ctas_per_sm;    /* resident snapshot CTAs per SM of the persistent grid
+                           (capped by occupancy; n > 64: scratch per CTA) */
+    int snaps_per_item; /* snapshots per phase-sum work item (the FP32 partial
+                           sums still hold at most 1024 pairs) */
+} msp_multi_tuning;
+
+/* Sizes of a heterogeneous batch; all pointers are HOST pointers, read only
+ * during msp_multi_plan_create. */
+typedef struct msp_multi_desc {
+    int num_systems;
+    const int *sys_n;          /* num_systems Hilbert dimensions: even (muon first),
+                                  2 .. MSP_MAX_DIM_LARGE */
+    const int *sys_snap_first; /* num_systems + 1: system k owns snapshots
+                                  [sys_snap_first[k], sys_snap_first[k + 1]) */
+    int num_times;
+    int uniform;               /* 1: t_k = t0 + k dt */
+    double t0, dt;
+    int precision;             /* MSP_PREC_* */
+    int max_sweeps;            /* Jacobi sweep cap, <= 0 selects 40 */
+    long long max_pairs_per_chunk; /* pair records a bucket holds at once; larger
+                                      buckets run in chunks (0: 2^26) */
+    const msp_multi_tuning *tuning;
+    int num_tuning;
+} msp_multi_desc;
+
+/* Device buffers of one run. */
+typedef struct msp_multi_io {
+    const double *Hsys_all;  /* every system's Hsys back to back, system order:
+                                n_k^2 complex128 each */
+    const double *Z_all;     /* every system's Z_x, Z_y, Z_z back to back: 3 n_k^2
+                                complex128 each */
+    const double *field;     /* num_snap*3 lab-frame field incl. intrinsic (T) */
+    const double *pol;       /* num_snap*3 lab-frame muon polarisation */
+    const double *wscale;    /* num_snap: orientation weight / averaged count */
+    const double *times;     /* num_times (ignored when uniform = 1) */
+    double *out;             /* num_systems*num_times: row k = system k (overwritten) */
+    int *status;             /* num_snap per-snapshot status (MSP_ITEM_*) */
+    void *workspace;         /* >= msp_multi_workspace bytes, 256-byte aligned; holds
+                                the plan's tables and scratch during a run */
+    size_t workspace_bytes;
+} msp_multi_io;
+
+typedef struct msp_multi_plan msp_multi_plan;
+
+/* One size bucket of a plan (msp_multi_plan_info). */
+typedef struct msp_multi_bucket_info {
+    int n, num_systems;
+    long long num_snap;
+    int num_chunks;
+    int snap_threads;
+    int grid;            /* persistent snapshot CTAs (0 until the first run for n <= 64) */
+    int pairs_per_item;
+    int max_items;
+    size_t scratch_bytes;
+} msp_multi_bucket_info;
+
+/* Plans a batch: buckets, chunks, work tables and the workspace size.  Host
+ * work only; streams, events and a pinned copy of the tables are made by
+ * the first run, on the device current then (every later run must have the
+ * same device current). */
+int msp_multi_plan_create(const msp_multi_desc *desc, msp_multi_plan **plan);
+int msp_multi_plan_destroy(msp_multi_plan *plan);
+int msp_multi_workspace(const msp_multi_plan *plan, size_t *bytes);
+/* Buckets in launch order; writes at most `capacity` entries of info. */
+int msp_multi_plan_info(const msp_multi_plan *plan, int *num_buckets,
+                        msp_multi_bucket_info *info, int capacity);
+/* Enqueues the batch on `stream`: table upload, output clear, per bucket
+ * msp_snap_fast / msp_large_fast (persistent), msp_phase_*, msp_reduce.
+ * Runs of one plan must not overlap (they share its streams). */
+int msp_multi_run(msp_multi_plan *plan, const msp_multi_io *io, void *stream);
+/* msp_multi_run through a CUDA graph: the first call (and any call whose io
+ * pointers differ from the captured ones) captures the launch sequence on a
+ * plan-owned stream and instantiates it; every call launches the graph on
+ * `stream`. */
+int msp_multi_run_graph(msp_multi_plan *plan, const msp_multi_io *io, void *stream);
+
 /* ---------------------------------------------------------------- adjoint
  * Gradient of a scalar loss L through the fast-path powder average
  * (K6).  The reference has no gradient: its fitting

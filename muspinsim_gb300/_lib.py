@@ -103,6 +103,69 @@ class AdjointArgs(ctypes.Structure):
     ]
 
 
+class MultiTuning(ctypes.Structure):
+    """Mirror of ``msp_multi_tuning``."""
+
+    _fields_ = [
+        ("n", ctypes.c_int),
+        ("snap_threads", ctypes.c_int),
+        ("ctas_per_sm", ctypes.c_int),
+        ("snaps_per_item", ctypes.c_int),
+    ]
+
+
+class MultiDesc(ctypes.Structure):
+    """Mirror of ``msp_multi_desc`` (host pointers)."""
+
+    _fields_ = [
+        ("num_systems", ctypes.c_int),
+        ("sys_n", ctypes.POINTER(ctypes.c_int)),
+        ("sys_snap_first", ctypes.POINTER(ctypes.c_int)),
+        ("num_times", ctypes.c_int),
+        ("uniform", ctypes.c_int),
+        ("t0", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("precision", ctypes.c_int),
+        ("max_sweeps", ctypes.c_int),
+        ("max_pairs_per_chunk", ctypes.c_longlong),
+        ("tuning", ctypes.POINTER(MultiTuning)),
+        ("num_tuning", ctypes.c_int),
+    ]
+
+
+class MultiIO(ctypes.Structure):
+    """Mirror of ``msp_multi_io`` (device pointers)."""
+
+    _fields_ = [
+        ("Hsys_all", _c_dp),
+        ("Z_all", _c_dp),
+        ("field", _c_dp),
+        ("pol", _c_dp),
+        ("wscale", _c_dp),
+        ("times", _c_dp),
+        ("out", _c_dp),
+        ("status", _c_dp),
+        ("workspace", _c_dp),
+        ("workspace_bytes", ctypes.c_size_t),
+    ]
+
+
+class MultiBucketInfo(ctypes.Structure):
+    """Mirror of ``msp_multi_bucket_info``."""
+
+    _fields_ = [
+        ("n", ctypes.c_int),
+        ("num_systems", ctypes.c_int),
+        ("num_snap", ctypes.c_longlong),
+        ("num_chunks", ctypes.c_int),
+        ("snap_threads", ctypes.c_int),
+        ("grid", ctypes.c_int),
+        ("pairs_per_item", ctypes.c_int),
+        ("max_items", ctypes.c_int),
+        ("scratch_bytes", ctypes.c_size_t),
+    ]
+
+
 TIMER_STAGES = 4
 TIMER_STAGE_NAMES = ("snapshots", "schedule", "phase", "reduce")
 
@@ -159,6 +222,15 @@ _SIGNATURES = {
         [ctypes.POINTER(AdjointArgs), ctypes.POINTER(ctypes.c_size_t)],
     ),
     "msp_adjoint_fast": (ctypes.c_int, [ctypes.POINTER(AdjointArgs)]),
+    "msp_multi_plan_create": (
+        ctypes.c_int, [ctypes.POINTER(MultiDesc), ctypes.POINTER(ctypes.c_void_p)]),
+    "msp_multi_plan_destroy": (ctypes.c_int, [_c_dp]),
+    "msp_multi_workspace": (ctypes.c_int, [_c_dp, ctypes.POINTER(ctypes.c_size_t)]),
+    "msp_multi_plan_info": (
+        ctypes.c_int,
+        [_c_dp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(MultiBucketInfo), ctypes.c_int]),
+    "msp_multi_run": (ctypes.c_int, [_c_dp, ctypes.POINTER(MultiIO), _c_dp]),
+    "msp_multi_run_graph": (ctypes.c_int, [_c_dp, ctypes.POINTER(MultiIO), _c_dp]),
     "msp_timer_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
     "msp_timer_destroy": (ctypes.c_int, [_c_dp]),
     "msp_timer_read": (

@@ -271,7 +271,7 @@ static cudaEvent_t *timer_slot(msp_timer *t) {
 
 struct Layout {
     size_t coef, omega, snap_const, slot_first, item_first, partial, large, total;
-    int P, SB, max_items, T;
+    int P, IP, max_items, T;
     bool phase_records;
 };
 
@@ -332,8 +332,8 @@ static Layout powder_layout(const msp_powder_args *a) {
     L.T = a->mode == MSP_MODE_INTEGRAL ? 1 : a->num_times;
     L.P = a->n * (a->n - 1) / 2;
     const int has_pairs = a->mode != MSP_MODE_INTEGRAL;
-    L.SB = phase_snaps_per_item(a->num_snap, L.P, a->precision);
-    L.max_items = has_pairs ? phase_max_items(a->num_snap, a->num_slots, L.SB) : 0;
+    L.IP = phase_pairs_per_item(a->num_snap, L.P, a->precision);
+    L.max_items = has_pairs ? phase_max_items(a->num_snap, a->num_slots, L.P, L.IP) : 0;
     const size_t ce = a->precision == MSP_PREC_MIXED ? 8 : 16;
     size_t off = 0;
     L.coef = off;
@@ -449,7 +449,7 @@ int msp_powder_run(const msp_powder_args *a) {
     pa.pair_omega = L.phase_records ? NULL : reinterpret_cast<const double *>(ws + L.omega);
     pa.pair_phase = L.phase_records ? reinterpret_cast<const float4 *>(ws + L.omega) : NULL;
     pa.P = L.P;
-    pa.SB = L.SB;
+    pa.IP = L.IP;
     pa.slot_first = reinterpret_cast<int *>(ws + L.slot_first);
     pa.item_first = reinterpret_cast<int *>(ws + L.item_first);
     pa.num_slots = a->num_slots;
@@ -460,7 +460,7 @@ int msp_powder_run(const msp_powder_args *a) {
     pa.partial = L.phase_records ? NULL : reinterpret_cast<double *>(ws + L.partial);
     pa.partial_f32 = L.phase_records ? reinterpret_cast<float *>(ws + L.partial) : NULL;
 
-    rc = cuda_check(launch_schedule(a->slot, a->num_snap, a->num_slots, L.SB,
+    rc = cuda_check(launch_schedule(a->slot, a->num_snap, a->num_slots, L.P, L.IP,
                                     a->mode != MSP_MODE_INTEGRAL,
                                     reinterpret_cast<int *>(ws + L.slot_first),
                                     reinterpret_cast<int *>(ws + L.item_first), a->status, st),

@@ -53,7 +53,46 @@ struct SnapArgs {
     double *snap_const;  // num_snap
     int *status;         // num_snap
     int coef_f32;        // n > 64 kernels: pair_coef holds float2 (MIXED) instead of double2
+    // Heterogeneous batches (msp_multi_*): when num_seg > 0 the launch's
+    // snapshots form num_seg segments; snapshot sn of segment j
+    // (seg_first[j] <= sn < seg_first[j + 1]) reads its field, polarisation
+    // and weight, and writes its status, at global snapshot
+    // seg_g0[j] + sn - seg_first[j], and its system's Hsys / Z start
+    // seg_hoff[j] / 3 seg_hoff[j] complex entries into Hsys / Z.  Pair
+    // records and snap_const stay indexed by sn.
+    int num_seg;
+    const int *seg_first;
+    const int *seg_g0;
+    const long long *seg_hoff;
 };
+
+// Global snapshot index and system matrices of launch-local snapshot sn.
+struct SnapSource {
+    int g;
+    const cx<double> *Hsys, *Z;
+};
+
+__device__ __forceinline__ SnapSource snap_source(const SnapArgs &a, int sn) {
+    SnapSource r;
+    r.g = sn;
+    r.Hsys = a.Hsys;
+    r.Z = a.Z;
+    if (a.num_seg > 0) {
+        int lo = 0, hi = a.num_seg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.seg_first[mid] <= sn)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        r.g = a.seg_g0[lo] + (sn - a.seg_first[lo]);
+        const long long o = a.seg_hoff[lo];
+        r.Hsys = a.Hsys + o;
+        r.Z = a.Z + 3 * o;
+    }
+    return r;
+}
 
 // Everything the phase-sum and reduction kernels read and write.
 struct PhaseArgs {
@@ -61,7 +100,7 @@ struct PhaseArgs {
     const double *pair_omega;
     const float4 *pair_phase;  // see SnapArgs::pair_phase
     int P;             // pairs per snapshot
-    int SB;            // snapshots per work item
+    int IP;            // pairs per work item (a work item never straddles two slots)
     const int *slot_first;
     const int *item_first;
     int num_slots;
@@ -70,10 +109,17 @@ struct PhaseArgs {
     const double *times;  // NULL for uniform grids
     double *partial;      // max_items * num_times
     float *partial_f32;   // mixed path on a uniform grid: FP32 partials instead
+    const int *slot_row;  // reduce: output row of each slot (NULL: row = slot)
+    int accumulate;       // reduce: out += sum instead of out = sum
 };
 
 size_t snap_smem_bytes(int n, int mode, int precision, int fac_len);
-cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStream_t st);
+cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStream_t st,
+                             int threads = 0, int grid = 0);
+// Threads per CTA of the snapshot kernels when the caller gives none.
+int snap_default_threads(int n);
+// CTAs of one snapshot kernel that fit on one SM with `threads` threads.
+int snap_occupancy(int n, int mode, int precision, int threads);
 cudaError_t launch_eigh(const double *H, int n, int batch, int precision, int max_sweeps,
                         double *evals, double *evecs, int *status, cudaStream_t st);
 cudaError_t launch_assemble(const double *Hsys, const double *Z, const double *fields, int n,
@@ -82,7 +128,7 @@ cudaError_t launch_basis_change(const double *U, long long u_stride, const doubl
                                 long long m_stride, int n, int batch, int adjoint, double *out,
                                 cudaStream_t st);
 
-cudaError_t launch_schedule(const int *slot, int num_snap, int num_slots, int SB,
+cudaError_t launch_schedule(const int *slot, int num_snap, int num_slots, int P, int IP,
                             int count_items, int *slot_first, int *item_first, int *status,
                             cudaStream_t st);
 cudaError_t launch_phase(const PhaseArgs &a, int precision, int max_items, int uniform,
@@ -108,12 +154,18 @@ cudaError_t launch_integrate(const double *evals, const double *rho, const doubl
 // matrix with `grid` CTAs, each owning large_scratch_bytes(n, 1) of scratch.
 cudaError_t launch_eigh_large(const double *H, int n, int batch, double *evals, double *evecs,
                               int *status, double *scratch, int grid, cudaStream_t st);
-cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cudaStream_t st);
+cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cudaStream_t st,
+                              int threads = 0);
+int large_threads(int n);
 size_t large_scratch_bytes(int n, int grid);
 int large_grid(int batch);
 
-// Work decomposition of the phase sum (host side).
+// Work decomposition of the phase sum (host side).  A work item sums at
+// most MSP_F32_ITEM_PAIRS pairs in FP32 (mixed precision): longer FP32
+// running sums lose ~1e-6 of P(t) to rounding at n ~ 100.
+#define MSP_F32_ITEM_PAIRS 1024
 int phase_snaps_per_item(int num_snap, int P, int precision);
-int phase_max_items(int num_snap, int num_slots, int SB);
+int phase_pairs_per_item(int num_snap, int P, int precision);
+int phase_max_items(int num_snap, int num_slots, int P, int IP);
 
 }  // namespace msp

@@ -322,18 +322,19 @@ __global__ void msp_large_fast_kernel(SnapArgs a, double *__restrict__ scratch) 
     __shared__ double red[32];
     const size_t nn = (size_t)n * n;
     for (int sn = blockIdx.x; sn < a.num_snap; sn += gridDim.x) {
-        const double bx = a.field[3 * (size_t)sn], by = a.field[3 * (size_t)sn + 1],
-                     bz = a.field[3 * (size_t)sn + 2];
+        const SnapSource src = snap_source(a, sn);
+        const size_t g = (size_t)src.g;
+        const double bx = a.field[3 * g], by = a.field[3 * g + 1], bz = a.field[3 * g + 2];
         for (size_t x = tid; x < nn; x += nt) {
-            const cx<double> hs = a.Hsys[x], z0 = a.Z[x], z1 = a.Z[nn + x], z2 = a.Z[2 * nn + x];
+            const cx<double> hs = src.Hsys[x], z0 = src.Z[x], z1 = src.Z[nn + x],
+                             z2 = src.Z[2 * nn + x];
             s.A[x] = mk<double>(hs.re + bx * z0.re + by * z1.re + bz * z2.re,
                                 hs.im + bx * z0.im + by * z1.im + bz * z2.im);
         }
         __syncthreads();
         const int st = large_eigh(s, n, smem);
         // W = (sigma_p (x) 1_d) U into A (free now)
-        const double px = a.pol[3 * (size_t)sn], py = a.pol[3 * (size_t)sn + 1],
-                     pz = a.pol[3 * (size_t)sn + 2];
+        const double px = a.pol[3 * g], py = a.pol[3 * g + 1], pz = a.pol[3 * g + 2];
         for (size_t x = tid; x < nn; x += nt) {
             const int i = (int)(x / n);
             cx<double> val;
@@ -349,7 +350,7 @@ __global__ void msp_large_fast_kernel(SnapArgs a, double *__restrict__ scratch) 
             s.A[x] = val;
         }
         __syncthreads();
-        const double scale = 0.5 * a.wscale[sn] / (double)d;
+        const double scale = 0.5 * a.wscale[g] / (double)d;
         double diag = 0.0;
         // pairs j >= k: G = sum_i conj(U_ij) W_ik, A = |G|^2
         const size_t ntri = (size_t)n * (n + 1) / 2;
@@ -389,7 +390,7 @@ __global__ void msp_large_fast_kernel(SnapArgs a, double *__restrict__ scratch) 
         diag = block_sum(diag, red);
         if (tid == 0) {
             a.snap_const[sn] = scale * 0.5 * diag;
-            a.status[sn] = st;
+            a.status[g] = st;
         }
         __syncthreads();
     }
@@ -410,8 +411,9 @@ cudaError_t launch_eigh_large(const double *H, int n, int batch, double *evals, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cudaStream_t st) {
-    const int threads = large_threads(a.n);
+cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cudaStream_t st,
+                              int threads) {
+    if (threads <= 0) threads = large_threads(a.n);
     const size_t smem = large_smem_bytes(a.n, threads);
     cudaError_t e = cudaFuncSetAttribute(msp_large_fast_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

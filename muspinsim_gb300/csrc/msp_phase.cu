@@ -39,7 +39,8 @@ __device__ __forceinline__ void sincos_t(double x, float *s, float *c) {
 }
 
 // Pair range [begin, end) of work item `item`; begin = -1 when the item does
-// not exist.  item_first / slot_first are num_slots + 1 prefix arrays.
+// not exist.  item_first / slot_first are num_slots + 1 prefix arrays; the
+// items of a slot cover its pairs in runs of IP.
 __device__ __forceinline__ void item_range(const PhaseArgs &a, int item, int *b, int *e) {
     const int total = a.item_first[a.num_slots];
     if (item >= total) {
@@ -55,11 +56,11 @@ __device__ __forceinline__ void item_range(const PhaseArgs &a, int item, int *b,
         else
             hi = mid - 1;
     }
-    const int sb = a.slot_first[lo] + (item - a.item_first[lo]) * a.SB;
-    int se = sb + a.SB;
-    if (se > a.slot_first[lo + 1]) se = a.slot_first[lo + 1];
-    *b = sb * a.P;
-    *e = se * a.P;
+    const int pb = a.slot_first[lo] * a.P + (item - a.item_first[lo]) * a.IP;
+    const int slot_end = a.slot_first[lo + 1] * a.P;
+    const int pe = pb + a.IP;
+    *b = pb;
+    *e = pe < slot_end ? pe : slot_end;
 }
 
 template <typename T>
@@ -410,11 +411,11 @@ __global__ void __launch_bounds__(256) msp_phase_direct_kernel(PhaseArgs a) {
 }
 
 // Slot bookkeeping: first snapshot of every output row, and the prefix of
-// work items (chunks of SB snapshots, never straddling two rows).  A slot
+// work items (runs of IP pairs, never straddling two rows).  A slot
 // index out of range or out of order marks the snapshot MSP_ITEM_BAD_SLOT
 // and empties the whole schedule.
-__global__ void msp_schedule_kernel(const int *__restrict__ slot, int S, int num_slots, int SB,
-                                    int count_items, int *__restrict__ slot_first,
+__global__ void msp_schedule_kernel(const int *__restrict__ slot, int S, int num_slots, int P,
+                                    int IP, int count_items, int *__restrict__ slot_first,
                                     int *__restrict__ item_first, int *__restrict__ status) {
     __shared__ int bad;
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -449,8 +450,8 @@ __global__ void msp_schedule_kernel(const int *__restrict__ slot, int S, int num
         for (int x = 0; x < num_slots; ++x) {
             item_first[x] = acc;
             if (count_items) {
-                const int len = slot_first[x + 1] - slot_first[x];
-                acc += (len + SB - 1) / SB;
+                const long long pairs = (long long)(slot_first[x + 1] - slot_first[x]) * P;
+                acc += (int)((pairs + IP - 1) / IP);
             }
         }
         item_first[num_slots] = acc;
@@ -458,7 +459,9 @@ __global__ void msp_schedule_kernel(const int *__restrict__ slot, int S, int num
 }
 
 // out[slot][t] = sum of the slot's snapshot constants + its items' partials,
-// in a fixed order (deterministic).  A block covers 32 times of one slot:
+// in a fixed order (deterministic); heterogeneous batches map slots to
+// output rows (slot_row) and add to the row (accumulate) when a system's
+// snapshots are split over several launches.  A block covers 32 times of one slot:
 // warp w sums items w, w + 8, w + 16, ... (several loads in flight per
 // thread), then the 8 warp sums are added in warp order.
 #define MSP_REDUCE_WARPS 8
@@ -497,28 +500,39 @@ __global__ void __launch_bounds__(32 * MSP_REDUCE_WARPS)
         for (int w = 0; w < MSP_REDUCE_WARPS; ++w) cs += red[w][32];
         double s = cs;
         for (int w = 0; w < MSP_REDUCE_WARPS; ++w) s += red[w][lane];
-        out[(size_t)sl * T + t] = s;
+        const size_t o = (size_t)(a.slot_row ? a.slot_row[sl] : sl) * T + t;
+        if (a.accumulate)
+            out[o] += s;
+        else
+            out[o] = s;
     }
 }
 
 int phase_snaps_per_item(int num_snap, int P, int precision) {
     if (P <= 0) return 1;
-    // about 1500 items for load balance; FP32 accumulates at most ~8k pairs
-    const int cap = (precision == MSP_PREC_MIXED ? 8192 : 65536) / P;
+    // about 1500 items for load balance; FP32 accumulates at most
+    // MSP_F32_ITEM_PAIRS pairs
+    const int cap = (precision == MSP_PREC_MIXED ? MSP_F32_ITEM_PAIRS : 65536) / P;
     int sb = (num_snap + 1499) / 1500;
     if (sb > cap) sb = cap;
     if (sb < 1) sb = 1;
     return sb;
 }
 
-int phase_max_items(int num_snap, int num_slots, int SB) {
-    return (num_snap + SB - 1) / SB + num_slots;
+int phase_pairs_per_item(int num_snap, int P, int precision) {
+    const long long ip = (long long)phase_snaps_per_item(num_snap, P, precision) * P;
+    const long long cap = precision == MSP_PREC_MIXED ? MSP_F32_ITEM_PAIRS : (1LL << 30);
+    return (int)(ip > cap ? cap : (ip < 1 ? 1 : ip));
 }
 
-cudaError_t launch_schedule(const int *slot, int num_snap, int num_slots, int SB,
+int phase_max_items(int num_snap, int num_slots, int P, int IP) {
+    return (int)(((long long)num_snap * P + IP - 1) / IP) + num_slots;
+}
+
+cudaError_t launch_schedule(const int *slot, int num_snap, int num_slots, int P, int IP,
                             int count_items, int *slot_first, int *item_first, int *status,
                             cudaStream_t st) {
-    msp_schedule_kernel<<<1, 1024, 0, st>>>(slot, num_snap, num_slots, SB, count_items,
+    msp_schedule_kernel<<<1, 1024, 0, st>>>(slot, num_snap, num_slots, P, IP, count_items,
                                             slot_first, item_first, status);
     return cudaGetLastError();
 }

@@ -453,13 +453,14 @@ __global__ void msp_snap_fast_kernel(SnapArgs a) {
     coef_t *coef = reinterpret_cast<coef_t *>(a.pair_coef);
 
     for (int sn = blockIdx.x; sn < a.num_snap; sn += gridDim.x) {
-        load_hamiltonian<T, REFINE>(a.Hsys, a.Z, a.field + 3 * (size_t)sn, n, m, s);
+        const SnapSource src = snap_source(a, sn);
+        const size_t g = (size_t)src.g;
+        load_hamiltonian<T, REFINE>(src.Hsys, src.Z, a.field + 3 * g, n, m, s);
         const int st = jacobi_sweeps<T>(s.w, m, a.max_sweeps);
         eigenpairs<T, REFINE>(s, n, m);
 
         // sigma_p = p . sigma (Pauli), applied on the muon (slowest) digit
-        const double px = a.pol[3 * (size_t)sn], py = a.pol[3 * (size_t)sn + 1],
-                     pz = a.pol[3 * (size_t)sn + 2];
+        const double px = a.pol[3 * g], py = a.pol[3 * g + 1], pz = a.pol[3 * g + 2];
         const cx<T> s00 = mk<T>((T)pz, T(0)), s01 = mk<T>((T)px, (T)(-py));
         const cx<T> s10 = mk<T>((T)px, (T)py), s11 = mk<T>((T)(-pz), T(0));
         cx<T> *M = s.w.H;  // free buffer
@@ -475,7 +476,7 @@ __global__ void msp_snap_fast_kernel(SnapArgs a) {
         }
         if (tid == 0) s.acc[0] = 0.0;
         __syncthreads();
-        const double scale = 0.5 * a.wscale[sn] / (double)d;
+        const double scale = 0.5 * a.wscale[g] / (double)d;
         const int ntri = n * (n + 1) / 2;
         double diag_local = 0.0;
         for (int e = tid; e < ntri; e += nt) {
@@ -500,7 +501,7 @@ __global__ void msp_snap_fast_kernel(SnapArgs a) {
         __syncthreads();
         if (tid == 0) {
             a.snap_const[sn] = scale * 0.5 * s.acc[0];
-            a.status[sn] = st;
+            a.status[g] = st;
         }
         __syncthreads();
     }
@@ -758,31 +759,70 @@ __global__ void msp_snap_rho_kernel(SnapArgs a) {
 
 // ------------------------------------------------------------------ launchers
 
+int snap_default_threads(int n) { return jacobi_threads(n + (n & 1)); }
+
+// Shared memory of a snapshot kernel launched with `threads` threads (the
+// reduction scratch grows with the warp count).
+static size_t snap_smem_threads(int n, int mode, int precision, int fac_len, int threads) {
+    const bool mixed = precision == MSP_PREC_MIXED;
+    return snap_layout(n, mixed ? 4 : 8, mixed, mode != MSP_MODE_FAST, fac_len, threads / 32)
+        .total;
+}
+
 template <typename K>
-static cudaError_t launch_snap(K kernel, const SnapArgs &a, int grid, size_t smem,
+static cudaError_t launch_snap(K kernel, const SnapArgs &a, int grid, int threads, size_t smem,
                                cudaStream_t st) {
-    const int m = a.n + (a.n & 1);
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    kernel<<<grid, jacobi_threads(m), smem, st>>>(a);
+    kernel<<<grid, threads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStream_t st) {
+template <typename K>
+static int occupancy_of(K kernel, int threads, size_t smem) {
+    int blocks = 0;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, threads, smem) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return blocks > 0 ? blocks : 1;
+}
+
+int snap_occupancy(int n, int mode, int precision, int threads) {
+    if (threads <= 0) threads = snap_default_threads(n);
+    const size_t smem = snap_smem_threads(n, mode, precision, 0, threads);
+    const bool mixed = precision == MSP_PREC_MIXED;
+    if (mode == MSP_MODE_FAST)
+        return mixed ? occupancy_of(msp_snap_fast_kernel<float, true>, threads, smem)
+                     : occupancy_of(msp_snap_fast_kernel<double, false>, threads, smem);
+    return 1;
+}
+
+// threads = 0: jacobi_threads(m); grid = 0: one CTA per snapshot.  Any
+// other grid runs persistent CTAs that stride over the snapshots.
+cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStream_t st,
+                             int threads, int grid) {
     if (a.num_snap <= 0) return cudaSuccess;
-    const size_t smem = snap_smem_bytes(a.n, mode, precision, a.fac_len);
-    const int grid = a.num_snap;
+    if (threads <= 0) threads = snap_default_threads(a.n);
+    const size_t smem = snap_smem_threads(a.n, mode, precision, a.fac_len, threads);
+    if (grid <= 0 || grid > a.num_snap) grid = a.num_snap;
     const bool mixed = precision == MSP_PREC_MIXED;
     if (mode == MSP_MODE_FAST) {
-        return mixed ? launch_snap(msp_snap_fast_kernel<float, true>, a, grid, smem, st)
-                     : launch_snap(msp_snap_fast_kernel<double, false>, a, grid, smem, st);
+        return mixed ? launch_snap(msp_snap_fast_kernel<float, true>, a, grid, threads, smem, st)
+                     : launch_snap(msp_snap_fast_kernel<double, false>, a, grid, threads, smem, st);
     } else if (mode == MSP_MODE_EVOLVE) {
-        return mixed ? launch_snap(msp_snap_rho_kernel<float, true, false>, a, grid, smem, st)
-                     : launch_snap(msp_snap_rho_kernel<double, false, false>, a, grid, smem, st);
+        return mixed
+                   ? launch_snap(msp_snap_rho_kernel<float, true, false>, a, grid, threads, smem, st)
+                   : launch_snap(msp_snap_rho_kernel<double, false, false>, a, grid, threads, smem,
+                                 st);
     }
-    return mixed ? launch_snap(msp_snap_rho_kernel<float, true, true>, a, grid, smem, st)
-                 : launch_snap(msp_snap_rho_kernel<double, false, true>, a, grid, smem, st);
+    return mixed ? launch_snap(msp_snap_rho_kernel<float, true, true>, a, grid, threads, smem, st)
+                 : launch_snap(msp_snap_rho_kernel<double, false, true>, a, grid, threads, smem,
+                               st);
 }
 
 cudaError_t launch_eigh(const double *H, int n, int batch, int precision, int max_sweeps,

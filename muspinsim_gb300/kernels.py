@@ -333,3 +333,113 @@ def adjoint_fast(n, Hsys, Z, field, pol, wscale, slot, num_slots, times, grad_ou
     a.stream = torch.cuda.current_stream().cuda_stream
     _lib.check(lib.msp_adjoint_fast(ctypes.byref(a)), "msp_adjoint_fast")
     return gH, gF, status[:S]
+
+
+class MultiPlan:
+    """A heterogeneous batch on the device (msp_multi_*): several spin
+    systems of uneven Hilbert dimension, each with its own snapshots, reduced
+    into one output row per system.
+
+    Hsys_list, Z_list: per system (n_k, n_k) and (3, n_k, n_k) complex
+    matrices; field, pol: (S, 3) lab-frame vectors of all snapshots, system
+    by system; wscale: (S,); snap_first: (num_systems + 1,) prefix of the
+    systems' snapshot counts; tuning: None or a list of dicts with keys n,
+    snap_threads, ctas_per_sm, snaps_per_item.  ``out`` has shape
+    (num_systems, len(times)).
+    """
+
+    def __init__(self, Hsys_list, Z_list, field, pol, wscale, snap_first, times,
+                 precision=_lib.PREC_MIXED, tuning=None, max_pairs_per_chunk=0, max_sweeps=0):
+        d = device()
+        lib = _lib.load()
+        ns = len(Hsys_list)
+        if len(Z_list) != ns or len(snap_first) != ns + 1:
+            raise ValueError("MultiPlan: one Hsys, one Z and one snapshot range per system")
+        dims = np.array([np.shape(h)[-1] for h in Hsys_list], dtype=np.int32)
+        first = np.ascontiguousarray(snap_first, dtype=np.int32)
+        th = times.detach().cpu().numpy() if isinstance(times, torch.Tensor) else np.asarray(times)
+        uni, t0, dt = uniform_grid(th)
+        desc = _lib.MultiDesc()
+        desc.num_systems = ns
+        desc.sys_n = dims.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        desc.sys_snap_first = first.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        desc.num_times = int(th.size)
+        desc.uniform = 1 if uni else 0
+        desc.t0, desc.dt = t0, dt
+        desc.precision = int(precision)
+        desc.max_sweeps = int(max_sweeps)
+        desc.max_pairs_per_chunk = int(max_pairs_per_chunk)
+        self._tuning = None
+        if tuning:
+            arr = (_lib.MultiTuning * len(tuning))()
+            for i, t in enumerate(tuning):
+                arr[i].n = int(t["n"])
+                arr[i].snap_threads = int(t.get("snap_threads", 0))
+                arr[i].ctas_per_sm = int(t.get("ctas_per_sm", 0))
+                arr[i].snaps_per_item = int(t.get("snaps_per_item", 0))
+            self._tuning = arr
+            desc.tuning = ctypes.cast(arr, ctypes.POINTER(_lib.MultiTuning))
+            desc.num_tuning = len(tuning)
+        h = ctypes.c_void_p(0)
+        _lib.check(lib.msp_multi_plan_create(ctypes.byref(desc), ctypes.byref(h)),
+                   "msp_multi_plan_create")
+        self.handle = h
+        self.dims = dims
+        self.snap_first = first
+        self.num_snap = int(first[-1])
+        self.Hs = torch.cat([dev(hm, torch.complex128).reshape(-1) for hm in Hsys_list])
+        self.Zd = torch.cat([dev(z, torch.complex128).reshape(-1) for z in Z_list])
+        self.F = dev(field, torch.float64).reshape(-1, 3)
+        self.Pl = dev(pol, torch.float64).reshape(-1, 3)
+        self.W = dev(wscale, torch.float64).reshape(-1)
+        if self.F.shape[0] != self.num_snap or self.Pl.shape[0] != self.num_snap or \
+                self.W.shape[0] != self.num_snap:
+            raise ValueError("MultiPlan: field, pol and wscale need one entry per snapshot")
+        self.T = dev(th, torch.float64).reshape(-1)
+        self.out = torch.empty((ns, int(th.size)), dtype=torch.float64, device=d)
+        self.status = torch.zeros((max(self.num_snap, 1),), dtype=torch.int32, device=d)
+        nbytes = ctypes.c_size_t(0)
+        _lib.check(lib.msp_multi_workspace(h, ctypes.byref(nbytes)), "msp_multi_workspace")
+        self.ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device=d)
+        io = _lib.MultiIO()
+        io.Hsys_all, io.Z_all = self.Hs.data_ptr(), self.Zd.data_ptr()
+        io.field, io.pol, io.wscale = self.F.data_ptr(), self.Pl.data_ptr(), self.W.data_ptr()
+        io.times = self.T.data_ptr()
+        io.out, io.status = self.out.data_ptr(), self.status.data_ptr()
+        io.workspace = self.ws.data_ptr() + ((-self.ws.data_ptr()) % 256)
+        io.workspace_bytes = int(nbytes.value)
+        self.io = io
+        self.workspace_bytes = int(nbytes.value)
+
+    def info(self):
+        """Buckets in launch order: list of dicts (n, num_systems, num_snap,
+        num_chunks, snap_threads, grid, pairs_per_item, max_items,
+        scratch_bytes)."""
+        lib = _lib.load()
+        nb = ctypes.c_int(0)
+        _lib.check(lib.msp_multi_plan_info(self.handle, ctypes.byref(nb), None, 0),
+                   "msp_multi_plan_info")
+        arr = (_lib.MultiBucketInfo * max(nb.value, 1))()
+        _lib.check(lib.msp_multi_plan_info(self.handle, ctypes.byref(nb), arr, nb.value),
+                   "msp_multi_plan_info")
+        return [{f: getattr(arr[i], f) for f, _ in _lib.MultiBucketInfo._fields_}
+                for i in range(nb.value)]
+
+    def run(self, graph=False):
+        """Enqueue the batch on the current stream (through a CUDA graph when
+        ``graph``); returns ``out``."""
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        name = "msp_multi_run_graph" if graph else "msp_multi_run"
+        _lib.check(getattr(_lib.load(), name)(self.handle, ctypes.byref(self.io), st), name)
+        return self.out
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            _lib.load().msp_multi_plan_destroy(self.handle)
+            self.handle = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

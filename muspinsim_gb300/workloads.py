@@ -163,3 +163,57 @@ def config5(seed=1005, n_orient=2000, n_times=1000):
         polarization=np.array([0.0, 0.0, 1.0]),
         times=np.linspace(0.0, 20.0, n_times),
     )
+
+
+# Spin lists of the heterogeneous batch, by Hilbert dimension: the muon,
+# at most one electron, one to five nuclei with I = 1/2 (1H) or I = 1 (14N).
+CONFIG4_SPINS = {
+    4: ["mu", "H"],
+    8: ["mu", "e", "H"],
+    12: ["mu", "e", "N"],
+    24: ["mu", "e", "H", "N"],
+    48: ["mu", "e", "H", "H", "N"],
+    96: ["mu", "e", "H", "H", "H", "N"],
+    192: ["mu", "e", "H", "H", "H", "H", "N"],
+}
+
+
+def random_system_workload(rng, dim, orientations, times, field=(0.0, 0.0, 0.01)):
+    """One seeded system of the heterogeneous batch: hyperfine of the muon
+    and of every nucleus to the electron (random anisotropic tensors as
+    above), muon-nucleus point dipoles at U(1, 3) A, and the 14N quadrupole
+    from a random EFG."""
+    spins = CONFIG4_SPINS[dim]
+    coup = []
+    has_e = "e" in spins
+    for i, s in enumerate(spins, start=1):
+        if s == "e":
+            continue
+        if has_e:
+            coup.append(("hyperfine", {"i": i}, random_hyperfine(rng)))
+        if i > 1:
+            coup.append(("dipolar", {"i": 1, "j": i}, random_vector(rng, 1.0, 3.0)))
+        if s == "N":
+            coup.append(("quadrupolar", {"i": i}, random_efg(rng)))
+    return Workload(
+        name=f"system_dim{dim}",
+        spins=list(spins),
+        couplings=coup,
+        orientations=orientations,
+        fields=np.array([field], dtype=float),
+        polarization=np.array([0.0, 0.0, 1.0]),
+        times=times,
+    )
+
+
+def config4(seed=1004, n_systems=4096, n_orient=256, n_times=2048,
+            dims=(4, 8, 12, 24, 48, 96, 192)):
+    """The heterogeneous batch: ``n_systems`` systems with dimensions drawn
+    uniformly from ``dims``, each on the same ZCW-style grid of
+    ``n_orient`` orientations, ``n_times`` times on 0-20 us, B = 0.01 T
+    along z, p = z.  Returns a list of Workloads."""
+    rng = np.random.default_rng(seed)
+    orients = zcw_gen(n_orient)
+    times = np.linspace(0.0, 20.0, n_times)
+    draws = rng.choice(np.asarray(dims), size=n_systems)
+    return [random_system_workload(rng, int(d), orients, times) for d in draws]
