@@ -164,6 +164,7 @@ int large_grid(int batch);
 // most MSP_F32_ITEM_PAIRS pairs in FP32 (mixed precision): longer FP32
 // running sums lose ~1e-6 of P(t) to rounding at n ~ 100.
 #define MSP_F32_ITEM_PAIRS 1024
+bool phase_use_tensor_cores();
 int phase_snaps_per_item(int num_snap, int P, int precision);
 int phase_pairs_per_item(int num_snap, int P, int precision);
 int phase_max_items(int num_snap, int num_slots, int P, int IP);

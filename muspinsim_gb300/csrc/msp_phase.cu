@@ -18,6 +18,8 @@
 // 512 w dt, w t_tile, reduced modulo 2 pi in FP64), their sin/cos, then
 // products of short power tables -- at most 16 rounding steps from an exact
 // value, which is the periodic resync.
+#include <stdlib.h>
+
 #include "msp_internal.cuh"
 
 namespace msp {
@@ -372,6 +374,315 @@ __global__ void __launch_bounds__(128, 4) msp_phase_uniform_f32_kernel(PhaseArgs
     }
 }
 
+// ---------------------------------------------------------------- tensor-core path
+//
+// Mixed precision on a uniform grid, on the 5th-generation tensor cores.
+// A time tile of 128 x N samples (k = N k1 + k0) is the GEMM
+//   D[k1][k0] = sum_m A[k1][m] B[k0][m],  m = 2 p + {0: re, 1: im},
+//   A[k1][2p] = Re X_p(k1),  A[k1][2p+1] = -Im X_p(k1),
+//   B[k0][2p] = Re Y_p(k0),  B[k0][2p+1] =  Im Y_p(k0),
+// with X and Y the factors of the SIMT kernel above (D = sum_p Re X_p Y_p).
+// Operands are FP32 values split as x = hi + lo, hi = tf32(x), lo =
+// tf32(x - hi) (round to nearest), and D accumulates hi.hi + hi.lo + lo.hi
+// (3xTF32: ~2^-22 relative per product) in FP32 in tensor memory.
+//
+// Per CTA (128 threads, one work item, one time tile):
+//   * stages of 16 pairs (K = 32 per stage, 4 MMAs of K = 8 per product),
+//     double-buffered in shared memory; all threads build a stage's power
+//     tables and operands (K-major, no swizzle: 8-row x 16-byte core
+//     matrices, the K-direction stride in the descriptor's leading byte
+//     offset, the 8-row-group stride in its stride byte offset) while the
+//     tensor core runs the previous stage;
+//   * one thread issues the stage's 12 tcgen05.mma (cta_group::1,
+//     kind::tf32, M = 128) and commits them to the buffer's mbarrier, which
+//     the thread building the stage after next waits on before overwriting
+//     the buffer;
+//   * the epilogue reads the 128 x N accumulator with tcgen05.ld (warp w owns
+//     TMEM lanes 32w .. 32w + 31 = rows k1), transposes it through shared
+//     memory and writes the item's FP32 partials coalesced.
+// Every wait is bounded; a wait that runs out marks the tile's partials NaN
+// (the powder average then reads NaN) and the CTA still releases its tensor
+// memory.
+
+#define MSP_TC_PS 16          // pairs per stage
+#define MSP_TC_WAIT (1 << 24)  // polls before a wait gives up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, no swizzle.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version (bits 46-48 = 0b001)
+    return d;
+}
+
+__device__ __forceinline__ float tf32_rn(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    uint32_t done = 0;
+    for (int it = 0; it < MSP_TC_WAIT && !done; ++it)
+        asm volatile(
+            "{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;"
+            " selp.b32 %0, 1, 0, p;}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc,
+                                       uint32_t acc) {
+    asm volatile(
+        "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;}" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+template <int N>
+struct TcLayout {
+    static constexpr int CA = 16 * 128;          // bytes of one A K-chunk (128 rows x 16 B)
+    static constexpr int CB = (N / 8) * 128;     // bytes of one B K-chunk
+    static constexpr int A_BYTES = 8 * CA;       // 8 K-chunks per stage (K = 32)
+    static constexpr int B_BYTES = 8 * CB;
+    static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;  // hi and lo of A and B
+    static constexpr int SMEM = 2 * STAGE;       // two stages
+};
+
+// Reads the 32-lane x N-column block of tensor memory at taddr (this warp's
+// lanes) into r[0..N).
+template <int N>
+__device__ __forceinline__ void tmem_load(uint32_t taddr, uint32_t (&r)[32]) {
+    if (N == 32) {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+            "%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31},"
+            " [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+              "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+              "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+              "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+              "=r"(r[31])
+            : "r"(taddr));
+    } else {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+            "%12,%13,%14,%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+              "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+    }
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Accumulation: the tensor core's own FP32 accumulation over hundreds of
+// MMAs loses ~1e-6 of a single crystallite's P(t), so every stage
+// accumulates into one of two tensor-memory blocks (alternating, 32 columns
+// each) that the threads drain into round-to-nearest FP32 registers once the
+// stage's MMAs have completed -- while the next stage's MMAs run into the
+// other block.
+template <int N>
+__global__ void __launch_bounds__(128) msp_phase_tc_kernel(PhaseArgs a) {
+    typedef TcLayout<N> L;
+    constexpr int PS = MSP_TC_PS, YH = N / 8;
+    extern __shared__ __align__(1024) char tsm[];
+    __shared__ __align__(16) cx<float> ylo[8][PS + 1], yhi[YH][PS + 1], xlo[8][PS + 1],
+        xhi[16][PS + 1];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_range[2];
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) {
+        item_range(a, blockIdx.x, &s_range[0], &s_range[1]);
+        s_fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    __syncthreads();
+    const int pbeg = s_range[0], pend = s_range[1];
+    if (pbeg < 0) return;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(
+            smem_u32(&s_tmem)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = s_tmem;
+    const uint32_t my_lanes = (uint32_t)(32 * warp) << 16;
+
+    const long long tile_base = (long long)blockIdx.y * (128 * N);
+    const float tile_steps = (float)tile_base;  // exact: < 2^24
+    const float2 *coef = reinterpret_cast<const float2 *>(a.pair_coef);
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+                           ((uint32_t)(128 >> 4) << 24);
+    const int nstage = (pend - pbeg + PS - 1) / PS;
+    int issued = 0;  // stages whose MMAs were committed (uniform across the CTA)
+    int drained = 0; // stages added into acc (uniform)
+    float acc[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) acc[j] = 0.f;
+    uint32_t r[32];
+
+    for (int s = 0; s < nstage; ++s) {
+        const int pb = pbeg + s * PS;
+        const int np = (pend - pb) < PS ? (pend - pb) : PS;
+        const int buf = s & 1;
+        char *A_hi = tsm + buf * L::STAGE;
+        char *A_lo = A_hi + L::A_BYTES;
+        char *B_hi = A_lo + L::A_BYTES;
+        char *B_lo = B_hi + L::B_BYTES;
+        // power tables: thread (chain c, pair i); chains Y: e^{i psi b}
+        // (b < 8), e^{i 8 psi a} (a < N/8); X: e^{i N psi b} (b < 8),
+        // c e^{i (phi0 + psi (tile + 8 N a))} (a < 16)
+        if (tid < 4 * PS) {
+            const int c = tid / PS, i = tid - c * PS;
+            const int len = c == 0 ? 8 : c == 1 ? YH : c == 2 ? 8 : 16;
+            cx<float> *dst = c == 0 ? &ylo[0][i] : c == 1 ? &yhi[0][i] : c == 2 ? &xlo[0][i]
+                                                                                   : &xhi[0][i];
+            cx<float> p = mk<float>(c == 3 ? 0.f : 1.f, 0.f), base = mk<float>(1.f, 0.f);
+            if (i < np) {
+                const float4 rec = a.pair_phase[pb + i];
+                const float sc = c == 0 ? 1.f : c == 1 ? 8.f : c == 2 ? (float)N : 8.f * N;
+                float h = rec.x * sc, l = rec.y * sc;  // exact power-of-two scaling
+                dw_reduce_2pi(h, l);
+                base = dw_expi(h, l);
+                if (c == 3) {
+                    float th = rec.z, tl = rec.w;
+                    if (tile_base > 0) {
+                        const float ph = rec.x * tile_steps;
+                        float bh = ph, bl = fmaf(rec.x, tile_steps, -ph) + rec.y * tile_steps;
+                        dw_reduce_2pi(bh, bl);
+                        dw_add(th, tl, bh, bl);
+                        dw_reduce_2pi(th, tl);
+                    }
+                    const float2 cf = coef[pb + i];
+                    p = mk<float>(cf.x, -cf.y);
+                    if (th != 0.f || tl != 0.f) p = cmul(p, dw_expi(th, tl));
+                }
+            }
+            for (int q = 0; q < len; ++q) {
+                dst[q * (PS + 1)] = p;
+                p = cmul(p, base);
+            }
+        }
+        // stage s - 2 (same operand buffer, same accumulator block) done?
+        if (tid == 0 && s >= 2 && !mbar_wait(smem_u32(&mbar[buf]), ((s >> 1) - 1) & 1))
+            s_fail = 1;
+        __syncthreads();
+        if (s_fail) break;
+        if (s >= 2) {  // drain stage s - 2's block before stage s overwrites it
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            tmem_load<N>(tmem + my_lanes + 32u * buf, r);
+#pragma unroll
+            for (int j = 0; j < N; ++j) acc[j] += __uint_as_float(r[j]);
+            drained = s - 1;
+        }
+        // A: thread = row k1; 2 pairs (one 16-byte K-chunk) at a time
+        {
+            const int k1 = tid;
+            const int off = (k1 >> 3) * 128 + (k1 & 7) * 16;
+#pragma unroll 2
+            for (int g = 0; g < PS / 2; ++g) {
+                const cx<float> x0 = cmul(xhi[k1 >> 3][2 * g], xlo[k1 & 7][2 * g]);
+                const cx<float> x1 = cmul(xhi[k1 >> 3][2 * g + 1], xlo[k1 & 7][2 * g + 1]);
+                const float4 v = make_float4(x0.re, -x0.im, x1.re, -x1.im);
+                const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+                const float4 lo = make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y),
+                                              tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
+                *reinterpret_cast<float4 *>(A_hi + g * L::CA + off) = h;
+                *reinterpret_cast<float4 *>(A_lo + g * L::CA + off) = lo;
+            }
+        }
+        // B: task = (row k0, pair group g)
+        for (int e = tid; e < N * (PS / 2); e += 128) {
+            const int k0 = e % N, g = e / N;
+            const cx<float> y0 = cmul(yhi[k0 >> 3][2 * g], ylo[k0 & 7][2 * g]);
+            const cx<float> y1 = cmul(yhi[k0 >> 3][2 * g + 1], ylo[k0 & 7][2 * g + 1]);
+            const float4 v = make_float4(y0.re, y0.im, y1.re, y1.im);
+            const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+            const float4 lo = make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y),
+                                          tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
+            const int off = g * L::CB + (k0 >> 3) * 128 + (k0 & 7) * 16;
+            *reinterpret_cast<float4 *>(B_hi + off) = h;
+            *reinterpret_cast<float4 *>(B_lo + off) = lo;
+        }
+        // operands written by the generic proxy, read by the tensor core;
+        // this thread's tensor-memory reads ordered before the next MMAs
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t ah = smem_u32(A_hi), al = smem_u32(A_lo);
+            const uint32_t bh = smem_u32(B_hi), bl = smem_u32(B_lo);
+            const uint32_t d = tmem + 32u * buf;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+                const uint32_t ao = ks * 2 * L::CA, bo = ks * 2 * L::CB;
+                const uint64_t dah = tc_desc(ah + ao, L::CA, 128), dal = tc_desc(al + ao, L::CA, 128);
+                const uint64_t dbh = tc_desc(bh + bo, L::CB, 128), dbl = tc_desc(bl + bo, L::CB, 128);
+                // the small products first, the block restarts at each stage
+                tc_mma(d, dal, dbh, idesc, ks > 0 ? 1u : 0u);
+                tc_mma(d, dah, dbl, idesc, 1u);
+                tc_mma(d, dah, dbh, idesc, 1u);
+            }
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    smem_u32(&mbar[buf]))
+                : "memory");
+        }
+        issued = s + 1;
+    }
+    // epilogue: wait for the last commit (it covers every MMA issued before
+    // it; waited for, bounded, even after a failed wait, so that no MMA still
+    // reads shared or tensor memory when the CTA releases them), then drain
+    // the blocks of the stages not yet added
+    const int last = issued - 1;
+    if (tid == 0 && last >= 0 && !mbar_wait(smem_u32(&mbar[last & 1]), (last >> 1) & 1))
+        s_fail = 1;
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const bool ok = !s_fail;
+    if (ok) {
+        for (int st = drained; st < issued; ++st) {  // at most two stages
+            tmem_load<N>(tmem + my_lanes + 32u * (st & 1), r);
+#pragma unroll
+            for (int j = 0; j < N; ++j) acc[j] += __uint_as_float(r[j]);
+        }
+    }
+    float *tile = reinterpret_cast<float *>(tsm);  // operand buffers are free now
+    {
+        const int k1 = tid;  // = 32 warp + lane: this thread's TMEM lane
+#pragma unroll
+        for (int j = 0; j < N; ++j) tile[k1 * (N + 1) + j] = ok ? acc[j] : __int_as_float(0x7fc00000);
+    }
+    __syncthreads();
+    float *out = a.partial_f32 + (size_t)blockIdx.x * a.num_times;
+    for (int e = tid; e < 128 * N; e += 128) {
+        const long long t = tile_base + e;
+        if (t < a.num_times) out[t] = tile[(e / N) * (N + 1) + (e % N)];
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+}
+
 // Arbitrary time grids: one thread per sample, every pair's phase reduced in
 // FP64 and evaluated with sincos.
 template <typename T>
@@ -508,6 +819,15 @@ __global__ void __launch_bounds__(32 * MSP_REDUCE_WARPS)
     }
 }
 
+// The mixed-precision uniform-grid phase sum runs on the tensor cores
+// unless MSP_PHASE_SIMT=1 is set in the environment (read at each launch),
+// which selects the FP32 SIMT kernel -- the two give the same sums to FP32
+// rounding; the parity tests compare them.
+bool phase_use_tensor_cores() {
+    const char *v = getenv("MSP_PHASE_SIMT");
+    return !(v != NULL && v[0] == '1');
+}
+
 int phase_snaps_per_item(int num_snap, int P, int precision) {
     if (P <= 0) return 1;
     // about 1500 items for load balance; FP32 accumulates at most
@@ -540,7 +860,23 @@ cudaError_t launch_schedule(const int *slot, int num_snap, int num_slots, int P,
 cudaError_t launch_phase(const PhaseArgs &a, int precision, int max_items, int uniform,
                          cudaStream_t st) {
     if (max_items <= 0 || a.num_times <= 0) return cudaSuccess;
-    if (uniform) {
+    if (uniform && precision == MSP_PREC_MIXED && phase_use_tensor_cores()) {
+        if (a.num_times > 2048) {
+            const int smem = TcLayout<32>::SMEM;
+            cudaError_t e = cudaFuncSetAttribute(msp_phase_tc_kernel<32>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            dim3 grid(max_items, (a.num_times + 4095) / 4096);
+            msp_phase_tc_kernel<32><<<grid, 128, smem, st>>>(a);
+        } else {
+            const int smem = TcLayout<16>::SMEM;
+            cudaError_t e = cudaFuncSetAttribute(msp_phase_tc_kernel<16>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            dim3 grid(max_items, (a.num_times + 2047) / 2048);
+            msp_phase_tc_kernel<16><<<grid, 128, smem, st>>>(a);
+        }
+    } else if (uniform) {
         dim3 grid(max_items, (a.num_times + 4095) / 4096);
         if (precision == MSP_PREC_MIXED)
             msp_phase_uniform_f32_kernel<<<grid, 128, 0, st>>>(a);

@@ -325,3 +325,23 @@ def test_powder_fast_large_vs_oracle():
     assert np.abs(got - ref).max() <= FP64_TOL
     got = _gpu_powder(wl, "mixed")
     assert np.abs(got - ref).max() <= MIXED_TOL
+
+
+@pytest.mark.parametrize("n_times,t_end", [(4096, 20.0), (1500, 10.0), (9000, 30.0)])
+def test_phase_tensor_cores_match_simt_and_oracle(monkeypatch, n_times, t_end):
+    """Mixed precision on a uniform grid: the tcgen05 (3xTF32) phase sum
+    against the FP32 SIMT kernel (same inputs, FP32-rounding agreement) and
+    the oracle (1e-6).  4096 times use 128 x 32 tiles, 1500 one 128 x 16
+    tile, 9000 three 128 x 32 tiles."""
+    from muspinsim_gb300 import workloads
+
+    wl = workloads.config2(n_orient=40, n_times=n_times)
+    wl.times = np.linspace(0.0, t_end, n_times)
+    tc = _gpu_powder(wl, "mixed")
+    monkeypatch.setenv("MSP_PHASE_SIMT", "1")
+    simt = _gpu_powder(wl, "mixed")
+    monkeypatch.delenv("MSP_PHASE_SIMT")
+    ref = oracle_powder(wl)
+    assert np.abs(tc - simt).max() <= 3e-7
+    assert np.abs(tc - ref).max() <= MIXED_TOL
+    assert np.abs(simt - ref).max() <= MIXED_TOL
