@@ -63,6 +63,9 @@ def parse_args():
     p.add_argument("--ref-orientations", type=int, default=400,
                    help="orientations per step of the --impl reference arm")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="config2",
+                   choices=["config1", "config2", "config3", "config4", "config5"],
+                   help="config2 (default) is the headline; the others print their own line")
     return p.parse_args()
 
 
@@ -385,7 +388,10 @@ def run_gb300(args, world, rank, local):
         if k >= args.warmup:
             e2e_ms.append((t1 - t0) * 1e3)
     dP_e2e = float(np.abs(r - res_fp64[0].cpu().numpy()).max())
-    h2d = (Hsys.size + Z.size) * 16 + S * (3 + 3 + 1 + 1) * 8 + S * 4 + T * 8
+    # per call: the orientation rows and the time grid go up (the system's
+    # Hsys and Z stay on the device after the first call, like a model's
+    # weights), the powder average and the per-snapshot status come back
+    h2d = int(np.asarray(wl.orientations).nbytes) + T * 8
     d2h = T * 8 + S * 4
 
     t_mixed = statistics.median(ms_mixed)
@@ -455,11 +461,276 @@ def run_gb300(args, world, rank, local):
     return 0
 
 
+# ---------------------------------------------------------------- other workloads
+
+def _events_ms(fn, steps, flush=None):
+    """Median milliseconds of fn() over `steps` runs, CUDA events on the
+    current stream, L2 flushed before each run when `flush` is given."""
+    import torch
+
+    stream = torch.cuda.current_stream()
+    ts = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def _wall_ms(fn, steps):
+    import torch
+
+    ts = []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        ts.append((time.perf_counter() - t0) * 1e3)
+    return statistics.median(ts)
+
+
+def _line(metric, value, unit, ms, args, world, workload, config, **extra):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "data": "synthetic (seeded couplings, ZCW-style grid)",
+            "config": dict({"workload": workload}, **config)}
+    line.update(extra)
+    return line
+
+
+def run_config1(args, world, rank, local):
+    """mu + e (dim 4), 1 orientation, 1000 times: the reference's own
+    CPU-sized case, plain FP64 as the reference computes it."""
+    import torch
+
+    from muspinsim_gb300 import _lib, kernels, workloads
+    from muspinsim_gb300.powder import powder_average
+
+    wl = workloads.config1()
+    sy = wl.system()
+    Hs, Z = sy.hamiltonian_matrix(), sy.zeeman_operators()
+    B = np.atleast_2d(wl.fields[0])
+    p = np.atleast_2d(wl.polarization)
+    T = len(wl.times)
+    plan = kernels.PowderPlan(4, Hs, Z, B, p, np.ones(1), np.zeros(1, np.int32), 1, wl.times,
+                              precision=_lib.PREC_FP64, dims=list(sy.dimension))
+    for _ in range(args.warmup):
+        plan.run()
+    ms = _events_ms(plan.run, args.steps)
+    call = lambda: powder_average(sy, wl.orientations, wl.fields[0], wl.polarization, wl.times)
+    for _ in range(args.warmup):
+        call()
+    e2e = _wall_ms(call, args.steps)
+    line = _line("P(t) samples/s, plain FP64", T / (ms * 1e-3), "samples/s", ms, args, world,
+                 "mu_e_dim4_1_orient_1000_t", {"orientations": 1, "times": T, "dim": 4},
+                 dtype="f64",
+                 e2e={"value": T / (e2e * 1e-3), "unit": "samples/s", "ms_per_step": e2e,
+                      "h2d_bytes_per_step": int(np.asarray(wl.orientations).nbytes) + T * 8,
+                      "d2h_bytes_per_step": T * 8 + 4, "api": "muspinsim_gb300.powder_average"},
+                 gpu_launches=4 * args.steps,
+                 note="launch-bound: one snapshot of a 4x4 Hamiltonian")
+    if not args.no_cpu_baseline:
+        from oracle import port
+        from tests.helpers import oracle_system
+
+        osy = oracle_system(wl.spins, wl.couplings)
+        t0 = time.perf_counter()
+        reps = 200
+        for _ in range(reps):
+            port.powder_average(osy, wl.orientations, wl.fields[0], wl.polarization, np.inf,
+                                wl.times)
+        dt = (time.perf_counter() - t0) / reps
+        line["cpu_baseline"] = {"value": T / dt, "unit": "samples/s", "cores": 1, "kind": "port",
+                                "sample": f"{reps} full runs (numpy eigh + C cosine sum)"}
+    return line
+
+
+def run_config3(args, world, rank, local):
+    """ALC field scan: mu, e, 3 x 1H (dim 32), 2000 fields x 1000
+    orientations, decaying integral with tau = MU_TAU.  Unit: one
+    (field, orientation) integral."""
+    import torch
+
+    from muspinsim_gb300 import _lib, kernels, workloads
+    from muspinsim_gb300 import quaternion as Q
+    from muspinsim_gb300.constants import MU_TAU
+    from muspinsim_gb300.orientations import orientation_rows_to_quats
+
+    wl = workloads.config3()
+    sy = wl.system()
+    qs, ws = orientation_rows_to_quats(wl.orientations)
+    No = len(qs)
+    ws = ws * (No / ws.sum())
+    Nf = len(wl.fields)
+    p_or = Q.rotate(qs, wl.polarization)
+    R = Q.rotation_matrix(qs)  # (No, 3, 3)
+    B_lab = np.einsum("oab,fb->foa", R, wl.fields).reshape(-1, 3)
+    p_lab = np.broadcast_to(p_or, (Nf, No, 3)).reshape(-1, 3)
+    wsc = np.broadcast_to(ws / No, (Nf, No)).reshape(-1)
+    slot = np.repeat(np.arange(Nf, dtype=np.int32), No)
+    units = Nf * No
+    Hs, Z = sy.hamiltonian_matrix(), sy.zeeman_operators()
+
+    def plan(prec, sub=None):
+        sl = slice(None) if sub is None else slice(0, sub * No)
+        nslots = Nf if sub is None else sub
+        return kernels.PowderPlan(32, Hs, Z, B_lab[sl], p_lab[sl], wsc[sl], slot[sl], nslots,
+                                  np.array([np.inf]), mode=_lib.MODE_INTEGRAL, precision=prec,
+                                  dims=list(sy.dimension), mu_index=0, gammas=sy.gammas,
+                                  tau=MU_TAU)
+
+    mixed = plan(_lib.PREC_MIXED)
+    for _ in range(args.warmup):
+        mixed.run()
+    ms = _events_ms(mixed.run, args.steps)
+    sub = 100  # FP64 on 100 fields x all orientations (5% of the scan)
+    f64 = plan(_lib.PREC_FP64, sub)
+    f64.run()
+    ms64 = _events_ms(f64.run, max(1, args.fp64_steps))
+    dP = float((mixed.out[:sub] - f64.out).abs().max().item())
+    line = _line("ALC (field, orientation) integrals/s, mixed precision", units / (ms * 1e-3),
+                 "integrals/s", ms, args, world, "mu_e_3H_dim32_alc_2000_fields_1000_orient",
+                 {"fields": Nf, "orientations": No, "dim": 32, "tau_us": MU_TAU,
+                  "l2": "inputs (96 MB of field/polarisation) resident; not flushed"},
+                 dtype="f32 Jacobi + df32 refinement + f64 integral",
+                 fp64={"value": sub * No / (ms64 * 1e-3), "unit": "integrals/s",
+                       "ms_per_step": ms64, "sample": f"{sub} of {Nf} fields x {No} orientations"},
+                 max_abs_dIntegral_mixed_vs_fp64=dP,
+                 status_max=int(mixed.status[:units].max().item()),
+                 gpu_launches=3 * args.steps)
+    if not args.no_cpu_baseline:
+        from oracle import port
+        from tests.helpers import oracle_system
+
+        osy = oracle_system(wl.spins, wl.couplings)
+        Hn, Zn = osy.hamiltonian(), osy.zeeman_operators()
+        nsamp = 200
+        t0 = time.perf_counter()
+        for k in range(nsamp):
+            f, o = (k * 10) % Nf, (k * 37) % No
+            q = port.orientation_quat(wl.orientations[o])[0]
+            port.snapshot(osy, Hn, Zn, q, 1.0, wl.fields[f], wl.polarization, np.inf,
+                          np.zeros(3), np.array([np.inf]), y="integral")
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": nsamp / dt, "unit": "integrals/s", "cores": 1,
+                                "kind": "port", "sample": f"{nsamp} (field, orientation) units"}
+    return line
+
+
+def run_config4(args, world, rank, local):
+    """Heterogeneous batch: spin systems of dimension 4 ... 192, one output
+    row each, through msp_multi_run (size buckets, persistent launches,
+    concurrent streams, CUDA graph).  Scaled to 512 systems x 32
+    orientations (the 4,096 x 256 configuration has the same per-snapshot
+    mix; its n = 192 FP64 eigensolves alone take about two minutes)."""
+    import torch
+
+    from muspinsim_gb300 import workloads
+    from muspinsim_gb300.multi import MultiSystemBatch
+
+    n_sys, n_or = 512, 32
+    wls = workloads.config4(n_systems=n_sys, n_orient=n_or)
+    systems = [w.system() for w in wls]
+    T = len(wls[0].times)
+    out = {}
+    for prec in ("mixed", "fp64"):
+        b = MultiSystemBatch(systems, wls[0].orientations, wls[0].fields[0],
+                             wls[0].polarization, wls[0].times, precision=prec)
+        b.run(graph=True)
+        torch.cuda.synchronize()
+        ms = _events_ms(lambda: b.run(graph=True), max(1, args.steps // 10))
+        out[prec] = (ms, b.plan.out.clone(), b.plan.info())
+        b.plan.close()
+    ms, res, info = out["mixed"]
+    samples = n_sys * n_or * T
+    dP = float((res - out["fp64"][1]).abs().max().item())
+    buckets = [{k: bi[k] for k in ("n", "num_systems", "num_snap", "num_chunks",
+                                    "snap_threads", "grid")} for bi in info]
+    return _line("heterogeneous-batch P(t) samples/s, mixed precision", samples / (ms * 1e-3),
+                 "samples/s", ms, args, world, "4_to_192_dim_systems_512x32_orient_2048_t",
+                 {"systems": n_sys, "orientations": n_or, "times": T,
+                  "dims": [4, 8, 12, 24, 48, 96, 192], "scaled_from": "4096 systems x 256",
+                  "graph": True},
+                 dtype="f32 (n <= 64 Jacobi, phase sum) / f64 (n > 64 Householder + QL)",
+                 fp64={"value": samples / (out["fp64"][0] * 1e-3), "ms_per_step": out["fp64"][0]},
+                 max_abs_dP_mixed_vs_fp64=dP, buckets=buckets)
+
+
+def run_config5(args, world, rank, local):
+    """Differentiable fit: F-mu-F (dim 8), 2000 orientations, 1000 times:
+    loss + analytic gradient (forward powder average and the adjoint
+    kernel) evaluations per second."""
+    import torch
+
+    from muspinsim_gb300 import workloads
+    from muspinsim_gb300.adjoint import GradientFitter, TorchSpinHamiltonian
+
+    wl = workloads.config5()
+    r = [np.asarray(v, dtype=float) for _, _, v in wl.couplings]
+    th = TorchSpinHamiltonian(wl.spins)
+    d = th.device
+    dirs = [torch.as_tensor(r[k] / np.linalg.norm(r[k]), device=d) for k in range(2)]
+    fixed = th.dipolar(1, 2, r[2])
+    B0 = torch.zeros(3, dtype=torch.float64, device=d)
+
+    def model(ps):
+        return th.dipolar(0, 1, ps[0] * dirs[0]) + th.dipolar(0, 2, ps[1] * dirs[1]) + fixed, B0
+
+    rng = np.random.default_rng(1005)
+    data = 0.5 * np.cos(np.linspace(0, 3, wl.times.size)) + rng.normal(0, 0.01, wl.times.size)
+    fit = GradientFitter(model, th.Z, wl.orientations, wl.times, data, wl.polarization)
+    ps = [torch.tensor(float(np.linalg.norm(r[k])), dtype=torch.float64, device=d,
+                       requires_grad=True) for k in range(2)]
+
+    def step():
+        L, g = fit.loss_and_grad(ps)
+        return L
+
+    for _ in range(args.warmup):
+        step()
+    ms = _wall_ms(step, args.steps)
+    line = _line("loss + gradient evaluations/s (adjoint), FP64", 1e3 / ms, "evaluations/s", ms,
+                 args, world, "F_mu_F_dim8_2000_orient_1000_t_fit",
+                 {"orientations": len(wl.orientations), "times": len(wl.times), "dim": 8,
+                  "parameters": 2},
+                 dtype="f64", e2e={"value": 1e3 / ms, "unit": "evaluations/s", "ms_per_step": ms,
+                                   "note": "wall clock of torch autograd loss + backward"})
+    if not args.no_cpu_baseline:
+        from oracle import port
+        from tests.helpers import oracle_system
+
+        osy = oracle_system(wl.spins, wl.couplings)
+        t0 = time.perf_counter()
+        port.powder_average(osy, wl.orientations, np.zeros(3), wl.polarization, np.inf, wl.times)
+        dt = time.perf_counter() - t0
+        # a central-difference gradient in 2 parameters costs 5 forward runs
+        line["cpu_baseline"] = {"value": 1.0 / (5 * dt), "unit": "evaluations/s", "cores": 1,
+                                "kind": "port",
+                                "sample": "one forward run; loss + central-FD gradient = 5 runs"}
+    return line
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         rc = run_reference(args, world, rank)
+    elif args.workload != "config2":
+        import torch
+
+        torch.cuda.set_device(local)
+        fn = {"config1": run_config1, "config3": run_config3, "config4": run_config4,
+              "config5": run_config5}[args.workload]
+        line = fn(args, world, rank, local)
+        if rank == 0:
+            print(json.dumps(line))
+        rc = 0
     else:
         rc = run_gb300(args, world, rank, local)
     if world > 1:

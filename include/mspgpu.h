@@ -128,6 +128,24 @@ int msp_evolve_phases(const double *evals, const double *rho, int n, const doubl
 int msp_integrate_decaying(const double *evals, const double *rho, const double *ops,
                            int n, int num_ops, double tau, double *out, void *stream);
 
+/* Lab-frame vectors of the snapshots of an orientation grid: for each row
+ * the stored conjugate quaternion q* of MuSpinConfig._validate_orient
+ * (muspinsim/simconfig.py:596-613; polar rows (theta, phi) as Euler
+ * (phi, theta, phi) 'zyz', muspinsim/utils.py:53-68) rotates the field and
+ * the polarisation as ExperimentRunner.load_config does
+ * (muspinsim/experiment.py:405-411): field = q*(B) + B_intr, pol = q*(p).
+ * rows: num_rows x row_len doubles (device); row_len 2 = (theta, phi),
+ * 3 = (a, b, c), 4 = (a, b, c, w); euler_mode 0 = 'zyz', 1 = 'zxz'.
+ * B, p, B_intr (may be NULL): HOST 3-vectors.  field, pol: num_rows*3
+ * outputs.  weight (may be NULL): num_rows outputs w_k * weight_norm, w_k
+ * the row weight (4-column rows, more than one row) or 1 -- weight_norm =
+ * 1 / sum(w) gives the normalised weights of muspinsim/simconfig.py:152-159
+ * divided by the averaged count. */
+int msp_orient_snapshots(const double *rows, int num_rows, int row_len, int euler_mode,
+                         const double *B, const double *p, const double *B_intr,
+                         double weight_norm, double *field, double *pol, double *weight,
+                         void *stream);
+
 /* ---- stage timer ---------------------------------------------------------- */
 
 /* Opaque set of CUDA events that msp_powder_run records around its stages

@@ -231,6 +231,11 @@ _SIGNATURES = {
         [_c_dp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(MultiBucketInfo), ctypes.c_int]),
     "msp_multi_run": (ctypes.c_int, [_c_dp, ctypes.POINTER(MultiIO), _c_dp]),
     "msp_multi_run_graph": (ctypes.c_int, [_c_dp, ctypes.POINTER(MultiIO), _c_dp]),
+    "msp_orient_snapshots": (
+        ctypes.c_int,
+        [_c_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_double,
+         _c_dp, _c_dp, _c_dp, _c_dp]),
     "msp_timer_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
     "msp_timer_destroy": (ctypes.c_int, [_c_dp]),
     "msp_timer_read": (

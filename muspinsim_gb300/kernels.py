@@ -147,6 +147,31 @@ def integrate_decaying(evals, rho, ops, tau):
     return out
 
 
+def orient_snapshots(rows, B, p, B_intr=(0.0, 0.0, 0.0), mode="zyz", weight_norm=None):
+    """Lab-frame field, polarisation and weight/N of every orientation row on
+    the device (msp_orient_snapshots).  ``rows``: (N, 2 | 3 | 4) array or
+    tensor.  Returns three device tensors: (N, 3), (N, 3), (N,)."""
+    d = device()
+    R = dev(rows, torch.float64)
+    if R.dim() != 2 or R.shape[1] not in (2, 3, 4):
+        raise ValueError("orientation rows must be (theta, phi), (a, b, c) or (a, b, c, w)")
+    N, L = int(R.shape[0]), int(R.shape[1])
+    if weight_norm is None:
+        if L == 4 and N > 1:
+            weight_norm = 1.0 / float(R[:, 3].sum().item())
+        else:
+            weight_norm = 1.0 / max(N, 1)
+    field = torch.empty((N, 3), dtype=torch.float64, device=d)
+    pol = torch.empty((N, 3), dtype=torch.float64, device=d)
+    w = torch.empty((N,), dtype=torch.float64, device=d)
+    vec = ctypes.c_double * 3
+    _lib.call("msp_orient_snapshots", ptr(R), N, L, 0 if mode == "zyz" else 1,
+              vec(*np.asarray(B, dtype=float)), vec(*np.asarray(p, dtype=float)),
+              vec(*np.asarray(B_intr, dtype=float)), float(weight_norm), ptr(field), ptr(pol),
+              ptr(w), stream())
+    return field, pol, w
+
+
 def uniform_grid(times, rtol=1e-12):
     """(is_uniform, t0, dt) for a 1-D time array."""
     t = np.asarray(times, dtype=np.float64)

@@ -47,31 +47,54 @@ def _rows_sorted(slot):
 
 
 def run_snapshots(system, B_lab, p_lab, T, wscale, slot, num_slots, times,
-                  y_axis="asymmetry", precision="fp64", max_sweeps=0, Hsys=None, Z=None):
+                  y_axis="asymmetry", precision="fp64", max_sweeps=0, Hsys=None, Z=None,
+                  fast_mask=None):
     """Evaluate and reduce a batch of snapshots on the GPU.
 
     B_lab, p_lab: (S, 3) lab-frame field (incl. intrinsic) and muon
     polarisation; T: scalar or (S,) temperatures; wscale: (S,) weight /
     averaged count; slot: (S,) output row.  Returns a device tensor of shape
     (num_slots, len(times)) for 'asymmetry' or (num_slots,) for 'integral',
-    and the per-snapshot status (host int array, original order)."""
+    and the per-snapshot status (host int array, original order).
+
+    ``fast_mask``: a precomputed fast-path decision (bool, one for all
+    snapshots); B_lab, p_lab and wscale may then be device tensors and
+    ``slot`` None (every snapshot in row 0)."""
     prec = precision_code(precision)
-    B_lab = np.ascontiguousarray(np.atleast_2d(B_lab), dtype=float)
-    p_lab = np.ascontiguousarray(np.atleast_2d(p_lab), dtype=float)
-    S = len(B_lab)
-    wscale = np.broadcast_to(np.asarray(wscale, dtype=float), (S,))
-    slot = np.broadcast_to(np.asarray(slot, dtype=np.int64), (S,))
+    dev = kernels.device()
+    if fast_mask is not None and isinstance(B_lab, torch.Tensor):
+        S = int(B_lab.shape[0])
+        if slot is None:
+            slot = torch.zeros(S, dtype=torch.int32, device=dev)
+    else:
+        B_lab = np.ascontiguousarray(np.atleast_2d(B_lab), dtype=float)
+        p_lab = np.ascontiguousarray(np.atleast_2d(p_lab), dtype=float)
+        S = len(B_lab)
+        wscale = np.broadcast_to(np.asarray(wscale, dtype=float), (S,))
+        slot = np.broadcast_to(np.asarray(0 if slot is None else slot, dtype=np.int64), (S,))
     Tarr = np.broadcast_to(np.asarray(T, dtype=float), (S,))
-    if Hsys is None:
-        Hsys = system.hamiltonian_matrix()
-    if Z is None:
-        Z = system.zeeman_operators()
-    n = Hsys.shape[0]
+    if Hsys is None and Z is None:
+        Hs, Zd = system.device_matrices(dev)
+        n = int(Hs.shape[0])
+    else:
+        if Hsys is None:
+            Hsys = system.hamiltonian_matrix()
+        if Z is None:
+            Z = system.zeeman_operators()
+        n = Hsys.shape[0]
+        Hs = kernels.dev(Hsys, torch.complex128)
+        Zd = kernels.dev(Z, torch.complex128)
     dims = list(system.dimension)
     mu = system.muon_index
-    dev = kernels.device()
-    Hs = kernels.dev(Hsys, torch.complex128)
-    Zd = kernels.dev(Z, torch.complex128)
+    if fast_mask is not None and isinstance(B_lab, torch.Tensor):
+        mode = _lib.MODE_INTEGRAL if y_axis == "integral" else (
+            _lib.MODE_FAST if fast_mask else _lib.MODE_EVOLVE)
+        out, st = kernels.powder_run(
+            n, Hs, Zd, B_lab, p_lab, wscale, slot, num_slots, times, mode=mode, precision=prec,
+            dims=dims, mu_index=mu, gammas=system.gammas,
+            temperature=None if mode == _lib.MODE_FAST else Tarr, tau=MU_TAU,
+            max_sweeps=max_sweeps)
+        return out, st.cpu().numpy()
 
     if y_axis == "integral":
         groups = [(_lib.MODE_INTEGRAL, np.ones(S, dtype=bool))]
@@ -100,6 +123,21 @@ def run_snapshots(system, B_lab, p_lab, T, wscale, slot, num_slots, times,
     return out, status
 
 
+def _fast_rule_uniform(field, intrinsic_field, temperature, mu_index):
+    """The reference's per-snapshot fast-path rule when it is the same for
+    every orientation, else None: T = inf makes the check 0 for any field;
+    with no intrinsic field |B_lab| = |B| for every orientation
+    (muspinsim/experiment.py:413-430)."""
+    T = np.asarray(temperature, dtype=float)
+    if T.ndim != 0:
+        return None
+    if np.isinf(T):
+        return mu_index == 0
+    if np.any(np.asarray(intrinsic_field, dtype=float) != 0.0):
+        return None
+    return bool(t_inf_speedup(np.atleast_2d(field), float(T), mu_index)[0])
+
+
 def powder_average(system, orientations, field=(0.0, 0.0, 0.0), polarization=(1.0, 0.0, 0.0),
                    times=None, temperature=np.inf, intrinsic_field=(0.0, 0.0, 0.0),
                    y_axis="asymmetry", precision="fp64", mode="zyz", max_sweeps=0):
@@ -109,23 +147,53 @@ def powder_average(system, orientations, field=(0.0, 0.0, 0.0), polarization=(1.
     reference's ``orientation`` keyword; weights are normalised to sum to N
     and the result is sum_k w_k P_k / N (muspinsim/simconfig.py:152-159,
     347-368).  ``field``: one 3-vector or a scalar along z (T).  Returns a
-    float64 numpy array over ``times`` (or a scalar for 'integral')."""
-    qs, ws = orientation_rows_to_quats(orientations, mode)
-    N = len(qs)
-    ws = ws * (N / ws.sum()) if N > 1 else np.ones(1)
+    float64 numpy array over ``times`` (or a scalar for 'integral').
+
+    A regular grid of rows is rotated on the device (msp_orient_snapshots)
+    and the system's matrices stay on the device between calls, so a call
+    moves the rows, the time grid and the result across the bus."""
     f = np.atleast_1d(np.asarray(field, dtype=float))
     if f.size == 1:
         f = np.array([0.0, 0.0, f[0]])
     p = np.asarray(polarization, dtype=float)
     p = p / np.linalg.norm(p)
-    B_lab = Q.rotate(qs, f) + np.asarray(intrinsic_field, dtype=float)
-    p_lab = Q.rotate(qs, p)
+    intr = np.atleast_1d(np.asarray(intrinsic_field, dtype=float))
+    if intr.size == 1:
+        intr = np.array([0.0, 0.0, intr[0]])
     if y_axis == "integral":
         times = np.array([np.inf])
     times = np.asarray(times, dtype=float)
-    out, status = run_snapshots(system, B_lab, p_lab, temperature, ws / N, np.zeros(N, np.int64),
-                                1, times, y_axis, precision, max_sweeps)
+    rows = None
+    if not _ragged_rows(orientations):
+        rows = np.ascontiguousarray(orientations, dtype=float)
+        if rows.ndim != 2 or rows.shape[1] not in (2, 3, 4):
+            rows = None
+    fast = _fast_rule_uniform(f + intr, intr, temperature, system.muon_index)
+    if rows is not None and fast is not None and len(rows) > 0:
+        N = len(rows)
+        wnorm = 1.0 / float(rows[:, 3].sum()) if (rows.shape[1] == 4 and N > 1) else 1.0 / N
+        F, Pl, W = kernels.orient_snapshots(rows, f, p, intr, mode, wnorm)
+        out, status = run_snapshots(system, F, Pl, temperature, W, None, 1, times, y_axis,
+                                    precision, max_sweeps, fast_mask=fast)
+    else:
+        qs, ws = orientation_rows_to_quats(orientations, mode)
+        N = len(qs)
+        ws = ws * (N / ws.sum()) if N > 1 else np.ones(1)
+        B_lab = Q.rotate(qs, f) + intr
+        p_lab = Q.rotate(qs, p)
+        out, status = run_snapshots(system, B_lab, p_lab, temperature, ws / N,
+                                    np.zeros(N, np.int64), 1, times, y_axis, precision,
+                                    max_sweeps)
     res = out.cpu().numpy()
     if np.any(status & _lib.MSP_ITEM_BAD_SLOT):
         raise RuntimeError("powder_average: invalid output rows")
     return res[0]
+
+
+def _ragged_rows(rows):
+    if isinstance(rows, np.ndarray):
+        return rows.dtype == object
+    try:
+        return len({len(np.atleast_1d(r)) for r in rows}) > 1
+    except TypeError:
+        return True

@@ -373,6 +373,18 @@ class SpinSystem(Clonable):
             cache[key] = build()
         return cache[key].copy()
 
+    def device_matrices(self, device):
+        """(Hsys, Z) as complex128 torch tensors on ``device``, uploaded once
+        per term list and device (the batched GPU paths reuse them)."""
+        import torch
+
+        key = ("device", tuple(id(t) for t in self._terms), str(device))
+        cache = self.__dict__.setdefault("_matrix_cache", {})
+        if key not in cache:
+            cache[key] = (torch.as_tensor(self.hamiltonian_matrix()).to(device),
+                          torch.as_tensor(self.zeeman_operators()).to(device))
+        return cache[key]
+
     def __len__(self):
         return len(self._gammas)
 

@@ -345,3 +345,27 @@ def test_phase_tensor_cores_match_simt_and_oracle(monkeypatch, n_times, t_end):
     assert np.abs(tc - simt).max() <= 3e-7
     assert np.abs(tc - ref).max() <= MIXED_TOL
     assert np.abs(simt - ref).max() <= MIXED_TOL
+
+
+@pytest.mark.parametrize("cols,mode", [(2, "zyz"), (3, "zyz"), (3, "zxz"), (4, "zyz"), (4, "zxz")])
+def test_orient_snapshots_match_host(K, cols, mode):
+    """Device rotation of B and p by the stored conjugate quaternions (and
+    the weight normalisation) against the host quaternion code."""
+    from muspinsim_gb300 import quaternion as Q
+    from muspinsim_gb300.orientations import orientation_rows_to_quats
+
+    rng = np.random.default_rng(9 + cols)
+    N = 57
+    rows = rng.uniform(0.0, 2.0 * np.pi, (N, cols))
+    if cols == 4:
+        rows[:, 3] = rng.uniform(0.1, 2.0, N)
+    B = np.array([0.1, -0.2, 0.3])
+    p = np.array([0.3, 0.4, 0.5])
+    p /= np.linalg.norm(p)
+    intr = np.array([0.01, 0.0, -0.02])
+    F, Pl, W = K.orient_snapshots(rows, B, p, intr, mode)
+    qs, ws = orientation_rows_to_quats(rows, mode)
+    ws = ws * (N / ws.sum())
+    assert np.abs(F.cpu().numpy() - (Q.rotate(qs, B) + intr)).max() <= 1e-15
+    assert np.abs(Pl.cpu().numpy() - Q.rotate(qs, p)).max() <= 1e-15
+    assert np.abs(W.cpu().numpy() - ws / N).max() <= 1e-15
