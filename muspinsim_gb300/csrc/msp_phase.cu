@@ -457,8 +457,8 @@ struct TcLayout {
     static constexpr int SMEM = 2 * STAGE;       // two stages
 };
 
-// Reads the 32-lane x N-column block of tensor memory at taddr (this warp's
-// lanes) into r[0..N).
+// Reads the 32-lane x N-column block (N = 32, 16 or 8) of tensor memory at
+// taddr (this warp's lanes) into r[0..N).
 template <int N>
 __device__ __forceinline__ void tmem_load(uint32_t taddr, uint32_t (&r)[32]) {
     if (N == 32) {
@@ -473,13 +473,19 @@ __device__ __forceinline__ void tmem_load(uint32_t taddr, uint32_t (&r)[32]) {
               "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
               "=r"(r[31])
             : "r"(taddr));
-    } else {
+    } else if (N == 16) {
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
             "%12,%13,%14,%15}, [%16];"
             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
               "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
               "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+    } else {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+              "=r"(r[7])
             : "r"(taddr));
     }
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -491,22 +497,82 @@ __device__ __forceinline__ void tmem_load(uint32_t taddr, uint32_t (&r)[32]) {
 // each) that the threads drain into round-to-nearest FP32 registers once the
 // stage's MMAs have completed -- while the next stage's MMAs run into the
 // other block.
+//
+// 256 threads: warps w and w + 4 own the same 32 TMEM lanes (rows k1) and
+// drain the two column halves; operand generation is spread over all
+// threads (A: 4 K-chunks of one row each, B: one K-chunk each); the power
+// tables are five chains of at most 8 products (the 16-entry X chain is
+// split in two, its second half started from its own exactly reduced
+// phase).
+#define MSP_TC_THREADS 256
+
+// Power tables of the 16 pairs of one stage, thread (chain c, pair i) for
+// c < 5: Y e^{i psi b} (b < 8), e^{i 8 psi a} (a < N/8); X e^{i N psi b}
+// (b < 8) and c e^{i (phi0 + psi (tile + 8 N a))} for a < 8 (c = 3) and
+// 8 <= a < 16 (c = 4, started from its own exactly reduced phase).
 template <int N>
-__global__ void __launch_bounds__(128) msp_phase_tc_kernel(PhaseArgs a) {
-    typedef TcLayout<N> L;
+struct TcTables {
+    cx<float> ylo[8][MSP_TC_PS + 1], yhi[N / 8][MSP_TC_PS + 1], xlo[8][MSP_TC_PS + 1],
+        xhi[16][MSP_TC_PS + 1];
+};
+
+template <int N>
+__device__ __forceinline__ void tc_build_tables(const PhaseArgs &a, TcTables<N> &tb, int pb,
+                                                int np, float tile_steps, int tid) {
     constexpr int PS = MSP_TC_PS, YH = N / 8;
+    if (tid >= 5 * PS) return;
+    const float2 *coef = reinterpret_cast<const float2 *>(a.pair_coef);
+    const int c = tid / PS, i = tid - c * PS;
+    const int len = c == 1 ? YH : 8;
+    cx<float> *dst = c == 0 ? &tb.ylo[0][i] : c == 1 ? &tb.yhi[0][i] : c == 2 ? &tb.xlo[0][i]
+                                                : c == 3 ? &tb.xhi[0][i] : &tb.xhi[8][i];
+    cx<float> p = mk<float>(c >= 3 ? 0.f : 1.f, 0.f), base = mk<float>(1.f, 0.f);
+    if (i < np) {
+        const float4 rec = a.pair_phase[pb + i];
+        const float sc = c == 0 ? 1.f : c == 1 ? 8.f : c == 2 ? (float)N : 8.f * N;
+        float h = rec.x * sc, l = rec.y * sc;  // exact power-of-two scaling
+        dw_reduce_2pi(h, l);
+        base = dw_expi(h, l);
+        if (c >= 3) {
+            float th = rec.z, tl = rec.w;
+            const float steps = tile_steps + (c == 4 ? 64.f * N : 0.f);  // exact
+            if (steps > 0.f) {
+                const float ph = rec.x * steps;
+                float bh = ph, bl = fmaf(rec.x, steps, -ph) + rec.y * steps;
+                dw_reduce_2pi(bh, bl);
+                dw_add(th, tl, bh, bl);
+                dw_reduce_2pi(th, tl);
+            }
+            const float2 cf = coef[pb + i];
+            p = mk<float>(cf.x, -cf.y);
+            if (th != 0.f || tl != 0.f) p = cmul(p, dw_expi(th, tl));
+        }
+    }
+    for (int q = 0; q < len; ++q) {
+        dst[q * (PS + 1)] = p;
+        p = cmul(p, base);
+    }
+}
+
+// 256 threads: warps w and w + 4 own the same 32 TMEM lanes (rows k1) and
+// drain the two column halves; operand generation is spread over all
+// threads (A: 4 K-chunks of one row each, B: one K-chunk each).  One
+// barrier per stage: every thread polls the stage mbarrier itself, and the
+// tables of stage s + 1 (double-buffered) are built after the operands of
+// stage s, so their latency overlaps the other warps' operand work.
+template <int N>
+__global__ void __launch_bounds__(MSP_TC_THREADS) msp_phase_tc_kernel(PhaseArgs a) {
+    typedef TcLayout<N> L;
+    constexpr int PS = MSP_TC_PS, NH = N / 2;
     extern __shared__ __align__(1024) char tsm[];
-    __shared__ __align__(16) cx<float> ylo[8][PS + 1], yhi[YH][PS + 1], xlo[8][PS + 1],
-        xhi[16][PS + 1];
+    __shared__ __align__(16) TcTables<N> tabs[2];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t s_tmem;
     __shared__ int s_range[2];
-    __shared__ int s_fail;
 
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0) {
         item_range(a, blockIdx.x, &s_range[0], &s_range[1]);
-        s_fail = 0;
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])));
         asm volatile("fence.mbarrier_init.release.cluster;");
@@ -514,118 +580,96 @@ __global__ void __launch_bounds__(128) msp_phase_tc_kernel(PhaseArgs a) {
     __syncthreads();
     const int pbeg = s_range[0], pend = s_range[1];
     if (pbeg < 0) return;
+    const long long tile_base = (long long)blockIdx.y * (128 * N);
+    const float tile_steps = (float)tile_base;  // exact: < 2^24
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(
             smem_u32(&s_tmem)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    tc_build_tables<N>(a, tabs[0], pbeg, (pend - pbeg) < PS ? (pend - pbeg) : PS, tile_steps,
+                       tid);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = s_tmem;
-    const uint32_t my_lanes = (uint32_t)(32 * warp) << 16;
+    // this warp's TMEM lanes and column half
+    const int half = warp >> 2;
+    const uint32_t my_tmem = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(half * NH);
 
-    const long long tile_base = (long long)blockIdx.y * (128 * N);
-    const float tile_steps = (float)tile_base;  // exact: < 2^24
-    const float2 *coef = reinterpret_cast<const float2 *>(a.pair_coef);
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
                            ((uint32_t)(128 >> 4) << 24);
     const int nstage = (pend - pbeg + PS - 1) / PS;
-    int issued = 0;  // stages whose MMAs were committed (uniform across the CTA)
-    int drained = 0; // stages added into acc (uniform)
-    float acc[N];
+    int issued = 0;   // stages whose MMAs were committed (uniform across the CTA)
+    int drained = 0;  // stages added into acc (uniform)
+    int fail = 0;     // uniform: set from the barrier's OR
+    float acc[NH];
 #pragma unroll
-    for (int j = 0; j < N; ++j) acc[j] = 0.f;
+    for (int j = 0; j < NH; ++j) acc[j] = 0.f;
     uint32_t r[32];
 
     for (int s = 0; s < nstage; ++s) {
-        const int pb = pbeg + s * PS;
-        const int np = (pend - pb) < PS ? (pend - pb) : PS;
         const int buf = s & 1;
         char *A_hi = tsm + buf * L::STAGE;
         char *A_lo = A_hi + L::A_BYTES;
         char *B_hi = A_lo + L::A_BYTES;
         char *B_lo = B_hi + L::B_BYTES;
-        // power tables: thread (chain c, pair i); chains Y: e^{i psi b}
-        // (b < 8), e^{i 8 psi a} (a < N/8); X: e^{i N psi b} (b < 8),
-        // c e^{i (phi0 + psi (tile + 8 N a))} (a < 16)
-        if (tid < 4 * PS) {
-            const int c = tid / PS, i = tid - c * PS;
-            const int len = c == 0 ? 8 : c == 1 ? YH : c == 2 ? 8 : 16;
-            cx<float> *dst = c == 0 ? &ylo[0][i] : c == 1 ? &yhi[0][i] : c == 2 ? &xlo[0][i]
-                                                                                   : &xhi[0][i];
-            cx<float> p = mk<float>(c == 3 ? 0.f : 1.f, 0.f), base = mk<float>(1.f, 0.f);
-            if (i < np) {
-                const float4 rec = a.pair_phase[pb + i];
-                const float sc = c == 0 ? 1.f : c == 1 ? 8.f : c == 2 ? (float)N : 8.f * N;
-                float h = rec.x * sc, l = rec.y * sc;  // exact power-of-two scaling
-                dw_reduce_2pi(h, l);
-                base = dw_expi(h, l);
-                if (c == 3) {
-                    float th = rec.z, tl = rec.w;
-                    if (tile_base > 0) {
-                        const float ph = rec.x * tile_steps;
-                        float bh = ph, bl = fmaf(rec.x, tile_steps, -ph) + rec.y * tile_steps;
-                        dw_reduce_2pi(bh, bl);
-                        dw_add(th, tl, bh, bl);
-                        dw_reduce_2pi(th, tl);
-                    }
-                    const float2 cf = coef[pb + i];
-                    p = mk<float>(cf.x, -cf.y);
-                    if (th != 0.f || tl != 0.f) p = cmul(p, dw_expi(th, tl));
-                }
-            }
-            for (int q = 0; q < len; ++q) {
-                dst[q * (PS + 1)] = p;
-                p = cmul(p, base);
-            }
-        }
-        // stage s - 2 (same operand buffer, same accumulator block) done?
-        if (tid == 0 && s >= 2 && !mbar_wait(smem_u32(&mbar[buf]), ((s >> 1) - 1) & 1))
-            s_fail = 1;
-        __syncthreads();
-        if (s_fail) break;
-        if (s >= 2) {  // drain stage s - 2's block before stage s overwrites it
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            tmem_load<N>(tmem + my_lanes + 32u * buf, r);
+        const TcTables<N> &tb = tabs[buf];
+        int my_fail = 0;
+        if (s >= 2) {
+            // stage s - 2 (same operand buffer, same accumulator block) done:
+            // drain its block before stage s overwrites it
+            if (mbar_wait(smem_u32(&mbar[buf]), ((s >> 1) - 1) & 1)) {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                tmem_load<NH>(my_tmem + 32u * buf, r);
 #pragma unroll
-            for (int j = 0; j < N; ++j) acc[j] += __uint_as_float(r[j]);
+                for (int j = 0; j < NH; ++j) acc[j] += __uint_as_float(r[j]);
+            } else {
+                my_fail = 1;
+            }
             drained = s - 1;
         }
-        // A: thread = row k1; 2 pairs (one 16-byte K-chunk) at a time
+        // A: thread = (row k1, half h): K-chunks g = h, h + 2, h + 4, h + 6
         {
-            const int k1 = tid;
+            const int k1 = tid & 127, h0 = tid >> 7;
             const int off = (k1 >> 3) * 128 + (k1 & 7) * 16;
 #pragma unroll 2
-            for (int g = 0; g < PS / 2; ++g) {
-                const cx<float> x0 = cmul(xhi[k1 >> 3][2 * g], xlo[k1 & 7][2 * g]);
-                const cx<float> x1 = cmul(xhi[k1 >> 3][2 * g + 1], xlo[k1 & 7][2 * g + 1]);
+            for (int gi = 0; gi < PS / 4; ++gi) {
+                const int g = h0 + 2 * gi;
+                const cx<float> x0 = cmul(tb.xhi[k1 >> 3][2 * g], tb.xlo[k1 & 7][2 * g]);
+                const cx<float> x1 = cmul(tb.xhi[k1 >> 3][2 * g + 1], tb.xlo[k1 & 7][2 * g + 1]);
                 const float4 v = make_float4(x0.re, -x0.im, x1.re, -x1.im);
-                const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
-                const float4 lo = make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y),
-                                              tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
-                *reinterpret_cast<float4 *>(A_hi + g * L::CA + off) = h;
+                const float4 hh = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+                // the tensor core reads lo as tf32 (truncated): |lo| <= 2^-11 |x|
+                const float4 lo = make_float4(v.x - hh.x, v.y - hh.y, v.z - hh.z, v.w - hh.w);
+                *reinterpret_cast<float4 *>(A_hi + g * L::CA + off) = hh;
                 *reinterpret_cast<float4 *>(A_lo + g * L::CA + off) = lo;
             }
         }
-        // B: task = (row k0, pair group g)
-        for (int e = tid; e < N * (PS / 2); e += 128) {
+        // B: task = (row k0, K-chunk g)
+        for (int e = tid; e < N * (PS / 2); e += MSP_TC_THREADS) {
             const int k0 = e % N, g = e / N;
-            const cx<float> y0 = cmul(yhi[k0 >> 3][2 * g], ylo[k0 & 7][2 * g]);
-            const cx<float> y1 = cmul(yhi[k0 >> 3][2 * g + 1], ylo[k0 & 7][2 * g + 1]);
+            const cx<float> y0 = cmul(tb.yhi[k0 >> 3][2 * g], tb.ylo[k0 & 7][2 * g]);
+            const cx<float> y1 = cmul(tb.yhi[k0 >> 3][2 * g + 1], tb.ylo[k0 & 7][2 * g + 1]);
             const float4 v = make_float4(y0.re, y0.im, y1.re, y1.im);
-            const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
-            const float4 lo = make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y),
-                                          tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
+            const float4 hh = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+            const float4 lo = make_float4(v.x - hh.x, v.y - hh.y, v.z - hh.z, v.w - hh.w);
             const int off = g * L::CB + (k0 >> 3) * 128 + (k0 & 7) * 16;
-            *reinterpret_cast<float4 *>(B_hi + off) = h;
+            *reinterpret_cast<float4 *>(B_hi + off) = hh;
             *reinterpret_cast<float4 *>(B_lo + off) = lo;
+        }
+        // tables of the next stage (the buffer last read by stage s - 1)
+        if (s + 1 < nstage) {
+            const int pb1 = pbeg + (s + 1) * PS;
+            tc_build_tables<N>(a, tabs[buf ^ 1], pb1, (pend - pb1) < PS ? (pend - pb1) : PS,
+                               tile_steps, tid);
         }
         // operands written by the generic proxy, read by the tensor core;
         // this thread's tensor-memory reads ordered before the next MMAs
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
+        fail = __syncthreads_or(my_fail);
+        if (fail) break;
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t ah = smem_u32(A_hi), al = smem_u32(A_lo);
@@ -653,27 +697,28 @@ __global__ void __launch_bounds__(128) msp_phase_tc_kernel(PhaseArgs a) {
     // reads shared or tensor memory when the CTA releases them), then drain
     // the blocks of the stages not yet added
     const int last = issued - 1;
-    if (tid == 0 && last >= 0 && !mbar_wait(smem_u32(&mbar[last & 1]), (last >> 1) & 1))
-        s_fail = 1;
-    __syncthreads();
+    int my_fail = 0;
+    if (last >= 0 && !mbar_wait(smem_u32(&mbar[last & 1]), (last >> 1) & 1)) my_fail = 1;
+    fail = __syncthreads_or(my_fail | fail);
     asm volatile("tcgen05.fence::after_thread_sync;");
-    const bool ok = !s_fail;
+    const bool ok = !fail;
     if (ok) {
         for (int st = drained; st < issued; ++st) {  // at most two stages
-            tmem_load<N>(tmem + my_lanes + 32u * (st & 1), r);
+            tmem_load<NH>(my_tmem + 32u * (st & 1), r);
 #pragma unroll
-            for (int j = 0; j < N; ++j) acc[j] += __uint_as_float(r[j]);
+            for (int j = 0; j < NH; ++j) acc[j] += __uint_as_float(r[j]);
         }
     }
     float *tile = reinterpret_cast<float *>(tsm);  // operand buffers are free now
     {
-        const int k1 = tid;  // = 32 warp + lane: this thread's TMEM lane
+        const int k1 = 32 * (warp & 3) + (tid & 31);  // this thread's TMEM lane
 #pragma unroll
-        for (int j = 0; j < N; ++j) tile[k1 * (N + 1) + j] = ok ? acc[j] : __int_as_float(0x7fc00000);
+        for (int j = 0; j < NH; ++j)
+            tile[k1 * (N + 1) + half * NH + j] = ok ? acc[j] : __int_as_float(0x7fc00000);
     }
     __syncthreads();
     float *out = a.partial_f32 + (size_t)blockIdx.x * a.num_times;
-    for (int e = tid; e < 128 * N; e += 128) {
+    for (int e = tid; e < 128 * N; e += MSP_TC_THREADS) {
         const long long t = tile_base + e;
         if (t < a.num_times) out[t] = tile[(e / N) * (N + 1) + (e % N)];
     }
@@ -867,14 +912,14 @@ cudaError_t launch_phase(const PhaseArgs &a, int precision, int max_items, int u
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e != cudaSuccess) return e;
             dim3 grid(max_items, (a.num_times + 4095) / 4096);
-            msp_phase_tc_kernel<32><<<grid, 128, smem, st>>>(a);
+            msp_phase_tc_kernel<32><<<grid, MSP_TC_THREADS, smem, st>>>(a);
         } else {
             const int smem = TcLayout<16>::SMEM;
             cudaError_t e = cudaFuncSetAttribute(msp_phase_tc_kernel<16>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e != cudaSuccess) return e;
             dim3 grid(max_items, (a.num_times + 2047) / 2048);
-            msp_phase_tc_kernel<16><<<grid, 128, smem, st>>>(a);
+            msp_phase_tc_kernel<16><<<grid, MSP_TC_THREADS, smem, st>>>(a);
         }
     } else if (uniform) {
         dim3 grid(max_items, (a.num_times + 4095) / 4096);

@@ -369,3 +369,25 @@ def test_orient_snapshots_match_host(K, cols, mode):
     assert np.abs(F.cpu().numpy() - (Q.rotate(qs, B) + intr)).max() <= 1e-15
     assert np.abs(Pl.cpu().numpy() - Q.rotate(qs, p)).max() <= 1e-15
     assert np.abs(W.cpu().numpy() - ws / N).max() <= 1e-15
+
+
+def test_mixed_degenerate_and_single_crystallites_vs_oracle():
+    """Mixed path (FP32 Jacobi + double-word refinement) against the oracle:
+    powder average, single crystallites and a degenerate zero-field
+    spectrum (isotropic couplings, clusters of equal levels)."""
+    from muspinsim_gb300 import workloads
+
+    wl = workloads.config2(n_orient=60, n_times=1024)
+    assert np.abs(_gpu_powder(wl, "mixed") - oracle_powder(wl)).max() <= MIXED_TOL
+    for o in wl.orientations[:6]:
+        ref = oracle_powder(wl, orientations=[o])
+        assert np.abs(_gpu_powder(wl, "mixed", orientations=[o]) - ref).max() <= 5e-7
+    iso = workloads.Workload(
+        name="iso", spins=["mu", "e", "H", "H"],
+        couplings=[("hyperfine", {"i": 1}, 400.0 * np.eye(3)),
+                   ("hyperfine", {"i": 3}, 50.0 * np.eye(3)),
+                   ("hyperfine", {"i": 4}, 50.0 * np.eye(3))],
+        orientations=workloads.zcw_gen(8), fields=np.zeros((1, 3)),
+        polarization=np.array([0.0, 0.0, 1.0]), times=np.linspace(0.0, 5.0, 512))
+    assert np.abs(_gpu_powder(iso, "mixed") - oracle_powder(iso)).max() <= MIXED_TOL
+    assert np.abs(_gpu_powder(iso, "fp64") - oracle_powder(iso)).max() <= FP64_TOL
