@@ -66,6 +66,23 @@ int msp_last_error(char *buf, size_t len);
 int msp_assemble(const double *Hsys, const double *Z, const double *fields, int n,
                  int batch, double *H, void *stream);
 
+/* Hamiltonians of rotated copies of a spin system (the tensor-rotation
+ * formulation of SpinSystem.rotate + .hamiltonian, muspinsim/spinsys.py:
+ * 103-110, 128-135, 594-626): for each rotation R_s (batch x 9 doubles,
+ * row-major)
+ *   H_s = sum_t sum_ab (R_s T_t R_s^T)_ab B[9 t + 3 a + b]
+ *       + sum_u (R_s v_u)_a B[9 num_double + 3 u + a].
+ * tensors: num_double 3x3 tensors T_t (9 doubles each); vectors: num_single
+ * 3-vectors v_u; basis: (9 num_double + 3 num_single) n x n complex128 --
+ * the Kronecker-embedded S^a_i S^b_j of each bilinear term (the product
+ * S^a_i S^b_i for a same-spin term) and S^a_i of each single term.  At most
+ * 64 terms of each kind.  H: batch x n x n complex128.  ExperimentRunner
+ * rotates the field instead (muspinsim/experiment.py:405-406); both give
+ * unitarily equivalent Hamiltonians. */
+int msp_assemble_rotated(const double *rot, int batch, const double *tensors, int num_double,
+                         const double *vectors, int num_single, const double *basis, int n,
+                         double *H, void *stream);
+
 /* Batched Hermitian eigensolve, 1 <= n <= MSP_MAX_DIM: cyclic Jacobi, one CTA
  * per matrix.  evals: batch*n ascending; evecs: batch*n*n complex128 with the
  * eigenvectors as COLUMNS (numpy.linalg.eigh layout); status: batch ints.

@@ -175,6 +175,10 @@ _SIGNATURES = {
     "msp_version": (ctypes.c_int, []),
     "msp_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "msp_assemble": (ctypes.c_int, [_c_dp, _c_dp, _c_dp, ctypes.c_int, ctypes.c_int, _c_dp, _c_dp]),
+    "msp_assemble_rotated": (
+        ctypes.c_int,
+        [_c_dp, ctypes.c_int, _c_dp, ctypes.c_int, _c_dp, ctypes.c_int, _c_dp, ctypes.c_int, _c_dp,
+         _c_dp]),
     "msp_eigh_batched": (
         ctypes.c_int,
         [_c_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp, _c_dp, _c_dp, _c_dp],

@@ -75,6 +75,25 @@ def assemble(Hsys, Z, fields):
     return out
 
 
+def assemble_rotated(system, rotations):
+    """Hamiltonians of rotated copies of ``system`` (msp_assemble_rotated):
+    for each 3x3 rotation R_s, the Hamiltonian of ``system.rotate(R_s)``
+    (bilinear tensors R T R^T, vectors R v).  Returns (S, n, n) complex128
+    on the device."""
+    tensors, vectors, B = system.rotation_basis()
+    d = device()
+    R = dev(np.asarray(rotations, dtype=float) if not isinstance(rotations, torch.Tensor)
+            else rotations, torch.float64).reshape(-1, 9)
+    S, n = int(R.shape[0]), int(B.shape[-1])
+    Td = dev(tensors.reshape(-1), torch.float64) if len(tensors) else None
+    Vd = dev(vectors.reshape(-1), torch.float64) if len(vectors) else None
+    Bd = dev(B, torch.complex128)
+    out = torch.empty((S, n, n), dtype=torch.complex128, device=d)
+    _lib.call("msp_assemble_rotated", ptr(R), S, ptr(Td), len(tensors), ptr(Vd), len(vectors),
+              ptr(Bd), n, ptr(out), stream())
+    return out
+
+
 def basis_change(U, M, adjoint=False):
     """U^dag M U (or U M U^dag when adjoint) for batched or single matrices."""
     Ud = dev(U, torch.complex128)

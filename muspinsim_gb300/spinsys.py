@@ -373,6 +373,38 @@ class SpinSystem(Clonable):
             cache[key] = build()
         return cache[key].copy()
 
+    def rotation_basis(self):
+        """Term tensors and operator basis of the tensor-rotation assembly
+        (msp_assemble_rotated): ``(tensors (Kd, 3, 3), vectors (Ks, 3),
+        basis (9 Kd + 3 Ks, n, n) complex)`` with, per bilinear term, the
+        nine Kronecker-embedded S^a_i S^b_j (the product S^a_i S^b_i for a
+        same-spin term) and, per single term, the three S^a_i -- the same
+        operators _recalc_operator sums (muspinsim/spinsys.py:34-69)."""
+        doubles = [t for t in self._terms if isinstance(t, DoubleTerm)]
+        singles = [t for t in self._terms if isinstance(t, SingleTerm)]
+        if len(doubles) + len(singles) != len(self._terms):
+            raise ValueError("rotation_basis: only single and double terms can be rotated")
+
+        def dense(op):
+            m = op.matrix
+            return m.toarray() if sparse.issparse(m) else np.asarray(m)
+
+        basis = []
+        for t in doubles:
+            i, j = int(t.i), int(t.j)
+            for a in "xyz":
+                for b in "xyz":
+                    spec = {i: [a, b]} if i == j else {i: a, j: b}
+                    basis.append(dense(self.operator(spec)))
+        for t in singles:
+            for a in "xyz":
+                basis.append(dense(self.operator({int(t.i): a})))
+        n = int(np.prod(self.dimension))
+        tensors = np.array([t.tensor for t in doubles], dtype=float).reshape(-1, 3, 3)
+        vectors = np.array([t.tensor for t in singles], dtype=float).reshape(-1, 3)
+        B = np.array(basis, dtype=complex).reshape(-1, n, n)
+        return tensors, vectors, B
+
     def device_matrices(self, device):
         """(Hsys, Z) as complex128 torch tensors on ``device``, uploaded once
         per term list and device (the batched GPU paths reuse them)."""

@@ -303,3 +303,24 @@ def test_capi_library_exports_header():
     assert lib.msp_powder_workspace(ctypes.byref(a), ctypes.byref(nbytes)) == _lib.MSP_ERR_UNSUPPORTED
     assert "fast path only" in _lib.last_error()
     assert ctypes.sizeof(_lib.PowderArgs) > 0
+
+
+def test_rotation_basis_reproduces_rotated_hamiltonians():
+    """The operator basis of the tensor-rotation assembly, contracted with
+    rotated tensors on the host, equals the Hamiltonian of
+    SpinSystem.rotate (muspinsim/spinsys.py:594-626)."""
+    from muspinsim_gb300 import quaternion as Q
+    from muspinsim_gb300 import workloads
+
+    sy = workloads.config2(n_orient=4, n_times=8).system()
+    sy.add_zeeman_term(2, [0.0, 0.1, 0.2])
+    tensors, vectors, B = sy.rotation_basis()
+    assert B.shape == (9 * len(tensors) + 3 * len(vectors), 24, 24)
+    rng = np.random.default_rng(3)
+    for q in Q.from_euler(*rng.uniform(0, 2 * np.pi, (3, 3)), "zyz"):
+        R = Q.rotation_matrix(q)
+        coef = np.concatenate([np.einsum("ac,tcd,bd->tab", R, tensors, R).reshape(-1),
+                               np.einsum("ab,ub->ua", R, vectors).reshape(-1)])
+        H = np.einsum("k,kij->ij", coef, B)
+        ref = sy.rotate(R).hamiltonian_matrix()
+        assert np.abs(H - ref).max() <= 1e-12 * np.abs(ref).max()
