@@ -280,6 +280,89 @@ def integrate_decaying(H, rho, tau, operators):
     return np.array(res)
 
 
+# ---------------------------------------------------------------- Lindblad
+def lindblad_matrix(H, dissipators=()):
+    """L = -i (H (x) 1 - 1 (x) H^T) + sum_k g_k [A_k (x) conj(A_k)
+    - 1/2 (A_k^H A_k (x) 1 + 1 (x) (A_k^H A_k)^T)], row-major vec
+    (muspinsim/lindbladian.py:17-41; superoperators muspinsim/spinop.py:
+    622-714)."""
+    n = H.shape[0]
+    one = np.eye(n)
+    L = -1.0j * (np.kron(H, one) - np.kron(one, H.T))
+    for A, g in dissipators:
+        M = A.conj().T @ A
+        L = L + g * (np.kron(A, A.conj()) - 0.5 * (np.kron(M, one) + np.kron(one, M.T)))
+    return L
+
+
+def lindblad_evolve(L, rho, times, operators):
+    """<O>(t) from the eigendecomposition of L: complex [T, n_ops]
+    (muspinsim/lindbladian.py:43-111)."""
+    evals, revecs = np.linalg.eig(L)
+    r0 = np.linalg.solve(revecs, rho.reshape(-1))
+    opsT = np.array([O.T.reshape(-1) @ revecs for O in operators])
+    times = np.asarray(times, dtype=float)
+    r = np.exp(2.0 * np.pi * evals[None, :] * times[:, None]) * r0[None, :]
+    return np.sum(opsT[None, :, :] * r[:, None, :], axis=-1)
+
+
+def lindblad_states(L, rho, times):
+    """Density matrices of lindblad_evolve without operators
+    (muspinsim/lindbladian.py:104-109)."""
+    n = rho.shape[0]
+    evals, revecs = np.linalg.eig(L)
+    r0 = np.linalg.solve(revecs, rho.reshape(-1))
+    times = np.asarray(times, dtype=float)
+    r = np.exp(2.0 * np.pi * evals[None, :] * times[:, None]) * r0[None, :]
+    return np.array([(revecs @ x).reshape(n, n) for x in r])
+
+
+def lindblad_integrate(L, rho, tau, operators):
+    """int_0^inf <O>(t) exp(-t/tau) dt (muspinsim/lindbladian.py:113-173)."""
+    evals, revecs = np.linalg.eig(L)
+    r0 = np.linalg.solve(revecs, rho.reshape(-1))
+    intops = np.array([(O.T.reshape(-1) @ revecs) / (1.0 / tau - 2.0 * np.pi * evals)
+                       for O in operators])
+    return np.sum(r0[None, :] * intops, axis=1)
+
+
+def get_xy(z):
+    """Two axes orthogonal to z (muspinsim/utils.py:71-93)."""
+    z = np.asarray(z, dtype=float)
+    z = z / np.linalg.norm(z)
+    if z[0] == 0 and z[1] == 0:
+        return np.array([1.0, 0, 0]), np.array([0, z[2], 0])
+    x = np.array([z[1], -z[0], 0.0]) / (z[0] ** 2 + z[1] ** 2) ** 0.5
+    y = np.array([z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2],
+                  z[0] * x[1] - z[1] * x[0]])
+    return x, y
+
+
+def dissipation_operators(system, B, T, dterms):
+    """(A, rate) pairs of the driver: per dissipative spin i with rate a,
+    S_+ and S_- about the field direction with rates a Zu / (pi (1 + Zu))
+    and a / (pi (1 + Zu)), Zu = exp(-h gamma_i |B| 1e6 / (k T))
+    (muspinsim/experiment.py:272-325)."""
+    Bn = np.linalg.norm(B)
+    g = system.gammas
+    if T > 0:
+        Zu = np.exp(-cnst.h * g * Bn * 1e6 / (cnst.k * T))
+    else:
+        Zu = g * 0.0
+    if Bn == 0:
+        x, y = np.array([1.0, 0, 0]), np.array([0, 1.0, 0])
+    else:
+        x, y = get_xy(np.asarray(B, dtype=float) / Bn)
+    ops = []
+    for i, a in dterms.items():
+        S = [embed(system.Is, {i: ax}) for ax in "xyz"]
+        ox = sum(S[k] * x[k] for k in range(3))
+        oy = sum(S[k] * y[k] for k in range(3))
+        ops.append((ox + 1.0j * oy, 1 / np.pi * a * Zu[i] / (1 + Zu[i])))
+        ops.append((ox - 1.0j * oy, 1 / np.pi * a / (1 + Zu[i])))
+    return ops
+
+
 _LIB = None
 
 
@@ -344,12 +427,24 @@ def t_inf_speedup(B, T, mu_i):
     return bool(check == 0) and mu_i == 0
 
 
-def snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y="asymmetry", nthreads=0):
+def snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y="asymmetry", nthreads=0,
+             dissipation=None):
     """One configuration: rotate B and p by q, add the intrinsic field, pick
-    the path, return real(data) * w (muspinsim/experiment.py:384-498)."""
+    the path, return real(data) * w (muspinsim/experiment.py:384-498).
+    ``dissipation``: {spin index: rate}; when given, the Lindbladian path
+    (muspinsim/experiment.py:332-341)."""
     Bl = quat_rotate(q, B) + np.asarray(intrinsic_B, dtype=float)
     pl = quat_rotate(q, p)
     H = Hsys + np.einsum("a,aij->ij", Bl, Z)
+    if dissipation:
+        L = lindblad_matrix(H, dissipation_operators(system, Bl, T, dissipation))
+        rho = rho0(system, Bl, pl, T)
+        O = system.muon_operator(pl)
+        if y == "integral":
+            data = lindblad_integrate(L, rho, MU_TAU, [O])[0] / MU_TAU
+        else:
+            data = lindblad_evolve(L, rho, times, [O])[:, 0]
+        return np.real(data) * w
     if y == "integral":
         rho = rho0(system, Bl, pl, T)
         O = system.muon_operator(pl)
@@ -365,7 +460,7 @@ def snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y="asymmetry", 
 
 
 def powder_average(system, orientations, B, p, T, times, intrinsic_B=(0, 0, 0),
-                   y="asymmetry", nthreads=0):
+                   y="asymmetry", nthreads=0, dissipation=None):
     """Orientation average: weights normalised to sum to N, result = sum_k
     w_k P_k / N (muspinsim/simconfig.py:152-159, 347-368)."""
     Hsys = system.hamiltonian()
@@ -379,7 +474,8 @@ def powder_average(system, orientations, B, p, T, times, intrinsic_B=(0, 0, 0),
         qs = [(q, 1.0) for q, _ in qs]
     acc = None
     for q, w in qs:
-        r = snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y, nthreads)
+        r = snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y, nthreads,
+                     dissipation)
         acc = r / N if acc is None else acc + r / N
     return acc
 

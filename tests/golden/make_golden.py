@@ -33,23 +33,27 @@ def _jsonable_couplings(couplings):
 
 
 def _run_reference(spins, couplings, times, orientations, fields, pol, temps, y_axis,
-                   x_axis, intrinsic=((0.0, 0.0, 0.0),), average_axes=("orientation",)):
+                   x_axis, intrinsic=((0.0, 0.0, 0.0),), average_axes=("orientation",),
+                   dissipation=None):
     from muspinsim.experiment import ExperimentRunner
 
     p = refshim.make_params(spins, couplings, times, orientations, field=fields,
                             intrinsic_field=intrinsic, polarization=pol, temperature=temps,
-                            y_axis=y_axis, x_axis=x_axis, average_axes=average_axes)
+                            y_axis=y_axis, x_axis=x_axis, average_axes=average_axes,
+                            dissipation=dissipation)
     er = ExperimentRunner(refshim.ParamsInput(p))
     return np.array(er.run())
 
 
 def save_experiment(name, spins, couplings, times, orientations, fields=((0.0, 0.0, 0.0),),
                     pol=(1.0, 0.0, 0.0), temps=(np.inf,), y_axis="asymmetry", x_axis="time",
-                    intrinsic=((0.0, 0.0, 0.0),), average_axes=("orientation",)):
+                    intrinsic=((0.0, 0.0, 0.0),), average_axes=("orientation",),
+                    dissipation=None):
     out = _run_reference(spins, couplings, times, orientations, fields, pol, temps, y_axis,
-                         x_axis, intrinsic, average_axes)
+                         x_axis, intrinsic, average_axes, dissipation)
     meta = {"spins": list(spins), "couplings": _jsonable_couplings(couplings),
-            "y_axis": y_axis, "x_axis": x_axis, "average_axes": list(average_axes)}
+            "y_axis": y_axis, "x_axis": x_axis, "average_axes": list(average_axes),
+            "dissipation": {str(k): float(v) for k, v in (dissipation or {}).items()}}
     np.savez_compressed(
         os.path.join(HERE, name + ".npz"),
         meta=np.array(json.dumps(meta)),
@@ -103,6 +107,37 @@ def save_direct(name):
     print(f"{name}: dim {Hm.shape[0]}")
 
 
+def save_lindblad_direct(name):
+    """Direct-API goldens of the Lindbladian: evolve with and without
+    operators and integrate_decaying, for a mu + e system in a field with
+    two dissipators (muspinsim/lindbladian.py:17-173)."""
+    from muspinsim.lindbladian import Lindbladian
+    from muspinsim.spinop import DensityOperator
+    from muspinsim.spinsys import MuonSpinSystem
+
+    sy = MuonSpinSystem(["mu", "e"])
+    sy.add_hyperfine_term(0, np.array([[120.0, 10.0, 0.0], [10.0, 80.0, 5.0], [0.0, 5.0, 60.0]]))
+    sy.add_zeeman_term(0, [0.001, 0.0, 0.004])
+    sy.add_zeeman_term(1, [0.001, 0.0, 0.004])
+    H = sy.hamiltonian
+    dops = [(sy.operator({1: "x"}), 0.7), (sy.operator({1: "+"}), 0.3),
+            (sy.operator({0: "z"}), 0.05)]
+    L = Lindbladian.from_hamiltonian(H, dops)
+    rho0 = DensityOperator.from_vectors([0.5, 0.5], [[0, 0, 1], [1, 0, 0]], [0, 0.3])
+    t = np.linspace(0, 1.5, 60)
+    ops = [sy.operator({0: "x"}), sy.operator({0: "z"}), sy.operator({1: "+"})]
+    ev = L.evolve(rho0, t, ops)
+    dens = np.array([d.matrix.toarray() for d in L.evolve(rho0, t[:5])])
+    integ = L.integrate_decaying(rho0, 2.19703, ops)
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        H=H.matrix.toarray(), L=L.matrix.toarray(), rho0=rho0.matrix.toarray(), times=t,
+        ops=np.array([o.matrix.toarray() for o in ops]),
+        dops=np.array([o.matrix.toarray() for o, _ in dops]),
+        rates=np.array([g for _, g in dops]), evolve=ev, density=dens, integral=integ)
+    print(f"{name}: L {L.matrix.shape}")
+
+
 def main():
     refshim.install()
     from muspinsim_gb300 import workloads
@@ -136,6 +171,18 @@ def main():
                     np.linspace(0, 10, 100), [(0.0, 0.0, 0.0)],
                     [(0.0, 0.0, 0.0), (0.0, 0.0, 10.0)], (1.0, 0.0, 0.0), temps=(np.inf, 0.0))
     save_direct("direct_dim24")
+    # Lindblad dissipation on the electron (muspinsim/experiment.py:272-341): finite and
+    # infinite temperature (file range), three orientations, powder average
+    save_experiment("lindblad_mu_e", ["mu", "e"], [("hyperfine", {"i": 1}, 50.0 * np.eye(3))],
+                    np.linspace(0, 2.0, 80),
+                    [(0.1, 0.2, 0.3, 1.0), (1.0, 2.0, 0.5, 2.0), (2.5, 0.4, 1.5, 0.5)],
+                    [(0.0, 0.0, 0.002)], (1.0, 0.0, 0.0), temps=(np.inf, 20.0),
+                    dissipation={2: 3.0})
+    save_experiment("lindblad_alc", ["mu", "e"], [("hyperfine", {"i": 1}, 80.0 * np.eye(3))],
+                    [0.0], [(0.0, 0.0, 0.0)], [(0.0, 0.0, b) for b in (0.0, 0.002, 0.005)],
+                    (0.0, 0.0, 1.0), temps=(5.0,), y_axis="integral", x_axis="field",
+                    dissipation={2: 1.5})
+    save_lindblad_direct("lindblad_direct")
 
 
 if __name__ == "__main__":

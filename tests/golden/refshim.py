@@ -211,6 +211,7 @@ def make_params(
     y_axis="asymmetry",
     x_axis="time",
     average_axes=("orientation",),
+    dissipation=None,
 ):
     """Build the evaluated-params dict for ``MuSpinConfig``.
 
@@ -243,4 +244,7 @@ def make_params(
     }
     for n, (kind, args, value) in enumerate(couplings):
         p["couplings"][f"{kind}_{n}"] = input_value(kind, [np.array(value, dtype=float)], args)
+    for i, rate in (dissipation or {}).items():  # 1-based spin index -> rate (MHz)
+        p["couplings"][f"dissipation_{i}"] = input_value(
+            "dissipation", [np.array([rate], dtype=float)], {"i": int(i)})
     return p

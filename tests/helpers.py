@@ -78,8 +78,9 @@ def golden_oracle(g, field_index=0, temp_index=0):
     if intr.size == 1:
         intr = np.array([0.0, 0.0, intr[0]])
     y = "integral" if g["y_axis"] == "integral" else "asymmetry"
+    diss = {int(k) - 1: float(v) for k, v in g.get("dissipation", {}).items()} or None
     return port.powder_average(sy, list(g["orientations"]), B, p, g["temperatures"][temp_index],
-                               g["times"], intrinsic_B=intr, y=y)
+                               g["times"], intrinsic_B=intr, y=y, dissipation=diss)
 
 
 def random_hermitian(rng, n, scale=100.0):

@@ -121,3 +121,52 @@ def test_cos_sum_c_matches_reference_formula():
                                              for j in range(n) for k in range(j))) / d
                     for ti in t])
     assert np.abs(port.fast_cos_sum(t, d, A, W) - ref).max() <= 1e-13
+
+
+# ---- Lindblad dissipation (muspinsim/lindbladian.py, muspinsim/experiment.py:272-341)
+
+def test_lindblad_experiment_goldens():
+    g = load_golden("lindblad_mu_e")
+    assert g["result"].shape == (2, 80)  # temperature file range x time
+    for t in range(2):
+        got = golden_oracle(g, temp_index=t)
+        assert np.abs(got - g["result"][t]).max() <= TOL
+    g = load_golden("lindblad_alc")
+    got = np.array([golden_oracle(g, field_index=f) for f in range(len(g["fields"]))])
+    assert np.abs(got - g["result"]).max() <= TOL
+
+
+def test_lindblad_direct_golden():
+    g = load_golden("lindblad_direct")
+    L = port.lindblad_matrix(g["H"], list(zip(g["dops"], g["rates"])))
+    assert np.abs(L - g["L"]).max() <= 1e-12 * np.abs(L).max()
+    ev = port.lindblad_evolve(L, g["rho0"], g["times"], list(g["ops"]))
+    assert np.abs(ev - g["evolve"]).max() <= TOL
+    dens = port.lindblad_states(L, g["rho0"], g["times"][:5])
+    assert np.abs(dens - g["density"]).max() <= TOL
+    integ = port.lindblad_integrate(L, g["rho0"], 2.19703, list(g["ops"]))
+    assert np.abs(integ - g["integral"]).max() <= TOL
+
+
+def test_lindblad_known_answers():
+    """muspinsim/tests/test_lindbladian.py:10-85 restated: the superoperator
+    of S_z with an S_x dissipator, damped precession, thermalisation."""
+    sx, sy_, sz = (port.spin_matrix(0.5, a) for a in "xyz")
+    sp, sm = sx + 1j * sy_, sx - 1j * sy_
+    assert np.allclose(port.lindblad_matrix(sz), 1j * np.diag([0, -1, 1, 0]))
+    assert np.allclose(port.lindblad_matrix(sz, [(sx, 0.1)]),
+                       [[-0.025, 0, 0, 0.025], [0, -0.025 - 1j, 0.025, 0],
+                        [0, 0.025, -0.025 + 1j, 0], [0.025, 0, 0, -0.025]])
+    rho0 = port.density_from_vector(0.5, [1, 0, 0])
+    t = np.linspace(0, 1, 100)
+    for g in [1.0, 2.0, 5.0, 10.0]:
+        ap = -0.5 * np.pi * g + complex((0.5 * np.pi * g) ** 2 - 4 * np.pi ** 2) ** 0.5
+        am = -0.5 * np.pi * g - complex((0.5 * np.pi * g) ** 2 - 4 * np.pi ** 2) ** 0.5
+        A = ap * am / (am - ap)
+        solx = np.real(0.5 * A * (np.exp(ap * t) / ap - np.exp(am * t) / am))
+        ev = port.lindblad_evolve(port.lindblad_matrix(sz, [(sx, g)]), rho0, t, [sx])
+        assert np.allclose(ev[:, 0], solx)
+        ev = port.lindblad_evolve(port.lindblad_matrix(sz, [(sp, 1.5 * g), (sm, 0.5 * g)]), rho0,
+                                  t, [sx, sz])
+        assert np.allclose(ev[:, 0], 0.5 * np.cos(2 * np.pi * t) * np.exp(-2 * np.pi * g * t))
+        assert np.allclose(ev[:, 1], 0.25 * (1 - np.exp(-4 * np.pi * g * t)))
