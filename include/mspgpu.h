@@ -349,6 +349,81 @@ int msp_multi_run(msp_multi_plan *plan, const msp_multi_io *io, void *stream);
  * `stream`. */
 int msp_multi_run_graph(msp_multi_plan *plan, const msp_multi_io *io, void *stream);
 
+/* ---- dissipation: Lindblad superoperators -------------------------------
+ * The reference switches to a Lindbladian when the configuration has
+ * dissipation terms (muspinsim/experiment.py:272-341) and diagonalises the
+ * n^2 x n^2 superoperator L with a dense non-Hermitian eig
+ * (muspinsim/lindbladian.py:43-173).  Here the same quantities come from
+ * exp(2 pi L dt) (scaling and squaring, FP64) and from a pivoted LU solve
+ * of (1/tau - 2 pi L): rho(t) = exp(2 pi L t) rho0 and
+ * int_0^inf <O>(t) e^{-t/tau} dt = vec(O^T) . (1/tau - 2 pi L)^-1 rho0.
+ * Superoperators act on row-major vec(rho); n <= 32. */
+
+/* Scratch bytes of msp_superop_evolve / _integrate for an n-level system. */
+int msp_superop_workspace(int n, int num_ops, size_t *bytes);
+
+/* <O_op>(t_k) = Tr(O_op rho(t_k)), rho(t) = exp(2 pi L t) rho0: the
+ * expectation series of Lindbladian.evolve (muspinsim/lindbladian.py:43-111).
+ * L: n^2 x n^2 complex128; rho0: n x n; ops: num_ops x n x n; out:
+ * num_times x num_ops complex128, or with num_ops = 0 the density matrices
+ * (num_times x n x n).  uniform = 1: t_k = t0 + k dt (times unused). */
+int msp_superop_evolve(const double *L, int n, const double *rho0, const double *ops,
+                       int num_ops, const double *times, int num_times, int uniform, double t0,
+                       double dt, double *out, void *workspace, size_t workspace_bytes,
+                       void *stream);
+
+/* int_0^inf <O_op>(t) e^{-t/tau} dt for each operator: Lindbladian.
+ * integrate_decaying (muspinsim/lindbladian.py:113-173); out: num_ops
+ * complex128. */
+int msp_superop_integrate(const double *L, int n, const double *rho0, const double *ops,
+                          int num_ops, double tau, double *out, void *workspace,
+                          size_t workspace_bytes, void *stream);
+
+/* A batch of dissipative snapshots of one spin system, reduced into output
+ * rows: run_single's Lindbladian branch plus store_time_slice
+ * (muspinsim/experiment.py:434-498, 272-341; muspinsim/simconfig.py:
+ * 347-368).  Per snapshot the kernel builds H = Hsys + b.Z, rho0 (muon along
+ * p, other spins thermal), the dissipators S+/- of every dissipative spin
+ * about the field direction with rates a Zu / (pi (1 + Zu)) and
+ * a / (pi (1 + Zu)), Zu = exp(-h gamma |B| 1e6 / (k T)), and L; then the
+ * time series (MSP_MODE_EVOLVE) or the decaying integral divided by tau
+ * (MSP_MODE_INTEGRAL), real part times wscale. */
+typedef struct msp_lindblad_args {
+    int n;                         /* Hilbert dimension, 2 .. 32 */
+    int num_spins;
+    int mu_index;
+    int dims[MSP_MAX_SPINS];       /* 2I+1 per spin (host), <= 10 */
+    double gammas[MSP_MAX_SPINS];  /* MHz/T (host) */
+    const double *Hsys;            /* n*n complex128 */
+    const double *Z;               /* 3*n*n complex128 */
+    const double *spin_ops;        /* num_spins x 3 x n x n complex128: S^x,y,z of
+                                      each spin, Kronecker-embedded */
+    int num_dissipative;
+    int dissipative_spin[MSP_MAX_SPINS];    /* host: spin indices */
+    double dissipative_rate[MSP_MAX_SPINS]; /* host: rates (MHz) */
+    int num_snap;
+    const double *field;           /* num_snap*3 (T) */
+    const double *pol;             /* num_snap*3 */
+    const double *wscale;          /* num_snap */
+    const int *slot;               /* num_snap, non-decreasing, < num_slots */
+    const double *temperature;     /* num_snap (K), NULL = inf */
+    int num_slots;
+    const double *times;           /* num_times (ignored when uniform = 1) */
+    int num_times;
+    int uniform;
+    double t0, dt;
+    double tau;                    /* INTEGRAL: decay time (us) */
+    int mode;                      /* MSP_MODE_EVOLVE or MSP_MODE_INTEGRAL */
+    double *out;                   /* num_slots*num_times (EVOLVE) or num_slots */
+    int *status;                   /* num_snap */
+    void *workspace;               /* >= msp_lindblad_workspace bytes, 256-byte aligned */
+    size_t workspace_bytes;
+    void *stream;
+} msp_lindblad_args;
+
+int msp_lindblad_workspace(const msp_lindblad_args *args, size_t *bytes);
+int msp_lindblad_run(const msp_lindblad_args *args);
+
 /* ---------------------------------------------------------------- adjoint
  * Gradient of a scalar loss L through the fast-path powder average
  * (K6).  The reference has no gradient: its fitting

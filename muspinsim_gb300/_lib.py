@@ -166,6 +166,43 @@ class MultiBucketInfo(ctypes.Structure):
     ]
 
 
+class LindbladArgs(ctypes.Structure):
+    """Mirror of ``msp_lindblad_args``."""
+
+    _fields_ = [
+        ("n", ctypes.c_int),
+        ("num_spins", ctypes.c_int),
+        ("mu_index", ctypes.c_int),
+        ("dims", ctypes.c_int * MAX_SPINS),
+        ("gammas", ctypes.c_double * MAX_SPINS),
+        ("Hsys", _c_dp),
+        ("Z", _c_dp),
+        ("spin_ops", _c_dp),
+        ("num_dissipative", ctypes.c_int),
+        ("dissipative_spin", ctypes.c_int * MAX_SPINS),
+        ("dissipative_rate", ctypes.c_double * MAX_SPINS),
+        ("num_snap", ctypes.c_int),
+        ("field", _c_dp),
+        ("pol", _c_dp),
+        ("wscale", _c_dp),
+        ("slot", _c_dp),
+        ("temperature", _c_dp),
+        ("num_slots", ctypes.c_int),
+        ("times", _c_dp),
+        ("num_times", ctypes.c_int),
+        ("uniform", ctypes.c_int),
+        ("t0", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("tau", ctypes.c_double),
+        ("mode", ctypes.c_int),
+        ("out", _c_dp),
+        ("status", _c_dp),
+        ("workspace", _c_dp),
+        ("workspace_bytes", ctypes.c_size_t),
+        ("stream", _c_dp),
+    ]
+
+
 TIMER_STAGES = 4
 TIMER_STAGE_NAMES = ("snapshots", "schedule", "phase", "reduce")
 
@@ -240,6 +277,19 @@ _SIGNATURES = {
         [_c_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_double,
          _c_dp, _c_dp, _c_dp, _c_dp]),
+    "msp_superop_workspace": (
+        ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    "msp_superop_evolve": (
+        ctypes.c_int,
+        [_c_dp, ctypes.c_int, _c_dp, _c_dp, ctypes.c_int, _c_dp, ctypes.c_int, ctypes.c_int,
+         ctypes.c_double, ctypes.c_double, _c_dp, _c_dp, ctypes.c_size_t, _c_dp]),
+    "msp_superop_integrate": (
+        ctypes.c_int,
+        [_c_dp, ctypes.c_int, _c_dp, _c_dp, ctypes.c_int, ctypes.c_double, _c_dp, _c_dp,
+         ctypes.c_size_t, _c_dp]),
+    "msp_lindblad_workspace": (
+        ctypes.c_int, [ctypes.POINTER(LindbladArgs), ctypes.POINTER(ctypes.c_size_t)]),
+    "msp_lindblad_run": (ctypes.c_int, [ctypes.POINTER(LindbladArgs)]),
     "msp_timer_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
     "msp_timer_destroy": (ctypes.c_int, [_c_dp]),
     "msp_timer_read": (

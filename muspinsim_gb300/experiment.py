@@ -13,12 +13,29 @@ one, and run on the GPU through the Hamiltonian methods.
 import numpy as np
 import scipy.constants as cnst
 
+from muspinsim_gb300 import kernels
 from muspinsim_gb300 import quaternion as Q
 from muspinsim_gb300.constants import MU_TAU
 from muspinsim_gb300.hamiltonian import Hamiltonian
+from muspinsim_gb300.lindbladian import Lindbladian
 from muspinsim_gb300.powder import run_snapshots, t_inf_speedup
 from muspinsim_gb300.simconfig import MuSpinConfig
-from muspinsim_gb300.spinop import DensityOperator, spin_projectors
+from muspinsim_gb300.spinop import DensityOperator, SpinOperator, spin_projectors
+
+
+def get_xy(z):
+    """Two axes x, y orthogonal to z, right-handed with it
+    (muspinsim/utils.py:71-93)."""
+    zn = np.linalg.norm(z)
+    if zn == 0:
+        raise ValueError("Can not find X and Y for null Z vector")
+    z = np.array(z) / zn
+    if z[0] == 0 and z[1] == 0:
+        return np.array([1.0, 0, 0]), np.array([0, z[2], 0])
+    x = np.array([z[1], -z[0], 0.0]) / (z[0] ** 2 + z[1] ** 2) ** 0.5
+    y = np.array([z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2],
+                  z[0] * x[1] - z[1] * x[0]])
+    return x, y
 
 
 def thermal_state(I, gamma, B, T):
@@ -137,10 +154,37 @@ class ExperimentRunner:
         return self._Hsys
 
     @property
+    def dissipation_operators(self):
+        """(operator, rate) pairs of the dissipative spins: S+ and S- about
+        the field direction with rates a Zu / (pi (1 + Zu)) and
+        a / (pi (1 + Zu)), Zu = exp(-h gamma |B| 1e6 / (k T))
+        (muspinsim/experiment.py:272-325)."""
+        B = np.linalg.norm(self._B)
+        g = np.array(self._system.gammas, dtype=float)
+        T = self._T
+        Zu = np.exp(-cnst.h * g * B * 1e6 / (cnst.k * T)) if T > 0 else g * 0.0
+        if B == 0:
+            x, y = np.array([1.0, 0, 0]), np.array([0, 1.0, 0])
+        else:
+            x, y = get_xy(self._B / B)
+        dops = []
+        for i, a in self._config.dissipation_terms.items():
+            S = [self._system.operator({i: ax}).matrix for ax in "xyz"]
+            op_x = sum(S[k] * x[k] for k in range(3))
+            op_y = sum(S[k] * y[k] for k in range(3))
+            dim = self._system.dimension
+            dops.append((SpinOperator(op_x + 1.0j * op_y, dim=dim), 1 / np.pi * a * Zu[i] / (1 + Zu[i])))
+            dops.append((SpinOperator(op_x - 1.0j * op_y, dim=dim), 1 / np.pi * a / (1 + Zu[i])))
+        return dops
+
+    @property
     def Htot(self):
+        """Hsys + Hz, or its Lindbladian when the configuration has
+        dissipation terms (muspinsim/experiment.py:332-341)."""
+        H = self.Hsys + self.Hz
         if len(self._config.dissipation_terms) > 0:
-            raise NotImplementedError("Lindblad dissipation is not supported by muspinsim_gb300")
-        return self.Hsys + self.Hz
+            H = Lindbladian.from_hamiltonian(H, self.dissipation_operators)
+        return H
 
     @property
     def p_operator(self):
@@ -162,7 +206,8 @@ class ExperimentRunner:
         self.p = q.rotate(cfg_snap.mupol)
         self.T = cfg_snap.T
         self.B = self._B + cfg_snap.intrinsic_B
-        self._T_inf_speedup = bool(t_inf_speedup(self._B, self._T, self._system.muon_index)[0])
+        self._T_inf_speedup = bool(t_inf_speedup(self._B, self._T, self._system.muon_index)[0]) \
+            and len(self._config.dissipation_terms) == 0
         return w
 
     def run_single(self, cfg_snap):
@@ -170,7 +215,7 @@ class ExperimentRunner:
         w = self.load_config(cfg_snap)
         H = self.Htot
         if cfg_snap.y == "asymmetry":
-            if self._T_inf_speedup:
+            if self._T_inf_speedup and not isinstance(H, Lindbladian):
                 other = int(np.prod(self._system.dimension)) // 2
                 data = H.fast_evolve(self._system.sigma_mu(self.p), cfg_snap.t, other)
             else:
@@ -235,12 +280,32 @@ class ExperimentRunner:
         nrows = int(np.prod(row_dims)) if row_dims else 1
         return B, intr, mupol, T, qs, ws, rows, nrows, res_dims, t_axis
 
+    def _run_lindblad(self, B_lab, p_lab, T, wscale, rows, nrows, times):
+        """Dissipative snapshots on the GPU (msp_lindblad_run, FP64 in both
+        precisions): every snapshot's Lindbladian is built and propagated on
+        the device, results reduced into the output rows."""
+        from muspinsim_gb300 import _lib
+        from muspinsim_gb300.powder import _rows_sorted
+
+        sy = self._system
+        order = _rows_sorted(np.asarray(rows))
+        n = int(np.prod(sy.dimension))
+        S_ops = np.array([[sy.operator({i: ax}).matrix.toarray() for ax in "xyz"]
+                          for i in range(len(sy.spins))], dtype=complex)
+        mode = _lib.MODE_INTEGRAL if self._config.y_axis == "integral" else _lib.MODE_EVOLVE
+        out, st = kernels.lindblad_run(
+            n, sy.hamiltonian_matrix(), sy.zeeman_operators(), S_ops, list(sy.dimension),
+            sy.muon_index, sy.gammas, self._config.dissipation_terms, B_lab[order], p_lab[order],
+            np.asarray(wscale)[order], np.asarray(rows)[order].astype(np.int32), nrows, times,
+            temperature=np.asarray(T, dtype=float)[order], mode=mode, tau=MU_TAU)
+        status = np.zeros(len(order), dtype=np.int32)
+        status[order] = st.cpu().numpy()
+        return out, status
+
     def run(self):
         """All snapshots, gathered into the results array; the results
         function is applied unless running with fitting variables
         (muspinsim/experiment.py:358-382)."""
-        if len(self._config.dissipation_terms) > 0:
-            raise NotImplementedError("Lindblad dissipation is not supported by muspinsim_gb300")
         cfg = self._config
         B, intr, mupol, T, qs, ws, rows, nrows, res_dims, t_axis = self._snapshot_arrays()
         B_lab = Q.rotate(qs, B) + intr
@@ -255,8 +320,11 @@ class ExperimentRunner:
                     # the reference's evolve rejects a scalar time (validate_times)
                     raise ValueError("times must be an array of values in microseconds")
             times = np.asarray(tval, dtype=float).reshape(-1)
-        out, status = run_snapshots(self._system, B_lab, p_lab, T, ws / cfg.avg_N, rows, nrows,
-                                    times, cfg.y_axis, self.precision)
+        if len(cfg.dissipation_terms) > 0:
+            out, status = self._run_lindblad(B_lab, p_lab, T, ws / cfg.avg_N, rows, nrows, times)
+        else:
+            out, status = run_snapshots(self._system, B_lab, p_lab, T, ws / cfg.avg_N, rows,
+                                        nrows, times, cfg.y_axis, self.precision)
         if np.any(status & 1):
             raise RuntimeError("Jacobi eigensolver did not converge for some snapshots")
         out = out.cpu().numpy()

@@ -311,6 +311,19 @@ class PowderPlan:
         self.workspace_bytes = int(nbytes.value)
         self.args = a
 
+    def rebind(self, field, pol, wscale, slot):
+        """Point the plan at new per-snapshot inputs of the same sizes (device
+        tensors), keeping its output, status and workspace."""
+        F = dev(field, torch.float64).reshape(-1, 3)
+        if F.shape[0] != self.num_snap:
+            raise ValueError("rebind: the snapshot count changed")
+        self.F, self.Pl = F, dev(pol, torch.float64).reshape(-1, 3)
+        self.W, self.Sl = dev(wscale, torch.float64).reshape(-1), dev(slot, torch.int32).reshape(-1)
+        a = self.args
+        a.field, a.pol = self.F.data_ptr(), self.Pl.data_ptr()
+        a.wscale, a.slot = self.W.data_ptr(), self.Sl.data_ptr()
+        return self
+
     def run(self, timer=None):
         """Enqueue the batch on the current stream; returns the output tensor."""
         self.args.stream = torch.cuda.current_stream().cuda_stream
@@ -487,3 +500,99 @@ class MultiPlan:
             self.close()
         except Exception:
             pass
+
+
+def _superop_ws(n, num_ops):
+    nbytes = ctypes.c_size_t(0)
+    _lib.call("msp_superop_workspace", int(n), int(num_ops), ctypes.byref(nbytes))
+    ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device=device())
+    return ws, ctypes.c_void_p(ws.data_ptr() + ((-ws.data_ptr()) % 256)), int(nbytes.value)
+
+
+def superop_evolve(L, n, rho0, ops, times):
+    """rho(t) = exp(2 pi L t) rho0 (msp_superop_evolve): (T, n_ops) complex
+    expectations Tr(O rho(t)), or (T, n*n) vec(rho(t)) when ``ops`` is empty."""
+    Ld = dev(L, torch.complex128)
+    r = dev(rho0, torch.complex128)
+    th = np.asarray(times, dtype=float)
+    o = dev(ops, torch.complex128).reshape(-1, n, n) if len(ops) else None
+    nops = 0 if o is None else int(o.shape[0])
+    uni, t0, dt = uniform_grid(th)
+    Td = dev(th, torch.float64)
+    out = torch.empty((th.size, nops if nops else n * n), dtype=torch.complex128, device=Ld.device)
+    ws, wp, nb = _superop_ws(n, nops)
+    _lib.call("msp_superop_evolve", ptr(Ld), int(n), ptr(r), ptr(o), nops, ptr(Td), int(th.size),
+              1 if uni else 0, t0, dt, ptr(out), wp, nb, stream())
+    return out
+
+
+def superop_integrate(L, n, rho0, ops, tau):
+    """int_0^inf Tr(O rho(t)) e^{-t/tau} dt for each operator
+    (msp_superop_integrate): (n_ops,) complex."""
+    Ld = dev(L, torch.complex128)
+    r = dev(rho0, torch.complex128)
+    o = dev(ops, torch.complex128).reshape(-1, n, n)
+    nops = int(o.shape[0])
+    out = torch.empty((nops,), dtype=torch.complex128, device=Ld.device)
+    ws, wp, nb = _superop_ws(n, nops)
+    _lib.call("msp_superop_integrate", ptr(Ld), int(n), ptr(r), ptr(o), nops, float(tau),
+              ptr(out), wp, nb, stream())
+    return out
+
+
+def lindblad_run(n, Hsys, Z, spin_ops, dims, mu_index, gammas, dissipation, field, pol, wscale,
+                 slot, num_slots, times, temperature=None, mode=_lib.MODE_EVOLVE, tau=1.0):
+    """A batch of dissipative snapshots reduced into output rows
+    (msp_lindblad_run).  ``dissipation``: {spin index: rate}; ``spin_ops``:
+    (num_spins, 3, n, n).  Returns (out, status): out (num_slots, T) or
+    (num_slots,) for MODE_INTEGRAL."""
+    d = device()
+    a = _lib.LindbladArgs()
+    a.n, a.num_spins, a.mu_index = int(n), len(dims), int(mu_index)
+    for i, x in enumerate(dims):
+        a.dims[i] = int(x)
+        a.gammas[i] = float(gammas[i])
+    keep = [dev(Hsys, torch.complex128), dev(Z, torch.complex128), dev(spin_ops, torch.complex128)]
+    a.Hsys, a.Z, a.spin_ops = (t.data_ptr() for t in keep)
+    a.num_dissipative = len(dissipation)
+    for k, (i, rate) in enumerate(sorted(dissipation.items())):
+        a.dissipative_spin[k] = int(i)
+        a.dissipative_rate[k] = float(rate)
+    F = dev(field, torch.float64).reshape(-1, 3)
+    S = int(F.shape[0])
+    vecs = [F, dev(pol, torch.float64).reshape(-1, 3), dev(wscale, torch.float64).reshape(-1),
+            dev(slot, torch.int32).reshape(-1)]
+    keep += vecs
+    a.num_snap = S
+    a.field, a.pol, a.wscale, a.slot = (t.data_ptr() for t in vecs)
+    if temperature is not None:
+        Tp = dev(np.ascontiguousarray(np.broadcast_to(np.asarray(temperature, float), (S,))),
+                 torch.float64)
+        keep.append(Tp)
+        a.temperature = Tp.data_ptr()
+    a.num_slots = int(num_slots)
+    if mode == _lib.MODE_INTEGRAL:
+        a.num_times, a.uniform = 1, 1
+        shape = (int(num_slots),)
+    else:
+        th = np.asarray(times, dtype=float)
+        uni, t0, dt = uniform_grid(th)
+        Td = dev(th, torch.float64)
+        keep.append(Td)
+        a.times, a.num_times, a.uniform, a.t0, a.dt = Td.data_ptr(), int(th.size), int(uni), t0, dt
+        shape = (int(num_slots), int(th.size))
+    a.tau, a.mode = float(tau), int(mode)
+    out = torch.empty(shape, dtype=torch.float64, device=d)
+    status = torch.zeros((max(S, 1),), dtype=torch.int32, device=d)
+    a.out, a.status = out.data_ptr(), status.data_ptr()
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(_lib.load().msp_lindblad_workspace(ctypes.byref(a), ctypes.byref(nbytes)),
+               "msp_lindblad_workspace")
+    ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device=d)
+    a.workspace = ws.data_ptr() + ((-ws.data_ptr()) % 256)
+    a.workspace_bytes = int(nbytes.value)
+    a.stream = torch.cuda.current_stream().cuda_stream
+    _lib.check(_lib.load().msp_lindblad_run(ctypes.byref(a)), "msp_lindblad_run")
+    out_status = (out, status[:S])
+    del keep  # inputs may be freed once the stream has consumed them (caching allocator)
+    return out_status

@@ -356,6 +356,77 @@ class DensityOperator(Operator):
         return np.sum(np.asarray(O) * _dense(R).T)
 
 
+class SuperOperator(Operator):
+    """Linear map on operators, as a matrix acting on row-major vec(rho)
+    (muspinsim/spinop.py:603-764).  Host algebra: the propagation it feeds
+    runs on the GPU (muspinsim_gb300.lindbladian)."""
+
+    def __init__(self, matrix, dim=None):
+        n = matrix.shape[0] ** 0.5
+        if int(n) != n:
+            raise ValueError("Matrix rank should be a perfect square")
+        if dim is None:
+            dim = (int(n), int(n))
+        super(SuperOperator, self).__init__(matrix, dim)
+
+    @classmethod
+    def left_multiplier(cls, operator):
+        """L rho = O rho: O (x) 1."""
+        m = operator.matrix
+        return cls(sparse.kron(m, sparse.eye(m.shape[0])), operator.dimension + operator.dimension)
+
+    @classmethod
+    def right_multiplier(cls, operator):
+        """L rho = rho O: 1 (x) O^T."""
+        m = operator.matrix
+        return cls(sparse.kron(sparse.eye(m.shape[0]), m.T), operator.dimension + operator.dimension)
+
+    @classmethod
+    def commutator(cls, operator):
+        return cls.left_multiplier(operator) - cls.right_multiplier(operator)
+
+    @classmethod
+    def anticommutator(cls, operator):
+        return cls.left_multiplier(operator) + cls.right_multiplier(operator)
+
+    @classmethod
+    def bracket(cls, operator):
+        """L rho = O rho O^dag: O (x) conj(O)."""
+        m = operator.matrix
+        return cls(sparse.kron(m, m.conjugate()), operator.dimension + operator.dimension)
+
+    def __add__(self, x):
+        if isinstance(x, (SuperOperator, Number)):
+            return super(SuperOperator, self).__add__(x)
+        raise TypeError("Unsupported operation for SuperOperator")
+
+    def __sub__(self, x):
+        if isinstance(x, (SuperOperator, Number)):
+            return super(SuperOperator, self).__sub__(x)
+        raise TypeError("Unsupported operation for SuperOperator")
+
+    def __mul__(self, x):
+        if isinstance(x, (SuperOperator, Number)):
+            return super(SuperOperator, self).__mul__(x)
+        elif isinstance(x, Operator):
+            m = _dense(x.matrix)
+            v = self.matrix.dot(m.reshape((-1,))).reshape(m.shape)
+            return Operator(v, x.dimension)
+        raise TypeError("Unsupported operation for Operator")
+
+    def __rmul__(self, x):
+        if isinstance(x, Number):
+            return self.__mul__(x)
+        elif isinstance(x, SuperOperator):
+            return x * self
+        raise TypeError("Unsupported operation for Operator")
+
+    def __truediv__(self, x):
+        if isinstance(x, Number):
+            return self * (1.0 / x)
+        raise TypeError("Unsupported operation for Operator")
+
+
 def spin_projectors(I, axis):
     """Spectral projectors of n . S for a single spin I along unit(axis).
 

@@ -115,7 +115,7 @@ class DoubleTerm(InteractionTerm):
 
 class DissipationTerm(Clonable):
     """Container of a dissipation operator and rate (muspinsim/spinsys.py:
-    143-158).  Lindblad propagation itself is not part of this library."""
+    143-158)."""
 
     def __init__(self, operator, gamma=0.0):
         self._op = operator
@@ -353,7 +353,12 @@ class SpinSystem(Clonable):
 
     @property
     def lindbladian(self):
-        raise NotImplementedError("Lindblad dissipation is not supported by muspinsim_gb300")
+        """Lindbladian of the Hamiltonian and the dissipation terms
+        (muspinsim/spinsys.py:628-634); propagated on the GPU."""
+        from muspinsim_gb300.lindbladian import Lindbladian
+
+        return Lindbladian.from_hamiltonian(self.hamiltonian,
+                                            [t.tuple for t in self._dissip_terms])
 
     def zeeman_operators(self):
         """Z_a = sum_i gamma_i S^a_i (dense, a = x, y, z): Hz(B) = sum_a B_a Z_a
