@@ -64,7 +64,7 @@ def parse_args():
                    help="orientations per step of the --impl reference arm")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="config2",
-                   choices=["config1", "config2", "config3", "config4", "config5"],
+                   choices=["config1", "config2", "config3", "config4", "config5", "lindblad"],
                    help="config2 (default) is the headline; the others print their own line")
     return p.parse_args()
 
@@ -716,6 +716,76 @@ def run_config5(args, world, rank, local):
     return line
 
 
+def run_lindblad(args, world, rank, local):
+    """Dissipative powder average (the Lindbladian branch of run_single):
+    mu, e, 1H (n = 8, superoperator 64 x 64), dissipation on the electron
+    and the proton, B = 3 mT, T = 20 K, 500 ZCW-style orientations, 1000
+    times on 0-10 us.  FP64 (exp(2 pi L dt) propagation on the device)."""
+    import torch
+
+    from muspinsim_gb300 import _lib, kernels, workloads
+    from muspinsim_gb300 import quaternion as Q
+    from muspinsim_gb300.orientations import orientation_rows_to_quats, zcw_gen
+
+    rng = np.random.default_rng(1006)
+    wl = workloads.Workload(
+        name="mu_e_H_lindblad", spins=["mu", "e", "H"],
+        couplings=[("hyperfine", {"i": 1}, workloads.random_hyperfine(rng, 30.0)),
+                   ("hyperfine", {"i": 3}, workloads.random_hyperfine(rng, 5.0))],
+        orientations=zcw_gen(500), fields=np.array([[0.0, 0.0, 0.003]]),
+        polarization=np.array([0.0, 0.0, 1.0]), times=np.linspace(0.0, 10.0, 1000),
+        temperature=20.0)
+    diss = {1: 2.0, 2: 0.3}
+    sy = wl.system()
+    qs, ws = orientation_rows_to_quats(wl.orientations)
+    N = len(qs)
+    ws = ws * (N / ws.sum())
+    B_lab, p_lab = Q.rotate(qs, wl.fields[0]), Q.rotate(qs, wl.polarization)
+    n = 8
+    S_ops = np.array([[sy.operator({i: ax}).matrix.toarray() for ax in "xyz"]
+                      for i in range(3)], dtype=complex)
+    T = len(wl.times)
+
+    def step():
+        return kernels.lindblad_run(n, sy.hamiltonian_matrix(), sy.zeeman_operators(), S_ops,
+                                    list(sy.dimension), 0, sy.gammas, diss, B_lab, p_lab, ws / N,
+                                    np.zeros(N, np.int32), 1, wl.times,
+                                    temperature=wl.temperature)[0]
+
+    for _ in range(args.warmup):
+        step()
+    ms = _events_ms(step, max(1, args.steps))
+    out = step().cpu().numpy()[0]
+    line = _line("dissipative powder P(t) samples/s, FP64", N * T / (ms * 1e-3), "samples/s", ms,
+                 args, world, "mu_e_H_lindblad_500_orient_1000_t",
+                 {"orientations": N, "times": T, "dim": n, "superoperator": n * n,
+                  "dissipation_MHz": {"e": 2.0, "H": 0.3}, "temperature_K": 20.0},
+                 dtype="f64", gpu_launches=3 * max(1, args.steps),
+                 note="e2e: every step uploads the orientation vectors (host inputs)")
+    if not args.no_cpu_baseline:
+        from oracle import port
+        from tests.helpers import oracle_system
+
+        osy = oracle_system(wl.spins, wl.couplings)
+        sample = 20
+        t0 = time.perf_counter()
+        ref = port.powder_average(osy, wl.orientations[:sample], wl.fields[0], wl.polarization,
+                                  wl.temperature, wl.times, dissipation=diss)
+        dt = time.perf_counter() - t0
+        gpu20 = kernels.lindblad_run(n, sy.hamiltonian_matrix(), sy.zeeman_operators(), S_ops,
+                                     list(sy.dimension), 0, sy.gammas, diss, B_lab[:sample],
+                                     p_lab[:sample],
+                                     (ws[:sample] * (sample / ws[:sample].sum())) / sample,
+                                     np.zeros(sample, np.int32), 1, wl.times,
+                                     temperature=wl.temperature)[0].cpu().numpy()[0]
+        line["max_abs_dP_vs_oracle_20_orient"] = float(np.abs(gpu20 - ref).max())
+        line["cpu_baseline"] = {"value": sample * T / dt, "unit": "samples/s", "cores": 1,
+                                "kind": "port",
+                                "sample": f"{sample} orientations (numpy eig of L per snapshot)"}
+    del out
+    return line
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args)
@@ -726,7 +796,7 @@ def main():
 
         torch.cuda.set_device(local)
         fn = {"config1": run_config1, "config3": run_config3, "config4": run_config4,
-              "config5": run_config5}[args.workload]
+              "config5": run_config5, "lindblad": run_lindblad}[args.workload]
         line = fn(args, world, rank, local)
         if rank == 0:
             print(json.dumps(line))
