@@ -472,6 +472,88 @@ int msp_adjoint_workspace(const msp_adjoint_args *args, size_t *bytes);
  * msp_adjoint_sum (deterministic sum over snapshots). */
 int msp_adjoint_fast(const msp_adjoint_args *args);
 
+/* ---------------------------------------------------------------- Celio's method
+ * Trotter evolution without diagonalisation: CelioHamiltonian.evolve and
+ * .fast_evolve (muspinsim/celio.py:210-476) and the reference's native
+ * module behind the latter (muspinsim/cpp/celio.cpp:23-64,
+ * muspinsim/cpp/parallel.cpp:126-262: celio_evolve, fast_measure_h,
+ * fast_evolve).  A state is a tensor of `num_digits` digits (spin
+ * multiplicities, digit 0 slowest).  One Trotter pass applies every factor
+ * in order -- factor f multiplies the D_f-element groups of its one or two
+ * digits (given in the factor's own order, the reference's spin_order) by
+ * the D_f x D_f complex matrix at factor_mat[f] in the snapshot's block --
+ * and one time step is trotter_k passes.  Per time sample, first measure,
+ * then step.
+ *   MSP_CELIO_PURE:    num_digits = spins, muon first (digit 0 of dimension
+ *                      2); states_per_snapshot random initial states
+ *                      mu_psi (x) exp(2 pi i r) / sqrt(d) per snapshot, r
+ *                      from `phases` ([S][A][d], uniform in [0,1)) or, when
+ *                      phases is NULL, from a counter-based generator keyed
+ *                      by `seed`; series[s][a][t] = Re <psi|(sigma_s (x) 1)|psi>.
+ *   MSP_CELIO_DENSITY: num_digits = 2 x spins (row digits, then column
+ *                      digits of rho); pass the factors as (U^dagger on the
+ *                      row digits, U^T on the column digits) so that a pass
+ *                      maps rho to U^dagger rho U as the reference's
+ *                      T^dag rho0 T does; series[s][t][j] = sum rho .* meas_j
+ *                      (meas_j = O_j^T, complex).
+ * rows_out[r][t] (optional) = sum over the snapshots row_start[r] ..
+ * row_start[r+1]-1 of wscale[s] * (PURE: 0.5 / A sum_a series, DENSITY:
+ * Re series of operator 0) -- the averaged, weighted result of
+ * ExperimentRunner.run_single.  All FP64.  States that fit in one CTA's
+ * shared memory run there from start to end; larger ones run from global
+ * memory (path: 0 automatic, 1 shared memory, 2 global memory). */
+#define MSP_CELIO_PURE 0
+#define MSP_CELIO_DENSITY 1
+
+typedef struct msp_celio_args {
+    int mode;                     /* MSP_CELIO_* */
+    int num_digits;               /* 1..32 */
+    const int *digit_dims;        /* host [num_digits] */
+    int num_factors;              /* 0..1024 factor applications per Trotter pass */
+    const int *factor_digits;     /* host [num_factors][2]; second digit -1 for one */
+    const long long *factor_mat;  /* host [num_factors]: matrix offset (complex entries) */
+    const double *mats;           /* device complex [num_snapshots or 1][mats_len] */
+    long long mats_len;
+    int mats_per_snapshot;        /* 1: one block per snapshot; 0: one shared block */
+    int num_snapshots;
+    int states_per_snapshot;      /* PURE: averages; DENSITY: 1 */
+    int trotter_k;                /* >= 1 */
+    int num_times;
+    const double *mu_psi;         /* PURE: device complex [S][2] */
+    const double *sigma;          /* PURE: device complex [S][2][2], Hermitian */
+    const double *phases;         /* PURE: device [S][A][d] or NULL */
+    unsigned long long seed;
+    const double *rho0;           /* DENSITY: device complex [S][N][N] */
+    const double *meas;           /* DENSITY: device complex [S or 1][num_ops][N][N] */
+    int num_ops;
+    int meas_per_snapshot;
+    void *series;                 /* device: PURE double [S][A][T]; DENSITY complex
+                                     [S][T][num_ops]; NULL = in the workspace */
+    const double *wscale;         /* device [S] or NULL (1) */
+    const int *row_start;         /* device [num_rows + 1], for rows_out */
+    int num_rows;
+    double *rows_out;             /* device [num_rows][T] or NULL */
+    int path;                     /* 0 automatic, 1 shared memory, 2 global memory */
+} msp_celio_args;
+
+int msp_celio_workspace(const msp_celio_args *args, size_t *bytes);
+int msp_celio_run(const msp_celio_args *args, void *workspace, size_t workspace_bytes,
+                  void *stream);
+
+/* Trotter factors that depend on the field, per snapshot: U = exp(-2 pi i
+ * tau (H0_f + sum_a B[s][a] G_f[a])) for each field-dependent factor f
+ * (a spin's Zeeman term, alone or merged with other one-spin terms:
+ * muspinsim/celio.py:145-160, muspinsim/experiment.py:251-267), tau =
+ * dt / k; written into each snapshot's block of `mats` as U, U^dagger and /
+ * or U^T at out_offsets[f][0..2] (-1 skips).  dims (host, 1..16 each) and
+ * out_offsets (host) describe up to 64 factors; H0 (device) holds their
+ * D_f x D_f complex matrices back to back and G (device) three per factor
+ * (x, y, z); fields (device) [S][3] in T. */
+int msp_celio_expm(int num_snapshots, int num_factors, const int *dims, const double *H0,
+                   const double *G, const double *fields, double tau,
+                   const long long *out_offsets, double *mats, long long mats_len,
+                   void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -203,6 +203,44 @@ class LindbladArgs(ctypes.Structure):
     ]
 
 
+CELIO_PURE = 0
+CELIO_DENSITY = 1
+
+
+class CelioArgs(ctypes.Structure):
+    """Mirror of ``msp_celio_args``."""
+
+    _fields_ = [
+        ("mode", ctypes.c_int),
+        ("num_digits", ctypes.c_int),
+        ("digit_dims", ctypes.POINTER(ctypes.c_int)),
+        ("num_factors", ctypes.c_int),
+        ("factor_digits", ctypes.POINTER(ctypes.c_int)),
+        ("factor_mat", ctypes.POINTER(ctypes.c_longlong)),
+        ("mats", _c_dp),
+        ("mats_len", ctypes.c_longlong),
+        ("mats_per_snapshot", ctypes.c_int),
+        ("num_snapshots", ctypes.c_int),
+        ("states_per_snapshot", ctypes.c_int),
+        ("trotter_k", ctypes.c_int),
+        ("num_times", ctypes.c_int),
+        ("mu_psi", _c_dp),
+        ("sigma", _c_dp),
+        ("phases", _c_dp),
+        ("seed", ctypes.c_ulonglong),
+        ("rho0", _c_dp),
+        ("meas", _c_dp),
+        ("num_ops", ctypes.c_int),
+        ("meas_per_snapshot", ctypes.c_int),
+        ("series", _c_dp),
+        ("wscale", _c_dp),
+        ("row_start", _c_dp),
+        ("num_rows", ctypes.c_int),
+        ("rows_out", _c_dp),
+        ("path", ctypes.c_int),
+    ]
+
+
 TIMER_STAGES = 4
 TIMER_STAGE_NAMES = ("snapshots", "schedule", "phase", "reduce")
 
@@ -290,6 +328,14 @@ _SIGNATURES = {
     "msp_lindblad_workspace": (
         ctypes.c_int, [ctypes.POINTER(LindbladArgs), ctypes.POINTER(ctypes.c_size_t)]),
     "msp_lindblad_run": (ctypes.c_int, [ctypes.POINTER(LindbladArgs)]),
+    "msp_celio_workspace": (
+        ctypes.c_int, [ctypes.POINTER(CelioArgs), ctypes.POINTER(ctypes.c_size_t)]),
+    "msp_celio_run": (
+        ctypes.c_int, [ctypes.POINTER(CelioArgs), _c_dp, ctypes.c_size_t, _c_dp]),
+    "msp_celio_expm": (
+        ctypes.c_int,
+        [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _c_dp, _c_dp, _c_dp,
+         ctypes.c_double, ctypes.POINTER(ctypes.c_longlong), _c_dp, ctypes.c_longlong, _c_dp]),
     "msp_timer_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
     "msp_timer_destroy": (ctypes.c_int, [_c_dp]),
     "msp_timer_read": (

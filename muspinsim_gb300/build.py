@@ -19,7 +19,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libmspgpu.so"
 SOURCES = ["msp_snap.cu", "msp_phase.cu", "msp_api.cu", "msp_static.cu", "msp_adjoint.cu", "msp_large.cu",
            "msp_multi.cu", "msp_orient.cu", "msp_assemble.cu",
-           "msp_lindblad.cu"]
+           "msp_lindblad.cu", "msp_celio.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
 

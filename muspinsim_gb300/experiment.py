@@ -17,6 +17,8 @@ from muspinsim_gb300 import kernels
 from muspinsim_gb300 import quaternion as Q
 from muspinsim_gb300.constants import MU_TAU
 from muspinsim_gb300.hamiltonian import Hamiltonian
+from muspinsim_gb300 import celio
+from muspinsim_gb300.celio import CelioHamiltonian
 from muspinsim_gb300.lindbladian import Lindbladian
 from muspinsim_gb300.powder import run_snapshots, t_inf_speedup
 from muspinsim_gb300.simconfig import MuSpinConfig
@@ -74,8 +76,6 @@ class ExperimentRunner:
         self._B = np.zeros(3)
         self._p = np.array([1.0, 0, 0])
         self._T = np.inf
-        if self._config.celio_k:
-            raise NotImplementedError("Celio's method is not supported by muspinsim_gb300")
         self._Hsys = self._system.hamiltonian
         self._rho0 = None
         self._Hz = None
@@ -143,7 +143,18 @@ class ExperimentRunner:
 
     @property
     def Hz(self):
-        """Zeeman Hamiltonian sum_i gamma_i B.S_i (muspinsim/experiment.py:239-269)."""
+        """Zeeman Hamiltonian sum_i gamma_i B.S_i (muspinsim/experiment.py:239-269);
+        with Celio's method, a CelioHamiltonian of one Zeeman term per spin
+        (none in zero field)."""
+        if self._Hz is None and self._config.celio_k:
+            from muspinsim_gb300.celio import CelioHamiltonian
+            from muspinsim_gb300.spinsys import SingleTerm
+
+            extra = []
+            if not np.array_equal(self._B, [0, 0, 0]):
+                extra = [SingleTerm(self._system, i, self._B * self._system.gammas[i],
+                                    label="Zeeman") for i in range(len(self._system.spins))]
+            self._Hz = CelioHamiltonian(extra, self._config.celio_k, self._system)
         if self._Hz is None:
             Z = self._system.zeeman_operators()
             self._Hz = Hamiltonian(np.einsum("a,aij->ij", self._B, Z), dim=self._system.dimension)
@@ -159,6 +170,8 @@ class ExperimentRunner:
         the field direction with rates a Zu / (pi (1 + Zu)) and
         a / (pi (1 + Zu)), Zu = exp(-h gamma |B| 1e6 / (k T))
         (muspinsim/experiment.py:272-325)."""
+        if self._config.celio_k:
+            raise NotImplementedError("Dissipation is not supported when using Celio's method")
         B = np.linalg.norm(self._B)
         g = np.array(self._system.gammas, dtype=float)
         T = self._T
@@ -215,7 +228,14 @@ class ExperimentRunner:
         w = self.load_config(cfg_snap)
         H = self.Htot
         if cfg_snap.y == "asymmetry":
-            if self._T_inf_speedup and not isinstance(H, Lindbladian):
+            if isinstance(H, CelioHamiltonian) and self._config.celio_averages:
+                if self.T != np.inf:
+                    raise ValueError(
+                        "The fast version of Celio's method requires T -> inf. Either remove "
+                        "the number of averages or don't use celio.")
+                data = H.fast_evolve(self._system.sigma_mu(self.p), cfg_snap.t,
+                                     self._config.celio_averages, True)
+            elif self._T_inf_speedup and not isinstance(H, (Lindbladian, CelioHamiltonian)):
                 other = int(np.prod(self._system.dimension)) // 2
                 data = H.fast_evolve(self._system.sigma_mu(self.p), cfg_snap.t, other)
             else:
@@ -320,7 +340,16 @@ class ExperimentRunner:
                     # the reference's evolve rejects a scalar time (validate_times)
                     raise ValueError("times must be an array of values in microseconds")
             times = np.asarray(tval, dtype=float).reshape(-1)
-        if len(cfg.dissipation_terms) > 0:
+        if cfg.celio_k:
+            if len(cfg.dissipation_terms) > 0:
+                raise NotImplementedError("Dissipation is not supported when using Celio's method")
+            if cfg.y_axis == "integral":
+                raise NotImplementedError(
+                    "integrate_decaying is not implemented for Celio's method")
+            out = celio.run_snapshots(self._system, cfg.celio_k, cfg.celio_averages, B_lab, p_lab,
+                                      T, ws / cfg.avg_N, rows, nrows, times)
+            status = np.zeros(len(B_lab), dtype=np.int32)
+        elif len(cfg.dissipation_terms) > 0:
             out, status = self._run_lindblad(B_lab, p_lab, T, ws / cfg.avg_N, rows, nrows, times)
         else:
             out, status = run_snapshots(self._system, B_lab, p_lab, T, ws / cfg.avg_N, rows,

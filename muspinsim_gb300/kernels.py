@@ -596,3 +596,100 @@ def lindblad_run(n, Hsys, Z, spin_ops, dims, mu_index, gammas, dissipation, fiel
     out_status = (out, status[:S])
     del keep  # inputs may be freed once the stream has consumed them (caching allocator)
     return out_status
+
+
+def celio_run(mode, digit_dims, factor_digits, factor_mat, mats, mats_per_snapshot,
+              num_snapshots, states_per_snapshot, trotter_k, num_times, mu_psi=None, sigma=None,
+              phases=None, seed=0, rho0=None, meas=None, meas_per_snapshot=False,
+              wscale=None, row_start=None, num_rows=0, path=0):
+    """Celio's method through ``msp_celio_run`` (FP64).
+
+    ``digit_dims``: multiplicity of each digit of a state (spins for
+    CELIO_PURE, row then column spins for CELIO_DENSITY);
+    ``factor_digits``: [(d0, d1 or -1)] per factor application of one
+    Trotter pass; ``factor_mat``: each factor's matrix offset (complex
+    entries) in a snapshot's block of ``mats`` ((S or 1, mats_len) complex).
+    Returns (series, rows): series (S, A, T) float64 for PURE or (S, T,
+    num_ops) complex128 for DENSITY; rows (num_rows, T) when ``row_start``
+    is given, else None."""
+    d = device()
+    digit_dims = np.ascontiguousarray(digit_dims, dtype=np.int32)
+    fd = np.ascontiguousarray(np.asarray(factor_digits, dtype=np.int32).reshape(-1, 2))
+    fm = np.ascontiguousarray(np.asarray(factor_mat, dtype=np.int64).reshape(-1))
+    nf = fd.shape[0]
+    mats_d = dev(mats, torch.complex128) if nf > 0 else None
+    mats_len = int(mats_d.shape[-1]) if mats_d is not None else 0
+    S, A, T = int(num_snapshots), int(states_per_snapshot), int(num_times)
+    a = _lib.CelioArgs()
+    a.mode = int(mode)
+    a.num_digits = len(digit_dims)
+    a.digit_dims = digit_dims.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    a.num_factors = nf
+    a.factor_digits = fd.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    a.factor_mat = fm.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))
+    a.mats = ptr(mats_d)
+    a.mats_len = mats_len
+    a.mats_per_snapshot = int(bool(mats_per_snapshot))
+    a.num_snapshots = S
+    a.states_per_snapshot = A
+    a.trotter_k = int(trotter_k)
+    a.num_times = T
+    keep = []
+    if mode == _lib.CELIO_PURE:
+        mu = dev(mu_psi, torch.complex128)
+        sg = dev(sigma, torch.complex128)
+        keep += [mu, sg]
+        a.mu_psi, a.sigma = ptr(mu), ptr(sg)
+        if phases is not None:
+            ph = dev(phases, torch.float64)
+            keep.append(ph)
+            a.phases = ptr(ph)
+        a.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+        series = torch.empty((S, A, T), dtype=torch.float64, device=d)
+    else:
+        r0 = dev(rho0, torch.complex128)
+        ms = dev(meas, torch.complex128)
+        keep += [r0, ms]
+        a.rho0, a.meas = ptr(r0), ptr(ms)
+        a.num_ops = int(ms.shape[-3]) if ms.dim() >= 3 else 1
+        a.meas_per_snapshot = int(bool(meas_per_snapshot))
+        series = torch.empty((S, T, a.num_ops), dtype=torch.complex128, device=d)
+    a.series = ptr(series)
+    rows = None
+    if row_start is not None:
+        rs = dev(row_start, torch.int32)
+        keep.append(rs)
+        rows = torch.empty((int(num_rows), T), dtype=torch.float64, device=d)
+        a.row_start, a.num_rows, a.rows_out = ptr(rs), int(num_rows), ptr(rows)
+        if wscale is not None:
+            ws_ = dev(wscale, torch.float64)
+            keep.append(ws_)
+            a.wscale = ptr(ws_)
+    a.path = int(path)
+    nbytes = ctypes.c_size_t(0)
+    _lib.call("msp_celio_workspace", ctypes.byref(a), ctypes.byref(nbytes))
+    ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device=d)
+    base = ws.data_ptr()
+    aligned = (base + 255) & ~255
+    _lib.call("msp_celio_run", ctypes.byref(a), ctypes.c_void_p(aligned),
+              ctypes.c_size_t(int(nbytes.value)), stream())
+    return series, rows
+
+
+def celio_expm(dims, H0, G, fields, tau, out_offsets, mats):
+    """Field-dependent Trotter factors in place: for every snapshot s and
+    factor f, exp(-2 pi i tau (H0_f + sum_a B[s, a] G_f[a])) written into
+    ``mats[s]`` (complex (S, mats_len), device) at out_offsets[f] (U,
+    U^dagger, U^T; -1 skips).  ``H0``: list of (D, D), ``G``: list of
+    (3, D, D) complex arrays."""
+    dims = np.ascontiguousarray(dims, dtype=np.int32)
+    h = np.concatenate([np.asarray(m, dtype=complex).reshape(-1) for m in H0])
+    g = np.concatenate([np.asarray(m, dtype=complex).reshape(-1) for m in G])
+    hd, gd = dev(h, torch.complex128), dev(g, torch.complex128)
+    B = dev(np.asarray(fields, dtype=float).reshape(-1, 3), torch.float64)
+    oo = np.ascontiguousarray(np.asarray(out_offsets, dtype=np.int64).reshape(-1, 3))
+    _lib.call("msp_celio_expm", int(B.shape[0]), len(dims),
+              dims.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), ptr(hd), ptr(gd), ptr(B),
+              float(tau), oo.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), ptr(mats),
+              int(mats.shape[-1]), stream())
+    return mats

@@ -35,16 +35,18 @@ class InteractionTerm(Clonable):
     def _recalc_operator(self):
         """Sum over all tensor index tuples of the Kronecker-embedded spin
         operators; a same-spin pair (quadrupole) multiplies S^a_i S^b_i
-        (muspinsim/spinsys.py:34-69)."""
+        (muspinsim/spinsys.py:34-69).  With Celio's method the operator
+        spans only the term's own spins (in ascending spin order)."""
         total = None
         d = len(self._tensor.shape)
         tuples = np.indices(self._tensor.shape).reshape((d, -1)).T if d > 0 else [[]]
+        only = bool(self._spinsys.celio_k)
         for ii in tuples:
             if len(self._indices) == 2 and self._indices[0] == self._indices[1]:
                 spec = {int(self._indices[0]): ["xyz"[ii[0]], "xyz"[ii[1]]]}
             else:
                 spec = {int(ind): "xyz"[ii[k]] for k, ind in enumerate(self._indices)}
-            op = self._spinsys.operator(spec) * self._tensor[tuple(ii)]
+            op = self._spinsys.operator(spec, include_only_given=only) * self._tensor[tuple(ii)]
             total = op if total is None else total + op
         self._operator = total
 
@@ -341,9 +343,12 @@ class SpinSystem(Clonable):
 
     @property
     def hamiltonian(self):
-        """Hsys = sum of term matrices (muspinsim/spinsys.py:613-626)."""
+        """Hsys = sum of term matrices (muspinsim/spinsys.py:613-626), or a
+        CelioHamiltonian of the terms with Celio's method."""
         if self._celio_k:
-            raise NotImplementedError("Celio's method is not supported by muspinsim_gb300")
+            from muspinsim_gb300.celio import CelioHamiltonian
+
+            return CelioHamiltonian(self._terms, self._celio_k, self)
         if len(self._terms) == 0:
             n = int(np.prod(self.dimension))
             H = sparse.csr_matrix((n, n), dtype=complex)

@@ -37,3 +37,15 @@ def validate_integrate_decaying_params(rho0, tau, operators):
         raise ValueError("At least one SpinOperator must be present in 'operators'")
     if not all([isinstance(o, SpinOperator) for o in operators]):
         raise ValueError("'operators' must be a SpinOperator or a list of SpinOperator objects")
+
+
+def validate_celio_params(terms, times):
+    """Celio's method needs interaction terms and a uniform time grid that
+    starts at 0 (muspinsim/validation.py:48-71)."""
+    if len(terms) == 0:
+        raise ValueError("No interaction terms to evolve")
+    if times[0] != 0:
+        raise ValueError("Cannot use Celio's method with a non-zero start time")
+    differences = np.diff(times)
+    if not np.isclose(differences, differences[0]).all():
+        raise ValueError("Cannot use Celio's method with uneven spacing between times")

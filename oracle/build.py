@@ -4,6 +4,11 @@ Two outputs, both git-ignored:
 
 * ``oracle/_build/liboracle.so`` -- the plain-C restatement of the phase-sum
   kernel (``oracle/fast_cos_sum.c``), compiled with gcc and OpenMP.
+* ``oracle/_ref/cpp<EXT_SUFFIX>`` -- the reference's pybind11 module of
+  Celio's method (``muspinsim/cpp/*.cpp``), compiled from its sources with
+  g++ and OpenMP where both the reference tree and pybind11 are present
+  (the golden-vector generator only; nothing on a machine without them
+  needs it).
 * ``oracle/_ref/_ref_parallel<EXT_SUFFIX>`` -- the reference's own Cython
   kernel (``muspinsim/cython/parallel.pyx``), compiled from the reference
   sources.  Where the reference tree is present, Cython first translates the
@@ -46,11 +51,12 @@ def ref_module_path():
 def build_port(force=False):
     """Compile the C restatement into oracle/_build/liboracle.so."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    src = os.path.join(HERE, "fast_cos_sum.c")
+    srcs = [os.path.join(HERE, f) for f in ("fast_cos_sum.c", "celio.c")]
     out = oracle_lib_path()
-    if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+    if not force and os.path.exists(out) and all(
+            os.path.getmtime(out) >= os.path.getmtime(s) for s in srcs):
         return out
-    _run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", src, "-o", out, "-lm"])
+    _run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared"] + srcs + ["-o", out, "-lm"])
     return out
 
 
@@ -75,6 +81,36 @@ def build_ref(force=False):
     cmd = ["gcc", "-w", "-O3", "-funroll-loops", "-fopenmp", "-fPIC", "-shared"]
     cmd += [f"-I{p}" for p in inc]
     cmd += [csrc, "-o", out, "-fopenmp", "-lm"]
+    _run(cmd)
+    return out
+
+
+REF_CPP = os.path.join(REFERENCE_ROOT, "muspinsim", "cpp")
+
+
+def ref_cpp_path():
+    return os.path.join(REF_DIR, "cpp" + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def build_ref_cpp(force=False):
+    """Compile the reference's pybind11 module (Celio's method) from its own
+    sources into oracle/_ref; returns its path, or None where the reference
+    tree or pybind11 is missing."""
+    try:
+        import pybind11
+    except ImportError:
+        return None
+    if not os.path.isdir(REF_CPP):
+        return None
+    os.makedirs(REF_DIR, exist_ok=True)
+    srcs = sorted(os.path.join(REF_CPP, f) for f in os.listdir(REF_CPP) if f.endswith(".cpp"))
+    out = ref_cpp_path()
+    if not force and os.path.exists(out) and all(
+            os.path.getmtime(out) >= os.path.getmtime(s) for s in srcs):
+        return out
+    inc = [sysconfig.get_paths()["include"], pybind11.get_include()]
+    cmd = ["g++", "-w", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared"]
+    cmd += [f"-I{p}" for p in inc] + srcs + ["-o", out]
     _run(cmd)
     return out
 

@@ -428,13 +428,31 @@ def t_inf_speedup(B, T, mu_i):
 
 
 def snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y="asymmetry", nthreads=0,
-             dissipation=None):
+             dissipation=None, celio=(0, 0), phases=None):
     """One configuration: rotate B and p by q, add the intrinsic field, pick
     the path, return real(data) * w (muspinsim/experiment.py:384-498).
     ``dissipation``: {spin index: rate}; when given, the Lindbladian path
-    (muspinsim/experiment.py:332-341)."""
+    (muspinsim/experiment.py:332-341).  ``celio``: (k, averages) of Celio's
+    method, with ``phases`` [averages, d] for its random initial states
+    (muspinsim/experiment.py:451-471)."""
     Bl = quat_rotate(q, B) + np.asarray(intrinsic_B, dtype=float)
     pl = quat_rotate(q, p)
+    if celio[0]:
+        if y == "integral":
+            raise NotImplementedError("integrate_decaying is not implemented for Celio's method")
+        k, avg = celio
+        times = np.asarray(times, dtype=float)
+        factors = celio_snapshot_factors(system, Bl, times[1] - times[0], k)
+        if avg:
+            if T != np.inf:
+                raise ValueError("The fast version of Celio's method requires T -> inf.")
+            if system.mu_i != 0:
+                raise ValueError("Muon must be the first spin in the system")
+            data = celio_fast_evolve(factors, list(system.dims), sigma_mu(pl), times, k, phases)
+        else:
+            data = celio_evolve(factors, list(system.dims), rho0(system, Bl, pl, T), times,
+                                [system.muon_operator(pl)], k)[:, 0]
+        return np.real(data) * w
     H = Hsys + np.einsum("a,aij->ij", Bl, Z)
     if dissipation:
         L = lindblad_matrix(H, dissipation_operators(system, Bl, T, dissipation))
@@ -460,9 +478,10 @@ def snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y="asymmetry", 
 
 
 def powder_average(system, orientations, B, p, T, times, intrinsic_B=(0, 0, 0),
-                   y="asymmetry", nthreads=0, dissipation=None):
+                   y="asymmetry", nthreads=0, dissipation=None, celio=(0, 0), phases=None):
     """Orientation average: weights normalised to sum to N, result = sum_k
-    w_k P_k / N (muspinsim/simconfig.py:152-159, 347-368)."""
+    w_k P_k / N (muspinsim/simconfig.py:152-159, 347-368).  ``phases``:
+    [orientations, averages, d] for Celio's method with averages."""
     Hsys = system.hamiltonian()
     Z = system.zeeman_operators()
     qs = [orientation_quat(o) for o in orientations]
@@ -473,9 +492,9 @@ def powder_average(system, orientations, B, p, T, times, intrinsic_B=(0, 0, 0),
     else:
         qs = [(q, 1.0) for q, _ in qs]
     acc = None
-    for q, w in qs:
+    for s_i, (q, w) in enumerate(qs):
         r = snapshot(system, Hsys, Z, q, w, B, p, T, intrinsic_B, times, y, nthreads,
-                     dissipation)
+                     dissipation, celio, None if phases is None else phases[s_i])
         acc = r / N if acc is None else acc + r / N
     return acc
 
@@ -538,3 +557,202 @@ def fast_powder_grad(system, orientations, B, p, times, g):
         GH += G
         GB.append([np.real(np.sum(np.conj(G) * Z[a])) for a in range(3)])
     return GH, np.array(GB)
+
+
+# ---------------------------------------------------------------- Celio's method
+def celio_term_matrix(system, indices, tensor):
+    """A term's operator over its own spins only, in ascending spin order
+    (``include_only_given``: muspinsim/spinsys.py:34-69, 545-592).  A
+    same-spin pair (quadrupole) multiplies S^a_i S^b_i."""
+    involved = sorted(set(int(i) for i in indices))
+    loc = {s: k for k, s in enumerate(involved)}
+    Is = [system.Is[s] for s in involved]
+    total = None
+    for ii in np.ndindex(*tensor.shape):
+        if len(indices) == 2 and indices[0] == indices[1]:
+            ops = {loc[indices[0]]: ["xyz"[ii[0]], "xyz"[ii[1]]]}
+        else:
+            ops = {loc[int(ind)]: "xyz"[ii[k]] for k, ind in enumerate(indices)}
+        m = embed(Is, ops) * tensor[ii]
+        total = m if total is None else total + m
+    return total
+
+
+def celio_terms(system, B=None):
+    """(indices, small matrix) for every term of the system, followed by the
+    field's Zeeman terms gamma_i B.S_i when B is not zero
+    (muspinsim/experiment.py:239-269: appended after the system's terms)."""
+    out = [(tuple(int(i) for i in ind), celio_term_matrix(system, ind, T))
+           for ind, T in system.terms]
+    if B is not None and not np.array_equal(np.asarray(B, dtype=float), [0, 0, 0]):
+        for i in range(len(system.spins)):
+            v = np.asarray(B, dtype=float) * system.gammas[i]
+            out.append(((i,), celio_term_matrix(system, (i,), v)))
+    return out
+
+
+def celio_contribs(dims, terms):
+    """Hamiltonian contributions H_c (muspinsim/celio.py:73-143): per spin i
+    in order, the terms whose first index is i, split into runs of equal
+    index tuples (itertools.groupby, so only consecutive terms merge), each
+    run summed.  Returns (matrix, other_dim, spin_order, spin_dims) with
+    spin_order = the run's indices (a repeated index once) followed by the
+    uninvolved spins in ascending order."""
+    import itertools
+
+    L = len(dims)
+    out = []
+    for i in range(L):
+        spin_ints = [t for t in terms if t[0][0] == i]
+        other = [s for s in range(L) if s != i]
+        for ind, grp in itertools.groupby(spin_ints, key=lambda t: t[0]):
+            grp = list(grp)
+            H = sum(m for _, m in grp)
+            unin = list(other)
+            for t in grp:
+                for j in t[0]:
+                    if j in unin:
+                        unin.remove(j)
+            other_dim = int(np.prod([dims[j] for j in unin])) if unin else 1
+            ind = list(ind)
+            if len(ind) == 2 and ind[0] == ind[1]:
+                ind.pop()
+            order = ind + unin
+            out.append((H, other_dim, order, [dims[s] for s in order]))
+    return out
+
+
+def celio_factors(contribs, dt, k):
+    """U_c = expm(-2 pi i H_c dt / k) (muspinsim/celio.py:145-208)."""
+    from scipy.linalg import expm
+
+    return [(expm(-2j * np.pi * H * dt / k), od, order, sd) for H, od, order, sd in contribs]
+
+
+def celio_index_map(dims, order):
+    """Flat index, in the system's ordering, of each element of the
+    permuted ordering (muspinsim/celio.py:171-177)."""
+    N = int(np.prod(dims))
+    return np.transpose(np.arange(N).reshape(dims), axes=order).flatten()
+
+
+def celio_apply(psi, U, idx):
+    """(U (x) 1_d) acting through the index map, in place
+    (muspinsim/cpp/parallel.cpp:236-262)."""
+    D = U.shape[0]
+    ix = idx.reshape(D, -1)
+    psi[ix] = U @ psi[ix]
+
+
+def celio_measure_h(psi, M, d):
+    """Re <psi|(M (x) 1_d)|psi> for Hermitian M, using the upper triangle
+    twice (muspinsim/cpp/parallel.cpp:126-160)."""
+    D = M.shape[0]
+    V = psi.reshape(D, d)
+    total = 0.0
+    for i in range(D):
+        term = M[i, i] * V[i]
+        for j in range(i + 1, D):
+            term = term + M[i, j] * V[j] * 2.0
+        total += np.sum(np.real(np.conj(V[i]) * term))
+    return total
+
+
+def celio_mu_psi(sig):
+    """The muon state of eigenvalue +1 of sigma_mu (muspinsim/celio.py:361-363)."""
+    evals, evecs = np.linalg.eig(np.asarray(sig) + np.eye(2))
+    return evecs[:, 1] if np.real(evals[1]) > 0.1 else evecs[:, 0]
+
+
+def celio_fast_evolve(factors, dims, sig, times, k, phases):
+    """Averaged random-state evolution (muspinsim/celio.py:318-476,
+    muspinsim/cpp/celio.cpp:23-64): psi = mu_psi (x) exp(2 pi i r) /
+    sqrt(d), then per time: measure, then k passes of every factor in
+    order.  ``phases``: [averages, d] uniform numbers r (the reference draws
+    them with np.random.rand(d) per average).  Returns 0.5 * mean."""
+    N = int(np.prod(dims))
+    half = N // 2
+    sig = np.asarray(sig, dtype=complex)
+    mu_psi = celio_mu_psi(sig)
+    maps = [celio_index_map(dims, order) for _, _, order, _ in factors]
+    res = np.zeros(len(times))
+    for r in np.atleast_2d(phases):
+        psi = np.kron(mu_psi, np.exp(2j * np.pi * r)) * (1.0 / np.sqrt(half))
+        for i in range(len(times)):
+            res[i] += celio_measure_h(psi, sig, half)
+            for _ in range(k):
+                for (U, _, _, _), idx in zip(factors, maps):
+                    celio_apply(psi, U, idx)
+    return res * (1.0 / len(np.atleast_2d(phases))) * 0.5
+
+
+def celio_full_factor(U, dims, order):
+    """The factor on the whole space: (U (x) 1) in the permuted ordering,
+    permuted back to the system's ordering (muspinsim/celio.py:180-206)."""
+    N = int(np.prod(dims))
+    D = U.shape[0]
+    F = np.kron(U, np.eye(N // D))
+    sd = [dims[s] for s in order]
+    L = len(dims)
+    perm = list(np.argsort(order))
+    F = F.reshape(sd + sd).transpose(perm + [L + p for p in perm]).reshape(N, N)
+    return F
+
+
+def celio_evolve(factors, dims, rho0, times, operators, k):
+    """Density-matrix variant (muspinsim/celio.py:210-293): E = (prod_c
+    F_c)^k with the factors multiplied left to right; per time t_i,
+    rho = T^dag rho0 T with T = E^i, result_j = sum(rho * O_j^T)."""
+    N = int(np.prod(dims))
+    E = np.eye(N, dtype=complex)
+    for U, _, order, _ in factors:
+        E = E @ celio_full_factor(U, dims, order)
+    E = np.linalg.matrix_power(E, k)
+    T = np.eye(N, dtype=complex)
+    out = np.zeros((len(times), len(operators)), dtype=complex)
+    for i in range(len(times)):
+        rho = T.conj().T @ (rho0 @ T)
+        for j, O in enumerate(operators):
+            out[i, j] = np.sum(rho * np.asarray(O).T)
+        T = T @ E
+    return out
+
+
+def celio_snapshot_factors(system, B, dt, k):
+    """Trotter factors of one snapshot: the system's terms plus the field's
+    Zeeman terms (muspinsim/experiment.py:239-269, 332-334)."""
+    dims = list(system.dims)
+    return celio_factors(celio_contribs(dims, celio_terms(system, B)), dt, k)
+
+
+def celio_fast_evolve_c(factors, dims, sig, times, k, phases, nthreads=0):
+    """celio_fast_evolve through the C restatement (oracle/celio.c), with
+    OpenMP inside every factor application as the reference's native
+    module does."""
+    lib = _oracle_lib()
+    if not getattr(lib, "_celio_bound", False):
+        vp = ctypes.c_void_p
+        lib.oracle_celio_evolve.argtypes = [ctypes.c_int, vp, vp, ctypes.c_long, ctypes.c_int,
+                                            ctypes.c_int, vp, vp, vp, vp, ctypes.c_long, vp,
+                                            ctypes.c_int]
+        lib._celio_bound = True
+    N = int(np.prod(dims))
+    half = N // 2
+    sig = np.ascontiguousarray(sig, dtype=complex)
+    mu_psi = celio_mu_psi(sig)
+    mats = np.ascontiguousarray(np.concatenate([U.reshape(-1) for U, _, _, _ in factors]),
+                                dtype=complex)
+    dims_f = np.array([U.shape[0] for U, _, _, _ in factors], dtype=np.int64)
+    other_f = np.array([N // U.shape[0] for U, _, _, _ in factors], dtype=np.int64)
+    idx = np.ascontiguousarray(np.concatenate(
+        [celio_index_map(dims, order) for _, _, order, _ in factors]).astype(np.uint64))
+    times = np.asarray(times, dtype=float)
+    res = np.zeros(len(times))
+    ph = np.atleast_2d(phases)
+    for r in ph:
+        psi = np.ascontiguousarray(np.kron(mu_psi, np.exp(2j * np.pi * r)) * (1.0 / np.sqrt(half)))
+        lib.oracle_celio_evolve(len(times), psi.ctypes.data, sig.ctypes.data, half, int(k),
+                                len(factors), mats.ctypes.data, dims_f.ctypes.data,
+                                other_f.ctypes.data, idx.ctypes.data, N, res.ctypes.data,
+                                int(nthreads))
+    return res * (1.0 / len(ph)) * 0.5

@@ -34,26 +34,33 @@ def _jsonable_couplings(couplings):
 
 def _run_reference(spins, couplings, times, orientations, fields, pol, temps, y_axis,
                    x_axis, intrinsic=((0.0, 0.0, 0.0),), average_axes=("orientation",),
-                   dissipation=None):
+                   dissipation=None, celio=(0, 0), seed=None):
     from muspinsim.experiment import ExperimentRunner
 
     p = refshim.make_params(spins, couplings, times, orientations, field=fields,
                             intrinsic_field=intrinsic, polarization=pol, temperature=temps,
                             y_axis=y_axis, x_axis=x_axis, average_axes=average_axes,
-                            dissipation=dissipation)
+                            dissipation=dissipation, celio=celio)
     er = ExperimentRunner(refshim.ParamsInput(p))
+    if seed is not None:
+        np.random.seed(seed)
     return np.array(er.run())
 
 
 def save_experiment(name, spins, couplings, times, orientations, fields=((0.0, 0.0, 0.0),),
                     pol=(1.0, 0.0, 0.0), temps=(np.inf,), y_axis="asymmetry", x_axis="time",
                     intrinsic=((0.0, 0.0, 0.0),), average_axes=("orientation",),
-                    dissipation=None):
+                    dissipation=None, celio=(0, 0), seed=None):
+    """Run the reference's ExperimentRunner and store inputs and result.
+    With Celio's method and averages, ``seed`` seeds numpy's global
+    generator before the run, so the random initial states are reproducible
+    (the reference draws np.random.rand(d) per snapshot and average)."""
     out = _run_reference(spins, couplings, times, orientations, fields, pol, temps, y_axis,
-                         x_axis, intrinsic, average_axes, dissipation)
+                         x_axis, intrinsic, average_axes, dissipation, celio, seed)
     meta = {"spins": list(spins), "couplings": _jsonable_couplings(couplings),
             "y_axis": y_axis, "x_axis": x_axis, "average_axes": list(average_axes),
-            "dissipation": {str(k): float(v) for k, v in (dissipation or {}).items()}}
+            "dissipation": {str(k): float(v) for k, v in (dissipation or {}).items()},
+            "celio": [int(c) for c in celio], "seed": seed}
     np.savez_compressed(
         os.path.join(HERE, name + ".npz"),
         meta=np.array(json.dumps(meta)),
@@ -138,8 +145,54 @@ def save_lindblad_direct(name):
     print(f"{name}: L {L.matrix.shape}")
 
 
-def main():
+def save_celio():
+    """Celio's method through ExperimentRunner (muspinsim/celio.py,
+    muspinsim/experiment.py:434-471): averaged random states (the native
+    module) and the density-matrix variant, with and without a field."""
+    # mu + 2 V (I = 7/2): mu-V dipolar (16 x 16 factors) and V quadrupoles
+    # (8 x 8), zero field, polarisation along x; 3 orientations x 4 averages
+    rng = np.random.default_rng(505)
+    coup = []
+    for v in (2, 3):
+        r = rng.normal(size=3)
+        coup.append(("dipolar", {"i": 1, "j": v}, 1.3 * r / np.linalg.norm(r)))
+        q = rng.normal(size=(3, 3)) * 0.02
+        q = q + q.T
+        coup.append(("quadrupolar", {"i": v}, q - np.trace(q) / 3 * np.eye(3)))
+    save_experiment("celio_fast_muVV", ["mu", "V", "V"], coup, np.linspace(0, 6.0, 40),
+                    [(0.1, 0.2, 0.3, 1.0), (1.0, 2.0, 0.5, 2.0), (2.5, 0.4, 1.5, 0.5)],
+                    [(0.0, 0.0, 0.0)], (1.0, 0.0, 0.0), celio=(10, 4), seed=1234)
+    # mu + e + H + F in a field: hyperfine, a descending-index dipolar term
+    # (F -> mu) and a user Zeeman term on F that merges with the field's
+    # Zeeman term into one factor; 4 orientations x 3 averages
+    A1 = 40.0 * np.array([[1.0, 0.1, 0.0], [0.1, 0.8, 0.05], [0.0, 0.05, 1.2]])
+    A2 = 5.0 * np.array([[0.3, 0.0, 0.1], [0.0, -0.2, 0.0], [0.1, 0.0, 0.5]])
+    coup = [("hyperfine", {"i": 1}, A1), ("hyperfine", {"i": 3}, A2),
+            ("dipolar", {"i": 4, "j": 1}, [0.4, 1.0, 0.9]), ("zeeman", {"i": 4}, [0.0, 0.0, 0.02])]
+    save_experiment("celio_fast_field", ["mu", "e", "H", "F"], coup, np.linspace(0, 1.5, 25),
+                    [(0.1, 0.2, 0.3, 1.0), (1.0, 2.0, 0.5, 2.0), (2.5, 0.4, 1.5, 0.5),
+                     (0.7, 1.1, 2.9, 1.5)],
+                    [(0.002, 0.001, 0.01)], (0.0, 0.0, 1.0), celio=(4, 3), seed=99)
+    # density-matrix variant at finite temperature in a field (mu, e, H)
+    save_experiment("celio_rho_T", ["mu", "e", "H"], coup[:2] + [("dipolar", {"i": 3, "j": 1},
+                                                                   [0.5, 1.1, 0.2])],
+                    np.linspace(0, 1.0, 30), [(0.1, 0.2, 0.3, 1.0), (1.0, 2.0, 0.5, 2.0)],
+                    [(0.0, 0.0, 0.003)], (1.0, 0.0, 0.0), temps=(20.0,), celio=(6, 0))
+    # density-matrix variant with a descending-index dipolar term between
+    # spins of different dimension (N -> mu) and a quadrupole, zero field
+    q = np.array([[0.2, 0.05, 0.0], [0.05, -0.5, 0.1], [0.0, 0.1, 0.3]])
+    save_experiment("celio_rho_desc", ["mu", "H", "N"],
+                    [("dipolar", {"i": 3, "j": 1}, [0.3, 0.9, 1.1]),
+                     ("dipolar", {"i": 2, "j": 1}, [1.0, 0.2, 0.3]), ("quadrupolar", {"i": 3}, q)],
+                    np.linspace(0, 3.0, 35), [(0.3, 0.6, 0.9, 1.0), (2.0, 1.0, 0.4, 1.0)],
+                    [(0.0, 0.0, 0.0)], (0.0, 1.0, 0.0), celio=(5, 0))
+
+
+def main(only=None):
     refshim.install()
+    if only == "celio":
+        save_celio()
+        return
     from muspinsim_gb300 import workloads
 
     w1 = workloads.config1()
@@ -183,7 +236,8 @@ def main():
                     (0.0, 0.0, 1.0), temps=(5.0,), y_axis="integral", x_axis="field",
                     dissipation={2: 1.5})
     save_lindblad_direct("lindblad_direct")
+    save_celio()
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

@@ -20,7 +20,17 @@ importing it:
 * ``qutip`` Pauli matrices with ``.data_as("csr_matrix")``
   (``muspinsim/spinsys.py:754-757``).
 * ``lark`` -- import-only placeholders; the text input language is not used.
-* ``muspinsim.cpp`` (Celio only) -- import-only placeholder.
+* ``muspinsim.cpp`` (Celio's method) -- the reference's own pybind11 module
+  compiled from its sources by ``oracle/build.py`` where pybind11 is
+  installed, else an import-only placeholder.
+* ``numpy.product`` -- removed in numpy 2; the reference's Celio code calls
+  it, so it is aliased to ``numpy.prod`` (the same function in numpy 1.x).
+* ``muspinsim.celio.np.sum`` -- the density-matrix branch of
+  ``CelioHamiltonian.evolve`` stores a 1x1 ``np.matrix`` into a complex
+  array element (``muspinsim/celio.py:286-288``), which numpy 1.26 (the
+  reference's pin) accepted and numpy 2 rejects.  The reference's ``celio``
+  module sees numpy through a proxy whose ``sum`` unwraps a size-1 matrix
+  to its scalar; every other name is numpy's own.
 * ``muspinsim.cython`` -- the reference's own Cython kernel compiled from its
   sources by ``oracle/build.py``.
 """
@@ -91,11 +101,46 @@ def _get_isotope_data(elems, prop, isotope_list=None):
 
 
 class _Qobj:
-    def __init__(self, m=None):
+    """Operator container: ``data_as('csr_matrix')`` and, for Celio's
+    method, ``permute(order)`` -- new subsystem i is old subsystem order[i]
+    (muspinsim/celio.py:193-204)."""
+
+    def __init__(self, m=None, arg=None, dims=None):
+        m = arg if m is None else m
+        if m is not None and sparse.issparse(m):
+            m = m.toarray()
         self._m = sparse.csr_matrix(np.asarray(m, dtype=complex)) if m is not None else None
+        self._dims = dims
+
+    def permute(self, order):
+        sd = list(self._dims[0])
+        L = len(sd)
+        order = [int(o) for o in order]
+        n = self._m.shape[0]
+        T = self._m.toarray().reshape(sd + sd).transpose(order + [L + o for o in order])
+        new = [sd[o] for o in order]
+        return _Qobj(T.reshape(n, n), dims=[new, new])
 
     def data_as(self, fmt):
         return self._m
+
+
+class _NumpyCompat(types.ModuleType):
+    """numpy with ``sum`` returning the scalar of a size-1 np.matrix, as
+    numpy 1.x's scalar assignment did implicitly."""
+
+    def __init__(self):
+        super().__init__("numpy")
+
+    def __getattr__(self, name):
+        return getattr(np, name)
+
+    @staticmethod
+    def sum(*args, **kwargs):
+        r = np.sum(*args, **kwargs)
+        if isinstance(r, np.matrix) and r.size == 1:
+            return r.item()
+        return r
 
 
 def _module(name, **attrs):
@@ -147,20 +192,21 @@ def install():
     _module("lark.exceptions", UnexpectedToken=Exception, UnexpectedInput=Exception)
 
     sys.path.insert(0, REFERENCE_ROOT)
-    _module(
-        "muspinsim.cpp",
-        Celio_EvolveContrib=None,
-        evolve_pwd=None,
-        fast_evolve=None,
-        fast_measure=None,
-        fast_measure_h=None,
-        celio_evolve=None,
-        celio_evolve_averaged=None,
-    )
+    if not hasattr(np, "product"):
+        np.product = np.prod
 
-    # the reference's Cython kernel, compiled from its own sources
+    # the reference's native modules, compiled from its own sources
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import build as oracle_build  # oracle/build.py
+
+    cpp_path = oracle_build.build_ref_cpp()
+    if cpp_path is not None:
+        spec = importlib.util.spec_from_file_location("cpp", cpp_path)
+        cpp = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(cpp)
+        sys.modules["muspinsim.cpp"] = cpp
+    else:
+        _module("muspinsim.cpp", Celio_EvolveContrib=None, celio_evolve=None)
 
     path = oracle_build.build_ref()
     spec = importlib.util.spec_from_file_location(oracle_build.REF_MODULE, path)
@@ -171,6 +217,9 @@ def install():
     import muspinsim.hamiltonian  # noqa: F401
     import muspinsim.spinsys  # noqa: F401
     import muspinsim.experiment  # noqa: F401
+    import muspinsim.celio
+
+    muspinsim.celio.np = _NumpyCompat()
 
     return sys.modules["muspinsim"]
 
@@ -212,6 +261,7 @@ def make_params(
     x_axis="time",
     average_axes=("orientation",),
     dissipation=None,
+    celio=(0, 0),
 ):
     """Build the evaluated-params dict for ``MuSpinConfig``.
 
@@ -224,7 +274,7 @@ def make_params(
     p = {
         "name": input_value("name", np.array([["test"]])),
         "spins": input_value("spins", np.array([list(spins)], dtype=object)),
-        "celio": input_value("celio", np.array([["0", "0"]])),
+        "celio": input_value("celio", np.array([[str(c) for c in celio]])),
         "y_axis": input_value("y_axis", np.array([[y_axis]])),
         "x_axis": input_value("x_axis", np.array([[x_axis]])),
         "average_axes": input_value("average_axes", np.array([list(average_axes)])),

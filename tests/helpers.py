@@ -79,8 +79,21 @@ def golden_oracle(g, field_index=0, temp_index=0):
         intr = np.array([0.0, 0.0, intr[0]])
     y = "integral" if g["y_axis"] == "integral" else "asymmetry"
     diss = {int(k) - 1: float(v) for k, v in g.get("dissipation", {}).items()} or None
+    celio = tuple(g.get("celio") or (0, 0))
+    phases = None
+    if celio[0] and celio[1]:
+        phases = celio_phases(g["seed"], len(g["orientations"]), celio[1], sy.n // 2)
     return port.powder_average(sy, list(g["orientations"]), B, p, g["temperatures"][temp_index],
-                               g["times"], intrinsic_B=intr, y=y, dissipation=diss)
+                               g["times"], intrinsic_B=intr, y=y, dissipation=diss, celio=celio,
+                               phases=phases)
+
+
+def celio_phases(seed, snapshots, averages, half):
+    """The uniform numbers the reference draws for Celio's random initial
+    states after np.random.seed(seed): np.random.rand(half) per snapshot and
+    average, in that order (muspinsim/celio.py:295-316, 471)."""
+    rs = np.random.RandomState(seed)
+    return rs.random_sample(snapshots * averages * half).reshape(snapshots, averages, half)
 
 
 def random_hermitian(rng, n, scale=100.0):
