@@ -63,8 +63,12 @@ def parse_args():
     p.add_argument("--ref-orientations", type=int, default=400,
                    help="orientations per step of the --impl reference arm")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--celio-orient", type=int, default=8,
+                   help="celio workload: orientations (19 random states each)")
+    p.add_argument("--celio-times", type=int, default=50, help="celio workload: time samples")
     p.add_argument("--workload", default="config2",
-                   choices=["config1", "config2", "config3", "config4", "config5", "lindblad"],
+                   choices=["config1", "config2", "config3", "config4", "config5", "lindblad",
+                            "celio"],
                    help="config2 (default) is the headline; the others print their own line")
     return p.parse_args()
 
@@ -786,6 +790,100 @@ def run_lindblad(args, world, rank, local):
     return line
 
 
+def celio_flops(dims, batch):
+    """Algorithmic flops of one msp_celio_run of `batch`: every factor
+    application multiplies V / D groups by a D x D complex matrix (8 real
+    flops per complex multiply-add), k passes per time step, T - 1 steps
+    per state; the measurements (O(V) per sample) are left out."""
+    V = int(np.prod(dims))
+    per_pass = sum(8 * V * (dims[d0] * (dims[d1] if d1 >= 0 else 1)) for d0, d1 in batch.digits)
+    return per_pass * batch.k * (batch.T - 1) * batch.S * batch.averages
+
+
+def run_celio(args, world, rank, local):
+    """Celio's method with averaged random initial states (the reference's
+    native fast variant, muspinsim/celio.py:318-476): mu + 4 51V (I = 7/2,
+    dimension 8192), the shape of the reference's own Celio example;
+    8 ZCW-style orientations x 19 random states = 152 states (one per SM),
+    k = 10, 50 times on 0-10 us.  FP64 in shared memory."""
+    import torch
+
+    from muspinsim_gb300 import celio, workloads
+    from muspinsim_gb300 import quaternion as Q
+    from muspinsim_gb300.orientations import orientation_rows_to_quats
+
+    wl = workloads.celio_v3si(n_orient=args.celio_orient, n_times=args.celio_times)
+    k, A = wl.meta["celio"]
+    steps = max(1, min(args.steps, 10))
+    sy = wl.system(celio_k=k)
+    qs, ws = orientation_rows_to_quats(wl.orientations)
+    N = len(qs)
+    ws = ws * (N / ws.sum())
+    B_lab, p_lab = Q.rotate(qs, wl.fields[0]), Q.rotate(qs, wl.polarization)
+    T = len(wl.times)
+    Tk = np.full(N, np.inf)
+    rows = np.zeros(N, dtype=np.int64)
+    np.random.seed(1234)
+    batch = celio.CelioBatch(sy, k, A, B_lab, p_lab, Tk, ws / N, rows, 1, wl.times)
+    for _ in range(args.warmup):
+        batch.run()
+    ms = _events_ms(batch.run, steps)
+
+    def e2e():
+        out = celio.CelioBatch(sy, k, A, B_lab, p_lab, Tk, ws / N, rows, 1, wl.times).run()
+        return out.cpu().numpy()
+
+    e2e()
+    e2e_ms = _wall_ms(e2e, steps)
+    dims = list(sy.dimension)
+    V = int(np.prod(dims))
+    flops = celio_flops(dims, batch)
+    peak = 1250.0  # GB300 FP64 nominal GFLOP/s: no measured FP64 figure on this pool
+    achieved = flops / (ms * 1e-3) / 1e9
+    samples = N * T
+    line = _line("Celio P(t) samples/s (orientation x time, 19 random states each), FP64",
+                 samples / (ms * 1e-3), "samples/s", ms, args, world,
+                 f"celio_muV4_dim8192_{N}_orient_{A}_states_{T}_t_k{k}",
+                 {"orientations": N, "states_per_orientation": A, "times": T, "dim": V,
+                  "trotter_k": k, "factors_per_pass": len(batch.digits),
+                  "l2": "states resident in shared memory; HBM traffic is the inputs only"},
+                 dtype="f64", gpu_launches=steps,
+                 state_steps_per_s=N * A * (T - 1) / (ms * 1e-3),
+                 roofline={"bound": "fp64", "achieved": achieved, "peak": peak,
+                           "unit": "GFLOP/s", "frac": achieved / peak, "traffic": None,
+                           "peak_source": "nominal FP64 (no measured FP64 peak)"},
+                 e2e={"value": samples / (e2e_ms * 1e-3), "unit": "samples/s",
+                      "ms": e2e_ms, "h2d_bytes_per_step": int(batch.phases.numel() * 8 +
+                                                             batch.mats.numel() * 16),
+                      "d2h_bytes_per_step": T * 8,
+                      "note": "host factor exponentials, np.random.rand states and uploads "
+                              "inside the timed region"})
+    if not args.no_cpu_baseline:
+        from oracle import port
+        from tests.helpers import oracle_system
+
+        osy = oracle_system(wl.spins, wl.couplings)
+        fac = port.celio_snapshot_factors(osy, None, wl.times[1] - wl.times[0], k)
+        np.random.seed(99)
+        one = celio.CelioBatch(sy, k, 2, B_lab[:1], p_lab[:1], Tk[:1], np.ones(1), rows[:1], 1,
+                               wl.times)
+        gpu = one.run().cpu().numpy()[0]
+        ph = one.phases.cpu().numpy()[0]
+        sig = port.sigma_mu(p_lab[0])
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref = port.celio_fast_evolve_c(fac, dims, sig, wl.times, k, ph, nthreads=threads)
+        dt = time.perf_counter() - t0
+        line["max_abs_dP_vs_oracle_1_orient_2_states"] = float(np.abs(gpu - ref).max())
+        # one state took dt / 2; an orientation sample needs A states
+        line["cpu_baseline"] = {"value": T / (dt / 2 * A), "unit": "samples/s", "cores": threads,
+                                "kind": "port",
+                                "sample": "1 orientation x 2 random states through oracle/celio.c "
+                                          "(the reference's native loop restated, OpenMP inside "
+                                          "each factor application)"}
+    return line
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args)
@@ -796,7 +894,7 @@ def main():
 
         torch.cuda.set_device(local)
         fn = {"config1": run_config1, "config3": run_config3, "config4": run_config4,
-              "config5": run_config5, "lindblad": run_lindblad}[args.workload]
+              "config5": run_config5, "lindblad": run_lindblad, "celio": run_celio}[args.workload]
         line = fn(args, world, rank, local)
         if rank == 0:
             print(json.dumps(line))

@@ -256,160 +256,187 @@ def _mu_psi(sig):
 
 
 # ---------------------------------------------------------------- batched snapshots
-def run_snapshots(system, k, averages, B_lab, p_lab, T, wscale, rows, nrows, times):
-    """Every snapshot of an ExperimentRunner with Celio's method, in one
-    batch (muspinsim/experiment.py:239-269, 434-471): the system's terms
-    plus, when any snapshot has a field, every spin's Zeeman term; factors
-    holding a Zeeman term are exponentiated per snapshot on the GPU.  With
-    ``averages`` > 0 the random initial states come from np.random.rand in
-    the reference's order (snapshot by snapshot, average by average).
-    Returns (nrows, T) float64 on the device."""
-    from muspinsim_gb300.spinsys import SingleTerm
+class CelioBatch:
+    """Every snapshot of an ExperimentRunner with Celio's method, prepared
+    once and run as one batch (muspinsim/experiment.py:239-269, 434-471).
 
-    times = np.asarray(times, dtype=float)
-    S = len(B_lab)
-    dims = list(system.dimension)
-    L = len(dims)
-    N = int(np.prod(dims))
-    any_field = any(not _field_zero(b) for b in B_lab)
-    zterms = []
-    if any_field:
-        zterms = [SingleTerm(system, i, np.array([0.0, 0.0, 1.0]) * system.gammas[i],
-                             label="Zeeman") for i in range(L)]
-    H = CelioHamiltonian(system.terms + zterms, k, system)
-    # a snapshot without field evolves under the system's terms alone
-    all_field = all(not _field_zero(b) for b in B_lab)
-    validate_celio_params(H._terms if all_field else system.terms, times)
-    dt = times[1] - times[0]
-    pure = averages > 0
-    if pure:
-        if np.any(np.asarray(T, dtype=float) != np.inf):
-            raise ValueError("The fast version of Celio's method requires T -> inf. Either "
-                             "remove the number of averages or don't use celio.")
-        if system.muon_index != 0:
-            raise ValueError("Muon must be the first spin in the system in order to use "
-                             "the fast Celio method")
+    The Trotter pass holds the system's terms plus, when any snapshot has a
+    field, every spin's Zeeman term; factors holding a Zeeman term are
+    exponentiated per snapshot on the GPU (``msp_celio_expm``), the others
+    once on the host.  With ``averages`` > 0 (random initial states) the
+    uniform numbers come from np.random.rand in the reference's order --
+    snapshot by snapshot, average by average -- or, with
+    ``device_phases``, from the library's counter-based generator keyed by
+    ``seed``.  Construction uploads everything; :meth:`run` launches
+    ``msp_celio_run`` only and returns the (nrows, T) results on the
+    device."""
 
-    # contributions; those holding a Zeeman term depend on the snapshot's field
-    zids = {id(t) for t in zterms}
-    static, field = [], []   # (position in the pass, U or (H0, G, spin), order)
-    for pos, (grp, unin, order) in enumerate(H._groups()):
-        Hs = None
-        for t in grp:
-            if id(t) in zids:
-                continue
-            Hs = _dense(t.matrix) if Hs is None else Hs + _dense(t.matrix)
-        zs = [t for t in grp if id(t) in zids]
-        if zs:
-            i = int(zs[0].indices[0])
-            D = dims[i]
-            G = np.array([system.gammas[i] * _dense(system._operators[i][ax].matrix)
-                          for ax in "xyz"], dtype=complex)
-            H0 = np.zeros((D, D), dtype=complex) if Hs is None else Hs
-            field.append((pos, H0, G, order))
-        else:
-            static.append((pos, expm(-2j * np.pi * Hs * dt / k), order))
+    def __init__(self, system, k, averages, B_lab, p_lab, T, wscale, rows, nrows, times,
+                 device_phases=False, seed=0):
+        import torch
 
-    nfac = len(static) + len(field)
-    per = 2 if not pure else 1
-    Ds = {}
-    for pos, U, order in static:
-        Ds[pos] = (U.shape[0], order)
-    for pos, H0, G, order in field:
-        Ds[pos] = (H0.shape[0], order)
-    offs, off = {}, 0
-    for pos in range(nfac):
-        D = Ds[pos][0]
-        offs[pos] = off
-        off += per * D * D
-    mats_len = max(off, 1)
-    digits, mat = [], []
-    for pos in range(nfac):
-        D, order = Ds[pos]
-        d0, d1 = _involved(order, D, dims)
+        from muspinsim_gb300.spinsys import SingleTerm
+
+        times = np.asarray(times, dtype=float)
+        B_lab = np.asarray(B_lab, dtype=float).reshape(-1, 3)
+        p_lab = np.asarray(p_lab, dtype=float).reshape(-1, 3)
+        S = len(B_lab)
+        dims = list(system.dimension)
+        L = len(dims)
+        N = int(np.prod(dims))
+        any_field = any(not _field_zero(b) for b in B_lab)
+        zterms = []
+        if any_field:
+            zterms = [SingleTerm(system, i, np.array([0.0, 0.0, 1.0]) * system.gammas[i],
+                                 label="Zeeman") for i in range(L)]
+        H = CelioHamiltonian(system.terms + zterms, k, system)
+        # a snapshot without field evolves under the system's terms alone
+        all_field = all(not _field_zero(b) for b in B_lab)
+        validate_celio_params(H._terms if all_field else system.terms, times)
+        dt = times[1] - times[0]
+        pure = averages > 0
         if pure:
+            if np.any(np.asarray(T, dtype=float) != np.inf):
+                raise ValueError("The fast version of Celio's method requires T -> inf. Either "
+                                 "remove the number of averages or don't use celio.")
+            if system.muon_index != 0:
+                raise ValueError("Muon must be the first spin in the system in order to use "
+                                 "the fast Celio method")
+
+        # contributions; those holding a Zeeman term depend on the snapshot's field
+        zids = {id(t) for t in zterms}
+        static, field = [], []
+        for pos, (grp, unin, order) in enumerate(H._groups()):
+            Hs = None
+            for t in grp:
+                if id(t) not in zids:
+                    Hs = _dense(t.matrix) if Hs is None else Hs + _dense(t.matrix)
+            zs = [t for t in grp if id(t) in zids]
+            if zs:
+                i = int(zs[0].indices[0])
+                D = dims[i]
+                G = np.array([system.gammas[i] * _dense(system._operators[i][ax].matrix)
+                              for ax in "xyz"], dtype=complex)
+                field.append((pos, np.zeros((D, D), dtype=complex) if Hs is None else Hs, G,
+                              order))
+            else:
+                static.append((pos, expm(-2j * np.pi * Hs * dt / k), order))
+
+        per = 1 if pure else 2
+        Ds = {pos: (U.shape[0], order) for pos, U, order in static}
+        Ds.update({pos: (H0.shape[0], order) for pos, H0, G, order in field})
+        nfac = len(Ds)
+        offs, off = {}, 0
+        for pos in range(nfac):
+            offs[pos] = off
+            off += per * Ds[pos][0] ** 2
+        mats_len = max(off, 1)
+        digits, mat = [], []
+        for pos in range(nfac):
+            D, order = Ds[pos]
+            d0, d1 = _involved(order, D, dims)
             digits.append((d0, d1))
             mat.append(offs[pos])
-        else:
-            digits.append((d0, d1))
-            mat.append(offs[pos])
-            digits.append((L + d0, L + d1 if d1 >= 0 else -1))
-            mat.append(offs[pos] + D * D)
-    block = np.zeros(mats_len, dtype=complex)
-    for pos, U, order in static:
-        D = U.shape[0]
-        o = offs[pos]
-        if pure:
-            block[o:o + D * D] = U.reshape(-1)
-        else:
-            block[o:o + D * D] = U.conj().T.reshape(-1)
-            block[o + D * D:o + 2 * D * D] = U.T.reshape(-1)
-
-    import torch
-
-    d = kernels.device()
-    if field:
-        mats = kernels.dev(np.broadcast_to(block, (S, mats_len)), torch.complex128).clone()
-        out_off = []
-        for pos, H0, G, order in field:
-            D = H0.shape[0]
+            if not pure:
+                digits.append((L + d0, L + d1 if d1 >= 0 else -1))
+                mat.append(offs[pos] + D * D)
+        block = np.zeros(mats_len, dtype=complex)
+        for pos, U, order in static:
+            D = U.shape[0]
             o = offs[pos]
-            out_off.append((o, -1, -1) if pure else (-1, o, o + D * D))
-        kernels.celio_expm([f[1].shape[0] for f in field], [f[1] for f in field],
-                           [f[2] for f in field], B_lab, dt / k, out_off, mats)
-        per_snap = True
-    else:
-        mats = block[None]
-        per_snap = False
+            if pure:
+                block[o:o + D * D] = U.reshape(-1)
+            else:
+                block[o:o + D * D] = U.conj().T.reshape(-1)
+                block[o + D * D:o + 2 * D * D] = U.T.reshape(-1)
 
-    order_s = np.argsort(np.asarray(rows), kind="stable")
-    inv = np.empty_like(order_s)
-    inv[order_s] = np.arange(S)
-    rows_sorted = np.asarray(rows)[order_s]
-    row_start = np.searchsorted(rows_sorted, np.arange(nrows + 1)).astype(np.int32)
-    if per_snap:
-        mats = mats[torch.as_tensor(order_s, device=d)]
-    ws_sorted = np.asarray(wscale, dtype=float)[order_s]
-    p_sorted = np.asarray(p_lab, dtype=float)[order_s]
+        d = kernels.device()
+        order_s = np.argsort(np.asarray(rows), kind="stable")
+        rows_sorted = np.asarray(rows)[order_s]
+        self.row_start = kernels.dev(
+            np.searchsorted(rows_sorted, np.arange(nrows + 1)).astype(np.int32), torch.int32)
+        if field:
+            mats = kernels.dev(np.broadcast_to(block, (S, mats_len)), torch.complex128).clone()
+            out_off = []
+            for pos, H0, G, order in field:
+                D = H0.shape[0]
+                o = offs[pos]
+                out_off.append((o, -1, -1) if pure else (-1, o, o + D * D))
+            kernels.celio_expm([f[1].shape[0] for f in field], [f[1] for f in field],
+                               [f[2] for f in field], B_lab[order_s], dt / k, out_off, mats)
+            self.per_snap = True
+        else:
+            mats = kernels.dev(block[None], torch.complex128)
+            self.per_snap = False
+        self.mats = mats
+        self.digits = np.array(digits, dtype=np.int32).reshape(-1, 2)
+        self.mat = np.array(mat, dtype=np.int64)
+        self.dims, self.k, self.S, self.T = dims, int(k), S, len(times)
+        self.nrows = int(nrows)
+        self.pure = pure
+        self.averages = int(averages)
+        self.wscale = kernels.dev(np.asarray(wscale, dtype=float)[order_s], torch.float64)
+        p_sorted = p_lab[order_s]
+        if pure:
+            half = N // 2
+            sig = np.empty((S, 2, 2), dtype=complex)
+            sig[:, 0, 0] = p_lab[:, 2]
+            sig[:, 0, 1] = p_lab[:, 0] - 1j * p_lab[:, 1]
+            sig[:, 1, 0] = p_lab[:, 0] + 1j * p_lab[:, 1]
+            sig[:, 1, 1] = -p_lab[:, 2]
+            mu = _mu_psi(sig) if S else np.zeros((0, 2), dtype=complex)
+            self.sigma = kernels.dev(sig[order_s], torch.complex128)
+            self.mu_psi = kernels.dev(mu[order_s], torch.complex128)
+            self.seed = int(seed)
+            self.phases = None
+            if not device_phases:
+                ph = np.random.rand(S * self.averages * half).reshape(S, self.averages, half)
+                self.phases = kernels.dev(ph[order_s], torch.float64)
+            return
 
-    if pure:
-        half = N // 2
-        sig = np.array([[[p[2], p[0] - 1j * p[1]], [p[0] + 1j * p[1], -p[2]]]
-                        for p in np.asarray(p_lab, dtype=float)], dtype=complex)
-        mu = _mu_psi(sig) if S else np.zeros((0, 2), dtype=complex)
-        phases = np.random.rand(S * averages * half).reshape(S, averages, half)
-        _, out = kernels.celio_run(
-            _lib.CELIO_PURE, dims, digits, mat, mats, per_snap, S, averages, k, len(times),
-            mu_psi=mu[order_s], sigma=sig[order_s], phases=phases[order_s], wscale=ws_sorted,
-            row_start=row_start, num_rows=nrows)
+        from muspinsim_gb300.experiment import thermal_state
+
+        rho = np.empty((S, N, N), dtype=complex)
+        for s_i, s in enumerate(order_s):
+            fac = []
+            for i in range(L):
+                if i == system.muon_index:
+                    fac.append(spin_projectors(system.I(i), p_lab[s])[0][1])
+                else:
+                    fac.append(thermal_state(system.I(i), system.gamma(i), B_lab[s], T[s]))
+            M = fac[0]
+            for m in fac[1:]:
+                M = np.kron(M, m)
+            rho[s_i] = M
+        self.rho0 = kernels.dev(rho, torch.complex128)
+        self.meas = kernels.dev(np.stack([_dense(system.operator({system.muon_index: ax}).matrix).T
+                                          for ax in "xyz"])[None], torch.complex128)
+        self.pol = torch.as_tensor(p_sorted, dtype=torch.complex128, device=d)
+        self.rows_sorted = torch.as_tensor(rows_sorted, dtype=torch.int64, device=d)
+
+    def run(self, path=0):
+        import torch
+
+        if self.pure:
+            _, out = kernels.celio_run(
+                _lib.CELIO_PURE, self.dims, self.digits, self.mat, self.mats, self.per_snap, self.S,
+                self.averages, self.k, self.T, mu_psi=self.mu_psi, sigma=self.sigma,
+                phases=self.phases, seed=self.seed, wscale=self.wscale, row_start=self.row_start,
+                num_rows=self.nrows, path=path)
+            return out
+        series, _ = kernels.celio_run(
+            _lib.CELIO_DENSITY, self.dims + self.dims, self.digits, self.mat, self.mats,
+            self.per_snap, self.S, 1, self.k, self.T, rho0=self.rho0, meas=self.meas, path=path)
+        vals = torch.real(torch.einsum("sta,sa->st", series, self.pol))
+        out = torch.zeros((self.nrows, self.T), dtype=torch.float64, device=vals.device)
+        out.index_add_(0, self.rows_sorted, vals * self.wscale[:, None])
         return out
 
-    from muspinsim_gb300.experiment import thermal_state
 
-    rho = np.empty((S, N, N), dtype=complex)
-    for s_i, s in enumerate(order_s):
-        mats_r = []
-        for i in range(L):
-            if i == system.muon_index:
-                mats_r.append(spin_projectors(system.I(i), p_lab[s])[0][1])
-            else:
-                mats_r.append(thermal_state(system.I(i), system.gamma(i), B_lab[s], T[s]))
-        M = mats_r[0]
-        for m in mats_r[1:]:
-            M = np.kron(M, m)
-        rho[s_i] = M
-    mu_ops = np.stack([_dense(system.operator({system.muon_index: ax}).matrix).T
-                       for ax in "xyz"])[None]
-    series, _ = kernels.celio_run(
-        _lib.CELIO_DENSITY, dims + dims, digits, mat, mats, per_snap, S, 1, k, len(times),
-        rho0=rho, meas=mu_ops, meas_per_snapshot=False)
-    pt = torch.as_tensor(p_sorted, dtype=torch.complex128, device=d)
-    vals = torch.real(torch.einsum("sta,sa->st", series, pt))
-    wt = torch.as_tensor(ws_sorted, dtype=torch.float64, device=d)
-    out = torch.zeros((nrows, len(times)), dtype=torch.float64, device=d)
-    rs = torch.as_tensor(rows_sorted, dtype=torch.int64, device=d)
-    out.index_add_(0, rs, vals * wt[:, None])
-    return out
+def run_snapshots(system, k, averages, B_lab, p_lab, T, wscale, rows, nrows, times):
+    """All snapshots of an ExperimentRunner with Celio's method: the
+    (nrows, T) float64 results on the device (see CelioBatch)."""
+    return CelioBatch(system, k, averages, B_lab, p_lab, T, wscale, rows, nrows, times).run()
 
 
 logging.getLogger(__name__).addHandler(logging.NullHandler())

@@ -16,6 +16,11 @@ GPU library and the CPU oracle, so both see identical inputs.
   2,000 fields on 0-1 T x 1,000 orientations, decaying integral (ALC).
 * ``config5`` -- mu, 19F, 19F (dim 8), dipoles at U(1.0, 1.4) A,
   2,000 orientations, 1000 times on 0-20 us.
+* ``celio_v3si`` -- Celio's method on mu + 4 51V (I = 7/2, dim
+  2 x 8^4 = 8192), the shape of the reference's Celio example: mu-V point
+  dipoles at U(1.6, 2.0) A, random traceless V EFGs with |V_zz| ~
+  U(0.02, 0.06) a.u., zero field, ZCW orientations (only the polarisation
+  turns), k = 10, random initial states averaged, 50 times on 0-10 us.
 """
 
 from dataclasses import dataclass, field
@@ -45,11 +50,11 @@ class Workload:
     def num_orientations(self):
         return len(self.orientations)
 
-    def system(self):
+    def system(self, celio_k=0):
         """The workload's MuonSpinSystem (muspinsim_gb300.spinsys)."""
         from muspinsim_gb300.spinsys import MuonSpinSystem
 
-        sy = MuonSpinSystem(list(self.spins))
+        sy = MuonSpinSystem(list(self.spins), celio_k)
         for kind, args, val in self.couplings:
             i = args["i"] - 1
             j = args.get("j")
@@ -217,3 +222,17 @@ def config4(seed=1004, n_systems=4096, n_orient=256, n_times=2048,
     times = np.linspace(0.0, 20.0, n_times)
     draws = rng.choice(np.asarray(dims), size=n_systems)
     return [random_system_workload(rng, int(d), orients, times) for d in draws]
+
+
+def celio_v3si(seed=1006, n_orient=8, n_times=50, k=10, averages=19):
+    """Celio's method on mu + 4 V (dim 8192); see the module docstring."""
+    rng = np.random.default_rng(seed)
+    spins = ["mu", "V", "V", "V", "V"]
+    coup = []
+    for v in range(2, 6):
+        coup.append(("dipolar", {"i": 1, "j": v}, random_vector(rng, 1.6, 2.0)))
+        coup.append(("quadrupolar", {"i": v}, random_efg(rng, 0.02, 0.06)))
+    orients = zcw_gen(n_orient) if n_orient > 1 else np.array([[0.0, 0.0]])
+    return Workload("celio_v3si", spins, coup, orients, np.zeros((1, 3)),
+                    np.array([1.0, 0.0, 0.0]), np.linspace(0, 10.0, n_times),
+                    meta={"celio": (int(k), int(averages))})
