@@ -805,9 +805,8 @@ def run_celio(args, world, rank, local):
     native fast variant, muspinsim/celio.py:318-476): mu + 4 51V (I = 7/2,
     dimension 8192), the shape of the reference's own Celio example;
     8 ZCW-style orientations x 19 random states = 152 states (one per SM),
-    k = 10, 50 times on 0-10 us.  FP64 in shared memory."""
-    import torch
-
+    k = 10, 50 times on 0-10 us.  States stay in shared memory; the line's
+    value is the double-word FP32 form, with the FP64 form beside it."""
     from muspinsim_gb300 import celio, workloads
     from muspinsim_gb300 import quaternion as Q
     from muspinsim_gb300.orientations import orientation_rows_to_quats
@@ -823,35 +822,56 @@ def run_celio(args, world, rank, local):
     T = len(wl.times)
     Tk = np.full(N, np.inf)
     rows = np.zeros(N, dtype=np.int64)
-    np.random.seed(1234)
-    batch = celio.CelioBatch(sy, k, A, B_lab, p_lab, Tk, ws / N, rows, 1, wl.times)
-    for _ in range(args.warmup):
-        batch.run()
-    ms = _events_ms(batch.run, steps)
+    batches, ms, outs = {}, {}, {}
+    for prec in ("fp64", "mixed"):
+        np.random.seed(1234)  # the same random states for both forms
+        b = celio.CelioBatch(sy, k, A, B_lab, p_lab, Tk, ws / N, rows, 1, wl.times,
+                             precision=prec)
+        for _ in range(args.warmup):
+            b.run()
+        ms[prec] = _events_ms(b.run, steps if prec == "mixed" else max(1, min(steps, 3)))
+        outs[prec] = b.run().cpu().numpy()[0]
+        batches[prec] = b
 
     def e2e():
-        out = celio.CelioBatch(sy, k, A, B_lab, p_lab, Tk, ws / N, rows, 1, wl.times).run()
+        out = celio.CelioBatch(sy, k, A, B_lab, p_lab, Tk, ws / N, rows, 1, wl.times,
+                               precision="mixed").run()
         return out.cpu().numpy()
 
     e2e()
     e2e_ms = _wall_ms(e2e, steps)
+    batch = batches["mixed"]
     dims = list(sy.dimension)
     V = int(np.prod(dims))
     flops = celio_flops(dims, batch)
-    peak = 1250.0  # GB300 FP64 nominal GFLOP/s: no measured FP64 figure on this machine
-    achieved = flops / (ms * 1e-3) / 1e9
+    cmacs = flops / 8
+    fp32_peak = 152 * 128 * 2 * 2.07  # GFLOP/s, nominal FP32 FMA rate at 2.07 GHz
+    achieved = flops / (ms["mixed"] * 1e-3) / 1e9
+    pipe_ops = cmacs * 24 / (ms["mixed"] * 1e-3) / 1e9  # FP32 ops issued per second (12 f32x2)
     samples = N * T
-    line = _line("Celio P(t) samples/s (orientation x time, 19 random states each), FP64",
-                 samples / (ms * 1e-3), "samples/s", ms, args, world,
-                 f"celio_muV4_dim8192_{N}_orient_{A}_states_{T}_t_k{k}",
+    line = _line("Celio P(t) samples/s (orientation x time, 19 random states each), "
+                 "double-word FP32", samples / (ms["mixed"] * 1e-3), "samples/s", ms["mixed"],
+                 args, world, f"celio_muV4_dim8192_{N}_orient_{A}_states_{T}_t_k{k}",
                  {"orientations": N, "states_per_orientation": A, "times": T, "dim": V,
                   "trotter_k": k, "factors_per_pass": len(batch.digits),
                   "l2": "states resident in shared memory; HBM traffic is the inputs only"},
-                 dtype="f64", gpu_launches=steps,
-                 state_steps_per_s=N * A * (T - 1) / (ms * 1e-3),
-                 roofline={"bound": "fp64", "achieved": achieved, "peak": peak,
-                           "unit": "GFLOP/s", "frac": achieved / peak, "traffic": None,
-                           "peak_source": "nominal FP64 (no measured FP64 peak)"},
+                 dtype="f32 double-word", gpu_launches=steps,
+                 state_steps_per_s=N * A * (T - 1) / (ms["mixed"] * 1e-3),
+                 fp64={"value": samples / (ms["fp64"] * 1e-3), "ms_per_step": ms["fp64"],
+                       "achieved_gflops": flops / (ms["fp64"] * 1e-3) / 1e9,
+                       "fp64_peak_gflops": 1250.0,
+                       "frac": flops / (ms["fp64"] * 1e-3) / 1e9 / 1250.0},
+                 mixed_over_fp64=ms["fp64"] / ms["mixed"],
+                 max_abs_dP_mixed_vs_fp64=float(np.abs(outs["mixed"] - outs["fp64"]).max()),
+                 roofline={"bound": "fp32", "achieved": pipe_ops, "peak": fp32_peak,
+                           "unit": "GFLOP/s", "frac": pipe_ops / fp32_peak, "traffic": None,
+                           "algorithmic_gflops": achieved,
+                           "note": "achieved = FP32 operations issued (12 packed f32x2 "
+                                   "instructions = 24 FP32 ops per complex multiply-add of "
+                                   "the anchored double-word product) per second; peak = "
+                                   "nominal FP32 "
+                                   "(152 SMs x 128 lanes x 2 x 2.07 GHz), no measured FP32 "
+                                   "figure on this pool"},
                  e2e={"value": samples / (e2e_ms * 1e-3), "unit": "samples/s",
                       "ms": e2e_ms, "h2d_bytes_per_step": int(batch.phases.numel() * 8 +
                                                              batch.mats.numel() * 16),
@@ -868,13 +888,16 @@ def run_celio(args, world, rank, local):
         one = celio.CelioBatch(sy, k, 2, B_lab[:1], p_lab[:1], Tk[:1], np.ones(1), rows[:1], 1,
                                wl.times)
         gpu = one.run().cpu().numpy()[0]
+        one.precision = batch.precision
+        gpu_mixed = one.run().cpu().numpy()[0]
         ph = one.phases.cpu().numpy()[0]
         sig = port.sigma_mu(p_lab[0])
         threads = os.cpu_count() or 1
         t0 = time.perf_counter()
         ref = port.celio_fast_evolve_c(fac, dims, sig, wl.times, k, ph, nthreads=threads)
         dt = time.perf_counter() - t0
-        line["max_abs_dP_vs_oracle_1_orient_2_states"] = float(np.abs(gpu - ref).max())
+        line["max_abs_dP_vs_oracle_1_orient_2_states"] = {
+            "fp64": float(np.abs(gpu - ref).max()), "mixed": float(np.abs(gpu_mixed - ref).max())}
         # one state took dt / 2; an orientation sample needs A states
         line["cpu_baseline"] = {"value": T / (dt / 2 * A), "unit": "samples/s", "cores": threads,
                                 "kind": "port",

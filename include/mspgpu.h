@@ -499,9 +499,10 @@ int msp_adjoint_fast(const msp_adjoint_args *args);
  * rows_out[r][t] (optional) = sum over the snapshots row_start[r] ..
  * row_start[r+1]-1 of wscale[s] * (PURE: 0.5 / A sum_a series, DENSITY:
  * Re series of operator 0) -- the averaged, weighted result of
- * ExperimentRunner.run_single.  All FP64.  States that fit in one CTA's
- * shared memory run there from start to end; larger ones run from global
- * memory (path: 0 automatic, 1 shared memory, 2 global memory). */
+ * ExperimentRunner.run_single.  FP64 by default; MSP_PREC_MIXED keeps states
+ * and factors as double-word FP32 (see `precision`).  States that fit in one
+ * CTA's shared memory run there from start to end; larger ones run from
+ * global memory (path: 0 automatic, 1 shared memory, 2 global memory). */
 #define MSP_CELIO_PURE 0
 #define MSP_CELIO_DENSITY 1
 
@@ -534,6 +535,9 @@ typedef struct msp_celio_args {
     int num_rows;
     double *rows_out;             /* device [num_rows][T] or NULL */
     int path;                     /* 0 automatic, 1 shared memory, 2 global memory */
+    int precision;                /* MSP_PREC_FP64, or MSP_PREC_MIXED: double-word FP32
+                                     (hi + lo, ~2^-44 per factor application) on the FP32
+                                     pipe, shared-memory states only */
 } msp_celio_args;
 
 int msp_celio_workspace(const msp_celio_args *args, size_t *bytes);

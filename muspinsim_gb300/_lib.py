@@ -238,6 +238,7 @@ class CelioArgs(ctypes.Structure):
         ("num_rows", ctypes.c_int),
         ("rows_out", _c_dp),
         ("path", ctypes.c_int),
+        ("precision", ctypes.c_int),
     ]
 
 

@@ -5,7 +5,8 @@ spins; one time step is the Trotter product (prod_c U_c)^k with U_c =
 exp(-2 pi i H_c dt / k) (Phys. Rev. Lett. 56, 2720 (1986)).  Building the
 contributions and exponentiating the field-independent ones are small host
 computations, as in the reference; every evolution runs on the GPU through
-``msp_celio_run`` (FP64), with the field-dependent factors of a batch of
+``msp_celio_run`` -- FP64, or double-word FP32 on the FP32 pipe for the
+'mixed' precision -- with the field-dependent factors of a batch of
 snapshots exponentiated on the device (``msp_celio_expm``).
 
 * ``CelioHamiltonian.fast_evolve``: averaged random initial states (the
@@ -272,7 +273,7 @@ class CelioBatch:
     device."""
 
     def __init__(self, system, k, averages, B_lab, p_lab, T, wscale, rows, nrows, times,
-                 device_phases=False, seed=0):
+                 device_phases=False, seed=0, precision="fp64"):
         import torch
 
         from muspinsim_gb300.spinsys import SingleTerm
@@ -372,6 +373,7 @@ class CelioBatch:
         self.digits = np.array(digits, dtype=np.int32).reshape(-1, 2)
         self.mat = np.array(mat, dtype=np.int64)
         self.dims, self.k, self.S, self.T = dims, int(k), S, len(times)
+        self.precision = _lib.PREC_MIXED if precision == "mixed" else _lib.PREC_FP64
         self.nrows = int(nrows)
         self.pure = pure
         self.averages = int(averages)
@@ -422,21 +424,25 @@ class CelioBatch:
                 _lib.CELIO_PURE, self.dims, self.digits, self.mat, self.mats, self.per_snap, self.S,
                 self.averages, self.k, self.T, mu_psi=self.mu_psi, sigma=self.sigma,
                 phases=self.phases, seed=self.seed, wscale=self.wscale, row_start=self.row_start,
-                num_rows=self.nrows, path=path)
+                num_rows=self.nrows, path=path, precision=self.precision)
             return out
         series, _ = kernels.celio_run(
             _lib.CELIO_DENSITY, self.dims + self.dims, self.digits, self.mat, self.mats,
-            self.per_snap, self.S, 1, self.k, self.T, rho0=self.rho0, meas=self.meas, path=path)
+            self.per_snap, self.S, 1, self.k, self.T, rho0=self.rho0, meas=self.meas, path=path,
+            precision=self.precision)
         vals = torch.real(torch.einsum("sta,sa->st", series, self.pol))
         out = torch.zeros((self.nrows, self.T), dtype=torch.float64, device=vals.device)
         out.index_add_(0, self.rows_sorted, vals * self.wscale[:, None])
         return out
 
 
-def run_snapshots(system, k, averages, B_lab, p_lab, T, wscale, rows, nrows, times):
+def run_snapshots(system, k, averages, B_lab, p_lab, T, wscale, rows, nrows, times,
+                  precision="fp64"):
     """All snapshots of an ExperimentRunner with Celio's method: the
-    (nrows, T) float64 results on the device (see CelioBatch)."""
-    return CelioBatch(system, k, averages, B_lab, p_lab, T, wscale, rows, nrows, times).run()
+    (nrows, T) float64 results on the device (see CelioBatch).  'mixed'
+    runs double-word FP32 where the state fits in shared memory."""
+    return CelioBatch(system, k, averages, B_lab, p_lab, T, wscale, rows, nrows, times,
+                      precision=precision).run()
 
 
 logging.getLogger(__name__).addHandler(logging.NullHandler())

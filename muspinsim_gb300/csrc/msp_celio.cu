@@ -45,6 +45,7 @@ constexpr int CE_MAX_DIGITS = 32;
 constexpr int CE_MAX_FACTORS = 1024;
 constexpr int CE_MAX_D = 128;
 constexpr int CE_THREADS = 256;
+constexpr int CE_DW_THREADS = 512;  // double-word kernel: 16 warps, <= 128 registers
 constexpr int CE_CHUNK = 8192;  // elements per CTA of the global measurement
 
 // One factor application: the digits it acts on, sorted by stride (A the
@@ -325,6 +326,323 @@ __global__ void __launch_bounds__(CE_THREADS) msp_celio_smem_kernel(CeArgs a) {
     }
 }
 
+// ----------------------------------------------------------- double-word FP32 path
+// GB300 runs FP32 at 64x its FP64 rate, so the mixed form keeps every
+// state entry and factor entry as an unevaluated sum hi + lo of two FP32
+// numbers (about 48 significant bits) and evaluates each group product
+// y_i = sum_j u_ij x_j on the FP32 pipe.  Lanes of packed f32x2 registers
+// carry (re, im) of x; two sums run side by side,
+//     S1 = sum (u_re, u_re) * (x_re, x_im),  S2 = sum (u_im, u_im) * (x_re, x_im),
+// and y = S1 + (-S2_im, S2_re) is formed once per output.
+//
+// Anchored accumulation: each sum starts at a power of two K >= 4 ||u_i||
+// ||x_group|| (Cauchy-Schwarz bounds every partial sum and every product
+// by ||u_i|| ||x||), so the running value s stays in [3K/4, 5K/4]:
+//     t = fma(u, x, s)       one rounding of s + u x,
+//     s - t                  exact (Sterbenz: s and t within a factor 2),
+//     r = fma(u, x, s - t)   that rounding error, rounded once more,
+// and r goes into a plain FP32 compensation c together with the hi x lo
+// and lo x hi cross terms; s - K is exact at the end.  Four packed
+// instructions per real product instead of TwoProduct + TwoSum's seven, so
+// a complex multiply-add costs 12 packed instructions.  The error of one
+// group product is about 2^-44 K, i.e. ~2^-40 relative to the output.
+typedef unsigned long long u64;
+
+__device__ __forceinline__ u64 add2(u64 a, u64 b) {
+    u64 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
+    u64 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// One factor entry as lane pairs: hi (u_re, u_re), (u_im, u_im) and lo.
+struct DwU {
+    u64 R, I, lR, lI;
+};
+
+__device__ __forceinline__ DwU dw_entry(double2 u) {
+    const float hr = (float)u.x, hi = (float)u.y;
+    const float lr = (float)(u.x - (double)hr), li = (float)(u.y - (double)hi);
+    DwU e;
+    e.R = f32x2(hr, hr);
+    e.I = f32x2(hi, hi);
+    e.lR = f32x2(lr, lr);
+    e.lI = f32x2(li, li);
+    return e;
+}
+
+__device__ __forceinline__ float4 dw_split(double2 v) {
+    const float hr = (float)v.x, hi = (float)v.y;
+    return make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
+}
+
+__device__ __forceinline__ double2 dw_join(float4 v) {
+    return make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
+}
+
+// s + p = t + err exactly (both lanes, no ordering needed); err goes into c
+__device__ __forceinline__ void two_sum2(u64 &s, u64 p, u64 &c) {
+    const u64 t = add2(s, p);
+    const u64 bb = sub2(t, s);
+    const u64 err = add2(sub2(s, sub2(t, bb)), sub2(p, bb));
+    s = t;
+    c = add2(c, err);
+}
+
+// (a, b) -> (-b, a): multiplication by i of a lane pair
+__device__ __forceinline__ u64 times_i(u64 v) {
+    float a, b;
+    split_f32x2(v, a, b);
+    return f32x2(-b, a);
+}
+
+// Shared-memory position of state entry x: the low three bits are XORed
+// with bits 3..5 (msk = 7; msk = 0 leaves the layout alone), so that the
+// eight 16-byte entries a quarter-warp reads at a stride of 8 entries (the
+// groups of a factor on the last, stride-1 digit) fall in distinct banks
+// while contiguous runs stay contiguous.  A permutation inside every
+// aligned block of 8 entries.
+template <typename I>
+__device__ __forceinline__ I swz(I x, int msk) {
+    return x ^ ((x >> 3) & (I)msk);
+}
+
+// Smallest power of two above b >= 0 (2^-126 for b = 0).
+__device__ __forceinline__ float pow2_above(float b) {
+    const unsigned e = (__float_as_uint(b) >> 23) & 0xffu;
+    return __uint_as_float((e + 1u) << 23);
+}
+
+template <int D, typename I>
+__device__ __forceinline__ void ce_group_dw(float4 *__restrict__ V, const DwU *__restrict__ U,
+                                            float rnorm, const CeFactor &f,
+                                            const I *__restrict__ off, I g, int msk) {
+    const I base = ce_base<I>(f, g);
+    u64 xh[D], xl[D];
+    float n2 = 0.f;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        const float4 v = V[swz<I>(base + off[j], msk)];
+        xh[j] = f32x2(v.x, v.y);
+        xl[j] = f32x2(v.z, v.w);
+        n2 = fmaf(v.x, v.x, fmaf(v.y, v.y, n2));
+    }
+    // 4.01 covers the lo parts and the rounding of n2 and of the square root
+    const float K = pow2_above(4.01f * rnorm * sqrtf(n2));
+    const u64 KK = f32x2(K, K);
+#pragma unroll 1
+    for (int i = 0; i < D; ++i) {
+        u64 s1 = KK, s2 = KK, c1 = 0ull, c2 = 0ull;
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            const DwU &u = U[i * D + j];
+            const u64 t1 = fma_f32x2(u.R, xh[j], s1);
+            const u64 t2 = fma_f32x2(u.I, xh[j], s2);
+            c1 = add2(c1, fma_f32x2(u.R, xh[j], sub2(s1, t1)));
+            c2 = add2(c2, fma_f32x2(u.I, xh[j], sub2(s2, t2)));
+            s1 = t1;
+            s2 = t2;
+            c1 = fma_f32x2(u.R, xl[j], c1);
+            c2 = fma_f32x2(u.I, xl[j], c2);
+            c1 = fma_f32x2(u.lR, xh[j], c1);
+            c2 = fma_f32x2(u.lI, xh[j], c2);
+        }
+        s1 = sub2(s1, KK);  // exact
+        s2 = sub2(s2, KK);
+        // y = S1 + i S2, then hi = s + c and lo = its rounding error
+        two_sum2(s1, times_i(s2), c1);
+        c1 = add2(c1, times_i(c2));
+        u64 hi = s1, lo = 0ull;
+        two_sum2(hi, c1, lo);
+        float hr, him, lr, lim;
+        split_f32x2(hi, hr, him);
+        split_f32x2(lo, lr, lim);
+        V[swz<I>(base + off[i], msk)] = make_float4(hr, him, lr, lim);
+    }
+}
+
+// Factors outside the register-resident set: one warp per group, FP64
+// arithmetic on the double-word values (rare: D = 7, 11, 13-15, > 16).
+template <int R, typename I>
+__device__ __forceinline__ void ce_group_dw_warp(float4 *__restrict__ V,
+                                                 const double2 *__restrict__ U,
+                                                 const CeFactor &f, const I *__restrict__ off, I g,
+                                                 int lane, int msk) {
+    const int D = f.D;
+    const I base = ce_base<I>(f, g);
+    double2 x[R], y[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int j = lane + 32 * r;
+        x[r] = j < D ? dw_join(V[swz<I>(base + off[j], msk)]) : make_double2(0.0, 0.0);
+        y[r] = make_double2(0.0, 0.0);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r2 = 0; r2 < R; ++r2) {
+        for (int jj = 0; jj < 32; ++jj) {
+            const int j = 32 * r2 + jj;
+            if (j >= D) break;
+            const double xr = __shfl_sync(0xffffffffu, x[r2].x, jj);
+            const double xi = __shfl_sync(0xffffffffu, x[r2].y, jj);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int i = lane + 32 * r;
+                if (i < D) {
+                    const double2 u = U[i * D + j];
+                    y[r].x = fma(u.x, xr, fma(-u.y, xi, y[r].x));
+                    y[r].y = fma(u.x, xi, fma(u.y, xr, y[r].y));
+                }
+            }
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int i = lane + 32 * r;
+        if (i < D) V[swz<I>(base + off[i], msk)] = dw_split(y[r]);
+    }
+}
+
+template <typename I>
+__device__ void ce_apply_dw(float4 *__restrict__ V, const DwU *__restrict__ U,
+                            const double2 *__restrict__ Ud, float rnorm, const CeFactor &f,
+                            const I *__restrict__ off, I G, int tid, int nt, int lane, int warp,
+                            int nw, int msk) {
+    switch (f.D) {
+#define CE_DW_CASE(DD)                                                                    \
+    case DD:                                                                              \
+        for (I g = tid; g < G; g += nt) ce_group_dw<DD, I>(V, U, rnorm, f, off, g, msk);  \
+        return;
+        CE_DW_CASE(1)
+        CE_DW_CASE(2)
+        CE_DW_CASE(3)
+        CE_DW_CASE(4)
+        CE_DW_CASE(5)
+        CE_DW_CASE(6)
+        CE_DW_CASE(8)
+        CE_DW_CASE(9)
+        CE_DW_CASE(10)
+        CE_DW_CASE(12)
+        CE_DW_CASE(16)
+#undef CE_DW_CASE
+        default:
+            break;
+    }
+    const int R = (f.D + 31) >> 5;
+    for (I g = warp; g < G; g += nw) {
+        if (R == 1)
+            ce_group_dw_warp<1, I>(V, Ud, f, off, g, lane, msk);
+        else if (R == 2)
+            ce_group_dw_warp<2, I>(V, Ud, f, off, g, lane, msk);
+        else if (R == 3)
+            ce_group_dw_warp<3, I>(V, Ud, f, off, g, lane, msk);
+        else
+            ce_group_dw_warp<4, I>(V, Ud, f, off, g, lane, msk);
+    }
+}
+
+// Shared memory of the double-word kernel: state (16 B per entry), factor
+// entries in lane patterns (48 B) and, for the warp-form factors, in FP64.
+__global__ void __launch_bounds__(CE_DW_THREADS) msp_celio_smem_dw_kernel(CeArgs a) {
+    extern __shared__ __align__(16) unsigned char ce_smem[];
+    float4 *V = reinterpret_cast<float4 *>(ce_smem);
+    DwU *Uw = reinterpret_cast<DwU *>(V + a.V);
+    double2 *Ud = reinterpret_cast<double2 *>(Uw + a.mats_len);
+    CeFactor *fac = reinterpret_cast<CeFactor *>(Ud + a.mats_len);
+    float *rnorm = reinterpret_cast<float *>(fac + a.nf);
+    int *offs = reinterpret_cast<int *>(rnorm + ((a.nf + 3) & ~3));
+    double *red = reinterpret_cast<double *>(offs + ((a.noffs + 3) & ~3));
+
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    for (int i = tid; i < a.nf; i += nt) fac[i] = a.fac[i];
+    for (int i = tid; i < a.noffs; i += nt) offs[i] = (int)a.offs[i];
+
+    const int V32 = (int)a.V;
+    const int msk = (V32 & 7) == 0 ? 7 : 0;
+    int loaded = -1;
+    for (int st = blockIdx.x; st < a.S * a.A; st += gridDim.x) {
+        const int s = st / a.A;
+        const int blk = a.mats_per_snap ? s : 0;
+        if (blk != loaded) {
+            const double2 *src = a.mats + (size_t)blk * a.mats_len;
+            for (long long i = tid; i < a.mats_len; i += nt) {
+                const double2 u = src[i];
+                Uw[i] = dw_entry(u);
+                Ud[i] = u;
+            }
+            // largest row 2-norm of each factor (1 for a unitary factor)
+            for (int fi = tid; fi < a.nf; fi += nt) {
+                const CeFactor &f = a.fac[fi];
+                const double2 *m = src + f.mat;
+                double best = 0.0;
+                for (int r = 0; r < f.D; ++r) {
+                    double q = 0.0;
+                    for (int c = 0; c < f.D; ++c) q += m[r * f.D + c].x * m[r * f.D + c].x +
+                                                       m[r * f.D + c].y * m[r * f.D + c].y;
+                    best = fmax(best, q);
+                }
+                rnorm[fi] = (float)(sqrt(best) * (1.0 + 1e-6));
+            }
+            loaded = blk;
+        }
+        if (a.mode == MSP_CELIO_PURE) {
+            for (int x = tid; x < V32; x += nt) V[swz(x, msk)] = dw_split(ce_init_pure(a, st, x));
+        } else {
+            const double2 *r0 = a.rho0 + (size_t)s * a.V;
+            for (int x = tid; x < V32; x += nt) V[swz(x, msk)] = dw_split(r0[x]);
+        }
+        __syncthreads();
+        for (int t = 0; t < a.T; ++t) {
+            if (a.mode == MSP_CELIO_PURE) {
+                const double2 *sg = a.sigma + 4 * s;
+                const double2 m00 = sg[0], m01 = sg[1], m11 = sg[3];
+                double m = 0.0, z = 0.0;
+                for (int kk = tid; kk < (int)a.half; kk += nt) {
+                    const double2 u = dw_join(V[swz(kk, msk)]);
+                    const double2 d = dw_join(V[swz(kk + (int)a.half, msk)]);
+                    const double tr = m00.x * u.x - m00.y * u.y + 2.0 * (m01.x * d.x - m01.y * d.y);
+                    const double ti = m00.x * u.y + m00.y * u.x + 2.0 * (m01.x * d.y + m01.y * d.x);
+                    m += u.x * tr + u.y * ti;
+                    const double sr = m11.x * d.x - m11.y * d.y, si = m11.x * d.y + m11.y * d.x;
+                    m += d.x * sr + d.y * si;
+                }
+                block_sum2(m, z, red);
+                if (tid == 0) a.series_pure[(size_t)st * a.T + t] = m;
+            } else {
+                const double2 *W0 = a.meas + (size_t)(a.meas_per_snap ? s : 0) * a.nops * a.V;
+                for (int j = 0; j < a.nops; ++j) {
+                    const double2 *W = W0 + (size_t)j * a.V;
+                    double re = 0.0, im = 0.0;
+                    for (int x = tid; x < V32; x += nt) {
+                        const double2 r = dw_join(V[swz(x, msk)]), w = W[x];
+                        re += r.x * w.x - r.y * w.y;
+                        im += r.x * w.y + r.y * w.x;
+                    }
+                    block_sum2(re, im, red);
+                    if (tid == 0)
+                        a.series_rho[((size_t)s * a.T + t) * a.nops + j] = make_double2(re, im);
+                }
+            }
+            if (t + 1 == a.T) break;
+            for (int r = 0; r < a.k; ++r) {
+                for (int fi = 0; fi < a.nf; ++fi) {
+                    const CeFactor &f = fac[fi];
+                    ce_apply_dw<int>(V, Uw + f.mat, Ud + f.mat, rnorm[fi], f, offs + f.off,
+                                     V32 / f.D, tid, nt, lane, warp, nw, msk);
+                    __syncthreads();
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ----------------------------------------------------------- global-memory path
 __global__ void msp_celio_init_kernel(CeArgs a) {
     const long long total = (long long)a.S * a.A * a.V;
@@ -560,6 +878,7 @@ struct CePlan {
     int chunks = 1;
     size_t smem = 0;
     bool use_smem = false;
+    bool dw = false;  // double-word FP32 shared-memory kernel
 };
 
 static int ce_plan(const msp_celio_args *a, CePlan &p) {
@@ -638,9 +957,14 @@ static int ce_plan(const msp_celio_args *a, CePlan &p) {
     const long long span = a->mode == MSP_CELIO_PURE ? p.half : V;
     p.chunks = (int)((span + CE_CHUNK - 1) / CE_CHUNK);
     if (p.chunks < 1) p.chunks = 1;
+    if (a->precision != MSP_PREC_FP64 && a->precision != MSP_PREC_MIXED)
+        return ce_fail(MSP_ERR_ARG, "msp_celio: precision must be MSP_PREC_FP64 or MSP_PREC_MIXED");
     const size_t offs_pad = (p.offs.size() + 3) & ~(size_t)3;
-    p.smem = (size_t)V * 16 + (size_t)a->mats_len * 16 + p.fac.size() * sizeof(CeFactor) +
-             offs_pad * 4 + 2 * (CE_THREADS / 32) * sizeof(double);
+    const bool mixed = a->precision == MSP_PREC_MIXED;
+    const size_t mats_b = (size_t)a->mats_len * (mixed ? 48 : 16);
+    const size_t rnorm_b = mixed ? ((p.fac.size() + 3) & ~(size_t)3) * 4 : 0;
+    p.smem = (size_t)V * 16 + mats_b + p.fac.size() * sizeof(CeFactor) + rnorm_b +
+             offs_pad * 4 + 2 * (CE_DW_THREADS / 32) * sizeof(double);
     int dev = 0, optin = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
@@ -648,9 +972,13 @@ static int ce_plan(const msp_celio_args *a, CePlan &p) {
         optin = 227 * 1024;
     }
     const bool fits = p.smem <= (size_t)optin && V < (1ll << 30);
+    if (a->precision == MSP_PREC_MIXED && (a->path == 2 || !fits))
+        return ce_fail(MSP_ERR_UNSUPPORTED,
+                       "msp_celio: MSP_PREC_MIXED runs states that fit in shared memory only");
     p.use_smem = a->path == 1 ? true : (a->path == 2 ? false : fits);
     if (p.use_smem && !fits)
         return ce_fail(MSP_ERR_UNSUPPORTED, "msp_celio: state does not fit in shared memory");
+    p.dw = a->precision == MSP_PREC_MIXED;
     return MSP_OK;
 }
 
@@ -753,19 +1081,22 @@ int msp_celio_run(const msp_celio_args *a, void *workspace, size_t workspace_byt
     k.chunks = p.chunks;
     const int sms = ce_sms();
     if (p.use_smem) {
-        rc = ce_cuda(cudaFuncSetAttribute(msp_celio_smem_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+        void (*kern)(CeArgs) = p.dw ? msp_celio_smem_dw_kernel : msp_celio_smem_kernel;
+        rc = ce_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)p.smem));
         if (rc != MSP_OK) return rc;
         int occ = 1;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, msp_celio_smem_kernel, CE_THREADS,
-                                                          p.smem) != cudaSuccess || occ < 1) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern,
+                                                          p.dw ? CE_DW_THREADS : CE_THREADS,
+                                                          p.smem) !=
+                cudaSuccess ||
+            occ < 1) {
             cudaGetLastError();
             occ = 1;
         }
         const long long cap = (long long)sms * occ;
         const int grid = (int)(p.states < cap ? p.states : cap);
-        msp_celio_smem_kernel<<<grid, CE_THREADS, p.smem, st>>>(k);
+        kern<<<grid, p.dw ? CE_DW_THREADS : CE_THREADS, p.smem, st>>>(k);
         rc = ce_cuda(cudaGetLastError());
         if (rc != MSP_OK) return rc;
     } else {

@@ -347,7 +347,7 @@ class ExperimentRunner:
                 raise NotImplementedError(
                     "integrate_decaying is not implemented for Celio's method")
             out = celio.run_snapshots(self._system, cfg.celio_k, cfg.celio_averages, B_lab, p_lab,
-                                      T, ws / cfg.avg_N, rows, nrows, times)
+                                      T, ws / cfg.avg_N, rows, nrows, times, self.precision)
             status = np.zeros(len(B_lab), dtype=np.int32)
         elif len(cfg.dissipation_terms) > 0:
             out, status = self._run_lindblad(B_lab, p_lab, T, ws / cfg.avg_N, rows, nrows, times)

@@ -601,8 +601,9 @@ def lindblad_run(n, Hsys, Z, spin_ops, dims, mu_index, gammas, dissipation, fiel
 def celio_run(mode, digit_dims, factor_digits, factor_mat, mats, mats_per_snapshot,
               num_snapshots, states_per_snapshot, trotter_k, num_times, mu_psi=None, sigma=None,
               phases=None, seed=0, rho0=None, meas=None, meas_per_snapshot=False,
-              wscale=None, row_start=None, num_rows=0, path=0):
-    """Celio's method through ``msp_celio_run`` (FP64).
+              wscale=None, row_start=None, num_rows=0, path=0, precision=_lib.PREC_FP64):
+    """Celio's method through ``msp_celio_run`` (FP64, or double-word FP32
+    with ``precision`` = PREC_MIXED).
 
     ``digit_dims``: multiplicity of each digit of a state (spins for
     CELIO_PURE, row then column spins for CELIO_DENSITY);
@@ -666,6 +667,7 @@ def celio_run(mode, digit_dims, factor_digits, factor_mat, mats, mats_per_snapsh
             keep.append(ws_)
             a.wscale = ptr(ws_)
     a.path = int(path)
+    a.precision = int(precision)
     nbytes = ctypes.c_size_t(0)
     _lib.call("msp_celio_workspace", ctypes.byref(a), ctypes.byref(nbytes))
     ws = torch.empty(int(nbytes.value) + 256, dtype=torch.uint8, device=d)

@@ -245,3 +245,43 @@ def test_device_generated_states():
     assert np.array_equal(outs[0], outs[1])
     assert np.abs(outs[0] - outs[2]).max() > 1e-6
     assert np.abs(outs[0]).max() <= 0.5 + 1e-12
+
+
+MIXED_TOL = 1e-9  # double-word FP32: ~2^-44 per factor application
+
+
+@pytest.mark.parametrize("name", ["celio_fast_muVV", "celio_fast_field", "celio_rho_desc"])
+def test_mixed_precision_goldens(name):
+    """The double-word FP32 form against the reference's golden runs."""
+    g = load_golden(name)
+    er = _runner(g)
+    er.precision = "mixed"
+    if g.get("seed") is not None:
+        np.random.seed(g["seed"])
+    res = er.run()
+    assert np.abs(res - g["result"]).max() <= MIXED_TOL
+
+
+def test_mixed_precision_all_factor_forms():
+    """Double-word FP32 with every factor form (register groups of D = 16,
+    8, 3, 4, 6 and the FP64 warp fallback of D = 24) against FP64, many
+    Trotter passes: the error stays at the 1e-11 level."""
+    from muspinsim_gb300 import _lib, kernels
+    from muspinsim_gb300.celio import _mu_psi, _pure_plan
+
+    spins, coup = _big_system()
+    osy = oracle_system(spins, coup)
+    dims = list(osy.dims)
+    t = np.linspace(0, 4.0, 80)
+    k = 10
+    fac = port.celio_snapshot_factors(osy, [0.001, 0.0, 0.003], t[1] - t[0], k)
+    plan = _pure_plan(dims, [(U, order) for U, _, order, _ in fac])
+    sig = port.sigma_mu([0.0, 0.6, 0.8])
+    ph = celio_phases(21, 1, 3, osy.n // 2)
+    outs = {}
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):
+        series, _ = kernels.celio_run(
+            _lib.CELIO_PURE, dims, plan["digits"], plan["mat"], plan["block"][None], False, 1, 3,
+            k, len(t), mu_psi=_mu_psi(sig)[None], sigma=sig[None], phases=ph, precision=prec)
+        outs[prec] = series.cpu().numpy()
+    assert np.abs(outs[_lib.PREC_MIXED] - outs[_lib.PREC_FP64]).max() <= MIXED_TOL
