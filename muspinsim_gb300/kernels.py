@@ -35,7 +35,10 @@ def dev(a, dtype):
     d = device()
     if isinstance(a, torch.Tensor):
         return a.to(device=d, dtype=dtype).contiguous()
-    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).to(d)
+    arr = np.ascontiguousarray(a)
+    if not arr.flags.writeable:  # e.g. a broadcast view: torch wants its own copy
+        arr = arr.copy()
+    return torch.as_tensor(arr, dtype=dtype).to(d)
 
 
 def eigh(H, precision=_lib.PREC_FP64, max_sweeps=0):
