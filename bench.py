@@ -66,6 +66,11 @@ def parse_args():
     p.add_argument("--celio-orient", type=int, default=8,
                    help="celio workload: orientations (19 random states each)")
     p.add_argument("--celio-times", type=int, default=50, help="celio workload: time samples")
+    p.add_argument("--celio-nuclei", type=int, default=4,
+                   help="celio workload: vanadium nuclei (4: dim 8192 in shared memory; "
+                        "5: dim 65536 from global memory)")
+    p.add_argument("--celio-states", type=int, default=19,
+                   help="celio workload: random states per orientation")
     p.add_argument("--workload", default="config2",
                    choices=["config1", "config2", "config3", "config4", "config5", "lindblad",
                             "celio"],
@@ -811,7 +816,8 @@ def run_celio(args, world, rank, local):
     from muspinsim_gb300 import quaternion as Q
     from muspinsim_gb300.orientations import orientation_rows_to_quats
 
-    wl = workloads.celio_v3si(n_orient=args.celio_orient, n_times=args.celio_times)
+    wl = workloads.celio_v3si(n_orient=args.celio_orient, n_times=args.celio_times,
+                              n_vanadium=args.celio_nuclei, averages=args.celio_states)
     k, A = wl.meta["celio"]
     steps = max(1, min(args.steps, 10))
     sy = wl.system(celio_k=k)
@@ -849,12 +855,15 @@ def run_celio(args, world, rank, local):
     achieved = flops / (ms["mixed"] * 1e-3) / 1e9
     pipe_ops = cmacs * 24 / (ms["mixed"] * 1e-3) / 1e9  # FP32 ops issued per second (12 f32x2)
     samples = N * T
-    line = _line("Celio P(t) samples/s (orientation x time, 19 random states each), "
+    line = _line(f"Celio P(t) samples/s (orientation x time, {A} random states each), "
                  "double-word FP32", samples / (ms["mixed"] * 1e-3), "samples/s", ms["mixed"],
-                 args, world, f"celio_muV4_dim8192_{N}_orient_{A}_states_{T}_t_k{k}",
+                 args, world,
+                 f"celio_muV{args.celio_nuclei}_dim{V}_{N}_orient_{A}_states_{T}_t_k{k}",
                  {"orientations": N, "states_per_orientation": A, "times": T, "dim": V,
                   "trotter_k": k, "factors_per_pass": len(batch.digits),
-                  "l2": "states resident in shared memory; HBM traffic is the inputs only"},
+                  "l2": ("states resident in shared memory; HBM traffic is the inputs only"
+                         if V <= 8192 else "states in global memory (L2-resident): one launch "
+                                           "per factor application")},
                  dtype="f32 double-word", gpu_launches=steps,
                  state_steps_per_s=N * A * (T - 1) / (ms["mixed"] * 1e-3),
                  fp64={"value": samples / (ms["fp64"] * 1e-3), "ms_per_step": ms["fp64"],

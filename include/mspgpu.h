@@ -536,8 +536,8 @@ typedef struct msp_celio_args {
     double *rows_out;             /* device [num_rows][T] or NULL */
     int path;                     /* 0 automatic, 1 shared memory, 2 global memory */
     int precision;                /* MSP_PREC_FP64, or MSP_PREC_MIXED: double-word FP32
-                                     (hi + lo, ~2^-44 per factor application) on the FP32
-                                     pipe, shared-memory states only */
+                                     (hi + lo, ~2^-40 per factor application) on the FP32
+                                     pipe, either memory path */
 } msp_celio_args;
 
 int msp_celio_workspace(const msp_celio_args *args, size_t *bytes);

@@ -80,9 +80,11 @@ struct CeArgs {
     int nops, meas_per_snap;
     double *series_pure;   // [S*A][T]
     double2 *series_rho;   // [S][T][nops]
-    double2 *state;        // global path: [S*A][V]
+    double2 *state;        // global path: [S*A][V] (double2, or float4 hi/lo pairs when dw)
     double *partial;       // global path: [S*A][chunks][2 nops]
     int chunks;
+    void *dwmats;          // global double-word path: factor entries in lane patterns
+    float *rnorms;         // global double-word path: [blocks][nf] row 2-norm bounds
 };
 
 // First element of group g of factor f (the element whose involved digits
@@ -644,14 +646,106 @@ __global__ void __launch_bounds__(CE_DW_THREADS) msp_celio_smem_dw_kernel(CeArgs
 }
 
 // ----------------------------------------------------------- global-memory path
+__device__ __forceinline__ double2 ce_ld(const double2 *V, long long x) { return V[x]; }
+__device__ __forceinline__ double2 ce_ld(const float4 *V, long long x) { return dw_join(V[x]); }
+__device__ __forceinline__ void ce_st(double2 *V, long long x, double2 v) { V[x] = v; }
+__device__ __forceinline__ void ce_st(float4 *V, long long x, double2 v) { V[x] = dw_split(v); }
+
+template <typename S>
 __global__ void msp_celio_init_kernel(CeArgs a) {
+    S *state = reinterpret_cast<S *>(a.state);
     const long long total = (long long)a.S * a.A * a.V;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
         const int st = (int)(e / a.V);
         const long long x = e - (long long)st * a.V;
-        a.state[e] = a.mode == MSP_CELIO_PURE ? ce_init_pure(a, st, x)
-                                              : a.rho0[(size_t)(st / a.A) * a.V + x];
+        ce_st(state, e, a.mode == MSP_CELIO_PURE ? ce_init_pure(a, st, x)
+                                                 : a.rho0[(size_t)(st / a.A) * a.V + x]);
+    }
+}
+
+// Global double-word path: factor entries in lane patterns and the row
+// 2-norm bound of every factor, once per run.
+__global__ void msp_celio_dw_prep_kernel(CeArgs a, int blocks) {
+    DwU *dst = reinterpret_cast<DwU *>(a.dwmats);
+    const long long total = (long long)blocks * a.mats_len;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x)
+        dst[e] = dw_entry(a.mats[e]);
+    const long long nfb = (long long)blocks * a.nf;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nfb;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(e / a.nf), fi = (int)(e - (long long)b * a.nf);
+        const CeFactor &f = a.fac[fi];
+        const double2 *m = a.mats + (size_t)b * a.mats_len + f.mat;
+        double best = 0.0;
+        for (int r = 0; r < f.D; ++r) {
+            double q = 0.0;
+            for (int c = 0; c < f.D; ++c)
+                q += m[r * f.D + c].x * m[r * f.D + c].x + m[r * f.D + c].y * m[r * f.D + c].y;
+            best = fmax(best, q);
+        }
+        a.rnorms[e] = (float)(sqrt(best) * (1.0 + 1e-6));
+    }
+}
+
+__global__ void msp_celio_apply_dw_kernel(CeArgs a, CeFactor f, int fi) {
+    const long long G = a.V / f.D;
+    const long long *off = a.offs + f.off;
+    const int states = a.S * a.A;
+    const long long total = G * states;
+    float4 *state = reinterpret_cast<float4 *>(a.state);
+    const DwU *dw = reinterpret_cast<const DwU *>(a.dwmats);
+    if (ce_thread_form(f.D)) {
+        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+             e += (long long)gridDim.x * blockDim.x) {
+            const int st = (int)(e / G);
+            const long long g = e - (long long)st * G;
+            const int blk = a.mats_per_snap ? st / a.A : 0;
+            float4 *V = state + (size_t)st * a.V;
+            const DwU *U = dw + (size_t)blk * a.mats_len + f.mat;
+            const float rn = a.rnorms[(size_t)blk * a.nf + fi];
+            switch (f.D) {
+#define CE_DWG_CASE(DD)                                          \
+    case DD:                                                     \
+        ce_group_dw<DD, long long>(V, U, rn, f, off, g, 0);      \
+        break;
+                CE_DWG_CASE(1)
+                CE_DWG_CASE(2)
+                CE_DWG_CASE(3)
+                CE_DWG_CASE(4)
+                CE_DWG_CASE(5)
+                CE_DWG_CASE(6)
+                CE_DWG_CASE(8)
+                CE_DWG_CASE(9)
+                CE_DWG_CASE(10)
+                CE_DWG_CASE(12)
+                CE_DWG_CASE(16)
+#undef CE_DWG_CASE
+                default:
+                    break;
+            }
+        }
+    } else {
+        const int lane = threadIdx.x & 31;
+        const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+        const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+        const int R = (f.D + 31) >> 5;
+        for (long long e = wid; e < total; e += nwarps) {
+            const int st = (int)(e / G);
+            const long long g = e - (long long)st * G;
+            const int blk = a.mats_per_snap ? st / a.A : 0;
+            float4 *V = state + (size_t)st * a.V;
+            const double2 *Ud = a.mats + (size_t)blk * a.mats_len + f.mat;
+            if (R == 1)
+                ce_group_dw_warp<1, long long>(V, Ud, f, off, g, lane, 0);
+            else if (R == 2)
+                ce_group_dw_warp<2, long long>(V, Ud, f, off, g, lane, 0);
+            else if (R == 3)
+                ce_group_dw_warp<3, long long>(V, Ud, f, off, g, lane, 0);
+            else
+                ce_group_dw_warp<4, long long>(V, Ud, f, off, g, lane, 0);
+        }
     }
 }
 
@@ -687,17 +781,26 @@ __global__ void msp_celio_apply_kernel(CeArgs a, CeFactor f) {
 }
 
 // Partial sums of one measurement: CTA (chunk c, state st).
+template <typename S>
 __global__ void __launch_bounds__(CE_THREADS) msp_celio_measure_kernel(CeArgs a) {
     __shared__ double red[2 * (CE_THREADS / 32)];
     const int c = blockIdx.x, st = blockIdx.y;
-    const double2 *V = a.state + (size_t)st * a.V;
+    const S *V = reinterpret_cast<const S *>(a.state) + (size_t)st * a.V;
     double *out = a.partial + ((size_t)st * a.chunks + c) * 2 * a.nops;
     if (a.mode == MSP_CELIO_PURE) {
         const long long lo = (long long)c * CE_CHUNK;
         const long long hi = lo + CE_CHUNK < a.half ? lo + CE_CHUNK : a.half;
-        double m = ce_measure_pure(V, a.half, a.sigma + 4 * (st / a.A), lo + threadIdx.x, hi,
-                                   blockDim.x),
-               z = 0.0;
+        const double2 *sg = a.sigma + 4 * (st / a.A);
+        const double2 m00 = sg[0], m01 = sg[1], m11 = sg[3];
+        double m = 0.0, z = 0.0;
+        for (long long kk = lo + threadIdx.x; kk < hi; kk += blockDim.x) {
+            const double2 u = ce_ld(V, kk), d = ce_ld(V, a.half + kk);
+            const double tr = m00.x * u.x - m00.y * u.y + 2.0 * (m01.x * d.x - m01.y * d.y);
+            const double ti = m00.x * u.y + m00.y * u.x + 2.0 * (m01.x * d.y + m01.y * d.x);
+            m += u.x * tr + u.y * ti;
+            const double sr = m11.x * d.x - m11.y * d.y, si = m11.x * d.y + m11.y * d.x;
+            m += d.x * sr + d.y * si;
+        }
         block_sum2(m, z, red);
         if (threadIdx.x == 0) out[0] = m;
     } else {
@@ -709,7 +812,7 @@ __global__ void __launch_bounds__(CE_THREADS) msp_celio_measure_kernel(CeArgs a)
             const double2 *W = W0 + (size_t)j * a.V;
             double re = 0.0, im = 0.0;
             for (long long x = lo + threadIdx.x; x < hi; x += blockDim.x) {
-                const double2 r = V[x], w = W[x];
+                const double2 r = ce_ld(V, x), w = W[x];
                 re += r.x * w.x - r.y * w.y;
                 im += r.x * w.y + r.y * w.x;
             }
@@ -972,9 +1075,6 @@ static int ce_plan(const msp_celio_args *a, CePlan &p) {
         optin = 227 * 1024;
     }
     const bool fits = p.smem <= (size_t)optin && V < (1ll << 30);
-    if (a->precision == MSP_PREC_MIXED && (a->path == 2 || !fits))
-        return ce_fail(MSP_ERR_UNSUPPORTED,
-                       "msp_celio: MSP_PREC_MIXED runs states that fit in shared memory only");
     p.use_smem = a->path == 1 ? true : (a->path == 2 ? false : fits);
     if (p.use_smem && !fits)
         return ce_fail(MSP_ERR_UNSUPPORTED, "msp_celio: state does not fit in shared memory");
@@ -992,6 +1092,11 @@ static size_t ce_workspace(const msp_celio_args *a, const CePlan &p) {
         b += ce_align((size_t)p.states * p.V * 16);
         const int nops = a->mode == MSP_CELIO_PURE ? 1 : a->num_ops;
         b += ce_align((size_t)p.states * p.chunks * 2 * nops * sizeof(double));
+        if (p.dw) {
+            const size_t blocks = a->mats_per_snapshot ? (size_t)a->num_snapshots : 1;
+            b += ce_align(blocks * (size_t)a->mats_len * 32 + 16);
+            b += ce_align(blocks * p.fac.size() * sizeof(float) + 16);
+        }
     }
     return b;
 }
@@ -1103,16 +1208,34 @@ int msp_celio_run(const msp_celio_args *a, void *workspace, size_t workspace_byt
         k.state = (double2 *)w;
         w += ce_align((size_t)p.states * p.V * 16);
         k.partial = (double *)w;
+        {
+            const int nops = a->mode == MSP_CELIO_PURE ? 1 : a->num_ops;
+            w += ce_align((size_t)p.states * p.chunks * 2 * nops * sizeof(double));
+        }
         const long long total = (long long)p.states * p.V;
         const int igrid = (int)((total + 255) / 256 < (long long)sms * 16 ? (total + 255) / 256
                                                                          : (long long)sms * 16);
-        msp_celio_init_kernel<<<igrid, 256, 0, st>>>(k);
+        if (p.dw) {
+            const int blocks = a->mats_per_snapshot ? a->num_snapshots : 1;
+            k.dwmats = (void *)w;
+            w += ce_align((size_t)blocks * (size_t)a->mats_len * 32 + 16);
+            k.rnorms = (float *)w;
+            w += ce_align((size_t)blocks * p.fac.size() * sizeof(float) + 16);
+            if (!p.fac.empty())
+                msp_celio_dw_prep_kernel<<<sms * 4, 256, 0, st>>>(k, blocks);
+            msp_celio_init_kernel<float4><<<igrid, 256, 0, st>>>(k);
+        } else {
+            msp_celio_init_kernel<double2><<<igrid, 256, 0, st>>>(k);
+        }
         rc = ce_cuda(cudaGetLastError());
         if (rc != MSP_OK) return rc;
         const dim3 mgrid(p.chunks, p.states);
         const int fin = (p.states * k.nops + 127) / 128;
         for (int t = 0; t < a->num_times; ++t) {
-            msp_celio_measure_kernel<<<mgrid, CE_THREADS, 0, st>>>(k);
+            if (p.dw)
+                msp_celio_measure_kernel<float4><<<mgrid, CE_THREADS, 0, st>>>(k);
+            else
+                msp_celio_measure_kernel<double2><<<mgrid, CE_THREADS, 0, st>>>(k);
             msp_celio_measure_finish_kernel<<<fin, 128, 0, st>>>(k, t);
             if (t + 1 == a->num_times) break;
             for (int r = 0; r < a->trotter_k; ++r) {
@@ -1122,7 +1245,10 @@ int msp_celio_run(const msp_celio_args *a, void *workspace, size_t workspace_byt
                                            (ce_thread_form(f.D) ? 1 : 32);
                     const long long blocks = (work + 255) / 256;
                     const int grid = (int)(blocks < (long long)sms * 8 ? blocks : (long long)sms * 8);
-                    msp_celio_apply_kernel<<<grid, 256, 0, st>>>(k, f);
+                    if (p.dw)
+                        msp_celio_apply_dw_kernel<<<grid, 256, 0, st>>>(k, f, (int)fi);
+                    else
+                        msp_celio_apply_kernel<<<grid, 256, 0, st>>>(k, f);
                 }
             }
             rc = ce_cuda(cudaGetLastError());

@@ -224,12 +224,13 @@ def config4(seed=1004, n_systems=4096, n_orient=256, n_times=2048,
     return [random_system_workload(rng, int(d), orients, times) for d in draws]
 
 
-def celio_v3si(seed=1006, n_orient=8, n_times=50, k=10, averages=19):
-    """Celio's method on mu + 4 V (dim 8192); see the module docstring."""
+def celio_v3si(seed=1006, n_orient=8, n_times=50, k=10, averages=19, n_vanadium=4):
+    """Celio's method on mu + n_vanadium V (dim 2 x 8^n; 8192 for the
+    default 4); see the module docstring."""
     rng = np.random.default_rng(seed)
-    spins = ["mu", "V", "V", "V", "V"]
+    spins = ["mu"] + ["V"] * n_vanadium
     coup = []
-    for v in range(2, 6):
+    for v in range(2, 2 + n_vanadium):
         coup.append(("dipolar", {"i": 1, "j": v}, random_vector(rng, 1.6, 2.0)))
         coup.append(("quadrupolar", {"i": v}, random_efg(rng, 0.02, 0.06)))
     orients = zcw_gen(n_orient) if n_orient > 1 else np.array([[0.0, 0.0]])

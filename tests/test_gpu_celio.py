@@ -262,10 +262,11 @@ def test_mixed_precision_goldens(name):
     assert np.abs(res - g["result"]).max() <= MIXED_TOL
 
 
-def test_mixed_precision_all_factor_forms():
+@pytest.mark.parametrize("path", [0, 2])
+def test_mixed_precision_all_factor_forms(path):
     """Double-word FP32 with every factor form (register groups of D = 16,
     8, 3, 4, 6 and the FP64 warp fallback of D = 24) against FP64, many
-    Trotter passes: the error stays at the 1e-11 level."""
+    Trotter passes, in shared memory and from global memory."""
     from muspinsim_gb300 import _lib, kernels
     from muspinsim_gb300.celio import _mu_psi, _pure_plan
 
@@ -282,6 +283,30 @@ def test_mixed_precision_all_factor_forms():
     for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):
         series, _ = kernels.celio_run(
             _lib.CELIO_PURE, dims, plan["digits"], plan["mat"], plan["block"][None], False, 1, 3,
-            k, len(t), mu_psi=_mu_psi(sig)[None], sigma=sig[None], phases=ph, precision=prec)
+            k, len(t), mu_psi=_mu_psi(sig)[None], sigma=sig[None], phases=ph, precision=prec,
+            path=path if prec == _lib.PREC_MIXED else 0)
         outs[prec] = series.cpu().numpy()
     assert np.abs(outs[_lib.PREC_MIXED] - outs[_lib.PREC_FP64]).max() <= MIXED_TOL
+
+
+def test_mixed_precision_density_global():
+    """The density-matrix form in double-word FP32 from global memory, with
+    the warp fallback for its D = 24 factors, against the oracle."""
+    from muspinsim_gb300 import _lib, kernels
+    from muspinsim_gb300.celio import _density_plan
+
+    spins, coup = _big_system()
+    osy = oracle_system(spins, coup)
+    dims = list(osy.dims)
+    t = np.linspace(0, 0.4, 6)
+    fac = port.celio_snapshot_factors(osy, [0.0, 0.0, 0.002], t[1] - t[0], 2)
+    rho = port.rho0(osy, np.array([0.0, 0.0, 0.002]), np.array([0.0, 0.0, 1.0]), np.inf)
+    ops = [osy.muon_operator([0.0, 0.0, 1.0])]
+    ref = port.celio_evolve(fac, dims, rho, t, ops, 2)
+    plan = _density_plan(dims, [(U, order) for U, _, order, _ in fac])
+    N = osy.n
+    series, _ = kernels.celio_run(
+        _lib.CELIO_DENSITY, dims + dims, plan["digits"], plan["mat"], plan["block"][None], False,
+        1, 1, 2, len(t), rho0=rho.reshape(1, N, N), meas=np.stack([o.T for o in ops])[None],
+        path=2, precision=_lib.PREC_MIXED)
+    assert np.abs(series.cpu().numpy()[0] - ref).max() <= MIXED_TOL
