@@ -62,8 +62,8 @@ def cache_key(device_name, n, num_times, uniform, precision, lib_version):
 
 def candidates(n):
     """Candidate values per parameter for dimension n (first = default)."""
-    if n > 64:
-        return {"snap_threads": [0, 256, 512, 128], "ctas_per_sm": [0, 2, 3],
+    if n > 64:  # default: 128 threads, as many CTAs per SM as fit
+        return {"snap_threads": [0, 64, 256], "ctas_per_sm": [0, 2, 4, 8],
                 "snaps_per_item": [0]}
     m = n + (n & 1)
     base = 32 if m <= 8 else 64 if m <= 16 else 128 if m <= 32 else 256

@@ -84,7 +84,7 @@ int msp_eigh_workspace(int n, int batch, size_t *bytes) {
     if (n > MSP_MAX_DIM_LARGE)
         return fail(MSP_ERR_UNSUPPORTED, "msp_eigh_workspace: n=%d exceeds %d", n,
                     MSP_MAX_DIM_LARGE);
-    *bytes = n <= MSP_MAX_DIM ? 0 : large_scratch_bytes(n, large_grid(batch));
+    *bytes = n <= MSP_MAX_DIM ? 0 : large_scratch_bytes(n, large_grid(batch, n));
     return MSP_OK;
 }
 
@@ -103,7 +103,7 @@ int msp_eigh_batched_ws(const double *H, int n, int batch, int precision, int ma
     MSP_CHECK_PTR(evals);
     MSP_CHECK_PTR(evecs);
     MSP_CHECK_PTR(status);
-    const int grid = large_grid(batch);
+    const int grid = large_grid(batch, n);
     const size_t need = large_scratch_bytes(n, grid);
     if (workspace == NULL || workspace_bytes < need)
         return fail(MSP_ERR_WORKSPACE, "msp_eigh_batched_ws: workspace %zu < %zu bytes",
@@ -352,7 +352,8 @@ static Layout powder_layout(const msp_powder_args *a) {
     L.partial = off;
     off += align256((size_t)L.max_items * L.T * (L.phase_records ? 4 : 8));
     L.large = off;
-    if (a->n > MSP_MAX_DIM) off += align256(large_scratch_bytes(a->n, large_grid(a->num_snap)));
+    if (a->n > MSP_MAX_DIM)
+        off += align256(large_scratch_bytes(a->n, large_grid(a->num_snap, a->n)));
     L.total = off;
     return L;
 }
@@ -436,7 +437,7 @@ int msp_powder_run(const msp_powder_args *a) {
     if (ev) cudaEventRecord(ev[0], st);
     if (large && a->num_snap > 0)
         rc = cuda_check(launch_large_fast(sa, reinterpret_cast<double *>(ws + L.large),
-                                          large_grid(a->num_snap), st),
+                                          large_grid(a->num_snap, a->n), st),
                         "msp_large_fast");
     else
         rc = cuda_check(launch_snapshots(sa, a->mode, a->precision, st), "msp_snap");

@@ -158,7 +158,8 @@ cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cuda
                               int threads = 0);
 int large_threads(int n);
 size_t large_scratch_bytes(int n, int grid);
-int large_grid(int batch);
+int large_ctas_per_sm(int n);
+int large_grid(int batch, int n);
 
 // Work decomposition of the phase sum (host side).  A work item sums at
 // most MSP_F32_ITEM_PAIRS pairs in FP32 (mixed precision): longer FP32

@@ -12,6 +12,12 @@
 // Parallelisation: warp-per-row matrix-vector products and elementwise
 // rank-2 updates (1), the QL rotations computed by one thread and applied to
 // all rows of Z by all threads (2), one column of U per thread (3).
+// Step 2's rotation sequence is a serial chain of FP64 operations, which on
+// GB300 (FP64 at 1/64 of the FP32 rate, long FP64 latency) took two thirds
+// of the solve: d and e live in shared memory, each rotation takes one
+// Newton reciprocal square root instead of a library hypot and two
+// divisions, and small CTAs (128 threads) run several to an SM so that one
+// matrix's serial QL overlaps other matrices' parallel phases.
 #include <math_constants.h>
 #include <stdio.h>
 
@@ -29,10 +35,23 @@ __host__ __device__ inline size_t large_scratch_doubles(int n) {
     return (size_t)5 * n * n + 5 * (size_t)n + 64;
 }
 
-struct LargeScratch {
-    cx<double> *A, *U;
-    double *Zt, *d, *e, *lam;
-    cx<double> *tau;
+template <typename T>
+struct LargeScratchT {
+    cx<T> *A, *U;
+    T *Zt, *d, *e, *lam;
+    cx<T> *tau;
+};
+using LargeScratch = LargeScratchT<double>;
+
+template <typename T>
+struct LargeEps;
+template <>
+struct LargeEps<double> {
+    static constexpr double eps = MSP_DBL_EPS;
+};
+template <>
+struct LargeEps<float> {
+    static constexpr float eps = 1.1920928955078125e-7f;  // 2^-23
 };
 
 __device__ __forceinline__ LargeScratch large_carve(double *base, int n) {
@@ -62,56 +81,82 @@ __device__ __forceinline__ T block_sum(T v, T *red) {
 }
 
 // Shared memory: v, p (n complex each), qc, qs (n doubles each), red.
+// (sized for T = double; the FP32 instance uses half of it)
 __host__ __device__ inline size_t large_smem_bytes(int n, int threads) {
-    return (size_t)n * 16 * 2 + (size_t)n * 8 * 2 + (size_t)(threads / 32) * 16 + 64;
+    return (size_t)n * 16 * 2 + (size_t)n * 8 * 4 + (size_t)(threads / 32) * 16 + 64;
+}
+
+// 1 / sqrt(x) for x > 0 in FP64 by Newton's method on f(y) = 1/y^2 - x,
+// y <- y (3 - x y^2) / 2, from a single-precision seed: each step squares
+// the relative error (2^-23 -> 2^-46 -> 2^-92), so the result is correct to
+// the last bit or two, in a dozen dependent FP64 operations.  Callers keep
+// x inside the seed's range (1e-36 .. 1e36).
+template <typename T>
+__device__ __forceinline__ T rsqrt_newton(T x);
+template <>
+__device__ __forceinline__ double rsqrt_newton<double>(double x) {
+    double y = (double)rsqrtf((float)x);
+    const double h = 0.5 * x;
+    y = y * fma(-h * y, y, 1.5);
+    y = y * fma(-h * y, y, 1.5);
+    return y;
+}
+// FP32: the hardware approximation and one Newton step
+template <>
+__device__ __forceinline__ float rsqrt_newton<float>(float x) {
+    const float y = rsqrtf(x);
+    return y * fmaf(-0.5f * x * y, y, 1.5f);
 }
 
 // Eigenpairs of the Hermitian matrix already in s.A (full, row-major):
 // ascending eigenvalues into s.lam, eigenvectors (columns) into s.U.
 // Returns MSP_ITEM_OK or MSP_ITEM_NOT_CONVERGED (QL iteration cap).
-__device__ int large_eigh(LargeScratch s, int n, char *smem) {
+template <typename T>
+__device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     const int nw = nt >> 5;
-    cx<double> *v = reinterpret_cast<cx<double> *>(smem);
-    cx<double> *p = v + n;
-    double *qc = reinterpret_cast<double *>(p + n);
-    double *qs = qc + n;
-    double *red = qs + n;
-    cx<double> *A = s.A;
+    cx<T> *v = reinterpret_cast<cx<T> *>(smem);
+    cx<T> *p = v + n;
+    T *qc = reinterpret_cast<T *>(p + n);
+    T *qs = qc + n;
+    T *dsm = qs + n;  // diagonal and off-diagonal of the tridiagonal matrix
+    T *esm = dsm + n;
+    T *red = esm + n;
+    cx<T> *A = s.A;
 
     // ---- 1. tridiagonalisation
     for (int k = 0; k + 1 < n; ++k) {
         const int m = n - k - 1;  // length of x = A[k+1.., k]
-        double xn2 = 0.0;
+        T xn2 = T(0);
         for (int i = 1 + tid; i < m; i += nt) xn2 += cabs2(A[(size_t)(k + 1 + i) * n + k]);
         xn2 = block_sum(xn2, red);
-        const cx<double> alpha = A[(size_t)(k + 1) * n + k];
-        cx<double> tau = mk<double>(0.0, 0.0);
-        double beta = alpha.re;
-        const bool reflect = !(xn2 == 0.0 && alpha.im == 0.0);
+        const cx<T> alpha = A[(size_t)(k + 1) * n + k];
+        cx<T> tau = mk<T>(T(0), T(0));
+        T beta = alpha.re;
+        const bool reflect = !(xn2 == T(0) && alpha.im == T(0));
         if (reflect) {
             beta = -copysign(sqrt(alpha.re * alpha.re + alpha.im * alpha.im + xn2), alpha.re);
-            tau = mk<double>((beta - alpha.re) / beta, -alpha.im / beta);
+            tau = mk<T>((beta - alpha.re) / beta, -alpha.im / beta);
             // v = x / (alpha - beta), v_0 = 1
-            const cx<double> den = mk<double>(alpha.re - beta, alpha.im);
-            const double dd = 1.0 / cabs2(den);
-            const cx<double> sc = mk<double>(den.re * dd, -den.im * dd);
+            const cx<T> den = mk<T>(alpha.re - beta, alpha.im);
+            const T dd = T(1) / cabs2(den);
+            const cx<T> sc = mk<T>(den.re * dd, -den.im * dd);
             for (int i = tid; i < m; i += nt)
-                v[i] = i == 0 ? mk<double>(1.0, 0.0) : cmul(A[(size_t)(k + 1 + i) * n + k], sc);
+                v[i] = i == 0 ? mk<T>(T(1), T(0)) : cmul(A[(size_t)(k + 1 + i) * n + k], sc);
         }
         if (tid == 0) {
-            s.d[k] = A[(size_t)k * n + k].re;
-            s.e[k] = beta;
+            dsm[k] = A[(size_t)k * n + k].re;
+            esm[k] = beta;
             s.tau[k] = tau;
         }
         __syncthreads();
         if (!reflect) continue;
         // p = tau * A22 v  (warp per row)
         for (int i = warp; i < m; i += nw) {
-            const cx<double> *row = A + (size_t)(k + 1 + i) * n + (k + 1);
-            double pr = 0.0, pi = 0.0;
+            const cx<T> *row = A + (size_t)(k + 1 + i) * n + (k + 1);
+            T pr = T(0), pi = T(0);
             for (int j = lane; j < m; j += 32) {
-                const cx<double> a = row[j], x = v[j];
+                const cx<T> a = row[j], x = v[j];
                 pr += a.re * x.re - a.im * x.im;
                 pi += a.re * x.im + a.im * x.re;
             }
@@ -120,89 +165,99 @@ __device__ int large_eigh(LargeScratch s, int n, char *smem) {
                 pr += __shfl_xor_sync(0xffffffffu, pr, o);
                 pi += __shfl_xor_sync(0xffffffffu, pi, o);
             }
-            if (lane == 0) p[i] = cmul(tau, mk<double>(pr, pi));
+            if (lane == 0) p[i] = cmul(tau, mk<T>(pr, pi));
         }
         __syncthreads();
         // alpha2 = -1/2 tau (p^H v); w = p + alpha2 v (in p)
-        double hr = 0.0, hi = 0.0;
+        T hr = T(0), hi = T(0);
         for (int i = tid; i < m; i += nt) {
-            const cx<double> c = cmulc(p[i], v[i]);  // conj(p_i) v_i
+            const cx<T> c = cmulc(p[i], v[i]);  // conj(p_i) v_i
             hr += c.re;
             hi += c.im;
         }
         hr = block_sum(hr, red);
         hi = block_sum(hi, red);
-        const cx<double> a2 = cscale(-0.5, cmul(tau, mk<double>(hr, hi)));
+        const cx<T> a2 = cscale(-T(0.5), cmul(tau, mk<T>(hr, hi)));
         for (int i = tid; i < m; i += nt) p[i] = cadd(p[i], cmul(a2, v[i]));
         __syncthreads();
         // A22 -= v w^H + w v^H
         for (int e = tid; e < m * m; e += nt) {
             const int i = e / m, j = e - i * m;  // FastDiv is exact only for m^3 < 2^20
-            const cx<double> vi = v[i], wi = p[i], vj = v[j], wj = p[j];
-            cx<double> &a = A[(size_t)(k + 1 + i) * n + (k + 1 + j)];
-            const cx<double> t1 = cmul(vi, conj(wj)), t2 = cmul(wi, conj(vj));
-            a = mk<double>(a.re - t1.re - t2.re, a.im - t1.im - t2.im);
+            const cx<T> vi = v[i], wi = p[i], vj = v[j], wj = p[j];
+            cx<T> &a = A[(size_t)(k + 1 + i) * n + (k + 1 + j)];
+            const cx<T> t1 = cmul(vi, conj(wj)), t2 = cmul(wi, conj(vj));
+            a = mk<T>(a.re - t1.re - t2.re, a.im - t1.im - t2.im);
         }
         // keep v for the back-transformation (column k below the subdiagonal)
         for (int i = 1 + tid; i < m; i += nt) A[(size_t)(k + 1 + i) * n + k] = v[i];
         __syncthreads();
     }
     if (tid == 0) {
-        s.d[n - 1] = A[(size_t)(n - 1) * n + (n - 1)].re;
-        s.e[n - 1] = 0.0;
+        dsm[n - 1] = A[(size_t)(n - 1) * n + (n - 1)].re;
+        esm[n - 1] = T(0);
     }
     // Z = I (column-major: Zt[col * n + row])
     for (size_t e = tid; e < (size_t)n * n; e += nt) {
         const int c = (int)(e / n), r = (int)(e - (size_t)c * n);
-        s.Zt[e] = r == c ? 1.0 : 0.0;
+        s.Zt[e] = r == c ? T(1) : T(0);
     }
     __syncthreads();
 
     // ---- 2. QL with implicit shifts; e[i] couples d[i], d[i+1]
     int status = MSP_ITEM_OK;
     __shared__ int s_ctl[4];  // m, iteration flag, rotation count, status
-    __shared__ double s_f, s_tst;
+    __shared__ T s_f, s_tst;
     if (tid == 0) {
-        s_f = 0.0;
-        s_tst = 0.0;
+        s_f = T(0);
+        s_tst = T(0);
         s_ctl[3] = MSP_ITEM_OK;
     }
     __syncthreads();
-    double *d = s.d, *e = s.e;
+    T *d = dsm, *e = esm;
     for (int l = 0; l < n; ++l) {
         for (int iter = 0;; ++iter) {
             if (tid == 0) {
                 if (iter == 0) s_tst = fmax(s_tst, fabs(d[l]) + fabs(e[l]));
                 int m = l;
-                while (m < n - 1 && fabs(e[m]) > MSP_DBL_EPS * s_tst) ++m;
+                while (m < n - 1 && fabs(e[m]) > LargeEps<T>::eps * s_tst) ++m;
                 s_ctl[0] = m;
                 s_ctl[1] = 0;
                 s_ctl[2] = 0;
                 if (m > l && iter < 60) {
                     // one QL step on rows l..m; rotations (c, s) for i = m-1 .. l
-                    double g = d[l];
-                    double pp = (d[l + 1] - g) / (2.0 * e[l]);
-                    double r = hypot(pp, 1.0);
+                    T g = d[l];
+                    T pp = (d[l + 1] - g) / (T(2) * e[l]);
+                    T r = hypot(pp, T(1));
                     d[l] = e[l] / (pp + copysign(r, pp));
                     d[l + 1] = e[l] * (pp + copysign(r, pp));
-                    const double dl1 = d[l + 1];
-                    double h = g - d[l];
+                    const T dl1 = d[l + 1];
+                    T h = g - d[l];
                     for (int i = l + 2; i < n; ++i) d[i] -= h;
                     s_f += h;
                     pp = d[m];
-                    double c = 1.0, c2 = 1.0, c3 = 1.0, sn = 0.0, s2 = 0.0;
-                    const double el1 = e[l + 1];
+                    T c = T(1), c2 = T(1), c3 = T(1), sn = T(0), s2 = T(0);
+                    const T el1 = e[l + 1];
                     int cnt = 0;
                     for (int i = m - 1; i >= l; --i) {
                         c3 = c2;
                         c2 = c;
                         s2 = sn;
-                        g = c * e[i];
+                        const T ei = e[i];
+                        g = c * ei;
                         h = c * pp;
-                        r = hypot(pp, e[i]);
-                        e[i + 1] = sn * r;
-                        sn = e[i] / r;
-                        c = pp / r;
+                        const T x2 = fma(pp, pp, ei * ei);
+                        if (x2 > T(1e-36) && x2 < T(1e36)) {
+                            const T y = rsqrt_newton<T>(x2);
+                            r = x2 * y;
+                            e[i + 1] = sn * r;
+                            sn = ei * y;
+                            c = pp * y;
+                        } else {  // outside the seed's range: the library route
+                            r = hypot(pp, ei);
+                            e[i + 1] = sn * r;
+                            sn = ei / r;
+                            c = pp / r;
+                        }
                         pp = c * d[i] - sn * g;
                         d[i + 1] = h + sn * (c * g + sn * d[i]);
                         qc[cnt] = c;
@@ -223,23 +278,39 @@ __device__ int large_eigh(LargeScratch s, int n, char *smem) {
             // apply the rotations to every row of Z: columns (i, i+1), i = m-1 .. l
             {
                 const int m = s_ctl[0], cnt = s_ctl[2];
+                T *__restrict__ Zt = s.Zt;
                 for (int row = tid; row < n; row += nt) {
-                    double hcarry = s.Zt[(size_t)m * n + row];  // Z[row][i+1] for i = m-1
-                    for (int q = 0; q < cnt; ++q) {
+                    T hcarry = Zt[(size_t)m * n + row];  // Z[row][i+1] for i = m-1
+                    int q = 0;
+                    // eight entries loaded ahead of the rotation chain: within a
+                    // sweep every entry is read before it is written
+                    for (; q + 8 <= cnt; q += 8) {
+                        T zi[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) zi[u] = Zt[(size_t)(m - 1 - q - u) * n + row];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int i = m - 1 - q - u;
+                            const T c = qc[q + u], sn = qs[q + u];
+                            Zt[(size_t)(i + 1) * n + row] = sn * zi[u] + c * hcarry;
+                            hcarry = c * zi[u] - sn * hcarry;
+                        }
+                    }
+                    for (; q < cnt; ++q) {
                         const int i = m - 1 - q;
-                        const double zi = s.Zt[(size_t)i * n + row];
-                        const double c = qc[q], sn = qs[q];
-                        s.Zt[(size_t)(i + 1) * n + row] = sn * zi + c * hcarry;
+                        const T zi = Zt[(size_t)i * n + row];
+                        const T c = qc[q], sn = qs[q];
+                        Zt[(size_t)(i + 1) * n + row] = sn * zi + c * hcarry;
                         hcarry = c * zi - sn * hcarry;
                     }
-                    s.Zt[(size_t)l * n + row] = hcarry;
+                    Zt[(size_t)l * n + row] = hcarry;
                 }
             }
             __syncthreads();
         }
         if (tid == 0) {
             d[l] += s_f;
-            e[l] = 0.0;
+            e[l] = T(0);
         }
         __syncthreads();
     }
@@ -248,28 +319,28 @@ __device__ int large_eigh(LargeScratch s, int n, char *smem) {
     // ---- 3. U = Q Z (complex), reflectors applied last to first; one column per thread
     for (size_t x = tid; x < (size_t)n * n; x += nt) {
         const int i = (int)(x / n), j = (int)(x - (size_t)i * n);
-        s.U[x] = mk<double>(s.Zt[(size_t)j * n + i], 0.0);
+        s.U[x] = mk<T>(s.Zt[(size_t)j * n + i], T(0));
     }
     __syncthreads();
     for (int k = n - 2; k >= 0; --k) {
-        const cx<double> tau = s.tau[k];
-        if (tau.re == 0.0 && tau.im == 0.0) continue;
+        const cx<T> tau = s.tau[k];
+        if (tau.re == T(0) && tau.im == T(0)) continue;
         const int m = n - k - 1;
         for (int j = tid; j < n; j += nt) {
             // s_j = v^H U[k+1.., j]; U[k+1.., j] -= tau v s_j
-            double sr = 0.0, si = 0.0;
+            T sr = T(0), si = T(0);
             for (int i = 0; i < m; ++i) {
-                const cx<double> vi = i == 0 ? mk<double>(1.0, 0.0) : A[(size_t)(k + 1 + i) * n + k];
-                const cx<double> u = s.U[(size_t)(k + 1 + i) * n + j];
+                const cx<T> vi = i == 0 ? mk<T>(T(1), T(0)) : A[(size_t)(k + 1 + i) * n + k];
+                const cx<T> u = s.U[(size_t)(k + 1 + i) * n + j];
                 sr += vi.re * u.re + vi.im * u.im;
                 si += vi.re * u.im - vi.im * u.re;
             }
-            const cx<double> ts = cmul(tau, mk<double>(sr, si));
+            const cx<T> ts = cmul(tau, mk<T>(sr, si));
             for (int i = 0; i < m; ++i) {
-                const cx<double> vi = i == 0 ? mk<double>(1.0, 0.0) : A[(size_t)(k + 1 + i) * n + k];
-                cx<double> &u = s.U[(size_t)(k + 1 + i) * n + j];
-                const cx<double> t = cmul(vi, ts);
-                u = mk<double>(u.re - t.re, u.im - t.im);
+                const cx<T> vi = i == 0 ? mk<T>(T(1), T(0)) : A[(size_t)(k + 1 + i) * n + k];
+                cx<T> &u = s.U[(size_t)(k + 1 + i) * n + j];
+                const cx<T> t = cmul(vi, ts);
+                u = mk<T>(u.re - t.re, u.im - t.im);
             }
         }
         __syncthreads();
@@ -396,7 +467,7 @@ __global__ void msp_large_fast_kernel(SnapArgs a, double *__restrict__ scratch) 
     }
 }
 
-int large_threads(int n) { return n <= 128 ? 256 : 512; }
+int large_threads(int n) { return 128; }
 
 cudaError_t launch_eigh_large(const double *H, int n, int batch, double *evals, double *evecs,
                               int *status, double *scratch, int grid, cudaStream_t st) {
@@ -424,16 +495,41 @@ cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cuda
 
 size_t large_scratch_bytes(int n, int grid) { return large_scratch_doubles(n) * 8 * (size_t)grid; }
 
-// One CTA per SM (the working matrices of all CTAs then fit in L2), at most
-// one per matrix.
-int large_grid(int batch) {
+// Resident CTAs of the large-n kernels per SM with large_threads(n)
+// threads, cut so that all CTAs' scratch stays within about 2 GB (large n
+// keeps one CTA per SM).
+int large_ctas_per_sm(int n) {
+    const int threads = large_threads(n);
+    int occ = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, msp_large_fast_kernel, threads,
+                                                      large_smem_bytes(n, threads)) !=
+            cudaSuccess ||
+        occ < 1) {
+        cudaGetLastError();
+        occ = 1;
+    }
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
         cudaGetLastError();
         sms = 152;
     }
-    return batch < sms ? (batch > 0 ? batch : 1) : sms;
+    const size_t per = large_scratch_doubles(n) * 8, budget = (size_t)2 << 30;
+    while (occ > 1 && (size_t)occ * sms * per > budget) --occ;
+    return occ;
+}
+
+// A persistent grid of SMs x large_ctas_per_sm(n) CTAs, at most one per
+// matrix.
+int large_grid(int batch, int n) {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    const int g = sms * large_ctas_per_sm(n);
+    return batch < g ? (batch > 0 ? batch : 1) : g;
 }
 
 }  // namespace msp

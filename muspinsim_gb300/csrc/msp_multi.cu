@@ -148,7 +148,8 @@ static int plan_layout(msp_multi_plan *p, const msp_multi_desc *d) {
         const msp_multi_tuning *t = find_tuning(d, n);
         b.threads = t && t->snap_threads > 0 ? t->snap_threads
                                              : (b.large ? large_threads(n) : snap_default_threads(n));
-        b.ctas_per_sm = t && t->ctas_per_sm > 0 ? t->ctas_per_sm : (b.large ? 1 : 0);
+        b.ctas_per_sm = t && t->ctas_per_sm > 0 ? t->ctas_per_sm
+                                                : (b.large ? large_ctas_per_sm(n) : 0);
         long long cap = max_pairs / (b.P > 0 ? b.P : 1);
         if (cap < 1) cap = 1;
         if (cap > b.num_snap) cap = b.num_snap > 0 ? b.num_snap : 1;
