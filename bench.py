@@ -755,22 +755,30 @@ def run_lindblad(args, world, rank, local):
                       for i in range(3)], dtype=complex)
     T = len(wl.times)
 
-    def step():
+    def step(prec=_lib.PREC_MIXED):
         return kernels.lindblad_run(n, sy.hamiltonian_matrix(), sy.zeeman_operators(), S_ops,
                                     list(sy.dimension), 0, sy.gammas, diss, B_lab, p_lab, ws / N,
                                     np.zeros(N, np.int32), 1, wl.times,
-                                    temperature=wl.temperature)[0]
+                                    temperature=wl.temperature, precision=prec)[0]
 
     for _ in range(args.warmup):
         step()
+        step(_lib.PREC_FP64)
     ms = _events_ms(step, max(1, args.steps))
+    ms64 = _events_ms(lambda: step(_lib.PREC_FP64), max(1, min(args.steps, 3)))
     out = step().cpu().numpy()[0]
-    line = _line("dissipative powder P(t) samples/s, FP64", N * T / (ms * 1e-3), "samples/s", ms,
+    out64 = step(_lib.PREC_FP64).cpu().numpy()[0]
+    line = _line("dissipative powder P(t) samples/s, double-word FP32 propagation",
+                 N * T / (ms * 1e-3), "samples/s", ms,
                  args, world, "mu_e_H_lindblad_500_orient_1000_t",
                  {"orientations": N, "times": T, "dim": n, "superoperator": n * n,
                   "dissipation_MHz": {"e": 2.0, "H": 0.3}, "temperature_K": 20.0},
-                 dtype="f64", gpu_launches=3 * max(1, args.steps),
-                 note="e2e: every step uploads the orientation vectors (host inputs)")
+                 dtype="f32 double-word (propagation), f64 (construction, measurement)",
+                 gpu_launches=5 * max(1, args.steps),
+                 fp64={"value": N * T / (ms64 * 1e-3), "ms_per_step": ms64},
+                 mixed_over_fp64=ms64 / ms,
+                 max_abs_dP_mixed_vs_fp64=float(np.abs(out - out64).max()),
+                 note="each step uploads the orientation vectors (host inputs)")
     if not args.no_cpu_baseline:
         from oracle import port
         from tests.helpers import oracle_system
@@ -787,7 +795,7 @@ def run_lindblad(args, world, rank, local):
                                      (ws[:sample] * (sample / ws[:sample].sum())) / sample,
                                      np.zeros(sample, np.int32), 1, wl.times,
                                      temperature=wl.temperature)[0].cpu().numpy()[0]
-        line["max_abs_dP_vs_oracle_20_orient"] = float(np.abs(gpu20 - ref).max())
+        line["max_abs_dP_vs_oracle_20_orient_fp64"] = float(np.abs(gpu20 - ref).max())
         line["cpu_baseline"] = {"value": sample * T / dt, "unit": "samples/s", "cores": 1,
                                 "kind": "port",
                                 "sample": f"{sample} orientations (numpy eig of L per snapshot)"}

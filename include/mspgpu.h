@@ -419,6 +419,9 @@ typedef struct msp_lindblad_args {
     void *workspace;               /* >= msp_lindblad_workspace bytes, 256-byte aligned */
     size_t workspace_bytes;
     void *stream;
+    int precision;                 /* MSP_PREC_FP64, or MSP_PREC_MIXED: for EVOLVE on a
+                                      uniform grid with n^2 <= 64, propagators and states
+                                      in double-word FP32 (hi + lo) on the FP32 pipe */
 } msp_lindblad_args;
 
 int msp_lindblad_workspace(const msp_lindblad_args *args, size_t *bytes);

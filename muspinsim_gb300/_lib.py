@@ -200,6 +200,7 @@ class LindbladArgs(ctypes.Structure):
         ("workspace", _c_dp),
         ("workspace_bytes", ctypes.c_size_t),
         ("stream", _c_dp),
+        ("precision", ctypes.c_int),
     ]
 
 

@@ -32,6 +32,7 @@
 
 #include <vector>
 
+#include "msp_dw.cuh"
 #include "msp_internal.cuh"
 
 namespace msp {
@@ -348,19 +349,6 @@ __global__ void __launch_bounds__(CE_THREADS) msp_celio_smem_kernel(CeArgs a) {
 // instructions per real product instead of TwoProduct + TwoSum's seven, so
 // a complex multiply-add costs 12 packed instructions.  The error of one
 // group product is about 2^-44 K, i.e. ~2^-40 relative to the output.
-typedef unsigned long long u64;
-
-__device__ __forceinline__ u64 add2(u64 a, u64 b) {
-    u64 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
-    u64 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-
 // One factor entry as lane pairs: hi (u_re, u_re), (u_im, u_im) and lo.
 struct DwU {
     u64 R, I, lR, lI;
@@ -377,31 +365,6 @@ __device__ __forceinline__ DwU dw_entry(double2 u) {
     return e;
 }
 
-__device__ __forceinline__ float4 dw_split(double2 v) {
-    const float hr = (float)v.x, hi = (float)v.y;
-    return make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
-}
-
-__device__ __forceinline__ double2 dw_join(float4 v) {
-    return make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
-}
-
-// s + p = t + err exactly (both lanes, no ordering needed); err goes into c
-__device__ __forceinline__ void two_sum2(u64 &s, u64 p, u64 &c) {
-    const u64 t = add2(s, p);
-    const u64 bb = sub2(t, s);
-    const u64 err = add2(sub2(s, sub2(t, bb)), sub2(p, bb));
-    s = t;
-    c = add2(c, err);
-}
-
-// (a, b) -> (-b, a): multiplication by i of a lane pair
-__device__ __forceinline__ u64 times_i(u64 v) {
-    float a, b;
-    split_f32x2(v, a, b);
-    return f32x2(-b, a);
-}
-
 // Shared-memory position of state entry x: the low three bits are XORed
 // with bits 3..5 (msk = 7; msk = 0 leaves the layout alone), so that the
 // eight 16-byte entries a quarter-warp reads at a stride of 8 entries (the
@@ -411,12 +374,6 @@ __device__ __forceinline__ u64 times_i(u64 v) {
 template <typename I>
 __device__ __forceinline__ I swz(I x, int msk) {
     return x ^ ((x >> 3) & (I)msk);
-}
-
-// Smallest power of two above b >= 0 (2^-126 for b = 0).
-__device__ __forceinline__ float pow2_above(float b) {
-    const unsigned e = (__float_as_uint(b) >> 23) & 0xffu;
-    return __uint_as_float((e + 1u) << 23);
 }
 
 template <int D, typename I>

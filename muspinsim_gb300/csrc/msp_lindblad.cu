@@ -22,6 +22,9 @@
 #include <math_constants.h>
 #include <string.h>
 
+#include <algorithm>
+
+#include "msp_dw.cuh"
 #include "msp_internal.cuh"
 #include "msp_rho.cuh"
 
@@ -384,6 +387,8 @@ struct LbArgs {
     double *res;             // num_snap x T (real part x wscale)
     zd *scratch;
     size_t scratch_entries;  // per CTA
+    int build_only;          // write L, rho0 and vec(O^T) per snapshot, do not propagate
+    zd *Lout, *vout, *oout;  // num_snap x N^2, N, N
 };
 
 // Two axes orthogonal to z (muspinsim/utils.py:71-93), z a unit vector.
@@ -526,6 +531,16 @@ __global__ void __launch_bounds__(MSP_LB_THREADS) msp_lindblad_kernel(LbArgs a) 
                 __syncthreads();
             }
         }
+        if (a.build_only) {
+            for (int e = tid; e < N * N; e += nt) a.Lout[(size_t)s * N * N + e] = w.L[e];
+            for (int e = tid; e < N; e += nt) {
+                a.vout[(size_t)s * N + e] = w.v[e];
+                a.oout[(size_t)s * N + e] = w.o[e];
+            }
+            if (tid == 0 && sa.status) sa.status[s] = MSP_ITEM_OK;
+            __syncthreads();
+            continue;
+        }
         const double weight = sa.wscale[s];
         double *res = a.res + (size_t)s * a.num_times;
         if (a.integral) {
@@ -538,6 +553,316 @@ __global__ void __launch_bounds__(MSP_LB_THREADS) msp_lindblad_kernel(LbArgs a) 
         if (tid == 0 && sa.status) sa.status[s] = MSP_ITEM_OK;
         __syncthreads();
     }
+}
+
+// ---------------------------------------------------------------- double-word propagation
+// The mixed precision of the evolution mode on a uniform grid, N = n^2 <= 64:
+// L, the propagators and rho live in shared memory as double-word FP32
+// (hi + lo pairs, about 48 significant bits), and every product runs on the
+// FP32 pipe with the anchored compensated accumulation of the Celio kernels:
+// each sum starts at a power of two K >= 4 ||row|| ||column|| (Cauchy-
+// Schwarz bounds every partial sum), so fma(u, x, s), the exact s - t and
+// fma(u, x, s - t) give the sum and its rounding error.  GB300 runs FP64 at
+// 1/64 of the FP32 rate with a 64-cycle dependent-FMA latency; the FP64
+// kernel above stays the reference form.
+constexpr int LBW_MAXN = 64;
+
+constexpr int LBW_CHUNK = 128;  // time steps recorded before they are measured
+
+struct LbDwArgs {
+    const zd *L, *v, *o;  // per snapshot: N x N, N, N (from the build-only pass)
+    int n, num_snap, num_times;
+    double t0, dt;
+    const double *wscale;
+    double *res;          // num_snap x T
+    float4 *hist;         // per CTA: LBW_CHUNK x N states awaiting measurement
+};
+
+// <O> of the recorded states hist[0 .. cnt) into res[k0 ..): two threads per
+// state, FP64 sums of the double-word values.
+__device__ void lbw_measure_chunk(const float4 *hist, const double2 *os, int N, int cnt,
+                                  double weight, double *res) {
+    const int tid = threadIdx.x, half = tid & 1, j = tid >> 1;
+    const int h = (N + 1) >> 1, e0 = half * h, e1 = min(N, e0 + h);
+    for (int jj = j; jj < ((cnt + 127) & ~127); jj += blockDim.x >> 1) {
+        double acc = 0.0;
+        if (jj < cnt)
+            for (int e = e0; e < e1; ++e) {
+                const double2 r = dw_join(hist[(size_t)jj * N + e]), o = os[e];
+                acc = fma(o.x, r.x, fma(-o.y, r.y, acc));
+            }
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        if (jj < cnt && half == 0) res[jj] = acc * weight;
+    }
+}
+
+// (h, l) * (ch, cl) for one real component, renormalised
+__device__ __forceinline__ void lbw_mul(float &h, float &l, float ch, float cl) {
+    const float p = h * ch;
+    float e = fmaf(h, ch, -p);
+    e = fmaf(h, cl, fmaf(l, ch, e));
+    h = p + e;
+    l = e - (h - p);
+}
+
+// (h, l) + 1 exactly to double-word precision
+__device__ __forceinline__ void lbw_add1(float &h, float &l) {
+    const float s = 1.0f + h;
+    const float bb = s - 1.0f;
+    const float err = (1.0f - (s - bb)) + (h - bb);
+    const float e = l + err;
+    h = s + e;
+    l = e - (h - s);
+}
+
+// Shared-memory position of matrix entry (i, k): odd rows are XOR-swizzled
+// by 4 entries (sw = 4 when N is a multiple of 8, else 0), so that the two
+// rows a quarter-warp reads in the matrix-vector product fall in disjoint
+// bank groups; a permutation inside every row.
+__device__ __forceinline__ int lbw_at(int i, int k, int N, int sw) {
+    return i * N + (k ^ ((i & 1) * sw));
+}
+
+// y = S1 + i S2 from the two anchored sums (s already minus K), renormalised
+__device__ __forceinline__ float4 lbw_finish(u64 s1, u64 c1, u64 s2, u64 c2) {
+    two_sum2(s1, times_i(s2), c1);
+    c1 = add2(c1, times_i(c2));
+    u64 hi = s1, lo = 0ull;
+    two_sum2(hi, c1, lo);
+    float hr, him, lr, lim;
+    split_f32x2(hi, hr, him);
+    split_f32x2(lo, lr, lim);
+    return make_float4(hr, him, lr, lim);
+}
+
+__device__ __forceinline__ void lbw_step(u64 &s1, u64 &c1, u64 &s2, u64 &c2, float4 a, float4 b) {
+    const u64 R = f32x2(a.x, a.x), I = f32x2(a.y, a.y), lR = f32x2(a.z, a.z),
+              lI = f32x2(a.w, a.w);
+    const u64 xh = f32x2(b.x, b.y), xl = f32x2(b.z, b.w);
+    const u64 t1 = fma_f32x2(R, xh, s1);
+    const u64 t2 = fma_f32x2(I, xh, s2);
+    c1 = add2(c1, fma_f32x2(R, xh, sub2(s1, t1)));
+    c2 = add2(c2, fma_f32x2(I, xh, sub2(s2, t2)));
+    s1 = t1;
+    s2 = t2;
+    c1 = fma_f32x2(R, xl, c1);
+    c2 = fma_f32x2(I, xl, c2);
+    c1 = fma_f32x2(lR, xh, c1);
+    c2 = fma_f32x2(lI, xh, c2);
+}
+
+// C = A B (N x N, shared memory); rn, cn: scratch for row / column norms
+__device__ void lbw_gemm(float4 *C, const float4 *A, const float4 *B, int N, float *rn, float *cn,
+                         int sw) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int q = tid; q < 2 * N; q += nt) {
+        float acc = 0.f;
+        if (q < N) {
+            for (int k = 0; k < N; ++k) {
+                const float4 a = A[q * N + k];  // a whole row, in any order
+                acc = fmaf(a.x, a.x, fmaf(a.y, a.y, acc));
+            }
+            rn[q] = sqrtf(acc);
+        } else {
+            const int j = q - N;
+            for (int k = 0; k < N; ++k) {
+                const float4 b = B[lbw_at(k, j, N, sw)];
+                acc = fmaf(b.x, b.x, fmaf(b.y, b.y, acc));
+            }
+            cn[j] = sqrtf(acc);
+        }
+    }
+    __syncthreads();
+    // a task is row i and the columns jb, jb + W, jb + 2W, jb + 3W (W = N / 4
+    // rounded up): consecutive threads read consecutive columns of B
+    const int W = (N + 3) >> 2;
+    for (int task = tid; task < N * W; task += nt) {
+        const int i = task / W, jb = task - i * W;
+        u64 s1[4], s2[4], c1[4], c2[4], KK[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int j = jb + q * W < N ? jb + q * W : N - 1;
+            const float K = pow2_above(4.01f * rn[i] * cn[j]);
+            KK[q] = f32x2(K, K);
+            s1[q] = s2[q] = KK[q];
+            c1[q] = c2[q] = 0ull;
+        }
+        for (int k = 0; k < N; ++k) {
+            const float4 a = A[lbw_at(i, k, N, sw)];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = jb + q * W < N ? jb + q * W : N - 1;
+                lbw_step(s1[q], c1[q], s2[q], c2[q], a, B[lbw_at(k, j, N, sw)]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (jb + q * W < N)
+                C[lbw_at(i, jb + q * W, N, sw)] =
+                    lbw_finish(sub2(s1[q], KK[q]), c1[q], sub2(s2[q], KK[q]), c2[q]);
+    }
+    __syncthreads();
+}
+
+// y = E x with four lanes per output (lane p of an output takes k = p, p + 4,
+// ...); xb bounds ||x||_2.
+__device__ void lbw_matvec(float4 *y, const float4 *E, const float4 *x, int N, const float *rE,
+                           float xb, int sw) {
+    const int tid = threadIdx.x, nt = blockDim.x, part = tid & 3;
+    for (int i0 = 0; i0 < N; i0 += nt >> 2) {
+        const int i = i0 + (tid >> 2);
+        const bool active = i < N;
+        const int ii = active ? i : 0;
+        const float K = pow2_above(4.01f * rE[ii] * xb);
+        const u64 KK = f32x2(K, K);
+        u64 s1 = KK, s2 = KK, c1 = 0ull, c2 = 0ull;
+        if (active)
+            for (int k = part; k < N; k += 4)
+                lbw_step(s1, c1, s2, c2, E[lbw_at(ii, k, N, sw)], x[k]);
+        s1 = sub2(s1, KK);
+        s2 = sub2(s2, KK);
+#pragma unroll
+        for (int off = 1; off <= 2; off <<= 1) {
+            const u64 o1 = __shfl_xor_sync(0xffffffffu, s1, off);
+            const u64 o2 = __shfl_xor_sync(0xffffffffu, s2, off);
+            const u64 d1 = __shfl_xor_sync(0xffffffffu, c1, off);
+            const u64 d2 = __shfl_xor_sync(0xffffffffu, c2, off);
+            two_sum2(s1, o1, c1);
+            two_sum2(s2, o2, c2);
+            c1 = add2(c1, d1);
+            c2 = add2(c2, d2);
+        }
+        if (active && part == 0) y[i] = lbw_finish(s1, c1, s2, c2);
+    }
+    __syncthreads();
+}
+
+// exp(f L) by scaling, Horner Taylor-13 and squaring; returns X or T
+__device__ float4 *lbw_expm(const float4 *Ls, float4 *X, float4 *T, int N, double f,
+                            double lnorm, float *rn, float *cn, int sw) {
+    const int tid = threadIdx.x, nt = blockDim.x, NN = N * N;
+    double nrm = lnorm * fabs(f);
+    int sq = 0;
+    while (nrm > 0.5 && sq < 64) {
+        nrm *= 0.5;
+        ++sq;
+    }
+    const double g = ldexp(f, -sq);
+    // logical column of physical entry e: the swizzle is its own inverse
+    for (int e = tid; e < NN; e += nt) {
+        const int i = e / N, j = (e - i * N) ^ ((i & 1) * sw);
+        X[e] = make_float4(i == j ? 1.f : 0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    for (int k = 13; k >= 1; --k) {  // X <- I + (g / k) L X
+        lbw_gemm(T, Ls, X, N, rn, cn, sw);
+        const double c = g / (double)k;
+        const float ch = (float)c, cl = (float)(c - (double)ch);
+        for (int e = tid; e < NN; e += nt) {
+            const int i = e / N, j = (e - i * N) ^ ((i & 1) * sw);
+            float4 t = T[e];
+            lbw_mul(t.x, t.z, ch, cl);
+            lbw_mul(t.y, t.w, ch, cl);
+            if (i == j) lbw_add1(t.x, t.z);
+            X[e] = t;
+        }
+        __syncthreads();
+    }
+    float4 *P = X, *Q = T;
+    for (int q = 0; q < sq; ++q) {
+        lbw_gemm(Q, P, P, N, rn, cn, sw);
+        float4 *t = P;
+        P = Q;
+        Q = t;
+    }
+    return P;
+}
+
+__global__ void __launch_bounds__(MSP_LB_THREADS) msp_lindblad_dw_kernel(LbDwArgs a) {
+    extern __shared__ __align__(16) unsigned char lbw_smem[];
+    __shared__ double red[64];
+    const int n = a.n, N = n * n, NN = N * N, tid = threadIdx.x, nt = blockDim.x;
+    float4 *Ls = reinterpret_cast<float4 *>(lbw_smem);
+    float4 *X = Ls + NN, *T = X + NN, *x0 = T + NN, *x1 = x0 + N;
+    double2 *os = reinterpret_cast<double2 *>(x1 + N);
+    float *rn = reinterpret_cast<float *>(os + N), *cn = rn + N, *rE = cn + N;
+    const int sw = (N & 7) == 0 ? 4 : 0;
+    for (int s = blockIdx.x; s < a.num_snap; s += gridDim.x) {
+        const zd *Lg = a.L + (size_t)s * NN;
+        for (int e = tid; e < NN; e += nt) {
+            const int i = e / N, k = e - i * N;
+            Ls[lbw_at(i, k, N, sw)] = dw_split(make_double2(Lg[e].re, Lg[e].im));
+        }
+        for (int e = tid; e < N; e += nt) {
+            const zd v = a.v[(size_t)s * N + e], o = a.o[(size_t)s * N + e];
+            x0[e] = dw_split(make_double2(v.re, v.im));
+            os[e] = make_double2(o.re, o.im);
+        }
+        // ||L||_1 (largest column sum, FP64) and ||rho0||_2
+        double cmax = 0.0, v2 = 0.0;
+        for (int j = tid; j < N; j += nt) {
+            double c = 0.0;
+            for (int i = 0; i < N; ++i) c += sqrt(Lg[(size_t)i * N + j].re * Lg[(size_t)i * N + j].re +
+                                                  Lg[(size_t)i * N + j].im * Lg[(size_t)i * N + j].im);
+            cmax = fmax(cmax, c);
+            const zd v = a.v[(size_t)s * N + j];
+            v2 += v.re * v.re + v.im * v.im;
+        }
+        const double lnorm = lb_block_max(cmax, red);
+        const zd vs = lb_block_csum(mk<double>(v2, 0.0), red);
+        // a density matrix keeps ||vec(rho)||_2 = sqrt(Tr rho^2) <= 1
+        const float xb = (float)(fmax(1.0, sqrt(vs.re)) * 1.01);
+        float4 *cur = x0, *nxt = x1;
+        if (a.t0 != 0.0) {
+            float4 *E0 = lbw_expm(Ls, X, T, N, 2.0 * CUDART_PI * a.t0, lnorm, rn, cn, sw);
+            for (int i = tid; i < N; i += nt) {
+                float q = 0.f;
+                for (int k = 0; k < N; ++k) q = fmaf(E0[i * N + k].x, E0[i * N + k].x,
+                                                     fmaf(E0[i * N + k].y, E0[i * N + k].y, q));
+                rE[i] = sqrtf(q) * 1.0001f;
+            }
+            __syncthreads();
+            lbw_matvec(nxt, E0, cur, N, rE, xb, sw);
+            float4 *t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+        float4 *E = nullptr;
+        if (a.num_times > 1) {
+            E = lbw_expm(Ls, X, T, N, 2.0 * CUDART_PI * a.dt, lnorm, rn, cn, sw);
+            for (int i = tid; i < N; i += nt) {
+                float q = 0.f;
+                for (int k = 0; k < N; ++k) q = fmaf(E[i * N + k].x, E[i * N + k].x,
+                                                     fmaf(E[i * N + k].y, E[i * N + k].y, q));
+                rE[i] = sqrtf(q) * 1.0001f;
+            }
+            __syncthreads();
+        }
+        const double weight = a.wscale[s];
+        double *res = a.res + (size_t)s * a.num_times;
+        float4 *hist = a.hist + (size_t)blockIdx.x * LBW_CHUNK * N;
+        for (int k0 = 0; k0 < a.num_times; k0 += LBW_CHUNK) {
+            const int cnt = min(LBW_CHUNK, a.num_times - k0);
+            // states k0 .. k0 + cnt - 1, each recorded for the measurement below
+            for (int q = 0; q < cnt; ++q) {
+                if (k0 + q > 0) {
+                    lbw_matvec(nxt, E, cur, N, rE, xb, sw);
+                    float4 *t = cur;
+                    cur = nxt;
+                    nxt = t;
+                }
+                for (int e = tid; e < N; e += nt) hist[(size_t)q * N + e] = cur[e];
+            }
+            __syncthreads();
+            lbw_measure_chunk(hist, os, N, cnt, weight, res + k0);
+            __syncthreads();
+        }
+    }
+}
+
+static size_t lbw_smem_bytes(int n) {
+    const size_t N = (size_t)n * n;
+    return 3 * N * N * 16 + 2 * N * 16 + N * 16 + 3 * N * 4 + 64;
 }
 
 // out[slot][t] = sum of the slot's snapshot results, in snapshot order
@@ -647,18 +972,35 @@ static int check_lindblad(const msp_lindblad_args *a) {
         return lb_fail(MSP_ERR_ARG, "msp_lindblad: tau must be > 0");
     if (a->mode == MSP_MODE_EVOLVE && (a->num_times < 1 || (!a->uniform && a->times == NULL)))
         return lb_fail(MSP_ERR_ARG, "msp_lindblad: times");
+    if (a->precision != MSP_PREC_FP64 && a->precision != MSP_PREC_MIXED)
+        return lb_fail(MSP_ERR_ARG, "msp_lindblad: precision");
     return MSP_OK;
 }
 
+// Upper bound of the double-word kernel's grid (SMs x 2): sizes the
+// per-CTA history buffers.
+static int lbw_grid_max() {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    return 2 * sms;
+}
+
 struct LbLayout {
-    size_t res, slot_first, item_first, scratch, total;
+    size_t res, slot_first, item_first, scratch, Lb, vb, ob, hb, total;
     int T, grid;
+    bool dw;  // double-word propagation (mixed, evolve, uniform grid, n^2 <= 64)
 };
 
 static LbLayout lb_layout(const msp_lindblad_args *a) {
     LbLayout L;
     L.T = a->mode == MSP_MODE_INTEGRAL ? 1 : a->num_times;
     L.grid = lb_grid(a->num_snap);
+    L.dw = a->precision == MSP_PREC_MIXED && a->mode == MSP_MODE_EVOLVE && a->uniform &&
+           a->n * a->n <= LBW_MAXN;
     size_t off = 0;
     auto take = [&](size_t b) {
         const size_t o = off;
@@ -669,6 +1011,14 @@ static LbLayout lb_layout(const msp_lindblad_args *a) {
     L.slot_first = take((size_t)(a->num_slots + 1) * 4);
     L.item_first = take((size_t)(a->num_slots + 1) * 4);
     L.scratch = take(lb_entries(a->n, 1) * sizeof(zd) * L.grid);
+    L.Lb = L.vb = L.ob = L.hb = 0;
+    if (L.dw) {
+        const size_t N = (size_t)a->n * a->n;
+        L.Lb = take((size_t)a->num_snap * N * N * sizeof(zd));
+        L.vb = take((size_t)a->num_snap * N * sizeof(zd));
+        L.ob = take((size_t)a->num_snap * N * sizeof(zd));
+        L.hb = take((size_t)lbw_grid_max() * LBW_CHUNK * N * 16);
+    }
     L.total = off;
     return L;
 }
@@ -728,7 +1078,49 @@ int msp_lindblad_run(const msp_lindblad_args *a) {
     la.res = reinterpret_cast<double *>(ws + Lo.res);
     la.scratch = reinterpret_cast<zd *>(ws + Lo.scratch);
     la.scratch_entries = lb_entries(a->n, 1);
-    if (a->num_snap > 0) {
+    if (a->num_snap > 0 && Lo.dw) {
+        la.build_only = 1;
+        la.Lout = reinterpret_cast<zd *>(ws + Lo.Lb);
+        la.vout = reinterpret_cast<zd *>(ws + Lo.vb);
+        la.oout = reinterpret_cast<zd *>(ws + Lo.ob);
+        msp_lindblad_kernel<<<Lo.grid, MSP_LB_THREADS, 0, st>>>(la);
+        rc = lb_cuda(cudaGetLastError());
+        if (rc != MSP_OK) return rc;
+        LbDwArgs da;
+        da.L = la.Lout;
+        da.v = la.vout;
+        da.o = la.oout;
+        da.n = a->n;
+        da.num_snap = a->num_snap;
+        da.num_times = Lo.T;
+        da.t0 = a->t0;
+        da.dt = a->dt;
+        da.wscale = a->wscale;
+        da.res = la.res;
+        da.hist = reinterpret_cast<float4 *>(ws + Lo.hb);
+        const size_t smem = lbw_smem_bytes(a->n);
+        rc = lb_cuda(cudaFuncSetAttribute(msp_lindblad_dw_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (rc != MSP_OK) return rc;
+        int occ = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, msp_lindblad_dw_kernel,
+                                                          MSP_LB_THREADS, smem) != cudaSuccess ||
+            occ < 1) {
+            cudaGetLastError();
+            occ = 1;
+        }
+        int dev = 0, sms = 152;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            sms = 152;
+        }
+        const int grid = (int)std::min<long long>(
+            a->num_snap, std::min<long long>((long long)sms * occ, lbw_grid_max()));
+        msp_lindblad_dw_kernel<<<grid, MSP_LB_THREADS, smem, st>>>(da);
+        rc = lb_cuda(cudaGetLastError());
+        if (rc != MSP_OK) return rc;
+    } else if (a->num_snap > 0) {
         msp_lindblad_kernel<<<Lo.grid, MSP_LB_THREADS, 0, st>>>(la);
         rc = lb_cuda(cudaGetLastError());
         if (rc != MSP_OK) return rc;

@@ -301,9 +301,11 @@ class ExperimentRunner:
         return B, intr, mupol, T, qs, ws, rows, nrows, res_dims, t_axis
 
     def _run_lindblad(self, B_lab, p_lab, T, wscale, rows, nrows, times):
-        """Dissipative snapshots on the GPU (msp_lindblad_run, FP64 in both
-        precisions): every snapshot's Lindbladian is built and propagated on
-        the device, results reduced into the output rows."""
+        """Dissipative snapshots on the GPU (msp_lindblad_run): every
+        snapshot's Lindbladian is built and propagated on the device, results
+        reduced into the output rows; the 'mixed' precision propagates in
+        double-word FP32 where that form applies (uniform time grid,
+        n^2 <= 64), FP64 otherwise."""
         from muspinsim_gb300 import _lib
         from muspinsim_gb300.powder import _rows_sorted
 
@@ -317,7 +319,8 @@ class ExperimentRunner:
             n, sy.hamiltonian_matrix(), sy.zeeman_operators(), S_ops, list(sy.dimension),
             sy.muon_index, sy.gammas, self._config.dissipation_terms, B_lab[order], p_lab[order],
             np.asarray(wscale)[order], np.asarray(rows)[order].astype(np.int32), nrows, times,
-            temperature=np.asarray(T, dtype=float)[order], mode=mode, tau=MU_TAU)
+            temperature=np.asarray(T, dtype=float)[order], mode=mode, tau=MU_TAU,
+            precision=_lib.PREC_MIXED if self.precision == "mixed" else _lib.PREC_FP64)
         status = np.zeros(len(order), dtype=np.int32)
         status[order] = st.cpu().numpy()
         return out, status

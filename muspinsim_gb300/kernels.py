@@ -544,11 +544,14 @@ def superop_integrate(L, n, rho0, ops, tau):
 
 
 def lindblad_run(n, Hsys, Z, spin_ops, dims, mu_index, gammas, dissipation, field, pol, wscale,
-                 slot, num_slots, times, temperature=None, mode=_lib.MODE_EVOLVE, tau=1.0):
+                 slot, num_slots, times, temperature=None, mode=_lib.MODE_EVOLVE, tau=1.0,
+                 precision=_lib.PREC_FP64):
     """A batch of dissipative snapshots reduced into output rows
     (msp_lindblad_run).  ``dissipation``: {spin index: rate}; ``spin_ops``:
-    (num_spins, 3, n, n).  Returns (out, status): out (num_slots, T) or
-    (num_slots,) for MODE_INTEGRAL."""
+    (num_spins, 3, n, n).  ``precision`` PREC_MIXED propagates in
+    double-word FP32 where it applies (evolution on a uniform grid,
+    n^2 <= 64).  Returns (out, status): out (num_slots, T) or (num_slots,)
+    for MODE_INTEGRAL."""
     d = device()
     a = _lib.LindbladArgs()
     a.n, a.num_spins, a.mu_index = int(n), len(dims), int(mu_index)
@@ -585,6 +588,7 @@ def lindblad_run(n, Hsys, Z, spin_ops, dims, mu_index, gammas, dissipation, fiel
         a.times, a.num_times, a.uniform, a.t0, a.dt = Td.data_ptr(), int(th.size), int(uni), t0, dt
         shape = (int(num_slots), int(th.size))
     a.tau, a.mode = float(tau), int(mode)
+    a.precision = int(precision)
     out = torch.empty(shape, dtype=torch.float64, device=d)
     status = torch.zeros((max(S, 1),), dtype=torch.int32, device=d)
     a.out, a.status = out.data_ptr(), status.data_ptr()

@@ -140,3 +140,41 @@ def test_lindblad_powder_vs_oracle_three_spins():
     res = _runner(g).run()
     ref = golden_oracle(g)
     assert np.abs(res - ref).max() <= TOL
+
+
+MIXED_TOL = 1e-9  # double-word FP32 propagation
+
+
+@pytest.mark.parametrize("name", ["lindblad_mu_e"])
+def test_mixed_precision_golden(name):
+    """The double-word propagation against the reference's golden run."""
+    g = load_golden(name)
+    er = _runner(g)
+    er.precision = "mixed"
+    res = er.run()
+    assert np.abs(res - g["result"]).max() <= MIXED_TOL
+
+
+def test_mixed_precision_three_spins_against_fp64():
+    """mu, e, 1H (L 64 x 64, the largest double-word size) with two
+    dissipative spins at finite temperature and a start time t0 > 0: the
+    double-word propagation against the FP64 one."""
+    from muspinsim_gb300 import workloads
+
+    rng = np.random.default_rng(31)
+    coup = [("hyperfine", {"i": 1}, workloads.random_hyperfine(rng, 30.0)),
+            ("hyperfine", {"i": 3}, workloads.random_hyperfine(rng, 5.0))]
+    orients = [(0.3, 0.5, 0.1, 1.0), (1.1, 2.0, 0.7, 0.5), (2.0, 0.2, 1.9, 2.0)]
+    g = {"spins": ["mu", "e", "H"], "couplings": coup, "times": np.linspace(0.2, 4.0, 300),
+         "orientations": np.array(orients), "fields": np.array([[0.001, 0.0, 0.003]]),
+         "intrinsic": np.zeros((1, 3)), "polarization": np.array([0.0, 0.0, 1.0]),
+         "temperatures": np.array([15.0]), "y_axis": "asymmetry", "x_axis": "time",
+         "average_axes": ["orientation"], "dissipation": {"2": 4.0, "3": 0.5}}
+    out = {}
+    for prec in ("fp64", "mixed"):
+        er = _runner(g)
+        er.precision = prec
+        out[prec] = er.run()
+    assert np.abs(out["mixed"] - out["fp64"]).max() <= MIXED_TOL
+    ref = golden_oracle(g)
+    assert np.abs(out["fp64"] - ref).max() <= TOL
