@@ -567,7 +567,8 @@ __global__ void __launch_bounds__(MSP_LB_THREADS) msp_lindblad_kernel(LbArgs a) 
 // kernel above stays the reference form.
 constexpr int LBW_MAXN = 64;
 
-constexpr int LBW_CHUNK = 128;  // time steps recorded before they are measured
+constexpr int LBW_THREADS = 256;  // one CTA per SM (shared memory); 512 measured slower
+constexpr int LBW_CHUNK = 256;    // time steps recorded before they are measured
 
 struct LbDwArgs {
     const zd *L, *v, *o;  // per snapshot: N x N, N, N (from the build-only pass)
@@ -584,7 +585,8 @@ __device__ void lbw_measure_chunk(const float4 *hist, const double2 *os, int N, 
                                   double weight, double *res) {
     const int tid = threadIdx.x, half = tid & 1, j = tid >> 1;
     const int h = (N + 1) >> 1, e0 = half * h, e1 = min(N, e0 + h);
-    for (int jj = j; jj < ((cnt + 127) & ~127); jj += blockDim.x >> 1) {
+    const int per = blockDim.x >> 1;  // states per pass; every thread runs every pass
+    for (int jj = j; jj < (cnt + per - 1) / per * per; jj += per) {
         double acc = 0.0;
         if (jj < cnt)
             for (int e = e0; e < e1; ++e) {
@@ -704,25 +706,30 @@ __device__ void lbw_gemm(float4 *C, const float4 *A, const float4 *B, int N, flo
     __syncthreads();
 }
 
-// y = E x with four lanes per output (lane p of an output takes k = p, p + 4,
-// ...); xb bounds ||x||_2.
+// y = E x with P lanes per output (P the largest power of two <= 32 with
+// N P <= threads; lane p of an output takes k = p, p + P, ...); xb bounds
+// ||x||_2.
 __device__ void lbw_matvec(float4 *y, const float4 *E, const float4 *x, int N, const float *rE,
                            float xb, int sw) {
-    const int tid = threadIdx.x, nt = blockDim.x, part = tid & 3;
-    for (int i0 = 0; i0 < N; i0 += nt >> 2) {
-        const int i = i0 + (tid >> 2);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    int P = 1;
+    while (P < 32 && N * P * 2 <= nt) P *= 2;
+    const int part = tid & (P - 1);
+    for (int i0 = 0; i0 < N; i0 += nt / P) {
+        const int i = i0 + tid / P;
         const bool active = i < N;
         const int ii = active ? i : 0;
         const float K = pow2_above(4.01f * rE[ii] * xb);
         const u64 KK = f32x2(K, K);
         u64 s1 = KK, s2 = KK, c1 = 0ull, c2 = 0ull;
-        if (active)
-            for (int k = part; k < N; k += 4)
+        if (active) {
+#pragma unroll 4
+            for (int k = part; k < N; k += P)
                 lbw_step(s1, c1, s2, c2, E[lbw_at(ii, k, N, sw)], x[k]);
+        }
         s1 = sub2(s1, KK);
         s2 = sub2(s2, KK);
-#pragma unroll
-        for (int off = 1; off <= 2; off <<= 1) {
+        for (int off = 1; off < P; off <<= 1) {
             const u64 o1 = __shfl_xor_sync(0xffffffffu, s1, off);
             const u64 o2 = __shfl_xor_sync(0xffffffffu, s2, off);
             const u64 d1 = __shfl_xor_sync(0xffffffffu, c1, off);
@@ -733,6 +740,17 @@ __device__ void lbw_matvec(float4 *y, const float4 *E, const float4 *x, int N, c
             c2 = add2(c2, d2);
         }
         if (active && part == 0) y[i] = lbw_finish(s1, c1, s2, c2);
+    }
+    __syncthreads();
+}
+
+// row 2-norms of a matrix (any order inside a row), slightly rounded up
+__device__ void lbw_row_norms(const float4 *E, int N, float *r) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        float q = 0.f;
+        for (int k = 0; k < N; ++k)
+            q = fmaf(E[i * N + k].x, E[i * N + k].x, fmaf(E[i * N + k].y, E[i * N + k].y, q));
+        r[i] = sqrtf(q) * 1.0001f;
     }
     __syncthreads();
 }
@@ -778,7 +796,7 @@ __device__ float4 *lbw_expm(const float4 *Ls, float4 *X, float4 *T, int N, doubl
     return P;
 }
 
-__global__ void __launch_bounds__(MSP_LB_THREADS) msp_lindblad_dw_kernel(LbDwArgs a) {
+__global__ void __launch_bounds__(LBW_THREADS) msp_lindblad_dw_kernel(LbDwArgs a) {
     extern __shared__ __align__(16) unsigned char lbw_smem[];
     __shared__ double red[64];
     const int n = a.n, N = n * n, NN = N * N, tid = threadIdx.x, nt = blockDim.x;
@@ -812,50 +830,39 @@ __global__ void __launch_bounds__(MSP_LB_THREADS) msp_lindblad_dw_kernel(LbDwArg
         const zd vs = lb_block_csum(mk<double>(v2, 0.0), red);
         // a density matrix keeps ||vec(rho)||_2 = sqrt(Tr rho^2) <= 1
         const float xb = (float)(fmax(1.0, sqrt(vs.re)) * 1.01);
-        float4 *cur = x0, *nxt = x1;
+        float4 *cur = x0;
         if (a.t0 != 0.0) {
             float4 *E0 = lbw_expm(Ls, X, T, N, 2.0 * CUDART_PI * a.t0, lnorm, rn, cn, sw);
-            for (int i = tid; i < N; i += nt) {
-                float q = 0.f;
-                for (int k = 0; k < N; ++k) q = fmaf(E0[i * N + k].x, E0[i * N + k].x,
-                                                     fmaf(E0[i * N + k].y, E0[i * N + k].y, q));
-                rE[i] = sqrtf(q) * 1.0001f;
-            }
-            __syncthreads();
-            lbw_matvec(nxt, E0, cur, N, rE, xb, sw);
-            float4 *t = cur;
-            cur = nxt;
-            nxt = t;
-        }
-        float4 *E = nullptr;
-        if (a.num_times > 1) {
-            E = lbw_expm(Ls, X, T, N, 2.0 * CUDART_PI * a.dt, lnorm, rn, cn, sw);
-            for (int i = tid; i < N; i += nt) {
-                float q = 0.f;
-                for (int k = 0; k < N; ++k) q = fmaf(E[i * N + k].x, E[i * N + k].x,
-                                                     fmaf(E[i * N + k].y, E[i * N + k].y, q));
-                rE[i] = sqrtf(q) * 1.0001f;
-            }
-            __syncthreads();
+            lbw_row_norms(E0, N, rE);
+            lbw_matvec(x1, E0, cur, N, rE, xb, sw);
+            cur = x1;
         }
         const double weight = a.wscale[s];
         double *res = a.res + (size_t)s * a.num_times;
         float4 *hist = a.hist + (size_t)blockIdx.x * LBW_CHUNK * N;
-        for (int k0 = 0; k0 < a.num_times; k0 += LBW_CHUNK) {
-            const int cnt = min(LBW_CHUNK, a.num_times - k0);
-            // states k0 .. k0 + cnt - 1, each recorded for the measurement below
-            for (int q = 0; q < cnt; ++q) {
-                if (k0 + q > 0) {
+        // state 0
+        for (int e = tid; e < N; e += nt) hist[e] = cur[e];
+        __syncthreads();
+        lbw_measure_chunk(hist, os, N, 1, weight, res);
+        __syncthreads();
+        if (a.num_times > 1) {
+            float4 *E = lbw_expm(Ls, X, T, N, 2.0 * CUDART_PI * a.dt, lnorm, rn, cn, sw);
+            lbw_row_norms(E, N, rE);
+            float4 *nxt = cur == x0 ? x1 : x0;
+            for (int k0 = 1; k0 < a.num_times; k0 += LBW_CHUNK) {
+                const int cnt = min(LBW_CHUNK, a.num_times - k0);
+                for (int q = 0; q < cnt; ++q) {
                     lbw_matvec(nxt, E, cur, N, rE, xb, sw);
                     float4 *t = cur;
                     cur = nxt;
                     nxt = t;
+                    // cur is only read until the next matvec, which writes nxt
+                    for (int e = tid; e < N; e += nt) hist[(size_t)q * N + e] = cur[e];
                 }
-                for (int e = tid; e < N; e += nt) hist[(size_t)q * N + e] = cur[e];
+                __syncthreads();
+                lbw_measure_chunk(hist, os, N, cnt, weight, res + k0);
+                __syncthreads();
             }
-            __syncthreads();
-            lbw_measure_chunk(hist, os, N, cnt, weight, res + k0);
-            __syncthreads();
         }
     }
 }
@@ -1104,7 +1111,7 @@ int msp_lindblad_run(const msp_lindblad_args *a) {
         if (rc != MSP_OK) return rc;
         int occ = 1;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, msp_lindblad_dw_kernel,
-                                                          MSP_LB_THREADS, smem) != cudaSuccess ||
+                                                          LBW_THREADS, smem) != cudaSuccess ||
             occ < 1) {
             cudaGetLastError();
             occ = 1;
@@ -1117,7 +1124,7 @@ int msp_lindblad_run(const msp_lindblad_args *a) {
         }
         const int grid = (int)std::min<long long>(
             a->num_snap, std::min<long long>((long long)sms * occ, lbw_grid_max()));
-        msp_lindblad_dw_kernel<<<grid, MSP_LB_THREADS, smem, st>>>(da);
+        msp_lindblad_dw_kernel<<<grid, LBW_THREADS, smem, st>>>(da);
         rc = lb_cuda(cudaGetLastError());
         if (rc != MSP_OK) return rc;
     } else if (a->num_snap > 0) {
