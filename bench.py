@@ -693,23 +693,46 @@ def run_config5(args, world, rank, local):
 
     rng = np.random.default_rng(1005)
     data = 0.5 * np.cos(np.linspace(0, 3, wl.times.size)) + rng.normal(0, 0.01, wl.times.size)
-    fit = GradientFitter(model, th.Z, wl.orientations, wl.times, data, wl.polarization)
+    fits = {p: GradientFitter(model, th.Z, wl.orientations, wl.times, data, wl.polarization,
+                              precision=p) for p in ("mixed", "fp64")}
     ps = [torch.tensor(float(np.linalg.norm(r[k])), dtype=torch.float64, device=d,
                        requires_grad=True) for k in range(2)]
 
-    def step():
-        L, g = fit.loss_and_grad(ps)
-        return L
+    def step(prec="mixed"):
+        L, g = fits[prec].loss_and_grad(ps)
+        return L, g
 
     for _ in range(args.warmup):
         step()
+        step("fp64")
     ms = _wall_ms(step, args.steps)
-    line = _line("loss + gradient evaluations/s (adjoint), FP64", 1e3 / ms, "evaluations/s", ms,
-                 args, world, "F_mu_F_dim8_2000_orient_1000_t_fit",
+    ms64 = _wall_ms(lambda: step("fp64"), args.steps)
+    Lm, gm = step()
+    Ld, gd = step("fp64")
+    gm = np.array([float(g) for g in gm])
+    gd = np.array([float(g) for g in gd])
+    # central finite differences of the FP64 loss
+    fd = []
+    with torch.no_grad():
+        for k in range(2):
+            h = 1e-5 * float(ps[k])
+            lo = [p.detach().clone() for p in ps]
+            hi = [p.detach().clone() for p in ps]
+            lo[k] -= h
+            hi[k] += h
+            fd.append((float(fits["fp64"].loss(hi)) - float(fits["fp64"].loss(lo))) / (2 * h))
+    fd = np.array(fd)
+    line = _line("loss + gradient evaluations/s (mixed forward, FP64 adjoint)", 1e3 / ms,
+                 "evaluations/s", ms, args, world, "F_mu_F_dim8_2000_orient_1000_t_fit",
                  {"orientations": len(wl.orientations), "times": len(wl.times), "dim": 8,
                   "parameters": 2},
-                 dtype="f64", e2e={"value": 1e3 / ms, "unit": "evaluations/s", "ms_per_step": ms,
-                                   "note": "wall clock of torch autograd loss + backward"})
+                 dtype="f32 Jacobi + double-word refinement (forward), f64 (adjoint)",
+                 fp64={"value": 1e3 / ms64, "ms_per_step": ms64},
+                 loss_rel_diff_mixed_vs_fp64=float(abs(float(Lm) - float(Ld)) / abs(float(Ld))),
+                 grad_rel_diff_mixed_vs_fp64=float(np.abs(gm - gd).max() / np.abs(gd).max()),
+                 grad_rel_err_fp64_vs_central_fd=float(np.abs(gd - fd).max() / np.abs(fd).max()),
+                 e2e={"value": 1e3 / ms, "unit": "evaluations/s", "ms_per_step": ms,
+                      "note": "wall clock of torch autograd loss + backward"})
     if not args.no_cpu_baseline:
         from oracle import port
         from tests.helpers import oracle_system
