@@ -666,7 +666,8 @@ def run_config4(args, world, rank, local):
                  {"systems": n_sys, "orientations": n_or, "times": T,
                   "dims": [4, 8, 12, 24, 48, 96, 192], "scaled_from": "4096 systems x 256",
                   "graph": True},
-                 dtype="f32 (n <= 64 Jacobi, phase sum) / f64 (n > 64 Householder + QL)",
+                 dtype="f32 (Jacobi for n <= 64, Householder + QL for n > 64; double-word "
+                       "refinement; phase sum)",
                  fp64={"value": samples / (out["fp64"][0] * 1e-3), "ms_per_step": out["fp64"][0]},
                  max_abs_dP_mixed_vs_fp64=dP, buckets=buckets)
 

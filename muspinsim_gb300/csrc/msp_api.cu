@@ -353,7 +353,8 @@ static Layout powder_layout(const msp_powder_args *a) {
     off += align256((size_t)L.max_items * L.T * (L.phase_records ? 4 : 8));
     L.large = off;
     if (a->n > MSP_MAX_DIM)
-        off += align256(large_scratch_bytes(a->n, large_grid(a->num_snap, a->n)));
+        off += align256(large_scratch_bytes(a->n, large_grid(a->num_snap, a->n, a->precision),
+                                            a->precision));
     L.total = off;
     return L;
 }
@@ -437,7 +438,8 @@ int msp_powder_run(const msp_powder_args *a) {
     if (ev) cudaEventRecord(ev[0], st);
     if (large && a->num_snap > 0)
         rc = cuda_check(launch_large_fast(sa, reinterpret_cast<double *>(ws + L.large),
-                                          large_grid(a->num_snap, a->n), st),
+                                          large_grid(a->num_snap, a->n, a->precision), st, 0,
+                                          a->precision),
                         "msp_large_fast");
     else
         rc = cuda_check(launch_snapshots(sa, a->mode, a->precision, st), "msp_snap");

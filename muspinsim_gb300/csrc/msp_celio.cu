@@ -410,17 +410,8 @@ __device__ __forceinline__ void ce_group_dw(float4 *__restrict__ V, const DwU *_
             c1 = fma_f32x2(u.lR, xh[j], c1);
             c2 = fma_f32x2(u.lI, xh[j], c2);
         }
-        s1 = sub2(s1, KK);  // exact
-        s2 = sub2(s2, KK);
-        // y = S1 + i S2, then hi = s + c and lo = its rounding error
-        two_sum2(s1, times_i(s2), c1);
-        c1 = add2(c1, times_i(c2));
-        u64 hi = s1, lo = 0ull;
-        two_sum2(hi, c1, lo);
-        float hr, him, lr, lim;
-        split_f32x2(hi, hr, him);
-        split_f32x2(lo, lr, lim);
-        V[swz<I>(base + off[i], msk)] = make_float4(hr, him, lr, lim);
+        // sub2 with the anchor is exact
+        V[swz<I>(base + off[i], msk)] = dw_finish(sub2(s1, KK), c1, sub2(s2, KK), c2);
     }
 }
 

@@ -45,6 +45,20 @@ __device__ __forceinline__ u64 times_i(u64 v) {
     return f32x2(-b, a);
 }
 
+// y = S1 + i S2 from the two anchored sums (s already minus the anchor K,
+// c their compensations), then hi = s + c and lo = its rounding error;
+// returned as (re_hi, im_hi, re_lo, im_lo).
+__device__ __forceinline__ float4 dw_finish(u64 s1, u64 c1, u64 s2, u64 c2) {
+    two_sum2(s1, times_i(s2), c1);
+    c1 = add2(c1, times_i(c2));
+    u64 hi = s1, lo = 0ull;
+    two_sum2(hi, c1, lo);
+    float hr, him, lr, lim;
+    split_f32x2(hi, hr, him);
+    split_f32x2(lo, lr, lim);
+    return make_float4(hr, him, lr, lim);
+}
+
 // Smallest power of two above b >= 0 (2^-126 for b = 0).
 __device__ __forceinline__ float pow2_above(float b) {
     const unsigned e = (__float_as_uint(b) >> 23) & 0xffu;

@@ -150,16 +150,18 @@ cudaError_t launch_evolve_phases(const double *evals, const double *rho, int n,
 cudaError_t launch_integrate(const double *evals, const double *rho, const double *ops, int n,
                              int num_ops, double tau, double *out, cudaStream_t st);
 
-// n > 64 (msp_large.cu): FP64 Householder + QL eigensolver, one CTA per
-// matrix with `grid` CTAs, each owning large_scratch_bytes(n, 1) of scratch.
+// n > 64 (msp_large.cu): Householder + QL eigensolver, one CTA per matrix
+// with `grid` CTAs, each owning large_scratch_bytes(n, 1, precision) of
+// scratch.  The eigensolver API (launch_eigh_large) is FP64; the fast path
+// runs FP64 or MIXED (FP32 solve, double-word refinement).
 cudaError_t launch_eigh_large(const double *H, int n, int batch, double *evals, double *evecs,
                               int *status, double *scratch, int grid, cudaStream_t st);
 cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cudaStream_t st,
-                              int threads = 0);
+                              int threads = 0, int precision = MSP_PREC_FP64);
 int large_threads(int n);
-size_t large_scratch_bytes(int n, int grid);
-int large_ctas_per_sm(int n);
-int large_grid(int batch, int n);
+size_t large_scratch_bytes(int n, int grid, int precision = MSP_PREC_FP64);
+int large_ctas_per_sm(int n, int precision = MSP_PREC_FP64);
+int large_grid(int batch, int n, int precision = MSP_PREC_FP64);
 
 // Work decomposition of the phase sum (host side).  A work item sums at
 // most MSP_F32_ITEM_PAIRS pairs in FP32 (mixed precision): longer FP32

@@ -625,18 +625,6 @@ __device__ __forceinline__ int lbw_at(int i, int k, int N, int sw) {
     return i * N + (k ^ ((i & 1) * sw));
 }
 
-// y = S1 + i S2 from the two anchored sums (s already minus K), renormalised
-__device__ __forceinline__ float4 lbw_finish(u64 s1, u64 c1, u64 s2, u64 c2) {
-    two_sum2(s1, times_i(s2), c1);
-    c1 = add2(c1, times_i(c2));
-    u64 hi = s1, lo = 0ull;
-    two_sum2(hi, c1, lo);
-    float hr, him, lr, lim;
-    split_f32x2(hi, hr, him);
-    split_f32x2(lo, lr, lim);
-    return make_float4(hr, him, lr, lim);
-}
-
 __device__ __forceinline__ void lbw_step(u64 &s1, u64 &c1, u64 &s2, u64 &c2, float4 a, float4 b) {
     const u64 R = f32x2(a.x, a.x), I = f32x2(a.y, a.y), lR = f32x2(a.z, a.z),
               lI = f32x2(a.w, a.w);
@@ -701,7 +689,7 @@ __device__ void lbw_gemm(float4 *C, const float4 *A, const float4 *B, int N, flo
         for (int q = 0; q < 4; ++q)
             if (jb + q * W < N)
                 C[lbw_at(i, jb + q * W, N, sw)] =
-                    lbw_finish(sub2(s1[q], KK[q]), c1[q], sub2(s2[q], KK[q]), c2[q]);
+                    dw_finish(sub2(s1[q], KK[q]), c1[q], sub2(s2[q], KK[q]), c2[q]);
     }
     __syncthreads();
 }
@@ -739,7 +727,7 @@ __device__ void lbw_matvec(float4 *y, const float4 *E, const float4 *x, int N, c
             c1 = add2(c1, d1);
             c2 = add2(c2, d2);
         }
-        if (active && part == 0) y[i] = lbw_finish(s1, c1, s2, c2);
+        if (active && part == 0) y[i] = dw_finish(s1, c1, s2, c2);
     }
     __syncthreads();
 }

@@ -149,7 +149,7 @@ static int plan_layout(msp_multi_plan *p, const msp_multi_desc *d) {
         b.threads = t && t->snap_threads > 0 ? t->snap_threads
                                              : (b.large ? large_threads(n) : snap_default_threads(n));
         b.ctas_per_sm = t && t->ctas_per_sm > 0 ? t->ctas_per_sm
-                                                : (b.large ? large_ctas_per_sm(n) : 0);
+                                                : (b.large ? large_ctas_per_sm(n, d->precision) : 0);
         long long cap = max_pairs / (b.P > 0 ? b.P : 1);
         if (cap < 1) cap = 1;
         if (cap > b.num_snap) cap = b.num_snap > 0 ? b.num_snap : 1;
@@ -260,7 +260,7 @@ static int plan_layout(msp_multi_plan *p, const msp_multi_desc *d) {
             if (g > b.cap_snap) g = b.cap_snap;
             if (g < 1) g = 1;
             b.grid = g;
-            off += al256(large_scratch_bytes(b.n, g));
+            off += al256(large_scratch_bytes(b.n, g, p->precision));
         }
         b.bytes = off - start;
     }
@@ -386,7 +386,8 @@ static int plan_enqueue(msp_multi_plan *p, const msp_multi_io *io, cudaStream_t 
             if (cs > 0) {
                 if (b.large)
                     rc = mcuda(launch_large_fast(sa, reinterpret_cast<double *>(ws + b.off_large),
-                                                 std::min(b.grid, cs), b.stream, b.threads),
+                                                 std::min(b.grid, cs), b.stream, b.threads,
+                                                 p->precision),
                                "msp_multi_run: large-n snapshots");
                 else
                     rc = mcuda(launch_snapshots(sa, MSP_MODE_FAST, p->precision, b.stream,

@@ -327,6 +327,48 @@ def test_powder_fast_large_vs_oracle():
     assert np.abs(got - ref).max() <= MIXED_TOL
 
 
+def _ragged_large_workload(field, n_orient=3, n_times=200, seed=162):
+    """mu + 4 x 14N: dim 162 (a row count that is not a multiple of 4),
+    muon-nitrogen point dipoles and 14N EFGs.  The total spin is
+    half-integer, so at zero field every level is an exact Kramers doublet;
+    1e-5 T splits the doublets by ~1e-4 of the spectral width."""
+    from muspinsim_gb300 import workloads
+
+    rng = np.random.default_rng(seed)
+    coup = []
+    for i in range(2, 6):
+        coup.append(("dipolar", {"i": 1, "j": i}, workloads.random_vector(rng, 0.3, 0.5)))
+        coup.append(("quadrupolar", {"i": i}, workloads.random_efg(rng)))
+    return workloads.Workload(
+        name="mu_4N_dim162", spins=["mu", "N", "N", "N", "N"], couplings=coup,
+        orientations=workloads.zcw_gen(n_orient), fields=np.array([[0.0, 0.0, field]]),
+        polarization=np.array([1.0, 0.0, 0.0]), times=np.linspace(0, 10, n_times))
+
+
+@pytest.mark.parametrize("field", [0.0, 1e-5, 0.01])
+def test_powder_fast_large_mixed_degenerate_and_ragged(field):
+    """The n > 64 mixed solver (FP32 Householder + QL, double-word
+    refinement) on exact and near doublets at n = 162."""
+    wl = _ragged_large_workload(field)
+    assert int(np.prod(wl.system().dimension)) == 162
+    ref = oracle_powder(wl)
+    assert np.abs(_gpu_powder(wl) - ref).max() <= FP64_TOL
+    assert np.abs(_gpu_powder(wl, "mixed") - ref).max() <= MIXED_TOL
+
+
+def test_powder_fast_large_mixed_dim192():
+    """A 192-dimensional system of the heterogeneous batch (mu, e, 14N and
+    protons; hyperfine, dipoles, EFG) in both precisions."""
+    from muspinsim_gb300 import workloads
+
+    rng = np.random.default_rng(1004)
+    wl = workloads.random_system_workload(rng, 192, workloads.zcw_gen(3),
+                                          np.linspace(0.0, 20.0, 300))
+    ref = oracle_powder(wl)
+    assert np.abs(_gpu_powder(wl) - ref).max() <= FP64_TOL
+    assert np.abs(_gpu_powder(wl, "mixed") - ref).max() <= MIXED_TOL
+
+
 @pytest.mark.parametrize("n_times,t_end", [(4096, 20.0), (1500, 10.0), (9000, 30.0)])
 def test_phase_tensor_cores_match_simt_and_oracle(monkeypatch, n_times, t_end):
     """Mixed precision on a uniform grid: the tcgen05 (3xTF32) phase sum
