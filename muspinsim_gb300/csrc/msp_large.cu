@@ -82,10 +82,19 @@ __device__ __forceinline__ T block_sum(T v, T *red) {
     return t;
 }
 
-// Shared memory: v, p (n complex each), qc, qs (n doubles each), red.
-// (sized for T = double; the FP32 instance uses half of it)
+// Row parts of the column-parallel products: RW = min(threads, 64) rows
+// (or columns) at a time, the reduction index split into G = threads / RW
+// parts whose partial sums meet in shared memory.
+__host__ __device__ inline int large_parts(int threads) {
+    const int rw = threads < 64 ? threads : 64;
+    return threads / rw;
+}
+
+// Shared memory: v, p, part (n, n, G n complex), qc, qs, d, e (n reals
+// each), red.  (Sized for T = double; the FP32 instance uses half of it.)
 __host__ __device__ inline size_t large_smem_bytes(int n, int threads) {
-    return (size_t)n * 16 * 2 + (size_t)n * 8 * 4 + (size_t)(threads / 32) * 16 + 64;
+    return (size_t)n * 16 * (2 + large_parts(threads)) + (size_t)n * 8 * 4 +
+           (size_t)(threads / 32) * 16 + 64;
 }
 
 // 1 / sqrt(x) for x > 0 in FP64 by Newton's method on f(y) = 1/y^2 - x,
@@ -117,9 +126,11 @@ template <typename T>
 __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     const int nw = nt >> 5;
+    const int RW = nt < 64 ? nt : 64, G = nt / RW, pr = tid % RW, pg = tid / RW;
     cx<T> *v = reinterpret_cast<cx<T> *>(smem);
     cx<T> *p = v + n;
-    T *qc = reinterpret_cast<T *>(p + n);
+    cx<T> *part = p + n;  // G x n partial sums
+    T *qc = reinterpret_cast<T *>(part + (size_t)G * n);
     T *qs = qc + n;
     T *dsm = qs + n;  // diagonal and off-diagonal of the tridiagonal matrix
     T *esm = dsm + n;
@@ -153,21 +164,41 @@ __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
         }
         __syncthreads();
         if (!reflect) continue;
-        // p = tau * A22 v  (warp per row)
-        for (int i = warp; i < m; i += nw) {
-            const cx<T> *row = A + (size_t)(k + 1 + i) * n + (k + 1);
-            T pr = T(0), pi = T(0);
-            for (int j = lane; j < m; j += 32) {
-                const cx<T> a = row[j], x = v[j];
-                pr += a.re * x.re - a.im * x.im;
-                pi += a.re * x.im + a.im * x.re;
+        // p = tau * A22 v.  A22 is Hermitian, so p_i = sum_j conj(A22_ji) v_j
+        // reads rows of A22 coalesced over i: thread (pr, pg) takes rows
+        // i = pr, pr + RW, ... and the pg-th of G parts of the j range, two
+        // independent accumulators, partial sums into `part`.
+        if (pg < G) {
+            const int jb = (int)((long long)m * pg / G), je = (int)((long long)m * (pg + 1) / G);
+            for (int i = pr; i < m; i += RW) {
+                const cx<T> *col = A + (size_t)(k + 1) * n + (k + 1 + i);
+                T r0 = T(0), i0 = T(0), r1 = T(0), i1 = T(0);
+                int j = jb;
+#pragma unroll 4
+                for (; j + 1 < je; j += 2) {
+                    const cx<T> a0 = col[(size_t)j * n], a1 = col[(size_t)(j + 1) * n];
+                    const cx<T> x0 = v[j], x1 = v[j + 1];
+                    r0 += a0.re * x0.re + a0.im * x0.im;
+                    i0 += a0.re * x0.im - a0.im * x0.re;
+                    r1 += a1.re * x1.re + a1.im * x1.im;
+                    i1 += a1.re * x1.im - a1.im * x1.re;
+                }
+                if (j < je) {
+                    const cx<T> a0 = col[(size_t)j * n], x0 = v[j];
+                    r0 += a0.re * x0.re + a0.im * x0.im;
+                    i0 += a0.re * x0.im - a0.im * x0.re;
+                }
+                part[(size_t)pg * n + i] = mk<T>(r0 + r1, i0 + i1);
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                pr += __shfl_xor_sync(0xffffffffu, pr, o);
-                pi += __shfl_xor_sync(0xffffffffu, pi, o);
+        }
+        __syncthreads();
+        for (int i = tid; i < m; i += nt) {
+            T sr = T(0), si = T(0);
+            for (int g = 0; g < G; ++g) {
+                sr += part[(size_t)g * n + i].re;
+                si += part[(size_t)g * n + i].im;
             }
-            if (lane == 0) p[i] = cmul(tau, mk<T>(pr, pi));
+            p[i] = cmul(tau, mk<T>(sr, si));
         }
         __syncthreads();
         // alpha2 = -1/2 tau (p^H v); w = p + alpha2 v (in p)
@@ -182,13 +213,16 @@ __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
         const cx<T> a2 = cscale(-T(0.5), cmul(tau, mk<T>(hr, hi)));
         for (int i = tid; i < m; i += nt) p[i] = cadd(p[i], cmul(a2, v[i]));
         __syncthreads();
-        // A22 -= v w^H + w v^H
-        for (int e = tid; e < m * m; e += nt) {
-            const int i = e / m, j = e - i * m;  // FastDiv is exact only for m^3 < 2^20
-            const cx<T> vi = v[i], wi = p[i], vj = v[j], wj = p[j];
-            cx<T> &a = A[(size_t)(k + 1 + i) * n + (k + 1 + j)];
-            const cx<T> t1 = cmul(vi, conj(wj)), t2 = cmul(wi, conj(vj));
-            a = mk<T>(a.re - t1.re - t2.re, a.im - t1.im - t2.im);
+        // A22 -= v w^H + w v^H: warps over rows, lanes over columns
+        for (int i = warp; i < m; i += nw) {
+            const cx<T> vi = v[i], wi = p[i];
+            cx<T> *row = A + (size_t)(k + 1 + i) * n + (k + 1);
+#pragma unroll 4
+            for (int j = lane; j < m; j += 32) {
+                const cx<T> vj = v[j], wj = p[j], a = row[j];
+                const cx<T> t1 = cmul(vi, conj(wj)), t2 = cmul(wi, conj(vj));
+                row[j] = mk<T>(a.re - t1.re - t2.re, a.im - t1.im - t2.im);
+            }
         }
         // keep v for the back-transformation (column k below the subdiagonal)
         for (int i = 1 + tid; i < m; i += nt) A[(size_t)(k + 1 + i) * n + k] = v[i];
@@ -326,23 +360,54 @@ __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
     __syncthreads();
     for (int k = n - 2; k >= 0; --k) {
         const cx<T> tau = s.tau[k];
-        if (tau.re == T(0) && tau.im == T(0)) continue;
+        if (tau.re == T(0) && tau.im == T(0)) continue;  // the same in every thread
         const int m = n - k - 1;
-        for (int j = tid; j < n; j += nt) {
-            // s_j = v^H U[k+1.., j]; U[k+1.., j] -= tau v s_j
-            T sr = T(0), si = T(0);
-            for (int i = 0; i < m; ++i) {
-                const cx<T> vi = i == 0 ? mk<T>(T(1), T(0)) : A[(size_t)(k + 1 + i) * n + k];
-                const cx<T> u = s.U[(size_t)(k + 1 + i) * n + j];
-                sr += vi.re * u.re + vi.im * u.im;
-                si += vi.re * u.im - vi.im * u.re;
+        for (int i = tid; i < m; i += nt)
+            v[i] = i == 0 ? mk<T>(T(1), T(0)) : A[(size_t)(k + 1 + i) * n + k];
+        __syncthreads();
+        // s_j = v^H U[k+1.., j]: thread (pr, pg) takes columns j = pr, pr + RW,
+        // ... and the pg-th of G parts of the rows
+        if (pg < G) {
+            const int ib = (int)((long long)m * pg / G), ie = (int)((long long)m * (pg + 1) / G);
+            for (int j = pr; j < n; j += RW) {
+                const cx<T> *col = s.U + (size_t)(k + 1) * n + j;
+                T r0 = T(0), i0 = T(0), r1 = T(0), i1 = T(0);
+                int i = ib;
+#pragma unroll 4
+                for (; i + 1 < ie; i += 2) {
+                    const cx<T> u0 = col[(size_t)i * n], u1 = col[(size_t)(i + 1) * n];
+                    const cx<T> v0 = v[i], v1 = v[i + 1];
+                    r0 += v0.re * u0.re + v0.im * u0.im;
+                    i0 += v0.re * u0.im - v0.im * u0.re;
+                    r1 += v1.re * u1.re + v1.im * u1.im;
+                    i1 += v1.re * u1.im - v1.im * u1.re;
+                }
+                if (i < ie) {
+                    const cx<T> u0 = col[(size_t)i * n], v0 = v[i];
+                    r0 += v0.re * u0.re + v0.im * u0.im;
+                    i0 += v0.re * u0.im - v0.im * u0.re;
+                }
+                part[(size_t)pg * n + j] = mk<T>(r0 + r1, i0 + i1);
             }
-            const cx<T> ts = cmul(tau, mk<T>(sr, si));
-            for (int i = 0; i < m; ++i) {
-                const cx<T> vi = i == 0 ? mk<T>(T(1), T(0)) : A[(size_t)(k + 1 + i) * n + k];
-                cx<T> &u = s.U[(size_t)(k + 1 + i) * n + j];
-                const cx<T> t = cmul(vi, ts);
-                u = mk<T>(u.re - t.re, u.im - t.im);
+        }
+        __syncthreads();
+        for (int j = tid; j < n; j += nt) {
+            T sr = T(0), si = T(0);
+            for (int g = 0; g < G; ++g) {
+                sr += part[(size_t)g * n + j].re;
+                si += part[(size_t)g * n + j].im;
+            }
+            p[j] = cmul(tau, mk<T>(sr, si));  // tau s_j
+        }
+        __syncthreads();
+        // U[k+1.., j] -= v tau s_j: warps over rows, lanes over columns
+        for (int i = warp; i < m; i += nw) {
+            const cx<T> vi = v[i];
+            cx<T> *row = s.U + (size_t)(k + 1 + i) * n;
+#pragma unroll 4
+            for (int j = lane; j < n; j += 32) {
+                const cx<T> t = cmul(vi, p[j]), u = row[j];
+                row[j] = mk<T>(u.re - t.re, u.im - t.im);
             }
         }
         __syncthreads();
@@ -534,13 +599,24 @@ __host__ __device__ inline size_t lm_layout(int n, LargeMixed *s, char *base) {
 
 __host__ __device__ inline size_t lm_scratch_bytes(int n) { return lm_layout(n, nullptr, nullptr); }
 
-// Refinement vectors in shared memory (the solver's shared memory is free
-// once it returns): 48 n + 16 bytes <= large_smem_bytes(n, threads).
+// Refinement vectors and GEMM slabs in shared memory (the solver's shared
+// memory is free once it returns).
+constexpr int LM_KT = 16;  // k depth of a GEMM slab
+
 struct LmVec {
     double *lam, *sd, *rd;
     float *lamf, *corr, *ed, *rn, *cn, *yn;
     int *step;
+    float4 *As, *Bs;  // GEMM slabs: A tile (TR x (LM_KT + 1)), B tile (LM_KT x 32)
 };
+
+__host__ __device__ inline size_t lm_smem_bytes(int n, int threads) {
+    const size_t vec = (48 * (size_t)n + 16 + 15) & ~size_t(15);
+    const size_t tr = 4 * (size_t)(threads / 32);
+    const size_t slabs = (tr * (LM_KT + 1) + LM_KT * 32) * 16;
+    const size_t need = vec + slabs, solver = large_smem_bytes(n, threads);
+    return need > solver ? need : solver;
+}
 
 __device__ __forceinline__ LmVec lm_vec(char *smem, int n) {
     LmVec v;
@@ -554,25 +630,201 @@ __device__ __forceinline__ LmVec lm_vec(char *smem, int n) {
     v.cn = v.rn + n;
     v.yn = v.cn + n;
     v.step = reinterpret_cast<int *>(v.yn + n);
+    const size_t vec = (48 * (size_t)n + 16 + 15) & ~size_t(15);
+    v.As = reinterpret_cast<float4 *>(smem + vec);
+    v.Bs = v.As + 4 * (blockDim.x >> 5) * (LM_KT + 1);
     return v;
-}
-
-// Anchored double-word accumulation of m * x into (s1 + i s2, c1 + i c2)
-// for a real multiplier pair: s1 += mR x, s2 += mI x with x = (re, im) on
-// the two lanes; the products' and sums' rounding errors go into c1, c2.
-__device__ __forceinline__ void lm_acc(u64 &s1, u64 &c1, u64 &s2, u64 &c2, u64 mR, u64 mI,
-                                       u64 x) {
-    const u64 t1 = fma_f32x2(mR, x, s1);
-    const u64 t2 = fma_f32x2(mI, x, s2);
-    c1 = add2(c1, fma_f32x2(mR, x, sub2(s1, t1)));
-    c2 = add2(c2, fma_f32x2(mI, x, sub2(s2, t2)));
-    s1 = t1;
-    s2 = t2;
 }
 
 __device__ __forceinline__ u64 lm_anchor(float bound) {
     const float K = pow2_above(4.01f * bound);
     return f32x2(K, K);
+}
+
+// Anchored double-word product-sum step: (s1 + i s2) += a * b for a complex
+// a = (a.x, a.y) (+ lo (a.z, a.w) when ALO) and b = (b.x, b.y) (+ lo (b.z,
+// b.w) when BLO); s1 = sum Re(a) b and s2 = sum Im(a) b on the two lanes
+// (the product is s1 + i s2), rounding errors into c1, c2.
+template <bool ALO, bool BLO>
+__device__ __forceinline__ void lm_step(u64 &s1, u64 &c1, u64 &s2, u64 &c2, float4 a, float4 b) {
+    const u64 R = f32x2(a.x, a.x), I = f32x2(a.y, a.y), bh = f32x2(b.x, b.y);
+    const u64 t1 = fma_f32x2(R, bh, s1);
+    const u64 t2 = fma_f32x2(I, bh, s2);
+    c1 = add2(c1, fma_f32x2(R, bh, sub2(s1, t1)));
+    c2 = add2(c2, fma_f32x2(I, bh, sub2(s2, t2)));
+    s1 = t1;
+    s2 = t2;
+    if (BLO) {
+        const u64 bl = f32x2(b.z, b.w);
+        c1 = fma_f32x2(R, bl, c1);
+        c2 = fma_f32x2(I, bl, c2);
+    }
+    if (ALO) {
+        c1 = fma_f32x2(f32x2(a.z, a.z), bh, c1);
+        c2 = fma_f32x2(f32x2(a.w, a.w), bh, c2);
+    }
+}
+
+// The three products of a refinement step, as one tiled kernel body: the
+// CTA walks output tiles of TR = 4 x warps rows by 32 columns; a thread
+// owns rows 4 w .. 4 w + 3 (w its warp) of column lane; A and B are staged
+// in shared memory LM_KT deep (A as [row][k] with a padded stride, so
+// that both fill orders are free of bank conflicts and the compute reads
+// are warp broadcasts; B as [k][column]).
+//   LM_HX: Y = H X            (H double-word, X FP32; anchored double-word)
+//   LM_SG: [S | G] = X^H [Y | X], tiles with no entry on or above the
+//          diagonal skipped; S_ij (i < j) -> SR[i][j], R_ij = -G_ij ->
+//          SR[j][i], S_ii -> sd, R_ii = 1 - G_ii -> rd
+//   LM_XE: X2 = X + X E       (FP32; E in SR, its diagonal included)
+enum { LM_HX = 0, LM_SG = 1, LM_XE = 2 };
+
+template <int MODE>
+__device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
+                        cx<float> *__restrict__ X2, const LmVec &v, int n) {
+    const int tid = threadIdx.x, nt = blockDim.x, w = tid >> 5, lane = tid & 31;
+    const int TR = 4 * (nt >> 5), AS = LM_KT + 1;
+    const int ncols = MODE == LM_SG ? 2 * n : n;
+    const int ti = (n + TR - 1) / TR, tj = (ncols + 31) >> 5;
+    float4 *__restrict__ As = v.As;
+    float4 *__restrict__ Bs = v.Bs;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int t = 0; t < ti * tj; ++t) {  // the same sequence in every thread
+        const int it = t / tj, i0 = it * TR, j0 = (t - it * tj) * 32;
+        if (MODE == LM_SG) {
+            const int jmax = j0 >= n ? min(j0 + 31, 2 * n - 1) - n : min(j0 + 31, n - 1);
+            if (jmax < i0) continue;  // no entry i <= j in this tile
+        }
+        const int j = j0 + lane;
+        // anchor of output (i0 + 4 w + q, j) (recomputed at the end rather
+        // than held in registers through the k loop)
+        auto anchor = [&](int q) -> u64 {
+            const int i = min(i0 + 4 * w + q, n - 1);
+            if (MODE == LM_HX) return lm_anchor(v.rn[i] * v.cn[min(j, n - 1)]);
+            return lm_anchor(v.cn[i] * (j < n ? v.yn[j] : v.cn[min(j - n, n - 1)]));
+        };
+        u64 s1[4], c1[4], s2[4], c2[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (MODE == LM_XE) {
+                const cx<float> x = j < n ? X[(size_t)(i0 + 4 * w + q < n ? i0 + 4 * w + q : 0) * n + j]
+                                          : mk<float>(0.f, 0.f);
+                s1[q] = f32x2(x.re, x.im);  // plain FP32 accumulator (re, im)
+                s2[q] = c1[q] = c2[q] = 0ull;
+            } else {
+                s1[q] = s2[q] = anchor(q);
+                c1[q] = c2[q] = 0ull;
+            }
+        }
+        for (int k0 = 0; k0 < n; k0 += LM_KT) {
+            // A tile: TR rows x LM_KT
+            for (int e = tid; e < TR * LM_KT; e += nt) {
+                int i, k;
+                if (MODE == LM_SG) {  // A(i, k) = conj(X[k][i]): contiguous in i
+                    i = e % TR;
+                    k = e / TR;
+                } else {  // A(i, k) = H[i][k] or X[i][k]: contiguous in k
+                    i = e / LM_KT;
+                    k = e % LM_KT;
+                }
+                const int gi = i0 + i, gk = k0 + k;
+                float4 a = zero4;
+                if (gi < n && gk < n) {
+                    if (MODE == LM_HX) {
+                        a = s.H[(size_t)gi * n + gk];
+                    } else if (MODE == LM_SG) {
+                        const cx<float> x = X[(size_t)gk * n + gi];
+                        a = make_float4(x.re, -x.im, 0.f, 0.f);
+                    } else {
+                        const cx<float> x = X[(size_t)gi * n + gk];
+                        a = make_float4(x.re, x.im, 0.f, 0.f);
+                    }
+                }
+                As[i * AS + k] = a;
+            }
+            // B tile: LM_KT x 32, contiguous in the column
+            for (int e = tid; e < LM_KT * 32; e += nt) {
+                const int k = e >> 5, jj = e & 31, gk = k0 + k, gj = j0 + jj;
+                float4 b = zero4;
+                if (gk < n && gj < ncols) {
+                    if (MODE == LM_HX) {
+                        const cx<float> x = X[(size_t)gk * n + gj];
+                        b = make_float4(x.re, x.im, 0.f, 0.f);
+                    } else if (MODE == LM_SG) {
+                        if (gj < n) {
+                            b = s.Y[(size_t)gk * n + gj];
+                        } else {
+                            const cx<float> x = X[(size_t)gk * n + gj - n];
+                            b = make_float4(x.re, x.im, 0.f, 0.f);
+                        }
+                    } else {
+                        const cx<float> E = s.SR[(size_t)gk * n + gj];
+                        b = make_float4(E.re, E.im, 0.f, 0.f);
+                    }
+                }
+                Bs[k * 32 + jj] = b;
+            }
+            __syncthreads();
+#pragma unroll 4
+            for (int k = 0; k < LM_KT; ++k) {
+                const float4 b = Bs[k * 32 + lane];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 a = As[(4 * w + q) * AS + k];
+                    if (MODE == LM_HX) {
+                        lm_step<true, false>(s1[q], c1[q], s2[q], c2[q], a, b);
+                    } else if (MODE == LM_SG) {
+                        lm_step<false, true>(s1[q], c1[q], s2[q], c2[q], a, b);
+                    } else {
+                        // (re, im) += (a.re, a.re) (b.re, b.im) + (a.im, a.im) (-b.im, b.re)
+                        s1[q] = fma_f32x2(f32x2(a.x, a.x), f32x2(b.x, b.y), s1[q]);
+                        s1[q] = fma_f32x2(f32x2(a.y, a.y), f32x2(-b.y, b.x), s1[q]);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = i0 + 4 * w + q;
+            if (i >= n || j >= ncols) continue;
+            if (MODE == LM_XE) {
+                float re, im;
+                split_f32x2(s1[q], re, im);
+                X2[(size_t)i * n + j] = mk<float>(re, im);
+                continue;
+            }
+            const u64 K = anchor(q);
+            const float4 r = dw_finish(sub2(s1[q], K), c1[q], sub2(s2[q], K), c2[q]);
+            if (MODE == LM_HX) {
+                s.Y[(size_t)i * n + j] = r;
+            } else if (j < n) {  // S
+                if (i == j)
+                    v.sd[i] = (double)r.x + (double)r.z;
+                else if (i < j)
+                    s.SR[(size_t)i * n + j] = mk<float>(r.x + r.z, r.y + r.w);
+            } else {  // G
+                const int jg = j - n;
+                if (i == jg)
+                    v.rd[i] = (1.0 - (double)r.x) - (double)r.z;
+                else if (i < jg)
+                    s.SR[(size_t)jg * n + i] = mk<float>(-(r.x + r.z), -(r.y + r.w));
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Column 2-norms of an n x n matrix of (re, im) pairs with element stride
+// `stride` floats (X: 2, the hi part of Y: 4).
+__device__ __forceinline__ void lm_colnorms(const float *M, int stride, int n, float *out) {
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        float acc = 0.f;
+        for (int k = 0; k < n; ++k) {
+            const float *e = M + ((size_t)k * n + j) * stride;
+            acc = fmaf(e[0], e[0], fmaf(e[1], e[1], acc));
+        }
+        out[j] = sqrtf(acc);
+    }
 }
 
 // One refinement step of the eigenvector columns X into X2 and of the
@@ -581,111 +833,14 @@ __device__ __forceinline__ u64 lm_anchor(float bound) {
 __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
                            cx<float> *__restrict__ X2, const LmVec &v, int n) {
     const int tid = threadIdx.x, nt = blockDim.x;
-    float4 *__restrict__ Y = s.Y;
     cx<float> *__restrict__ SR = s.SR;
-    for (int j = tid; j < n; j += nt) {
-        float acc = 0.f;
-        for (int k = 0; k < n; ++k) {
-            const cx<float> x = X[(size_t)k * n + j];
-            acc = fmaf(x.re, x.re, fmaf(x.im, x.im, acc));
-        }
-        v.cn[j] = sqrtf(acc);
-    }
+    lm_colnorms(reinterpret_cast<const float *>(X), 2, n, v.cn);
     if (tid == 0) *v.step = 0;
     __syncthreads();
-    // Y = H X: a task is rows i0 .. i0 + 3 and column j (lanes take
-    // consecutive j: H entries are broadcast, X rows coalesced)
-    const int nb4 = (n + 3) >> 2;
-    for (int task = tid; task < nb4 * n; task += nt) {
-        const int ib = task / n, j = task - ib * n, i0 = 4 * ib;
-        int row[4];
-        u64 s1[4], c1[4], s2[4], c2[4], KK[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            row[q] = min(i0 + q, n - 1);
-            KK[q] = lm_anchor(v.rn[row[q]] * v.cn[j]);
-            s1[q] = s2[q] = KK[q];
-            c1[q] = c2[q] = 0ull;
-        }
-#pragma unroll 1
-        for (int k = 0; k < n; ++k) {
-            const cx<float> x = X[(size_t)k * n + j];
-            const u64 xh = f32x2(x.re, x.im);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float4 h = s.H[(size_t)row[q] * n + k];
-                lm_acc(s1[q], c1[q], s2[q], c2[q], f32x2(h.x, h.x), f32x2(h.y, h.y), xh);
-                c1[q] = fma_f32x2(f32x2(h.z, h.z), xh, c1[q]);  // lo part of H
-                c2[q] = fma_f32x2(f32x2(h.w, h.w), xh, c2[q]);
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (i0 + q < n)
-                Y[(size_t)(i0 + q) * n + j] =
-                    dw_finish(sub2(s1[q], KK[q]), c1[q], sub2(s2[q], KK[q]), c2[q]);
-    }
+    lm_gemm<LM_HX>(s, X, X2, v, n);
+    lm_colnorms(reinterpret_cast<const float *>(s.Y), 4, n, v.yn);
     __syncthreads();
-    for (int j = tid; j < n; j += nt) {
-        float acc = 0.f;
-        for (int k = 0; k < n; ++k) {
-            const float4 y = Y[(size_t)k * n + j];
-            acc = fmaf(y.x, y.x, fmaf(y.y, y.y, acc));
-        }
-        v.yn[j] = sqrtf(acc);
-    }
-    __syncthreads();
-    // S_ij = X_i^H Y_j and G_ij = X_i^H X_j for i <= j: a task is rows
-    // i0, i0 + 1 and column j >= i0.  S_ij (i < j) goes to SR[i][j], R_ij =
-    // -G_ij to SR[j][i]; S_ii and R_ii = 1 - G_ii to v.sd, v.rd.
-    const int nb2 = (n + 1) >> 1;
-    for (int task = tid; task < nb2 * n; task += nt) {
-        const int ib = task / n, j = task - ib * n, i0 = 2 * ib;
-        if (j < i0) continue;
-        int col[2];
-        u64 a1[2], ac1[2], a2[2], ac2[2], KS[2], g1[2], gc1[2], g2[2], gc2[2], KG[2];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            col[q] = min(i0 + q, n - 1);
-            KS[q] = lm_anchor(v.cn[col[q]] * v.yn[j]);
-            KG[q] = lm_anchor(v.cn[col[q]] * v.cn[j]);
-            a1[q] = a2[q] = KS[q];
-            g1[q] = g2[q] = KG[q];
-            ac1[q] = ac2[q] = gc1[q] = gc2[q] = 0ull;
-        }
-#pragma unroll 1
-        for (int k = 0; k < n; ++k) {
-            const float4 y = Y[(size_t)k * n + j];
-            const u64 yh = f32x2(y.x, y.y), yl = f32x2(y.z, y.w);
-            const cx<float> xj = X[(size_t)k * n + j];
-            const u64 xjh = f32x2(xj.re, xj.im);
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                // conj(a) y = a_re y + i (-a_im) y
-                const cx<float> xa = X[(size_t)k * n + col[q]];
-                const u64 mR = f32x2(xa.re, xa.re), mI = f32x2(-xa.im, -xa.im);
-                lm_acc(a1[q], ac1[q], a2[q], ac2[q], mR, mI, yh);
-                ac1[q] = fma_f32x2(mR, yl, ac1[q]);
-                ac2[q] = fma_f32x2(mI, yl, ac2[q]);
-                lm_acc(g1[q], gc1[q], g2[q], gc2[q], mR, mI, xjh);
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int i = i0 + q;
-            if (i >= n || i > j) continue;
-            const float4 Sv = dw_finish(sub2(a1[q], KS[q]), ac1[q], sub2(a2[q], KS[q]), ac2[q]);
-            const float4 Gv = dw_finish(sub2(g1[q], KG[q]), gc1[q], sub2(g2[q], KG[q]), gc2[q]);
-            if (i == j) {
-                v.sd[i] = (double)Sv.x + (double)Sv.z;
-                v.rd[i] = (1.0 - (double)Gv.x) - (double)Gv.z;
-            } else {
-                SR[(size_t)i * n + j] = mk<float>(Sv.x + Sv.z, Sv.y + Sv.w);
-                SR[(size_t)j * n + i] = mk<float>(-(Gv.x + Gv.z), -(Gv.y + Gv.w));
-            }
-        }
-    }
-    __syncthreads();
+    lm_gemm<LM_SG>(s, X, X2, v, n);
     for (int i = tid; i < n; i += nt) {
         const double l = v.sd[i] / (1.0 - v.rd[i]);
         v.lam[i] = l;
@@ -749,32 +904,7 @@ __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
     for (int j = tid; j < n; j += nt)
         SR[(size_t)j * n + j] = mk<float>((float)(0.5 * v.rd[j]) + v.ed[j], 0.f);
     __syncthreads();
-    // X2 = X + X E: a task is rows k0 .. k0 + 3 and column j
-    for (int task = tid; task < nb4 * (int)n; task += nt) {
-        const int kb = task / n, j = task - kb * n, k0 = 4 * kb;
-        int row[4];
-        float ar[4], ai[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            row[q] = min(k0 + q, n - 1);
-            const cx<float> x = X[(size_t)row[q] * n + j];
-            ar[q] = x.re;
-            ai[q] = x.im;
-        }
-#pragma unroll 1
-        for (int i = 0; i < n; ++i) {
-            const cx<float> E = SR[(size_t)i * n + j];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const cx<float> x = X[(size_t)row[q] * n + i];
-                ar[q] = fmaf(x.re, E.re, fmaf(-x.im, E.im, ar[q]));
-                ai[q] = fmaf(x.re, E.im, fmaf(x.im, E.re, ai[q]));
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (k0 + q < n) X2[(size_t)(k0 + q) * n + j] = mk<float>(ar[q], ai[q]);
-    }
+    lm_gemm<LM_XE>(s, X, X2, v, n);
     for (int i = tid; i < n; i += nt) v.lam[i] += (double)v.corr[i];
     __syncthreads();
     const float step = __int_as_float(*v.step);
@@ -896,7 +1026,7 @@ cudaError_t launch_large_fast(const SnapArgs &a, double *scratch, int grid, cuda
     if (threads <= 0) threads = large_threads(a.n);
     const bool mixed = precision == MSP_PREC_MIXED;
     if ((threads & 31) || (mixed && threads > 256)) return cudaErrorInvalidValue;
-    const size_t smem = large_smem_bytes(a.n, threads);
+    const size_t smem = mixed ? lm_smem_bytes(a.n, threads) : large_smem_bytes(a.n, threads);
     const void *fn = mixed ? reinterpret_cast<const void *>(msp_large_fast_mixed_kernel)
                            : reinterpret_cast<const void *>(msp_large_fast_kernel);
     cudaError_t e =
@@ -924,8 +1054,8 @@ int large_ctas_per_sm(int n, int precision) {
     const bool mixed = precision == MSP_PREC_MIXED;
     const void *fn = mixed ? reinterpret_cast<const void *>(msp_large_fast_mixed_kernel)
                            : reinterpret_cast<const void *>(msp_large_fast_kernel);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads,
-                                                      large_smem_bytes(n, threads)) !=
+    const size_t smem = mixed ? lm_smem_bytes(n, threads) : large_smem_bytes(n, threads);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem) !=
             cudaSuccess ||
         occ < 1) {
         cudaGetLastError();
