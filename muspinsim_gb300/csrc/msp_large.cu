@@ -22,6 +22,8 @@
 #include <math_constants.h>
 #include <stdio.h>
 
+#include <type_traits>
+
 #include "msp_dw.cuh"
 #include "msp_internal.cuh"
 
@@ -607,14 +609,17 @@ struct LmVec {
     double *lam, *sd, *rd;
     float *lamf, *corr, *ed, *rn, *cn, *yn;
     int *step;
-    float4 *As, *Bs;  // GEMM slabs: A tile (TR x (LM_KT + 1)), B tile (LM_KT x 32)
+    char *slab;  // two stages of GEMM slabs (A: TR x LM_KT, B: LM_KT x 32)
 };
+
+// Bytes of one slab stage: A and B at up to 16 bytes per element.
+__host__ __device__ inline size_t lm_stage_bytes(int threads) {
+    return ((size_t)4 * (threads / 32) * LM_KT + (size_t)LM_KT * 32) * 16;
+}
 
 __host__ __device__ inline size_t lm_smem_bytes(int n, int threads) {
     const size_t vec = (48 * (size_t)n + 16 + 15) & ~size_t(15);
-    const size_t tr = 4 * (size_t)(threads / 32);
-    const size_t slabs = (tr * (LM_KT + 1) + LM_KT * 32) * 16;
-    const size_t need = vec + slabs, solver = large_smem_bytes(n, threads);
+    const size_t need = vec + 2 * lm_stage_bytes(threads), solver = large_smem_bytes(n, threads);
     return need > solver ? need : solver;
 }
 
@@ -631,8 +636,7 @@ __device__ __forceinline__ LmVec lm_vec(char *smem, int n) {
     v.yn = v.cn + n;
     v.step = reinterpret_cast<int *>(v.yn + n);
     const size_t vec = (48 * (size_t)n + 16 + 15) & ~size_t(15);
-    v.As = reinterpret_cast<float4 *>(smem + vec);
-    v.Bs = v.As + 4 * (blockDim.x >> 5) * (LM_KT + 1);
+    v.slab = smem + vec;
     return v;
 }
 
@@ -665,49 +669,110 @@ __device__ __forceinline__ void lm_step(u64 &s1, u64 &c1, u64 &s2, u64 &c2, floa
     }
 }
 
-// The three products of a refinement step, as one tiled kernel body: the
-// CTA walks output tiles of TR = 4 x warps rows by 32 columns; a thread
-// owns rows 4 w .. 4 w + 3 (w its warp) of column lane; A and B are staged
-// in shared memory LM_KT deep (A as [row][k] with a padded stride, so
-// that both fill orders are free of bank conflicts and the compute reads
-// are warp broadcasts; B as [k][column]).
-//   LM_HX: Y = H X            (H double-word, X FP32; anchored double-word)
-//   LM_SG: [S | G] = X^H [Y | X], tiles with no entry on or above the
-//          diagonal skipped; S_ij (i < j) -> SR[i][j], R_ij = -G_ij ->
-//          SR[j][i], S_ii -> sd, R_ii = 1 - G_ii -> rd
-//   LM_XE: X2 = X + X E       (FP32; E in SR, its diagonal included)
-enum { LM_HX = 0, LM_SG = 1, LM_XE = 2 };
+// Asynchronous global -> shared copies of one element (8 or 16 bytes);
+// `valid` false writes zeros (nothing is read; src is still a valid
+// address).  One commit group per slab; wait_group 1 leaves the newest
+// group in flight.
+__device__ __forceinline__ void lm_cp8(void *dst, const void *src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src),
+                 "r"(valid ? 8 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void lm_cp16(void *dst, const void *src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src),
+                 "r"(valid ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void lm_cp(float4 *dst, const float4 *src, bool valid) {
+    lm_cp16(dst, src, valid);
+}
+__device__ __forceinline__ void lm_cp(float2 *dst, const float2 *src, bool valid) {
+    lm_cp8(dst, src, valid);
+}
+__device__ __forceinline__ void lm_cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void lm_cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+__device__ __forceinline__ float4 lm_f4(float4 a) { return a; }
+__device__ __forceinline__ float4 lm_f4(float2 a) { return make_float4(a.x, a.y, 0.f, 0.f); }
+
+// The four products of a refinement step, one tiled kernel body: the CTA
+// walks output tiles of TR = 4 x warps rows by 32 columns; a thread owns
+// rows 4 w .. 4 w + 3 (w its warp) of column `lane`.  A and B are staged in
+// shared memory LM_KT deep, as stored in global memory (no conversion), by
+// cp.async in two stages: the next slab's copies are in flight while the
+// current one is multiplied.  The A reads of the multiply are warp
+// broadcasts; A is kept in the order that makes the copies contiguous.
+//   LM_HX: Y = H X        A = H [i][k] (double-word)   B = X [k][j]
+//   LM_S:  S = X^H Y      A = X [k][i] (conjugated)    B = Y [k][j] (double-word)
+//   LM_G:  G = X^H X      A = X [k][i] (conjugated)    B = X [k][j]
+//   LM_XE: X2 = X + X E   A = X [i][k]                 B = E [k][j]   (plain FP32)
+// S and G: tiles with no entry on or above the diagonal are skipped; S_ij
+// (i < j) -> SR[i][j], S_ii -> sd; R_ij = -G_ij (i < j) -> SR[j][i],
+// R_ii = 1 - G_ii -> rd.
+enum { LM_HX = 0, LM_S = 1, LM_G = 2, LM_XE = 3 };
 
 template <int MODE>
 __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
                         cx<float> *__restrict__ X2, const LmVec &v, int n) {
+    typedef typename std::conditional<MODE == LM_HX, float4, float2>::type AT;
+    typedef typename std::conditional<MODE == LM_S, float4, float2>::type BT;
+    constexpr bool A_KI = MODE == LM_S || MODE == LM_G;  // A tile stored [k][i]
     const int tid = threadIdx.x, nt = blockDim.x, w = tid >> 5, lane = tid & 31;
-    const int TR = 4 * (nt >> 5), AS = LM_KT + 1;
-    const int ncols = MODE == LM_SG ? 2 * n : n;
-    const int ti = (n + TR - 1) / TR, tj = (ncols + 31) >> 5;
-    float4 *__restrict__ As = v.As;
-    float4 *__restrict__ Bs = v.Bs;
-    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int TR = 4 * (nt >> 5);
+    const int ti = (n + TR - 1) / TR, tj = (n + 31) >> 5, nslab = (n + LM_KT - 1) / LM_KT;
+    const AT *Ag = MODE == LM_HX ? reinterpret_cast<const AT *>(s.H)
+                                 : reinterpret_cast<const AT *>(X);
+    const BT *Bg = MODE == LM_S    ? reinterpret_cast<const BT *>(s.Y)
+                   : MODE == LM_XE ? reinterpret_cast<const BT *>(s.SR)
+                                   : reinterpret_cast<const BT *>(X);
+    const size_t stage = lm_stage_bytes(nt);
+    AT *As0 = reinterpret_cast<AT *>(v.slab);
+    BT *Bs0 = reinterpret_cast<BT *>(v.slab + (size_t)TR * LM_KT * 16);
+    // copies of slab sl into stage sl & 1
+    auto issue = [&](int i0, int j0, int sl) {
+        AT *As = reinterpret_cast<AT *>(reinterpret_cast<char *>(As0) + (sl & 1) * stage);
+        BT *Bs = reinterpret_cast<BT *>(reinterpret_cast<char *>(Bs0) + (sl & 1) * stage);
+        const int k0 = sl * LM_KT;
+        for (int e = tid; e < TR * LM_KT; e += nt) {
+            int i, k;
+            if (A_KI) {
+                i = e % TR;
+                k = e / TR;
+            } else {
+                i = e / LM_KT;
+                k = e % LM_KT;
+            }
+            const int gi = i0 + i, gk = k0 + k;
+            const bool ok = gi < n && gk < n;
+            const size_t off = ok ? (A_KI ? (size_t)gk * n + gi : (size_t)gi * n + gk) : 0;
+            lm_cp(As + e, Ag + off, ok);
+        }
+        for (int e = tid; e < LM_KT * 32; e += nt) {
+            const int k = e >> 5, gk = k0 + k, gj = j0 + (e & 31);
+            const bool ok = gk < n && gj < n;
+            lm_cp(Bs + e, Bg + (ok ? (size_t)gk * n + gj : 0), ok);
+        }
+        lm_cp_commit();
+    };
     for (int t = 0; t < ti * tj; ++t) {  // the same sequence in every thread
         const int it = t / tj, i0 = it * TR, j0 = (t - it * tj) * 32;
-        if (MODE == LM_SG) {
-            const int jmax = j0 >= n ? min(j0 + 31, 2 * n - 1) - n : min(j0 + 31, n - 1);
-            if (jmax < i0) continue;  // no entry i <= j in this tile
-        }
+        if ((MODE == LM_S || MODE == LM_G) && min(j0 + 31, n - 1) < i0) continue;
         const int j = j0 + lane;
         // anchor of output (i0 + 4 w + q, j) (recomputed at the end rather
         // than held in registers through the k loop)
         auto anchor = [&](int q) -> u64 {
-            const int i = min(i0 + 4 * w + q, n - 1);
-            if (MODE == LM_HX) return lm_anchor(v.rn[i] * v.cn[min(j, n - 1)]);
-            return lm_anchor(v.cn[i] * (j < n ? v.yn[j] : v.cn[min(j - n, n - 1)]));
+            const int i = min(i0 + 4 * w + q, n - 1), jc = min(j, n - 1);
+            if (MODE == LM_HX) return lm_anchor(v.rn[i] * v.cn[jc]);
+            return lm_anchor(v.cn[i] * (MODE == LM_S ? v.yn[jc] : v.cn[jc]));
         };
         u64 s1[4], c1[4], s2[4], c2[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             if (MODE == LM_XE) {
-                const cx<float> x = j < n ? X[(size_t)(i0 + 4 * w + q < n ? i0 + 4 * w + q : 0) * n + j]
-                                          : mk<float>(0.f, 0.f);
+                const int i = i0 + 4 * w + q;
+                const cx<float> x = j < n && i < n ? X[(size_t)i * n + j] : mk<float>(0.f, 0.f);
                 s1[q] = f32x2(x.re, x.im);  // plain FP32 accumulator (re, im)
                 s2[q] = c1[q] = c2[q] = 0ull;
             } else {
@@ -715,65 +780,30 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
                 c1[q] = c2[q] = 0ull;
             }
         }
-        for (int k0 = 0; k0 < n; k0 += LM_KT) {
-            // A tile: TR rows x LM_KT
-            for (int e = tid; e < TR * LM_KT; e += nt) {
-                int i, k;
-                if (MODE == LM_SG) {  // A(i, k) = conj(X[k][i]): contiguous in i
-                    i = e % TR;
-                    k = e / TR;
-                } else {  // A(i, k) = H[i][k] or X[i][k]: contiguous in k
-                    i = e / LM_KT;
-                    k = e % LM_KT;
-                }
-                const int gi = i0 + i, gk = k0 + k;
-                float4 a = zero4;
-                if (gi < n && gk < n) {
-                    if (MODE == LM_HX) {
-                        a = s.H[(size_t)gi * n + gk];
-                    } else if (MODE == LM_SG) {
-                        const cx<float> x = X[(size_t)gk * n + gi];
-                        a = make_float4(x.re, -x.im, 0.f, 0.f);
-                    } else {
-                        const cx<float> x = X[(size_t)gi * n + gk];
-                        a = make_float4(x.re, x.im, 0.f, 0.f);
-                    }
-                }
-                As[i * AS + k] = a;
-            }
-            // B tile: LM_KT x 32, contiguous in the column
-            for (int e = tid; e < LM_KT * 32; e += nt) {
-                const int k = e >> 5, jj = e & 31, gk = k0 + k, gj = j0 + jj;
-                float4 b = zero4;
-                if (gk < n && gj < ncols) {
-                    if (MODE == LM_HX) {
-                        const cx<float> x = X[(size_t)gk * n + gj];
-                        b = make_float4(x.re, x.im, 0.f, 0.f);
-                    } else if (MODE == LM_SG) {
-                        if (gj < n) {
-                            b = s.Y[(size_t)gk * n + gj];
-                        } else {
-                            const cx<float> x = X[(size_t)gk * n + gj - n];
-                            b = make_float4(x.re, x.im, 0.f, 0.f);
-                        }
-                    } else {
-                        const cx<float> E = s.SR[(size_t)gk * n + gj];
-                        b = make_float4(E.re, E.im, 0.f, 0.f);
-                    }
-                }
-                Bs[k * 32 + jj] = b;
-            }
+        issue(i0, j0, 0);
+        for (int sl = 0; sl < nslab; ++sl) {
+            if (sl + 1 < nslab)
+                issue(i0, j0, sl + 1);
+            else
+                lm_cp_commit();  // an empty group keeps wait_group 1 exact
+            lm_cp_wait1();
             __syncthreads();
+            const AT *As = reinterpret_cast<const AT *>(reinterpret_cast<const char *>(As0) +
+                                                         (sl & 1) * stage);
+            const BT *Bs = reinterpret_cast<const BT *>(reinterpret_cast<const char *>(Bs0) +
+                                                         (sl & 1) * stage);
 #pragma unroll 4
             for (int k = 0; k < LM_KT; ++k) {
-                const float4 b = Bs[k * 32 + lane];
+                const float4 b = lm_f4(Bs[k * 32 + lane]);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const float4 a = As[(4 * w + q) * AS + k];
+                    const int r = 4 * w + q;
+                    float4 a = lm_f4(As[A_KI ? k * TR + r : r * LM_KT + k]);
                     if (MODE == LM_HX) {
                         lm_step<true, false>(s1[q], c1[q], s2[q], c2[q], a, b);
-                    } else if (MODE == LM_SG) {
-                        lm_step<false, true>(s1[q], c1[q], s2[q], c2[q], a, b);
+                    } else if (MODE == LM_S || MODE == LM_G) {
+                        a.y = -a.y;  // conj(X)
+                        lm_step<false, MODE == LM_S>(s1[q], c1[q], s2[q], c2[q], a, b);
                     } else {
                         // (re, im) += (a.re, a.re) (b.re, b.im) + (a.im, a.im) (-b.im, b.re)
                         s1[q] = fma_f32x2(f32x2(a.x, a.x), f32x2(b.x, b.y), s1[q]);
@@ -781,12 +811,12 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
                     }
                 }
             }
-            __syncthreads();
+            __syncthreads();  // the stage is refilled two slabs later
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int i = i0 + 4 * w + q;
-            if (i >= n || j >= ncols) continue;
+            if (i >= n || j >= n) continue;
             if (MODE == LM_XE) {
                 float re, im;
                 split_f32x2(s1[q], re, im);
@@ -797,17 +827,16 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
             const float4 r = dw_finish(sub2(s1[q], K), c1[q], sub2(s2[q], K), c2[q]);
             if (MODE == LM_HX) {
                 s.Y[(size_t)i * n + j] = r;
-            } else if (j < n) {  // S
+            } else if (MODE == LM_S) {
                 if (i == j)
                     v.sd[i] = (double)r.x + (double)r.z;
                 else if (i < j)
                     s.SR[(size_t)i * n + j] = mk<float>(r.x + r.z, r.y + r.w);
-            } else {  // G
-                const int jg = j - n;
-                if (i == jg)
+            } else {
+                if (i == j)
                     v.rd[i] = (1.0 - (double)r.x) - (double)r.z;
-                else if (i < jg)
-                    s.SR[(size_t)jg * n + i] = mk<float>(-(r.x + r.z), -(r.y + r.w));
+                else if (i < j)
+                    s.SR[(size_t)j * n + i] = mk<float>(-(r.x + r.z), -(r.y + r.w));
             }
         }
     }
@@ -840,7 +869,8 @@ __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
     lm_gemm<LM_HX>(s, X, X2, v, n);
     lm_colnorms(reinterpret_cast<const float *>(s.Y), 4, n, v.yn);
     __syncthreads();
-    lm_gemm<LM_SG>(s, X, X2, v, n);
+    lm_gemm<LM_S>(s, X, X2, v, n);
+    lm_gemm<LM_G>(s, X, X2, v, n);
     for (int i = tid; i < n; i += nt) {
         const double l = v.sd[i] / (1.0 - v.rd[i]);
         v.lam[i] = l;
