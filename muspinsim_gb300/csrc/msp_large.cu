@@ -122,9 +122,11 @@ __device__ __forceinline__ float rsqrt_newton<float>(float x) {
 }
 
 // Eigenpairs of the Hermitian matrix already in s.A (full, row-major):
-// ascending eigenvalues into s.lam, eigenvectors (columns) into s.U.
-// Returns MSP_ITEM_OK or MSP_ITEM_NOT_CONVERGED (QL iteration cap).
-template <typename T>
+// eigenvalues into s.lam, eigenvectors (columns) into s.U.  Returns
+// MSP_ITEM_OK or MSP_ITEM_NOT_CONVERGED (QL iteration cap).  BACK = false
+// stops after the QL step (s.Zt holds Z, s.A the reflectors, s.tau their
+// scalars) for a caller that back-transforms by itself.
+template <typename T, bool BACK = true>
 __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     const int nw = nt >> 5;
@@ -354,65 +356,67 @@ __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
     }
     status = s_ctl[3];
 
-    // ---- 3. U = Q Z (complex), reflectors applied last to first; one column per thread
-    for (size_t x = tid; x < (size_t)n * n; x += nt) {
-        const int i = (int)(x / n), j = (int)(x - (size_t)i * n);
-        s.U[x] = mk<T>(s.Zt[(size_t)j * n + i], T(0));
-    }
-    __syncthreads();
-    for (int k = n - 2; k >= 0; --k) {
-        const cx<T> tau = s.tau[k];
-        if (tau.re == T(0) && tau.im == T(0)) continue;  // the same in every thread
-        const int m = n - k - 1;
-        for (int i = tid; i < m; i += nt)
-            v[i] = i == 0 ? mk<T>(T(1), T(0)) : A[(size_t)(k + 1 + i) * n + k];
+    // ---- 3. U = Q Z (complex), reflectors applied last to first
+    if (BACK) {
+        for (size_t x = tid; x < (size_t)n * n; x += nt) {
+            const int i = (int)(x / n), j = (int)(x - (size_t)i * n);
+            s.U[x] = mk<T>(s.Zt[(size_t)j * n + i], T(0));
+        }
         __syncthreads();
-        // s_j = v^H U[k+1.., j]: thread (pr, pg) takes columns j = pr, pr + RW,
-        // ... and the pg-th of G parts of the rows
-        if (pg < G) {
-            const int ib = (int)((long long)m * pg / G), ie = (int)((long long)m * (pg + 1) / G);
-            for (int j = pr; j < n; j += RW) {
-                const cx<T> *col = s.U + (size_t)(k + 1) * n + j;
-                T r0 = T(0), i0 = T(0), r1 = T(0), i1 = T(0);
-                int i = ib;
+        for (int k = n - 2; k >= 0; --k) {
+            const cx<T> tau = s.tau[k];
+            if (tau.re == T(0) && tau.im == T(0)) continue;  // the same in every thread
+            const int m = n - k - 1;
+            for (int i = tid; i < m; i += nt)
+                v[i] = i == 0 ? mk<T>(T(1), T(0)) : A[(size_t)(k + 1 + i) * n + k];
+            __syncthreads();
+            // s_j = v^H U[k+1.., j]: thread (pr, pg) takes columns j = pr, pr + RW,
+            // ... and the pg-th of G parts of the rows
+            if (pg < G) {
+                const int ib = (int)((long long)m * pg / G), ie = (int)((long long)m * (pg + 1) / G);
+                for (int j = pr; j < n; j += RW) {
+                    const cx<T> *col = s.U + (size_t)(k + 1) * n + j;
+                    T r0 = T(0), i0 = T(0), r1 = T(0), i1 = T(0);
+                    int i = ib;
 #pragma unroll 4
-                for (; i + 1 < ie; i += 2) {
-                    const cx<T> u0 = col[(size_t)i * n], u1 = col[(size_t)(i + 1) * n];
-                    const cx<T> v0 = v[i], v1 = v[i + 1];
-                    r0 += v0.re * u0.re + v0.im * u0.im;
-                    i0 += v0.re * u0.im - v0.im * u0.re;
-                    r1 += v1.re * u1.re + v1.im * u1.im;
-                    i1 += v1.re * u1.im - v1.im * u1.re;
+                    for (; i + 1 < ie; i += 2) {
+                        const cx<T> u0 = col[(size_t)i * n], u1 = col[(size_t)(i + 1) * n];
+                        const cx<T> v0 = v[i], v1 = v[i + 1];
+                        r0 += v0.re * u0.re + v0.im * u0.im;
+                        i0 += v0.re * u0.im - v0.im * u0.re;
+                        r1 += v1.re * u1.re + v1.im * u1.im;
+                        i1 += v1.re * u1.im - v1.im * u1.re;
+                    }
+                    if (i < ie) {
+                        const cx<T> u0 = col[(size_t)i * n], v0 = v[i];
+                        r0 += v0.re * u0.re + v0.im * u0.im;
+                        i0 += v0.re * u0.im - v0.im * u0.re;
+                    }
+                    part[(size_t)pg * n + j] = mk<T>(r0 + r1, i0 + i1);
                 }
-                if (i < ie) {
-                    const cx<T> u0 = col[(size_t)i * n], v0 = v[i];
-                    r0 += v0.re * u0.re + v0.im * u0.im;
-                    i0 += v0.re * u0.im - v0.im * u0.re;
+            }
+            __syncthreads();
+            for (int j = tid; j < n; j += nt) {
+                T sr = T(0), si = T(0);
+                for (int g = 0; g < G; ++g) {
+                    sr += part[(size_t)g * n + j].re;
+                    si += part[(size_t)g * n + j].im;
                 }
-                part[(size_t)pg * n + j] = mk<T>(r0 + r1, i0 + i1);
+                p[j] = cmul(tau, mk<T>(sr, si));  // tau s_j
             }
-        }
-        __syncthreads();
-        for (int j = tid; j < n; j += nt) {
-            T sr = T(0), si = T(0);
-            for (int g = 0; g < G; ++g) {
-                sr += part[(size_t)g * n + j].re;
-                si += part[(size_t)g * n + j].im;
-            }
-            p[j] = cmul(tau, mk<T>(sr, si));  // tau s_j
-        }
-        __syncthreads();
-        // U[k+1.., j] -= v tau s_j: warps over rows, lanes over columns
-        for (int i = warp; i < m; i += nw) {
-            const cx<T> vi = v[i];
-            cx<T> *row = s.U + (size_t)(k + 1 + i) * n;
+            __syncthreads();
+            // U[k+1.., j] -= v tau s_j: warps over rows, lanes over columns
+            for (int i = warp; i < m; i += nw) {
+                const cx<T> vi = v[i];
+                cx<T> *row = s.U + (size_t)(k + 1 + i) * n;
 #pragma unroll 4
-            for (int j = lane; j < n; j += 32) {
-                const cx<T> t = cmul(vi, p[j]), u = row[j];
-                row[j] = mk<T>(u.re - t.re, u.im - t.im);
+                for (int j = lane; j < n; j += 32) {
+                    const cx<T> t = cmul(vi, p[j]), u = row[j];
+                    row[j] = mk<T>(u.re - t.re, u.im - t.im);
+                }
             }
+            __syncthreads();
         }
-        __syncthreads();
     }
     for (int i = tid; i < n; i += nt) s.lam[i] = d[i];
     __syncthreads();
@@ -617,8 +621,16 @@ __host__ __device__ inline size_t lm_stage_bytes(int threads) {
     return ((size_t)4 * (threads / 32) * LM_KT + (size_t)LM_KT * 32) * 16;
 }
 
+// Bytes of the refinement vectors (also the back-transformation's two
+// LM_KT x LM_KT complex matrices).
+__host__ __device__ inline size_t lm_vec_bytes(int n) {
+    size_t b = 48 * (size_t)n + 16;
+    if (b < 2 * LM_KT * LM_KT * 8) b = 2 * LM_KT * LM_KT * 8;
+    return (b + 15) & ~size_t(15);
+}
+
 __host__ __device__ inline size_t lm_smem_bytes(int n, int threads) {
-    const size_t vec = (48 * (size_t)n + 16 + 15) & ~size_t(15);
+    const size_t vec = lm_vec_bytes(n);
     const size_t need = vec + 2 * lm_stage_bytes(threads), solver = large_smem_bytes(n, threads);
     return need > solver ? need : solver;
 }
@@ -635,8 +647,7 @@ __device__ __forceinline__ LmVec lm_vec(char *smem, int n) {
     v.cn = v.rn + n;
     v.yn = v.cn + n;
     v.step = reinterpret_cast<int *>(v.yn + n);
-    const size_t vec = (48 * (size_t)n + 16 + 15) & ~size_t(15);
-    v.slab = smem + vec;
+    v.slab = smem + lm_vec_bytes(n);
     return v;
 }
 
@@ -697,88 +708,61 @@ __device__ __forceinline__ void lm_cp_wait1() { asm volatile("cp.async.wait_grou
 __device__ __forceinline__ float4 lm_f4(float4 a) { return a; }
 __device__ __forceinline__ float4 lm_f4(float2 a) { return make_float4(a.x, a.y, 0.f, 0.f); }
 
-// The four products of a refinement step, one tiled kernel body: the CTA
-// walks output tiles of TR = 4 x warps rows by 32 columns; a thread owns
-// rows 4 w .. 4 w + 3 (w its warp) of column `lane`.  A and B are staged in
-// shared memory LM_KT deep, as stored in global memory (no conversion), by
-// cp.async in two stages: the next slab's copies are in flight while the
-// current one is multiplied.  The A reads of the multiply are warp
-// broadcasts; A is kept in the order that makes the copies contiguous.
-//   LM_HX: Y = H X        A = H [i][k] (double-word)   B = X [k][j]
-//   LM_S:  S = X^H Y      A = X [k][i] (conjugated)    B = Y [k][j] (double-word)
-//   LM_G:  G = X^H X      A = X [k][i] (conjugated)    B = X [k][j]
-//   LM_XE: X2 = X + X E   A = X [i][k]                 B = E [k][j]   (plain FP32)
-// S and G: tiles with no entry on or above the diagonal are skipped; S_ij
-// (i < j) -> SR[i][j], S_ii -> sd; R_ij = -G_ij (i < j) -> SR[j][i],
-// R_ii = 1 - G_ii -> rd.
-enum { LM_HX = 0, LM_S = 1, LM_G = 2, LM_XE = 3 };
+// Tiled product C(i, j) = sum_k op(A)(i, k) B(k, j), i < M, j < N, k < K,
+// as one CTA-wide kernel body.  The CTA walks output tiles of TR = 4 x
+// warps rows by 32 columns; a thread owns rows 4 w .. 4 w + 3 (w its warp)
+// of column `lane`.  A and B are staged in shared memory LM_KT deep as they
+// are stored in global memory (no conversion), by cp.async in two stages:
+// the next slab's copies are in flight while the current one is
+// multiplied.  A(i, k) is read from Ag[k * lda + i] (A_KI) or
+// Ag[i * lda + k], B(k, j) from Bg[k * ldb + j]; the A reads of the multiply
+// are warp broadcasts.  Accumulation (ACC):
+//   LM_DW_ALO   anchored double-word, A double-word (float4), B FP32
+//   LM_DW_CBLO  anchored double-word, conj(A) FP32, B double-word
+//   LM_DW_C     anchored double-word, conj(A) and B FP32
+//   LM_PLAIN    FP32, (s1) += A B
+//   LM_PLAIN_C  FP32, (s1) += conj(A) B
+// skip(i0, j0) drops a whole tile; init(i, j, s1, c1, s2, c2) seeds an
+// accumulator (the anchor, or a start value); epi(i, j, s1, c1, s2, c2)
+// consumes it (i < M, j < N only).
+enum { LM_DW_ALO = 0, LM_DW_CBLO = 1, LM_DW_C = 2, LM_PLAIN = 3, LM_PLAIN_C = 4 };
 
-template <int MODE>
-__device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
-                        cx<float> *__restrict__ X2, const LmVec &v, int n) {
-    typedef typename std::conditional<MODE == LM_HX, float4, float2>::type AT;
-    typedef typename std::conditional<MODE == LM_S, float4, float2>::type BT;
-    constexpr bool A_KI = MODE == LM_S || MODE == LM_G;  // A tile stored [k][i]
+template <int ACC, bool A_KI, typename AT, typename BT, typename Skip, typename Init, typename Epi>
+__device__ void lm_tiles(int M, int N, int K, const AT *__restrict__ Ag, int lda,
+                         const BT *__restrict__ Bg, int ldb, const LmVec &v, Skip skip, Init init,
+                         Epi epi) {
     const int tid = threadIdx.x, nt = blockDim.x, w = tid >> 5, lane = tid & 31;
     const int TR = 4 * (nt >> 5);
-    const int ti = (n + TR - 1) / TR, tj = (n + 31) >> 5, nslab = (n + LM_KT - 1) / LM_KT;
-    const AT *Ag = MODE == LM_HX ? reinterpret_cast<const AT *>(s.H)
-                                 : reinterpret_cast<const AT *>(X);
-    const BT *Bg = MODE == LM_S    ? reinterpret_cast<const BT *>(s.Y)
-                   : MODE == LM_XE ? reinterpret_cast<const BT *>(s.SR)
-                                   : reinterpret_cast<const BT *>(X);
+    const int ti = (M + TR - 1) / TR, tj = (N + 31) >> 5, nslab = (K + LM_KT - 1) / LM_KT;
     const size_t stage = lm_stage_bytes(nt);
-    AT *As0 = reinterpret_cast<AT *>(v.slab);
-    BT *Bs0 = reinterpret_cast<BT *>(v.slab + (size_t)TR * LM_KT * 16);
-    // copies of slab sl into stage sl & 1
+    char *A0 = v.slab, *B0 = v.slab + (size_t)TR * LM_KT * 16;
     auto issue = [&](int i0, int j0, int sl) {
-        AT *As = reinterpret_cast<AT *>(reinterpret_cast<char *>(As0) + (sl & 1) * stage);
-        BT *Bs = reinterpret_cast<BT *>(reinterpret_cast<char *>(Bs0) + (sl & 1) * stage);
+        AT *As = reinterpret_cast<AT *>(A0 + (sl & 1) * stage);
+        BT *Bs = reinterpret_cast<BT *>(B0 + (sl & 1) * stage);
         const int k0 = sl * LM_KT;
         for (int e = tid; e < TR * LM_KT; e += nt) {
-            int i, k;
-            if (A_KI) {
-                i = e % TR;
-                k = e / TR;
-            } else {
-                i = e / LM_KT;
-                k = e % LM_KT;
-            }
+            const int i = A_KI ? e % TR : e / LM_KT, k = A_KI ? e / TR : e % LM_KT;
             const int gi = i0 + i, gk = k0 + k;
-            const bool ok = gi < n && gk < n;
-            const size_t off = ok ? (A_KI ? (size_t)gk * n + gi : (size_t)gi * n + gk) : 0;
+            const bool ok = gi < M && gk < K;
+            const size_t off = ok ? (A_KI ? (size_t)gk * lda + gi : (size_t)gi * lda + gk) : 0;
             lm_cp(As + e, Ag + off, ok);
         }
         for (int e = tid; e < LM_KT * 32; e += nt) {
-            const int k = e >> 5, gk = k0 + k, gj = j0 + (e & 31);
-            const bool ok = gk < n && gj < n;
-            lm_cp(Bs + e, Bg + (ok ? (size_t)gk * n + gj : 0), ok);
+            const int gk = k0 + (e >> 5), gj = j0 + (e & 31);
+            const bool ok = gk < K && gj < N;
+            lm_cp(Bs + e, Bg + (ok ? (size_t)gk * ldb + gj : 0), ok);
         }
         lm_cp_commit();
     };
     for (int t = 0; t < ti * tj; ++t) {  // the same sequence in every thread
         const int it = t / tj, i0 = it * TR, j0 = (t - it * tj) * 32;
-        if ((MODE == LM_S || MODE == LM_G) && min(j0 + 31, n - 1) < i0) continue;
+        if (skip(i0, j0)) continue;
         const int j = j0 + lane;
-        // anchor of output (i0 + 4 w + q, j) (recomputed at the end rather
-        // than held in registers through the k loop)
-        auto anchor = [&](int q) -> u64 {
-            const int i = min(i0 + 4 * w + q, n - 1), jc = min(j, n - 1);
-            if (MODE == LM_HX) return lm_anchor(v.rn[i] * v.cn[jc]);
-            return lm_anchor(v.cn[i] * (MODE == LM_S ? v.yn[jc] : v.cn[jc]));
-        };
         u64 s1[4], c1[4], s2[4], c2[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            if (MODE == LM_XE) {
-                const int i = i0 + 4 * w + q;
-                const cx<float> x = j < n && i < n ? X[(size_t)i * n + j] : mk<float>(0.f, 0.f);
-                s1[q] = f32x2(x.re, x.im);  // plain FP32 accumulator (re, im)
-                s2[q] = c1[q] = c2[q] = 0ull;
-            } else {
-                s1[q] = s2[q] = anchor(q);
-                c1[q] = c2[q] = 0ull;
-            }
+            s1[q] = c1[q] = s2[q] = c2[q] = 0ull;
+            init(i0 + 4 * w + q, j, s1[q], c1[q], s2[q], c2[q]);
         }
         issue(i0, j0, 0);
         for (int sl = 0; sl < nslab; ++sl) {
@@ -788,10 +772,8 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
                 lm_cp_commit();  // an empty group keeps wait_group 1 exact
             lm_cp_wait1();
             __syncthreads();
-            const AT *As = reinterpret_cast<const AT *>(reinterpret_cast<const char *>(As0) +
-                                                         (sl & 1) * stage);
-            const BT *Bs = reinterpret_cast<const BT *>(reinterpret_cast<const char *>(Bs0) +
-                                                         (sl & 1) * stage);
+            const AT *As = reinterpret_cast<const AT *>(A0 + (sl & 1) * stage);
+            const BT *Bs = reinterpret_cast<const BT *>(B0 + (sl & 1) * stage);
 #pragma unroll 4
             for (int k = 0; k < LM_KT; ++k) {
                 const float4 b = lm_f4(Bs[k * 32 + lane]);
@@ -799,11 +781,13 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
                 for (int q = 0; q < 4; ++q) {
                     const int r = 4 * w + q;
                     float4 a = lm_f4(As[A_KI ? k * TR + r : r * LM_KT + k]);
-                    if (MODE == LM_HX) {
+                    if (ACC == LM_DW_CBLO || ACC == LM_DW_C || ACC == LM_PLAIN_C) a.y = -a.y;
+                    if (ACC == LM_DW_ALO) {
                         lm_step<true, false>(s1[q], c1[q], s2[q], c2[q], a, b);
-                    } else if (MODE == LM_S || MODE == LM_G) {
-                        a.y = -a.y;  // conj(X)
-                        lm_step<false, MODE == LM_S>(s1[q], c1[q], s2[q], c2[q], a, b);
+                    } else if (ACC == LM_DW_CBLO) {
+                        lm_step<false, true>(s1[q], c1[q], s2[q], c2[q], a, b);
+                    } else if (ACC == LM_DW_C) {
+                        lm_step<false, false>(s1[q], c1[q], s2[q], c2[q], a, b);
                     } else {
                         // (re, im) += (a.re, a.re) (b.re, b.im) + (a.im, a.im) (-b.im, b.re)
                         s1[q] = fma_f32x2(f32x2(a.x, a.x), f32x2(b.x, b.y), s1[q]);
@@ -816,31 +800,177 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int i = i0 + 4 * w + q;
-            if (i >= n || j >= n) continue;
-            if (MODE == LM_XE) {
-                float re, im;
-                split_f32x2(s1[q], re, im);
-                X2[(size_t)i * n + j] = mk<float>(re, im);
-                continue;
-            }
-            const u64 K = anchor(q);
-            const float4 r = dw_finish(sub2(s1[q], K), c1[q], sub2(s2[q], K), c2[q]);
-            if (MODE == LM_HX) {
-                s.Y[(size_t)i * n + j] = r;
-            } else if (MODE == LM_S) {
+            if (i < M && j < N) epi(i, j, s1[q], c1[q], s2[q], c2[q]);
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ cx<float> lm_plain(u64 acc) {
+    float re, im;
+    split_f32x2(acc, re, im);
+    return mk<float>(re, im);
+}
+
+// The four products of a refinement step (n x n):
+//   Y = H X (H double-word), S = X^H Y (Y double-word), G = X^H X, and
+//   X2 = X + X E (FP32, E in SR with its diagonal).
+// S and G skip tiles with no entry on or above the diagonal; S_ij (i < j)
+// -> SR[i][j], S_ii -> sd; R_ij = -G_ij (i < j) -> SR[j][i], R_ii = 1 - G_ii
+// -> rd.
+enum { LM_HX = 0, LM_S = 1, LM_G = 2, LM_XE = 3 };
+
+template <int MODE>
+__device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
+                        cx<float> *__restrict__ X2, const LmVec &v, int n) {
+    const float2 *Xf = reinterpret_cast<const float2 *>(X);
+    auto noskip = [](int, int) { return false; };
+    auto upper = [n](int i0, int j0) { return min(j0 + 31, n - 1) < i0; };
+    auto dw_init = [&](int i, int j, u64 &s1, u64 &c1, u64 &s2, u64 &c2, float bound) {
+        (void)i;
+        (void)j;
+        s1 = s2 = lm_anchor(bound);
+        c1 = c2 = 0ull;
+    };
+    if (MODE == LM_HX) {
+        auto bound = [&](int i, int j) { return v.rn[min(i, n - 1)] * v.cn[min(j, n - 1)]; };
+        lm_tiles<LM_DW_ALO, false>(
+            n, n, n, s.H, n, Xf, n, v, noskip,
+            [&](int i, int j, u64 &s1, u64 &c1, u64 &s2, u64 &c2) {
+                dw_init(i, j, s1, c1, s2, c2, bound(i, j));
+            },
+            [&](int i, int j, u64 s1, u64 c1, u64 s2, u64 c2) {
+                const u64 K = lm_anchor(bound(i, j));
+                s.Y[(size_t)i * n + j] = dw_finish(sub2(s1, K), c1, sub2(s2, K), c2);
+            });
+    } else if (MODE == LM_S) {
+        auto bound = [&](int i, int j) { return v.cn[min(i, n - 1)] * v.yn[min(j, n - 1)]; };
+        lm_tiles<LM_DW_CBLO, true>(
+            n, n, n, Xf, n, s.Y, n, v, upper,
+            [&](int i, int j, u64 &s1, u64 &c1, u64 &s2, u64 &c2) {
+                dw_init(i, j, s1, c1, s2, c2, bound(i, j));
+            },
+            [&](int i, int j, u64 s1, u64 c1, u64 s2, u64 c2) {
+                const u64 K = lm_anchor(bound(i, j));
+                const float4 r = dw_finish(sub2(s1, K), c1, sub2(s2, K), c2);
                 if (i == j)
                     v.sd[i] = (double)r.x + (double)r.z;
                 else if (i < j)
                     s.SR[(size_t)i * n + j] = mk<float>(r.x + r.z, r.y + r.w);
-            } else {
+            });
+    } else if (MODE == LM_G) {
+        auto bound = [&](int i, int j) { return v.cn[min(i, n - 1)] * v.cn[min(j, n - 1)]; };
+        lm_tiles<LM_DW_C, true>(
+            n, n, n, Xf, n, Xf, n, v, upper,
+            [&](int i, int j, u64 &s1, u64 &c1, u64 &s2, u64 &c2) {
+                dw_init(i, j, s1, c1, s2, c2, bound(i, j));
+            },
+            [&](int i, int j, u64 s1, u64 c1, u64 s2, u64 c2) {
+                const u64 K = lm_anchor(bound(i, j));
+                const float4 r = dw_finish(sub2(s1, K), c1, sub2(s2, K), c2);
                 if (i == j)
                     v.rd[i] = (1.0 - (double)r.x) - (double)r.z;
                 else if (i < j)
                     s.SR[(size_t)j * n + i] = mk<float>(-(r.x + r.z), -(r.y + r.w));
-            }
-        }
+            });
+    } else {
+        lm_tiles<LM_PLAIN, false>(
+            n, n, n, Xf, n, reinterpret_cast<const float2 *>(s.SR), n, v, noskip,
+            [&](int i, int j, u64 &s1, u64 &, u64 &, u64 &) {
+                const cx<float> x = i < n && j < n ? X[(size_t)i * n + j] : mk<float>(0.f, 0.f);
+                s1 = f32x2(x.re, x.im);
+            },
+            [&](int i, int j, u64 s1, u64, u64, u64) { X2[(size_t)i * n + j] = lm_plain(s1); });
     }
+}
+
+// Blocked back-transformation U = Q Z for the FP32 solver (the compact WY
+// form of LAPACK zlarft, forward, columnwise): reflectors kb .. kb + nb - 1
+// (nb <= LM_KT) act together as P = I - V T V^H on rows kb + 1 .. n - 1 of
+// U, with V (m x nb, unit lower trapezoidal) copied out of the reflector
+// storage, T upper triangular from tau and the Gram matrix V^H V:
+//   T_ii = tau_i,  T[0:i, i] = T[0:i, 0:i] (-tau_i (V^H V)[0:i, i]);
+// then W = V^H U_b, W2 = -T W, U_b += V W2 -- three tiled products that read
+// U twice per block instead of twice per reflector.  Blocks run last to
+// first (U = H_0 H_1 ... H_{n-2} Z).  Scratch: SR (free during the solve)
+// holds V, W and W2; the refinement vectors' shared memory holds V^H V and T.
+__device__ void lm_back(const LargeMixed &s, const LmVec &v, int n) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    cx<float> *U = s.X;
+    for (size_t x = tid; x < (size_t)n * n; x += nt) {
+        const int i = (int)(x / n), j = (int)(x - (size_t)i * n);
+        U[x] = mk<float>(s.sol.Zt[(size_t)j * n + i], 0.f);
+    }
+    float2 *Vb = reinterpret_cast<float2 *>(s.SR);  // m x LM_KT
+    float2 *W = Vb + (size_t)n * LM_KT;            // LM_KT x n
+    float2 *W2 = W + (size_t)n * LM_KT;            // LM_KT x n
+    cx<float> *Gs = reinterpret_cast<cx<float> *>(v.lam);  // LM_KT x LM_KT
+    cx<float> *Ts = Gs + LM_KT * LM_KT;
+    const cx<float> *A = s.sol.A;
+    const int nref = n - 1;
+    auto noskip = [](int, int) { return false; };
+    auto zero = [](int, int, u64 &s1, u64 &, u64 &, u64 &) { s1 = 0ull; };
     __syncthreads();
+    for (int kb = ((nref - 1) / LM_KT) * LM_KT; kb >= 0; kb -= LM_KT) {
+        const int nb = min(LM_KT, nref - kb), m = n - kb - 1;
+        for (int e = tid; e < m * LM_KT; e += nt) {
+            const int r = e / LM_KT, c = e % LM_KT;
+            cx<float> val = mk<float>(0.f, 0.f);
+            if (c < nb && r >= c)
+                val = r == c ? mk<float>(1.f, 0.f) : A[(size_t)(kb + 1 + r) * n + kb + c];
+            Vb[e] = make_float2(val.re, val.im);
+        }
+        __syncthreads();
+        // V^H V
+        lm_tiles<LM_PLAIN_C, true>(nb, nb, m, Vb, LM_KT, Vb, LM_KT, v, noskip, zero,
+                                   [&](int i, int j, u64 s1, u64, u64, u64) {
+                                       Gs[i * LM_KT + j] = lm_plain(s1);
+                                   });
+        // T, one column at a time (nb <= 16 threads per column)
+        for (int i = 0; i < nb; ++i) {
+            const cx<float> taui = s.sol.tau[kb + i];
+            if (tid < i) {
+                // t_c = -tau_i G[c][i], then T[c][i] = sum_{c' >= c} T[c][c'] t_c'
+                cx<float> acc = mk<float>(0.f, 0.f);
+                for (int c2 = tid; c2 < i; ++c2) {
+                    const cx<float> t = cmul(taui, Gs[c2 * LM_KT + i]);
+                    acc = cadd(acc, cmul(Ts[tid * LM_KT + c2], mk<float>(-t.re, -t.im)));
+                }
+                Ts[tid * LM_KT + i] = acc;
+            }
+            if (tid == 0) {
+                Ts[i * LM_KT + i] = taui;
+                for (int r = i + 1; r < LM_KT; ++r) Ts[r * LM_KT + i] = mk<float>(0.f, 0.f);
+            }
+            __syncthreads();
+        }
+        // W = V^H U_b
+        cx<float> *Ub = U + (size_t)(kb + 1) * n;
+        lm_tiles<LM_PLAIN_C, true>(nb, n, m, Vb, LM_KT, reinterpret_cast<const float2 *>(Ub), n, v,
+                                   noskip, zero, [&](int i, int j, u64 s1, u64, u64, u64) {
+                                       const cx<float> r = lm_plain(s1);
+                                       W[(size_t)i * n + j] = make_float2(r.re, r.im);
+                                   });
+        // W2 = -T W
+        for (int e = tid; e < nb * n; e += nt) {
+            const int c = e / n, j = e - c * n;
+            cx<float> acc = mk<float>(0.f, 0.f);
+            for (int c2 = c; c2 < nb; ++c2) {
+                const float2 wv = W[(size_t)c2 * n + j];
+                acc = cadd(acc, cmul(Ts[c * LM_KT + c2], mk<float>(wv.x, wv.y)));
+            }
+            W2[(size_t)c * n + j] = make_float2(-acc.re, -acc.im);
+        }
+        __syncthreads();
+        // U_b += V W2
+        lm_tiles<LM_PLAIN, false>(
+            m, n, nb, Vb, LM_KT, W2, n, v, noskip,
+            [&](int i, int j, u64 &s1, u64 &, u64 &, u64 &) {
+                const cx<float> u = i < m && j < n ? Ub[(size_t)i * n + j] : mk<float>(0.f, 0.f);
+                s1 = f32x2(u.re, u.im);
+            },
+            [&](int i, int j, u64 s1, u64, u64, u64) { Ub[(size_t)i * n + j] = lm_plain(s1); });
+    }
 }
 
 // Column 2-norms of an n x n matrix of (re, im) pairs with element stride
@@ -970,7 +1100,8 @@ __global__ void __maxnreg__(96) msp_large_fast_mixed_kernel(SnapArgs a, char *sc
             s.sol.A[x] = mk<float>(h.x, h.y);
         }
         __syncthreads();
-        const int st = large_eigh<float>(s.sol, n, smem);
+        const int st = large_eigh<float, false>(s.sol, n, smem);
+        lm_back(s, v, n);
         for (int i = tid; i < n; i += nt) {
             float acc = 0.f;
             for (int k = 0; k < n; ++k) {
