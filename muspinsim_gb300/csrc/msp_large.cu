@@ -92,10 +92,11 @@ __host__ __device__ inline int large_parts(int threads) {
     return threads / rw;
 }
 
-// Shared memory: v, p, part (n, n, G n complex), qc, qs, d, e (n reals
-// each), red.  (Sized for T = double; the FP32 instance uses half of it.)
+// Shared memory: v, p, part (n, n, G n complex), qc, qs (2 n reals each:
+// two rotation batches), d, e (n reals each), red.  (Sized for T = double;
+// the FP32 instance uses half of it.)
 __host__ __device__ inline size_t large_smem_bytes(int n, int threads) {
-    return (size_t)n * 16 * (2 + large_parts(threads)) + (size_t)n * 8 * 4 +
+    return (size_t)n * 16 * (2 + large_parts(threads)) + (size_t)n * 8 * 6 +
            (size_t)(threads / 32) * 16 + 64;
 }
 
@@ -134,9 +135,9 @@ __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
     cx<T> *v = reinterpret_cast<cx<T> *>(smem);
     cx<T> *p = v + n;
     cx<T> *part = p + n;  // G x n partial sums
-    T *qc = reinterpret_cast<T *>(part + (size_t)G * n);
-    T *qs = qc + n;
-    T *dsm = qs + n;  // diagonal and off-diagonal of the tridiagonal matrix
+    T *qc = reinterpret_cast<T *>(part + (size_t)G * n);  // two batches of n
+    T *qs = qc + 2 * n;
+    T *dsm = qs + 2 * n;  // diagonal and off-diagonal of the tridiagonal matrix
     T *esm = dsm + n;
     T *red = esm + n;
     cx<T> *A = s.A;
@@ -243,118 +244,133 @@ __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
     }
     __syncthreads();
 
-    // ---- 2. QL with implicit shifts; e[i] couples d[i], d[i+1]
-    int status = MSP_ITEM_OK;
-    __shared__ int s_ctl[4];  // m, iteration flag, rotation count, status
-    __shared__ T s_f, s_tst;
-    if (tid == 0) {
-        s_f = T(0);
-        s_tst = T(0);
-        s_ctl[3] = MSP_ITEM_OK;
-    }
-    __syncthreads();
+    // ---- 2. QL with implicit shifts; e[i] couples d[i], d[i+1].
+    // Thread 0 runs the serial part (convergence tests, shifts and the
+    // rotation chain of one QL step: a "batch" of rotations for columns
+    // l .. m of Z) one batch ahead of the other warps, which apply the
+    // previous batch to the rows of Z meanwhile; qc / qs hold two batches.
+    __shared__ int s_bat[2][3];  // per batch: m, l, rotation count (-1: done)
+    __shared__ int s_status;
     T *d = dsm, *e = esm;
-    for (int l = 0; l < n; ++l) {
-        for (int iter = 0;; ++iter) {
-            if (tid == 0) {
-                if (iter == 0) s_tst = fmax(s_tst, fabs(d[l]) + fabs(e[l]));
-                int m = l;
-                while (m < n - 1 && fabs(e[m]) > LargeEps<T>::eps * s_tst) ++m;
-                s_ctl[0] = m;
-                s_ctl[1] = 0;
-                s_ctl[2] = 0;
-                if (m > l && iter < 60) {
-                    // one QL step on rows l..m; rotations (c, s) for i = m-1 .. l
-                    T g = d[l];
-                    T pp = (d[l + 1] - g) / (T(2) * e[l]);
-                    T r = hypot(pp, T(1));
-                    d[l] = e[l] / (pp + copysign(r, pp));
-                    d[l + 1] = e[l] * (pp + copysign(r, pp));
-                    const T dl1 = d[l + 1];
-                    T h = g - d[l];
-                    for (int i = l + 2; i < n; ++i) d[i] -= h;
-                    s_f += h;
-                    pp = d[m];
-                    T c = T(1), c2 = T(1), c3 = T(1), sn = T(0), s2 = T(0);
-                    const T el1 = e[l + 1];
-                    int cnt = 0;
-                    for (int i = m - 1; i >= l; --i) {
-                        c3 = c2;
-                        c2 = c;
-                        s2 = sn;
-                        const T ei = e[i];
-                        g = c * ei;
-                        h = c * pp;
-                        const T x2 = fma(pp, pp, ei * ei);
-                        if (x2 > T(1e-36) && x2 < T(1e36)) {
-                            const T y = rsqrt_newton<T>(x2);
-                            r = x2 * y;
-                            e[i + 1] = sn * r;
-                            sn = ei * y;
-                            c = pp * y;
-                        } else {  // outside the seed's range: the library route
-                            r = hypot(pp, ei);
-                            e[i + 1] = sn * r;
-                            sn = ei / r;
-                            c = pp / r;
-                        }
-                        pp = c * d[i] - sn * g;
-                        d[i + 1] = h + sn * (c * g + sn * d[i]);
-                        qc[cnt] = c;
-                        qs[cnt] = sn;
-                        ++cnt;
-                    }
-                    pp = -sn * s2 * c3 * el1 * e[l] / dl1;
-                    e[l] = sn * pp;
-                    d[l] = c * pp;
-                    s_ctl[1] = 1;
-                    s_ctl[2] = cnt;
-                } else if (m > l) {
-                    s_ctl[3] = MSP_ITEM_NOT_CONVERGED;
-                }
+    // producer state (thread 0 only)
+    int pl = 0, piter = 0, pstatus = MSP_ITEM_OK;
+    T pf = T(0), ptst = T(0);
+    // Next batch into slot `slot`: deflates converged eigenvalues, then one
+    // QL step (or marks the end).
+    auto produce = [&](int slot) {
+        T *bc = qc + slot * n, *bs = qs + slot * n;
+        for (;;) {
+            if (pl >= n) {
+                s_bat[slot][2] = -1;
+                s_status = pstatus;
+                return;
             }
-            __syncthreads();
-            if (!s_ctl[1]) break;
-            // apply the rotations to every row of Z: columns (i, i+1), i = m-1 .. l
-            {
-                const int m = s_ctl[0], cnt = s_ctl[2];
-                T *__restrict__ Zt = s.Zt;
-                for (int row = tid; row < n; row += nt) {
-                    T hcarry = Zt[(size_t)m * n + row];  // Z[row][i+1] for i = m-1
-                    int q = 0;
-                    // eight entries loaded ahead of the rotation chain: within a
-                    // sweep every entry is read before it is written
-                    for (; q + 8 <= cnt; q += 8) {
-                        T zi[8];
-#pragma unroll
-                        for (int u = 0; u < 8; ++u) zi[u] = Zt[(size_t)(m - 1 - q - u) * n + row];
-#pragma unroll
-                        for (int u = 0; u < 8; ++u) {
-                            const int i = m - 1 - q - u;
-                            const T c = qc[q + u], sn = qs[q + u];
-                            Zt[(size_t)(i + 1) * n + row] = sn * zi[u] + c * hcarry;
-                            hcarry = c * zi[u] - sn * hcarry;
-                        }
-                    }
-                    for (; q < cnt; ++q) {
-                        const int i = m - 1 - q;
-                        const T zi = Zt[(size_t)i * n + row];
-                        const T c = qc[q], sn = qs[q];
-                        Zt[(size_t)(i + 1) * n + row] = sn * zi + c * hcarry;
-                        hcarry = c * zi - sn * hcarry;
-                    }
-                    Zt[(size_t)l * n + row] = hcarry;
-                }
+            const int l = pl;
+            if (piter == 0) ptst = fmax(ptst, fabs(d[l]) + fabs(e[l]));
+            int m = l;
+            while (m < n - 1 && fabs(e[m]) > LargeEps<T>::eps * ptst) ++m;
+            if (m == l || piter >= 60) {
+                if (m != l) pstatus = MSP_ITEM_NOT_CONVERGED;
+                d[l] += pf;
+                e[l] = T(0);
+                ++pl;
+                piter = 0;
+                continue;
             }
-            __syncthreads();
+            // one QL step on rows l..m; rotations (c, s) for i = m-1 .. l
+            T g = d[l];
+            T pp = (d[l + 1] - g) / (T(2) * e[l]);
+            T r = hypot(pp, T(1));
+            d[l] = e[l] / (pp + copysign(r, pp));
+            d[l + 1] = e[l] * (pp + copysign(r, pp));
+            const T dl1 = d[l + 1];
+            T h = g - d[l];
+            for (int i = l + 2; i < n; ++i) d[i] -= h;
+            pf += h;
+            pp = d[m];
+            T c = T(1), c2 = T(1), c3 = T(1), sn = T(0), s2 = T(0);
+            const T el1 = e[l + 1];
+            int cnt = 0;
+            for (int i = m - 1; i >= l; --i) {
+                c3 = c2;
+                c2 = c;
+                s2 = sn;
+                const T ei = e[i];
+                g = c * ei;
+                h = c * pp;
+                const T x2 = fma(pp, pp, ei * ei);
+                if (x2 > T(1e-36) && x2 < T(1e36)) {
+                    const T y = rsqrt_newton<T>(x2);
+                    r = x2 * y;
+                    e[i + 1] = sn * r;
+                    sn = ei * y;
+                    c = pp * y;
+                } else {  // outside the seed's range: the library route
+                    r = hypot(pp, ei);
+                    e[i + 1] = sn * r;
+                    sn = ei / r;
+                    c = pp / r;
+                }
+                pp = c * d[i] - sn * g;
+                d[i + 1] = h + sn * (c * g + sn * d[i]);
+                bc[cnt] = c;
+                bs[cnt] = sn;
+                ++cnt;
+            }
+            pp = -sn * s2 * c3 * el1 * e[l] / dl1;
+            e[l] = sn * pp;
+            d[l] = c * pp;
+            ++piter;
+            s_bat[slot][0] = m;
+            s_bat[slot][1] = l;
+            s_bat[slot][2] = cnt;
+            return;
         }
-        if (tid == 0) {
-            d[l] += s_f;
-            e[l] = T(0);
+    };
+    // appliers: warps 1.. (all threads when the CTA is one warp)
+    const int a0 = nt >= 64 ? 32 : 0, na = nt - a0;
+    if (tid == 0) produce(0);
+    __syncthreads();
+    for (int b = 0;; ++b) {
+        const int cur = b & 1;
+        if (s_bat[cur][2] < 0) break;  // the same in every thread
+        const int m = s_bat[cur][0], l = s_bat[cur][1], cnt = s_bat[cur][2];
+        if (tid == 0) produce(cur ^ 1);
+        if (tid >= a0) {
+            // apply the batch to every row of Z: columns (i, i+1), i = m-1 .. l
+            const T *bc = qc + cur * n, *bs = qs + cur * n;
+            T *__restrict__ Zt = s.Zt;
+            for (int row = tid - a0; row < n; row += na) {
+                T hcarry = Zt[(size_t)m * n + row];  // Z[row][i+1] for i = m-1
+                int q = 0;
+                // eight entries loaded ahead of the rotation chain: within a
+                // batch every entry is read before it is written
+                for (; q + 8 <= cnt; q += 8) {
+                    T zi[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) zi[u] = Zt[(size_t)(m - 1 - q - u) * n + row];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int i = m - 1 - q - u;
+                        const T c = bc[q + u], sn = bs[q + u];
+                        Zt[(size_t)(i + 1) * n + row] = sn * zi[u] + c * hcarry;
+                        hcarry = c * zi[u] - sn * hcarry;
+                    }
+                }
+                for (; q < cnt; ++q) {
+                    const int i = m - 1 - q;
+                    const T zi = Zt[(size_t)i * n + row];
+                    const T c = bc[q], sn = bs[q];
+                    Zt[(size_t)(i + 1) * n + row] = sn * zi + c * hcarry;
+                    hcarry = c * zi - sn * hcarry;
+                }
+                Zt[(size_t)l * n + row] = hcarry;
+            }
         }
         __syncthreads();
     }
-    status = s_ctl[3];
+    const int status = s_status;
+
 
     // ---- 3. U = Q Z (complex), reflectors applied last to first
     if (BACK) {
@@ -1139,25 +1155,21 @@ __global__ void __maxnreg__(96) msp_large_fast_mixed_kernel(SnapArgs a, char *sc
         __syncthreads();
         const double scale = 0.5 * a.wscale[g] / (double)d;
         double diag = 0.0;
-        const size_t ntri = (size_t)n * (n + 1) / 2;
-        for (size_t x = tid; x < ntri; x += nt) {
-            int j = (int)((sqrt(8.0 * (double)x + 1.0) - 1.0) * 0.5);
-            while ((size_t)(j + 1) * (j + 2) / 2 <= x) ++j;
-            while ((size_t)j * (j + 1) / 2 > x) --j;
-            const int k = (int)(x - (size_t)j * (j + 1) / 2);
-            float gr = 0.f, gi = 0.f;
-            for (int i = 0; i < n; ++i) {
-                const cx<float> u = X[(size_t)i * n + j], w = X2[(size_t)i * n + k];
-                gr = fmaf(u.re, w.re, fmaf(u.im, w.im, gr));
-                gi = fmaf(u.re, w.im, fmaf(-u.im, w.re, gi));
-            }
-            const double Am = (double)(gr * gr + gi * gi);
-            if (j == k)
-                diag += Am;
-            else
-                large_store_pair(a, (size_t)sn * P + (size_t)j * (j - 1) / 2 + k, scale * Am,
-                                 6.283185307179586476925 * (v.lam[j] - v.lam[k]));
-        }
+        // G = X^H W (tiles with an entry j >= k only); A_jk = |G_jk|^2
+        lm_tiles<LM_PLAIN_C, true>(
+            n, n, n, reinterpret_cast<const float2 *>(X), n, reinterpret_cast<const float2 *>(X2),
+            n, v, [](int i0, int j0) { return i0 + 4 * (int)(blockDim.x >> 5) - 1 < j0; },
+            [](int, int, u64 &, u64 &, u64 &, u64 &) {},
+            [&](int j, int k, u64 s1, u64, u64, u64) {
+                if (j < k) return;
+                const cx<float> G = lm_plain(s1);
+                const double Am = (double)(G.re * G.re + G.im * G.im);
+                if (j == k)
+                    diag += Am;
+                else
+                    large_store_pair(a, (size_t)sn * P + (size_t)j * (j - 1) / 2 + k, scale * Am,
+                                     6.283185307179586476925 * (v.lam[j] - v.lam[k]));
+            });
         diag = block_sum(diag, red);
         if (tid == 0) {
             a.snap_const[sn] = scale * 0.5 * diag;
