@@ -92,12 +92,40 @@ __host__ __device__ inline int large_parts(int threads) {
     return threads / rw;
 }
 
-// Shared memory: v, p, part (n, n, G n complex), qc, qs (2 n reals each:
-// two rotation batches), d, e (n reals each), red.  (Sized for T = double;
-// the FP32 instance uses half of it.)
+// Shared memory of the solver: v, p (n complex each), part (G x (n + 32)
+// complex partial sums), y (32 complex), qc, qs (2 n reals each: two
+// rotation batches), d, e (n reals each), red (one real per warp).
+template <typename T>
+struct LargeSm {
+    cx<T> *v, *p, *part, *y;
+    T *qc, *qs, *d, *e, *red;
+};
+
+template <typename T>
+__host__ __device__ inline size_t large_sm_bytes(int n, int threads) {
+    const size_t c = sizeof(cx<T>), r = sizeof(T);
+    return c * (2 * (size_t)n + (size_t)large_parts(threads) * (n + 32) + 32) +
+           r * (6 * (size_t)n + threads / 32) + 64;
+}
+
+template <typename T>
+__device__ __forceinline__ LargeSm<T> large_sm(char *smem, int n, int threads) {
+    LargeSm<T> m;
+    m.v = reinterpret_cast<cx<T> *>(smem);
+    m.p = m.v + n;
+    m.part = m.p + n;
+    m.y = m.part + (size_t)large_parts(threads) * (n + 32);
+    m.qc = reinterpret_cast<T *>(m.y + 32);  // two batches of n
+    m.qs = m.qc + 2 * n;
+    m.d = m.qs + 2 * n;  // diagonal and off-diagonal of the tridiagonal matrix
+    m.e = m.d + n;
+    m.red = m.e + n;
+    return m;
+}
+
+// (The FP64 kernels' dynamic shared memory.)
 __host__ __device__ inline size_t large_smem_bytes(int n, int threads) {
-    return (size_t)n * 16 * (2 + large_parts(threads)) + (size_t)n * 8 * 6 +
-           (size_t)(threads / 32) * 16 + 64;
+    return large_sm_bytes<double>(n, threads);
 }
 
 // 1 / sqrt(x) for x > 0 in FP64 by Newton's method on f(y) = 1/y^2 - x,
@@ -126,24 +154,21 @@ __device__ __forceinline__ float rsqrt_newton<float>(float x) {
 // eigenvalues into s.lam, eigenvectors (columns) into s.U.  Returns
 // MSP_ITEM_OK or MSP_ITEM_NOT_CONVERGED (QL iteration cap).  BACK = false
 // stops after the QL step (s.Zt holds Z, s.A the reflectors, s.tau their
-// scalars) for a caller that back-transforms by itself.
-template <typename T, bool BACK = true>
+// scalars) for a caller that back-transforms by itself; TRI = false starts
+// at the QL step (the caller left d and e in this layout's shared memory,
+// the reflectors in s.A and s.tau).
+template <typename T, bool BACK = true, bool TRI = true>
 __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     const int nw = nt >> 5;
     const int RW = nt < 64 ? nt : 64, G = nt / RW, pr = tid % RW, pg = tid / RW;
-    cx<T> *v = reinterpret_cast<cx<T> *>(smem);
-    cx<T> *p = v + n;
-    cx<T> *part = p + n;  // G x n partial sums
-    T *qc = reinterpret_cast<T *>(part + (size_t)G * n);  // two batches of n
-    T *qs = qc + 2 * n;
-    T *dsm = qs + 2 * n;  // diagonal and off-diagonal of the tridiagonal matrix
-    T *esm = dsm + n;
-    T *red = esm + n;
+    const LargeSm<T> sm = large_sm<T>(smem, n, nt);
+    cx<T> *v = sm.v, *p = sm.p, *part = sm.part;
+    T *qc = sm.qc, *qs = sm.qs, *dsm = sm.d, *esm = sm.e, *red = sm.red;
     cx<T> *A = s.A;
 
     // ---- 1. tridiagonalisation
-    for (int k = 0; k + 1 < n; ++k) {
+    for (int k = 0; TRI && k + 1 < n; ++k) {
         const int m = n - k - 1;  // length of x = A[k+1.., k]
         T xn2 = T(0);
         for (int i = 1 + tid; i < m; i += nt) xn2 += cabs2(A[(size_t)(k + 1 + i) * n + k]);
@@ -193,15 +218,15 @@ __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
                     r0 += a0.re * x0.re + a0.im * x0.im;
                     i0 += a0.re * x0.im - a0.im * x0.re;
                 }
-                part[(size_t)pg * n + i] = mk<T>(r0 + r1, i0 + i1);
+                part[(size_t)pg * (n + 32) + i] = mk<T>(r0 + r1, i0 + i1);
             }
         }
         __syncthreads();
         for (int i = tid; i < m; i += nt) {
             T sr = T(0), si = T(0);
             for (int g = 0; g < G; ++g) {
-                sr += part[(size_t)g * n + i].re;
-                si += part[(size_t)g * n + i].im;
+                sr += part[(size_t)g * (n + 32) + i].re;
+                si += part[(size_t)g * (n + 32) + i].im;
             }
             p[i] = cmul(tau, mk<T>(sr, si));
         }
@@ -233,7 +258,7 @@ __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
         for (int i = 1 + tid; i < m; i += nt) A[(size_t)(k + 1 + i) * n + k] = v[i];
         __syncthreads();
     }
-    if (tid == 0) {
+    if (TRI && tid == 0) {
         dsm[n - 1] = A[(size_t)(n - 1) * n + (n - 1)].re;
         esm[n - 1] = T(0);
     }
@@ -408,15 +433,15 @@ __device__ int large_eigh(LargeScratchT<T> s, int n, char *smem) {
                         r0 += v0.re * u0.re + v0.im * u0.im;
                         i0 += v0.re * u0.im - v0.im * u0.re;
                     }
-                    part[(size_t)pg * n + j] = mk<T>(r0 + r1, i0 + i1);
+                    part[(size_t)pg * (n + 32) + j] = mk<T>(r0 + r1, i0 + i1);
                 }
             }
             __syncthreads();
             for (int j = tid; j < n; j += nt) {
                 T sr = T(0), si = T(0);
                 for (int g = 0; g < G; ++g) {
-                    sr += part[(size_t)g * n + j].re;
-                    si += part[(size_t)g * n + j].im;
+                    sr += part[(size_t)g * (n + 32) + j].re;
+                    si += part[(size_t)g * (n + 32) + j].im;
                 }
                 p[j] = cmul(tau, mk<T>(sr, si));  // tau s_j
             }
@@ -645,10 +670,17 @@ __host__ __device__ inline size_t lm_vec_bytes(int n) {
     return (b + 15) & ~size_t(15);
 }
 
+// The slabs sit above both the refinement vectors and the FP32 solver's
+// shared memory (the blocked tridiagonalisation uses both at once).
+__host__ __device__ inline size_t lm_slab_offset(int n, int threads) {
+    size_t o = lm_vec_bytes(n);
+    const size_t sol = large_sm_bytes<float>(n, threads);
+    if (sol > o) o = sol;
+    return (o + 15) & ~size_t(15);
+}
+
 __host__ __device__ inline size_t lm_smem_bytes(int n, int threads) {
-    const size_t vec = lm_vec_bytes(n);
-    const size_t need = vec + 2 * lm_stage_bytes(threads), solver = large_smem_bytes(n, threads);
-    return need > solver ? need : solver;
+    return lm_slab_offset(n, threads) + 2 * lm_stage_bytes(threads);
 }
 
 __device__ __forceinline__ LmVec lm_vec(char *smem, int n) {
@@ -663,7 +695,7 @@ __device__ __forceinline__ LmVec lm_vec(char *smem, int n) {
     v.cn = v.rn + n;
     v.yn = v.cn + n;
     v.step = reinterpret_cast<int *>(v.yn + n);
-    v.slab = smem + lm_vec_bytes(n);
+    v.slab = smem + lm_slab_offset(n, blockDim.x);
     return v;
 }
 
@@ -1088,6 +1120,174 @@ __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
     return step;
 }
 
+// Blocked tridiagonalisation for the FP32 solver (the panel scheme of
+// LAPACK zlatrd / zhetrd, lower form, full storage): columns are reduced
+// LM_KT at a time.  Within a panel the trailing matrix stays as it was at
+// the panel start ("stale"); reflector j of the panel keeps v_j and w_j in
+// VW (rows: V in columns 0..15, W in 16..31), so that the true trailing
+// matrix is the stale one minus V W^H + W V^H:
+//   1. column k (rows k..) is brought up to date from the panel's V, W;
+//   2. its reflector (as in the unblocked form; d_k, e_k, tau_k);
+//   3. p = A22 v over the stale matrix, in the same column-parallel pass
+//      as y = VW^H v (32 extra "columns" read from VW);
+//   4. p -= V (W^H v) + W (V^H v), p *= tau, alpha = -tau (p^H v) / 2,
+//      w = p + alpha v;
+// and after the panel one rank-2 LM_KT update of the trailing matrix,
+// A22 += [V W] [-W^H; -V^H], through the tile engine.  The trailing matrix
+// is read about 1.2 times per column instead of three times.  Leaves d, e
+// in the solver's shared memory, the reflectors in A (below the
+// subdiagonal) and their scalars in tau.  Scratch: SR (free during the
+// solve) holds VW (n x 32) and the update's right operand (32 x n).
+__device__ void lm_tridiag(const LargeMixed &s, const LmVec &vv, char *smem, int n) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int RW = nt < 64 ? nt : 64, G = nt / RW, pr = tid % RW, pg = tid / RW;
+    const LargeSm<float> sm = large_sm<float>(smem, n, nt);
+    cx<float> *A = s.sol.A;
+    cx<float> *VW = s.SR;                   // n x 32
+    cx<float> *Bt = s.SR + (size_t)n * 32;  // 32 x n
+    cx<float> *v = sm.v, *p = sm.p, *part = sm.part, *y = sm.y;
+    const size_t pst = (size_t)n + 32;  // stride of the partial sums
+    auto noskip = [](int, int) { return false; };
+    for (int k0 = 0; k0 + 1 < n; k0 += LM_KT) {
+        const int nbp = min(LM_KT, n - 1 - k0);
+        for (size_t x = (size_t)k0 * 32 + tid; x < (size_t)n * 32; x += nt)
+            VW[x] = mk<float>(0.f, 0.f);
+        __syncthreads();
+        for (int j = 0; j < nbp; ++j) {
+            const int k = k0 + j, m = n - k - 1;
+            // 1. column k, rows k.., minus the panel's V W^H + W V^H
+            if (j > 0) {
+                const cx<float> *vk = VW + (size_t)k * 32;
+                for (int r = k + tid; r < n; r += nt) {
+                    const cx<float> *vr = VW + (size_t)r * 32;
+                    cx<float> a = A[(size_t)r * n + k];
+                    for (int c = 0; c < j; ++c) {
+                        const cx<float> t1 = cmul(vr[c], conj(vk[16 + c]));
+                        const cx<float> t2 = cmul(vr[16 + c], conj(vk[c]));
+                        a = mk<float>(a.re - t1.re - t2.re, a.im - t1.im - t2.im);
+                    }
+                    A[(size_t)r * n + k] = a;
+                }
+                __syncthreads();
+            }
+            // 2. reflector of A[k+1.., k]
+            float xn2 = 0.f;
+            for (int i = 1 + tid; i < m; i += nt) xn2 += cabs2(A[(size_t)(k + 1 + i) * n + k]);
+            xn2 = block_sum(xn2, sm.red);
+            const cx<float> alpha = A[(size_t)(k + 1) * n + k];
+            cx<float> tau = mk<float>(0.f, 0.f);
+            float beta = alpha.re;
+            const bool reflect = !(xn2 == 0.f && alpha.im == 0.f);
+            if (reflect) {
+                beta = -copysignf(sqrtf(alpha.re * alpha.re + alpha.im * alpha.im + xn2), alpha.re);
+                tau = mk<float>((beta - alpha.re) / beta, -alpha.im / beta);
+                const cx<float> den = mk<float>(alpha.re - beta, alpha.im);
+                const float dd = 1.f / cabs2(den);
+                const cx<float> sc = mk<float>(den.re * dd, -den.im * dd);
+                for (int i = tid; i < m; i += nt)
+                    v[i] = i == 0 ? mk<float>(1.f, 0.f) : cmul(A[(size_t)(k + 1 + i) * n + k], sc);
+            } else {
+                for (int i = tid; i < m; i += nt) v[i] = mk<float>(0.f, 0.f);  // V and W columns stay 0
+            }
+            if (tid == 0) {
+                sm.d[k] = A[(size_t)k * n + k].re;
+                sm.e[k] = beta;
+                s.sol.tau[k] = tau;
+            }
+            __syncthreads();
+            // 3. p = A22 v (stale A22, Hermitian: p_i = sum_l conj(A22_li) v_l) and
+            //    y = VW^H v in extra columns i = m .. m + 31
+            if (pg < G) {
+                const int lb = (int)((long long)m * pg / G), le = (int)((long long)m * (pg + 1) / G);
+                for (int i = pr; i < m + 32; i += RW) {
+                    const cx<float> *col = i < m ? A + (size_t)(k + 1) * n + (k + 1 + i)
+                                                 : VW + (size_t)(k + 1) * 32 + (i - m);
+                    const size_t ld = i < m ? (size_t)n : 32;
+                    float r0 = 0.f, i0 = 0.f, r1 = 0.f, i1 = 0.f;
+                    int l = lb;
+#pragma unroll 4
+                    for (; l + 1 < le; l += 2) {
+                        const cx<float> a0 = col[(size_t)l * ld], a1 = col[(size_t)(l + 1) * ld];
+                        const cx<float> x0 = v[l], x1 = v[l + 1];
+                        r0 += a0.re * x0.re + a0.im * x0.im;
+                        i0 += a0.re * x0.im - a0.im * x0.re;
+                        r1 += a1.re * x1.re + a1.im * x1.im;
+                        i1 += a1.re * x1.im - a1.im * x1.re;
+                    }
+                    if (l < le) {
+                        const cx<float> a0 = col[(size_t)l * ld], x0 = v[l];
+                        r0 += a0.re * x0.re + a0.im * x0.im;
+                        i0 += a0.re * x0.im - a0.im * x0.re;
+                    }
+                    part[(size_t)pg * pst + i] = mk<float>(r0 + r1, i0 + i1);
+                }
+            }
+            __syncthreads();
+            for (int i = tid; i < m + 32; i += nt) {
+                float sr = 0.f, si = 0.f;
+                for (int g = 0; g < G; ++g) {
+                    sr += part[(size_t)g * pst + i].re;
+                    si += part[(size_t)g * pst + i].im;
+                }
+                if (i < m)
+                    p[i] = mk<float>(sr, si);
+                else
+                    y[i - m] = mk<float>(sr, si);  // V^H v in 0..15, W^H v in 16..31
+            }
+            __syncthreads();
+            // 4. p = tau (p - V (W^H v) - W (V^H v)); w = p + alpha v
+            float hr = 0.f, hi = 0.f;
+            for (int i = tid; i < m; i += nt) {
+                cx<float> acc = p[i];
+                const cx<float> *vr = VW + (size_t)(k + 1 + i) * 32;
+                for (int c = 0; c < j; ++c) {
+                    const cx<float> t1 = cmul(vr[c], y[16 + c]), t2 = cmul(vr[16 + c], y[c]);
+                    acc = mk<float>(acc.re - t1.re - t2.re, acc.im - t1.im - t2.im);
+                }
+                acc = cmul(tau, acc);
+                p[i] = acc;
+                const cx<float> c = cmulc(acc, v[i]);  // conj(p_i) v_i
+                hr += c.re;
+                hi += c.im;
+            }
+            hr = block_sum(hr, sm.red);
+            hi = block_sum(hi, sm.red);
+            const cx<float> a2 = cscale(-0.5f, cmul(tau, mk<float>(hr, hi)));
+            for (int i = tid; i < m; i += nt) {
+                const cx<float> vi = v[i];
+                VW[(size_t)(k + 1 + i) * 32 + j] = vi;
+                VW[(size_t)(k + 1 + i) * 32 + 16 + j] = cadd(p[i], cmul(a2, vi));
+                if (i > 0 && reflect) A[(size_t)(k + 1 + i) * n + k] = vi;  // for the back-transformation
+            }
+            __syncthreads();
+        }
+        // rank-2 LM_KT update of the trailing matrix (rows and columns k1..)
+        const int k1 = k0 + nbp, mt = n - k1;
+        if (mt > 0) {
+            for (int x = tid; x < 32 * mt; x += nt) {
+                const int kk = x / mt, jj = x - kk * mt;
+                const cx<float> w = VW[(size_t)(k1 + jj) * 32 + (kk < 16 ? 16 + kk : kk - 16)];
+                Bt[(size_t)kk * n + jj] = mk<float>(-w.re, w.im);  // -conj
+            }
+            __syncthreads();
+            cx<float> *At = A + (size_t)k1 * n + k1;
+            lm_tiles<LM_PLAIN, false>(
+                mt, mt, 32, reinterpret_cast<const float2 *>(VW + (size_t)k1 * 32), 32,
+                reinterpret_cast<const float2 *>(Bt), n, vv, noskip,
+                [&](int i, int j, u64 &s1, u64 &, u64 &, u64 &) {
+                    const cx<float> a = i < mt && j < mt ? At[(size_t)i * n + j] : mk<float>(0.f, 0.f);
+                    s1 = f32x2(a.re, a.im);
+                },
+                [&](int i, int j, u64 s1, u64, u64, u64) { At[(size_t)i * n + j] = lm_plain(s1); });
+        }
+    }
+    if (tid == 0) {
+        sm.d[n - 1] = A[(size_t)(n - 1) * n + (n - 1)].re;
+        sm.e[n - 1] = 0.f;
+    }
+    __syncthreads();
+}
+
 // The fast path for n > 64 in MIXED precision: H = Hsys + b . Z in FP64,
 // split into hi + lo; the FP32 solver on hi; refinement steps until the
 // correction drops below 2e-4 (at most four; one step leaves an error of
@@ -1116,7 +1316,15 @@ __global__ void __maxnreg__(96) msp_large_fast_mixed_kernel(SnapArgs a, char *sc
             s.sol.A[x] = mk<float>(h.x, h.y);
         }
         __syncthreads();
-        const int st = large_eigh<float, false>(s.sol, n, smem);
+        // the blocked reduction pays from n ~ 128 (measured: 20% faster at
+        // n = 192, 20% slower at n = 96)
+        int st;
+        if (n >= 128) {
+            lm_tridiag(s, v, smem, n);
+            st = large_eigh<float, false, false>(s.sol, n, smem);
+        } else {
+            st = large_eigh<float, false, true>(s.sol, n, smem);
+        }
         lm_back(s, v, n);
         for (int i = tid; i < n; i += nt) {
             float acc = 0.f;
@@ -1246,7 +1454,10 @@ int large_ctas_per_sm(int n, int precision) {
 }
 
 // A persistent grid of SMs x large_ctas_per_sm(n, precision) CTAs, at most
-// one per matrix.
+// one per matrix.  (Spreading the matrices evenly over fewer CTAs to avoid
+// a short last round was measured slower: a snapshot's time is set by
+// latency, not by how many CTAs share the SM, so more resident matrices
+// win.)
 int large_grid(int batch, int n, int precision) {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) != cudaSuccess ||
