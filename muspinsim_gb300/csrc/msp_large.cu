@@ -704,28 +704,58 @@ __device__ __forceinline__ u64 lm_anchor(float bound) {
     return f32x2(K, K);
 }
 
-// Anchored double-word product-sum step: (s1 + i s2) += a * b for a complex
-// a = (a.x, a.y) (+ lo (a.z, a.w) when ALO) and b = (b.x, b.y) (+ lo (b.z,
-// b.w) when BLO); s1 = sum Re(a) b and s2 = sum Im(a) b on the two lanes
-// (the product is s1 + i s2), rounding errors into c1, c2.
+// Anchored double-word product-sum step for one complex product a b:
+// ah = (a.re, a.im) as stored (one 64-bit register pair), bx = (b.re,
+// b.re), by = (b.im, b.im) (duplicated once per k and shared by a
+// thread's four outputs):
+//   S1 += ah bx = (a.re b.re, a.im b.re),  S2 += ah by = (a.re b.im, a.im b.im),
+// so that a b = S1 + i S2 (lane-wise: re = S1.x - S2.y, im = S1.y + S2.x)
+// and conj(a) b = conj(S1) + i conj(S2); rounding errors into c1, c2.  The
+// lo parts: al (A's, ALO) times bx, by; ah times blx, bly (B's, BLO).
 template <bool ALO, bool BLO>
-__device__ __forceinline__ void lm_step(u64 &s1, u64 &c1, u64 &s2, u64 &c2, float4 a, float4 b) {
-    const u64 R = f32x2(a.x, a.x), I = f32x2(a.y, a.y), bh = f32x2(b.x, b.y);
-    const u64 t1 = fma_f32x2(R, bh, s1);
-    const u64 t2 = fma_f32x2(I, bh, s2);
-    c1 = add2(c1, fma_f32x2(R, bh, sub2(s1, t1)));
-    c2 = add2(c2, fma_f32x2(I, bh, sub2(s2, t2)));
+__device__ __forceinline__ void lm_step(u64 &s1, u64 &c1, u64 &s2, u64 &c2, u64 ah, u64 al, u64 bx,
+                                        u64 by, u64 blx, u64 bly) {
+    const u64 t1 = fma_f32x2(ah, bx, s1);
+    const u64 t2 = fma_f32x2(ah, by, s2);
+    c1 = add2(c1, fma_f32x2(ah, bx, sub2(s1, t1)));
+    c2 = add2(c2, fma_f32x2(ah, by, sub2(s2, t2)));
     s1 = t1;
     s2 = t2;
     if (BLO) {
-        const u64 bl = f32x2(b.z, b.w);
-        c1 = fma_f32x2(R, bl, c1);
-        c2 = fma_f32x2(I, bl, c2);
+        c1 = fma_f32x2(ah, blx, c1);
+        c2 = fma_f32x2(ah, bly, c2);
     }
     if (ALO) {
-        c1 = fma_f32x2(f32x2(a.z, a.z), bh, c1);
-        c2 = fma_f32x2(f32x2(a.w, a.w), bh, c2);
+        c1 = fma_f32x2(al, bx, c1);
+        c2 = fma_f32x2(al, by, c2);
     }
+}
+
+// (re, im) -> (re, -im) on a lane pair: the sign bit of the upper lane
+__device__ __forceinline__ u64 lm_conj2(u64 v) { return v ^ 0x8000000000000000ull; }
+
+// The double-word value of an anchored sum pair (a b, or conj(a) b when
+// CONJ), anchor K removed: (re_hi, im_hi, re_lo, im_lo).
+template <bool CONJ>
+__device__ __forceinline__ float4 lm_dw(u64 s1, u64 c1, u64 s2, u64 c2, u64 K) {
+    s1 = sub2(s1, K);  // exact
+    s2 = sub2(s2, K);
+    if (CONJ) {
+        s1 = lm_conj2(s1);
+        c1 = lm_conj2(c1);
+        s2 = lm_conj2(s2);
+        c2 = lm_conj2(c2);
+    }
+    return dw_finish(s1, c1, s2, c2);
+}
+
+// The FP32 value of a plain sum pair (a b, or conj(a) b when CONJ).
+template <bool CONJ>
+__device__ __forceinline__ cx<float> lm_plain(u64 s1, u64 s2) {
+    float ax, ay, bx, by;
+    split_f32x2(s1, ax, ay);
+    split_f32x2(s2, bx, by);
+    return CONJ ? mk<float>(ax + by, bx - ay) : mk<float>(ax - by, ay + bx);
 }
 
 // Asynchronous global -> shared copies of one element (8 or 16 bytes);
@@ -753,8 +783,16 @@ __device__ __forceinline__ void lm_cp(float2 *dst, const float2 *src, bool valid
 __device__ __forceinline__ void lm_cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void lm_cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
-__device__ __forceinline__ float4 lm_f4(float4 a) { return a; }
-__device__ __forceinline__ float4 lm_f4(float2 a) { return make_float4(a.x, a.y, 0.f, 0.f); }
+// A stored element as its hi and lo lane pairs (lo = 0 for FP32 elements)
+__device__ __forceinline__ void lm_pairs(const float4 *p, u64 &h, u64 &l) {
+    const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(p);
+    h = v.x;
+    l = v.y;
+}
+__device__ __forceinline__ void lm_pairs(const float2 *p, u64 &h, u64 &l) {
+    h = *reinterpret_cast<const u64 *>(p);
+    l = 0ull;
+}
 
 // Tiled product C(i, j) = sum_k op(A)(i, k) B(k, j), i < M, j < N, k < K,
 // as one CTA-wide kernel body.  The CTA walks output tiles of TR = 4 x
@@ -768,8 +806,9 @@ __device__ __forceinline__ float4 lm_f4(float2 a) { return make_float4(a.x, a.y,
 //   LM_DW_ALO   anchored double-word, A double-word (float4), B FP32
 //   LM_DW_CBLO  anchored double-word, conj(A) FP32, B double-word
 //   LM_DW_C     anchored double-word, conj(A) and B FP32
-//   LM_PLAIN    FP32, (s1) += A B
-//   LM_PLAIN_C  FP32, (s1) += conj(A) B
+//   LM_PLAIN    FP32 sums of A B
+//   LM_PLAIN_C  FP32 sums of conj(A) B
+// (the pair (s1, s2) of lm_step; lm_dw / lm_plain turn it into the value).
 // skip(i0, j0) drops a whole tile; init(i, j, s1, c1, s2, c2) seeds an
 // accumulator (the anchor, or a start value); epi(i, j, s1, c1, s2, c2)
 // consumes it (i < M, j < N only).
@@ -824,22 +863,32 @@ __device__ void lm_tiles(int M, int N, int K, const AT *__restrict__ Ag, int lda
             const BT *Bs = reinterpret_cast<const BT *>(B0 + (sl & 1) * stage);
 #pragma unroll 4
             for (int k = 0; k < LM_KT; ++k) {
-                const float4 b = lm_f4(Bs[k * 32 + lane]);
+                u64 bh, bl;
+                lm_pairs(Bs + k * 32 + lane, bh, bl);
+                float b0, b1;
+                split_f32x2(bh, b0, b1);
+                const u64 bx = f32x2(b0, b0), by = f32x2(b1, b1);
+                u64 blx = 0ull, bly = 0ull;
+                if (ACC == LM_DW_CBLO) {
+                    split_f32x2(bl, b0, b1);
+                    blx = f32x2(b0, b0);
+                    bly = f32x2(b1, b1);
+                }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const int r = 4 * w + q;
-                    float4 a = lm_f4(As[A_KI ? k * TR + r : r * LM_KT + k]);
-                    if (ACC == LM_DW_CBLO || ACC == LM_DW_C || ACC == LM_PLAIN_C) a.y = -a.y;
+                    u64 ah, al;
+                    lm_pairs(As + (A_KI ? k * TR + r : r * LM_KT + k), ah, al);
                     if (ACC == LM_DW_ALO) {
-                        lm_step<true, false>(s1[q], c1[q], s2[q], c2[q], a, b);
+                        lm_step<true, false>(s1[q], c1[q], s2[q], c2[q], ah, al, bx, by, 0ull, 0ull);
                     } else if (ACC == LM_DW_CBLO) {
-                        lm_step<false, true>(s1[q], c1[q], s2[q], c2[q], a, b);
+                        lm_step<false, true>(s1[q], c1[q], s2[q], c2[q], ah, 0ull, bx, by, blx, bly);
                     } else if (ACC == LM_DW_C) {
-                        lm_step<false, false>(s1[q], c1[q], s2[q], c2[q], a, b);
+                        lm_step<false, false>(s1[q], c1[q], s2[q], c2[q], ah, 0ull, bx, by, 0ull,
+                                              0ull);
                     } else {
-                        // (re, im) += (a.re, a.re) (b.re, b.im) + (a.im, a.im) (-b.im, b.re)
-                        s1[q] = fma_f32x2(f32x2(a.x, a.x), f32x2(b.x, b.y), s1[q]);
-                        s1[q] = fma_f32x2(f32x2(a.y, a.y), f32x2(-b.y, b.x), s1[q]);
+                        s1[q] = fma_f32x2(ah, bx, s1[q]);
+                        s2[q] = fma_f32x2(ah, by, s2[q]);
                     }
                 }
             }
@@ -854,11 +903,6 @@ __device__ void lm_tiles(int M, int N, int K, const AT *__restrict__ Ag, int lda
     __syncthreads();
 }
 
-__device__ __forceinline__ cx<float> lm_plain(u64 acc) {
-    float re, im;
-    split_f32x2(acc, re, im);
-    return mk<float>(re, im);
-}
 
 // The four products of a refinement step (n x n):
 //   Y = H X (H double-word), S = X^H Y (Y double-word), G = X^H X, and
@@ -889,7 +933,7 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
             },
             [&](int i, int j, u64 s1, u64 c1, u64 s2, u64 c2) {
                 const u64 K = lm_anchor(bound(i, j));
-                s.Y[(size_t)i * n + j] = dw_finish(sub2(s1, K), c1, sub2(s2, K), c2);
+                s.Y[(size_t)i * n + j] = lm_dw<false>(s1, c1, s2, c2, K);
             });
     } else if (MODE == LM_S) {
         auto bound = [&](int i, int j) { return v.cn[min(i, n - 1)] * v.yn[min(j, n - 1)]; };
@@ -900,7 +944,7 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
             },
             [&](int i, int j, u64 s1, u64 c1, u64 s2, u64 c2) {
                 const u64 K = lm_anchor(bound(i, j));
-                const float4 r = dw_finish(sub2(s1, K), c1, sub2(s2, K), c2);
+                const float4 r = lm_dw<true>(s1, c1, s2, c2, K);
                 if (i == j)
                     v.sd[i] = (double)r.x + (double)r.z;
                 else if (i < j)
@@ -915,7 +959,7 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
             },
             [&](int i, int j, u64 s1, u64 c1, u64 s2, u64 c2) {
                 const u64 K = lm_anchor(bound(i, j));
-                const float4 r = dw_finish(sub2(s1, K), c1, sub2(s2, K), c2);
+                const float4 r = lm_dw<true>(s1, c1, s2, c2, K);
                 if (i == j)
                     v.rd[i] = (1.0 - (double)r.x) - (double)r.z;
                 else if (i < j)
@@ -928,7 +972,9 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
                 const cx<float> x = i < n && j < n ? X[(size_t)i * n + j] : mk<float>(0.f, 0.f);
                 s1 = f32x2(x.re, x.im);
             },
-            [&](int i, int j, u64 s1, u64, u64, u64) { X2[(size_t)i * n + j] = lm_plain(s1); });
+            [&](int i, int j, u64 s1, u64, u64 s2, u64) {
+                X2[(size_t)i * n + j] = lm_plain<false>(s1, s2);
+            });
     }
 }
 
@@ -971,8 +1017,8 @@ __device__ void lm_back(const LargeMixed &s, const LmVec &v, int n) {
         __syncthreads();
         // V^H V
         lm_tiles<LM_PLAIN_C, true>(nb, nb, m, Vb, LM_KT, Vb, LM_KT, v, noskip, zero,
-                                   [&](int i, int j, u64 s1, u64, u64, u64) {
-                                       Gs[i * LM_KT + j] = lm_plain(s1);
+                                   [&](int i, int j, u64 s1, u64, u64 s2, u64) {
+                                       Gs[i * LM_KT + j] = lm_plain<true>(s1, s2);
                                    });
         // T, one column at a time (nb <= 16 threads per column)
         for (int i = 0; i < nb; ++i) {
@@ -995,8 +1041,8 @@ __device__ void lm_back(const LargeMixed &s, const LmVec &v, int n) {
         // W = V^H U_b
         cx<float> *Ub = U + (size_t)(kb + 1) * n;
         lm_tiles<LM_PLAIN_C, true>(nb, n, m, Vb, LM_KT, reinterpret_cast<const float2 *>(Ub), n, v,
-                                   noskip, zero, [&](int i, int j, u64 s1, u64, u64, u64) {
-                                       const cx<float> r = lm_plain(s1);
+                                   noskip, zero, [&](int i, int j, u64 s1, u64, u64 s2, u64) {
+                                       const cx<float> r = lm_plain<true>(s1, s2);
                                        W[(size_t)i * n + j] = make_float2(r.re, r.im);
                                    });
         // W2 = -T W
@@ -1017,7 +1063,9 @@ __device__ void lm_back(const LargeMixed &s, const LmVec &v, int n) {
                 const cx<float> u = i < m && j < n ? Ub[(size_t)i * n + j] : mk<float>(0.f, 0.f);
                 s1 = f32x2(u.re, u.im);
             },
-            [&](int i, int j, u64 s1, u64, u64, u64) { Ub[(size_t)i * n + j] = lm_plain(s1); });
+            [&](int i, int j, u64 s1, u64, u64 s2, u64) {
+                Ub[(size_t)i * n + j] = lm_plain<false>(s1, s2);
+            });
     }
 }
 
@@ -1278,7 +1326,9 @@ __device__ void lm_tridiag(const LargeMixed &s, const LmVec &vv, char *smem, int
                     const cx<float> a = i < mt && j < mt ? At[(size_t)i * n + j] : mk<float>(0.f, 0.f);
                     s1 = f32x2(a.re, a.im);
                 },
-                [&](int i, int j, u64 s1, u64, u64, u64) { At[(size_t)i * n + j] = lm_plain(s1); });
+                [&](int i, int j, u64 s1, u64, u64 s2, u64) {
+                    At[(size_t)i * n + j] = lm_plain<false>(s1, s2);
+                });
         }
     }
     if (tid == 0) {
@@ -1368,9 +1418,9 @@ __global__ void __maxnreg__(96) msp_large_fast_mixed_kernel(SnapArgs a, char *sc
             n, n, n, reinterpret_cast<const float2 *>(X), n, reinterpret_cast<const float2 *>(X2),
             n, v, [](int i0, int j0) { return i0 + 4 * (int)(blockDim.x >> 5) - 1 < j0; },
             [](int, int, u64 &, u64 &, u64 &, u64 &) {},
-            [&](int j, int k, u64 s1, u64, u64, u64) {
+            [&](int j, int k, u64 s1, u64, u64 s2, u64) {
                 if (j < k) return;
-                const cx<float> G = lm_plain(s1);
+                const cx<float> G = lm_plain<true>(s1, s2);
                 const double Am = (double)(G.re * G.re + G.im * G.im);
                 if (j == k)
                     diag += Am;
