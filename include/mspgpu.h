@@ -50,7 +50,7 @@ extern "C" {
 #define MSP_MODE_INTEGRAL 2 /* exponentially weighted time integral */
 
 #define MSP_MAX_DIM 64   /* largest Hilbert dimension of the Jacobi kernels */
-#define MSP_MAX_DIM_LARGE 1024 /* largest n of the Householder + QL path (FP64) */
+#define MSP_MAX_DIM_LARGE 1024 /* largest n of the Householder + QL path */
 #define MSP_MAX_SPINS 16
 
 /* ---- library information ---------------------------------------------- */
@@ -108,9 +108,9 @@ int msp_eigh_batched_ws(const double *H, int n, int batch, int precision, int ma
                         size_t workspace_bytes, void *stream);
 
 /* out[b] = U[b]^dag M[b] U[b]  (adjoint = 0)  or  U[b] M[b] U[b]^dag
- * (adjoint = 1).  m_stride = complex elements between consecutive M
- * matrices (0 broadcasts one M), u_stride likewise for U.  Replaces
- * Operator.basis_change (muspinsim/spinop.py:330-355). */
+ * (adjoint = 1), 1 <= n <= MSP_MAX_DIM_LARGE.  m_stride = complex elements
+ * between consecutive M matrices (0 broadcasts one M), u_stride likewise
+ * for U.  Replaces Operator.basis_change (muspinsim/spinop.py:330-355). */
 int msp_basis_change(const double *U, long long u_stride, const double *M,
                      long long m_stride, int n, int batch, int adjoint, double *out,
                      void *stream);
@@ -122,7 +122,8 @@ int msp_fast_cos_sum(const double *times, int num_times, int other_dimension,
                      const double *A, const double *W, int n, double *out, void *stream);
 
 /* A = |U^dag (sigma (x) 1_d) U|^2, W = 2 pi (l_j - l_k); sigma: 2x2
- * complex128 (muon first).  Replaces muspinsim/hamiltonian.py:204-211. */
+ * complex128 (muon first), n <= MSP_MAX_DIM_LARGE.  Replaces
+ * muspinsim/hamiltonian.py:204-211. */
 int msp_fast_amplitudes(const double *evals, const double *evecs, const double *sigma,
                         int n, int other_dimension, double *A, double *W, void *stream);
 
@@ -189,7 +190,10 @@ int msp_timer_read(msp_timer *timer, double *ms, int *runs);
  * 358-382, 434-498; muspinsim/simconfig.py:347-368).  All pointers are
  * device pointers except where noted. */
 typedef struct msp_powder_args {
-    int n;                    /* Hilbert dimension, 2 .. MSP_MAX_DIM */
+    int n;                    /* Hilbert dimension, 2 .. MSP_MAX_DIM_LARGE; above
+                                 MSP_MAX_DIM the Householder + QL kernels run
+                                 (FAST: FP64, or FP32 + double-word refinement
+                                 for MIXED; EVOLVE / INTEGRAL: FP64) */
     int num_spins;            /* spins in the system, <= MSP_MAX_SPINS */
     int mu_index;             /* position of the muon in the spin order */
     int dims[MSP_MAX_SPINS];  /* per-spin multiplicity 2I+1 (host values) */

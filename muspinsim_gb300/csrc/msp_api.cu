@@ -120,8 +120,9 @@ int msp_basis_change(const double *U, long long u_stride, const double *M, long 
                      int n, int batch, int adjoint, double *out, void *stream) {
     if (n < 1 || batch < 0 || u_stride < 0 || m_stride < 0)
         return fail(MSP_ERR_ARG, "msp_basis_change: n=%d batch=%d", n, batch);
-    if (n > MSP_MAX_DIM)
-        return fail(MSP_ERR_UNSUPPORTED, "msp_basis_change: n=%d exceeds %d", n, MSP_MAX_DIM);
+    if (n > MSP_MAX_DIM_LARGE)
+        return fail(MSP_ERR_UNSUPPORTED, "msp_basis_change: n=%d exceeds %d", n,
+                    MSP_MAX_DIM_LARGE);
     if (batch == 0) return MSP_OK;
     MSP_CHECK_PTR(U);
     MSP_CHECK_PTR(M);
@@ -151,8 +152,9 @@ int msp_fast_amplitudes(const double *evals, const double *evecs, const double *
     if (n < 2 || other_dimension < 1 || 2 * other_dimension != n)
         return fail(MSP_ERR_ARG, "msp_fast_amplitudes: n=%d d=%d (need n = 2 d)", n,
                     other_dimension);
-    if (n > MSP_MAX_DIM)
-        return fail(MSP_ERR_UNSUPPORTED, "msp_fast_amplitudes: n=%d exceeds %d", n, MSP_MAX_DIM);
+    if (n > MSP_MAX_DIM_LARGE)
+        return fail(MSP_ERR_UNSUPPORTED, "msp_fast_amplitudes: n=%d exceeds %d", n,
+                    MSP_MAX_DIM_LARGE);
     MSP_CHECK_PTR(evals);
     MSP_CHECK_PTR(evecs);
     MSP_CHECK_PTR(sigma);
@@ -277,15 +279,18 @@ struct Layout {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Complex entries of rho0's Kronecker factors (sum of dims^2).
+static int powder_fac_len(const msp_powder_args *a) {
+    int fac = 0;
+    for (int s = 0; s < a->num_spins; ++s) fac += a->dims[s] * a->dims[s];
+    return fac;
+}
+
 static int check_powder(const msp_powder_args *a) {
     if (a == NULL) return fail(MSP_ERR_ARG, "msp_powder: args is NULL");
     if (a->n < 2) return fail(MSP_ERR_ARG, "msp_powder: n=%d", a->n);
     if (a->n > MSP_MAX_DIM_LARGE)
         return fail(MSP_ERR_UNSUPPORTED, "msp_powder: n=%d exceeds %d", a->n, MSP_MAX_DIM_LARGE);
-    if (a->n > MSP_MAX_DIM && a->mode != MSP_MODE_FAST)
-        return fail(MSP_ERR_UNSUPPORTED,
-                    "msp_powder: n=%d > %d runs the fast path only (muon first, T = inf)", a->n,
-                    MSP_MAX_DIM);
     if (a->num_snap < 0 || a->num_slots < 1)
         return fail(MSP_ERR_ARG, "msp_powder: num_snap=%d num_slots=%d", a->num_snap,
                     a->num_slots);
@@ -352,9 +357,14 @@ static Layout powder_layout(const msp_powder_args *a) {
     L.partial = off;
     off += align256((size_t)L.max_items * L.T * (L.phase_records ? 4 : 8));
     L.large = off;
-    if (a->n > MSP_MAX_DIM)
-        off += align256(large_scratch_bytes(a->n, large_grid(a->num_snap, a->n, a->precision),
-                                            a->precision));
+    if (a->n > MSP_MAX_DIM) {
+        if (a->mode == MSP_MODE_FAST)
+            off += align256(large_scratch_bytes(
+                a->n, large_grid(a->num_snap, a->n, a->precision), a->precision));
+        else
+            off += align256(large_rho_scratch_bytes(
+                a->n, large_rho_grid(a->num_snap, a->n, powder_fac_len(a))));
+    }
     L.total = off;
     return L;
 }
@@ -436,11 +446,16 @@ int msp_powder_run(const msp_powder_args *a) {
 
     cudaEvent_t *ev = timer_slot(a->timer);
     if (ev) cudaEventRecord(ev[0], st);
-    if (large && a->num_snap > 0)
+    if (large && a->num_snap > 0 && a->mode == MSP_MODE_FAST)
         rc = cuda_check(launch_large_fast(sa, reinterpret_cast<double *>(ws + L.large),
                                           large_grid(a->num_snap, a->n, a->precision), st, 0,
                                           a->precision),
                         "msp_large_fast");
+    else if (large && a->num_snap > 0)
+        rc = cuda_check(launch_large_rho(sa, reinterpret_cast<double *>(ws + L.large),
+                                         large_rho_grid(a->num_snap, a->n, sa.fac_len), st,
+                                         a->mode == MSP_MODE_INTEGRAL),
+                        "msp_large_rho");
     else
         rc = cuda_check(launch_snapshots(sa, a->mode, a->precision, st), "msp_snap");
     if (rc != MSP_OK) return rc;

@@ -162,6 +162,11 @@ int large_threads(int n);
 size_t large_scratch_bytes(int n, int grid, int precision = MSP_PREC_FP64);
 int large_ctas_per_sm(int n, int precision = MSP_PREC_FP64);
 int large_grid(int batch, int n, int precision = MSP_PREC_FP64);
+// General path for n > 64 (EVOLVE / INTEGRAL, FP64 in both precisions).
+cudaError_t launch_large_rho(const SnapArgs &a, double *scratch, int grid, cudaStream_t st,
+                             int integral);
+size_t large_rho_scratch_bytes(int n, int grid);
+int large_rho_grid(int batch, int n, int fac_len);
 
 // Work decomposition of the phase sum (host side).  A work item sums at
 // most MSP_F32_ITEM_PAIRS pairs in FP32 (mixed precision): longer FP32

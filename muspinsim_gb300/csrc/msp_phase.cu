@@ -1007,9 +1007,44 @@ __global__ void msp_fast_amplitudes_kernel(const double *__restrict__ evals,
     }
 }
 
+// n > 64: one CTA per column k from global memory: (sigma (x) 1_d) U[:, k]
+// staged in shared memory, then A_jk, W_jk for every j.
+__global__ void msp_fast_amplitudes_col_kernel(const double *__restrict__ evals,
+                                               const cx<double> *__restrict__ U,
+                                               const cx<double> *__restrict__ sig, int n, int d,
+                                               double *__restrict__ A, double *__restrict__ W) {
+    extern __shared__ __align__(16) char smem[];
+    cx<double> *uc = reinterpret_cast<cx<double> *>(smem);
+    cx<double> *wc = uc + n;
+    const int k = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+    for (int i = tid; i < n; i += nt) uc[i] = U[(size_t)i * n + k];
+    __syncthreads();
+    const cx<double> s00 = sig[0], s01 = sig[1], s10 = sig[2], s11 = sig[3];
+    for (int i = tid; i < n; i += nt)
+        wc[i] = i < d ? cadd(cmul(s00, uc[i]), cmul(s01, uc[i + d]))
+                      : cadd(cmul(s10, uc[i - d]), cmul(s11, uc[i]));
+    __syncthreads();
+    for (int j = tid; j < n; j += nt) {
+        double gr = 0, gi = 0;
+        for (int i = 0; i < n; ++i) {
+            const cx<double> u = U[(size_t)i * n + j], mm = wc[i];
+            gr += u.re * mm.re + u.im * mm.im;
+            gi += u.re * mm.im - u.im * mm.re;
+        }
+        A[(size_t)j * n + k] = gr * gr + gi * gi;
+        W[(size_t)j * n + k] = 6.283185307179586476925 * (evals[j] - evals[k]);
+    }
+}
+
 cudaError_t launch_fast_amplitudes(const double *evals, const double *evecs,
                                    const double *sigma, int n, int d, double *A, double *W,
                                    cudaStream_t st) {
+    if (n > MSP_MAX_DIM) {
+        msp_fast_amplitudes_col_kernel<<<n, 256, (size_t)2 * n * sizeof(cx<double>), st>>>(
+            evals, reinterpret_cast<const cx<double> *>(evecs),
+            reinterpret_cast<const cx<double> *>(sigma), n, d, A, W);
+        return cudaGetLastError();
+    }
     const size_t smem = (size_t)2 * n * n * sizeof(cx<double>);
     cudaError_t e = cudaFuncSetAttribute(msp_fast_amplitudes_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -827,9 +827,76 @@ __global__ void msp_basis_change_kernel(const cx<double> *__restrict__ U, long l
     }
 }
 
+// n > 64: the same product from global memory in two launches, one CTA
+// per (column j, matrix): T = M op(U) into out (op(U) = U, or U^dag when
+// adjoint), then out = op'(U) T (op'(U) = U^dag, or U).  Each CTA first
+// stages its column (of op(U), then of T) in shared memory, so the second
+// pass overwrites column j in place.
+__global__ void msp_basis_change_col1_kernel(const cx<double> *__restrict__ U, long long u_stride,
+                                             const cx<double> *__restrict__ M, long long m_stride,
+                                             int n, int adjoint, int b0,
+                                             cx<double> *__restrict__ out) {
+    extern __shared__ __align__(16) char smem[];
+    cx<double> *col = reinterpret_cast<cx<double> *>(smem);
+    const int j = blockIdx.x, b = b0 + blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+    const cx<double> *Ub = U + (size_t)b * u_stride;
+    const cx<double> *Mb = M + (size_t)b * m_stride;
+    cx<double> *Ob = out + (size_t)b * n * n;
+    for (int l = tid; l < n; l += nt)
+        col[l] = adjoint ? conj(Ub[(size_t)j * n + l]) : Ub[(size_t)l * n + j];
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+        const cx<double> *row = Mb + (size_t)i * n;
+        double tr = 0, ti = 0;
+        for (int l = 0; l < n; ++l) {
+            const cx<double> mv = row[l], uv = col[l];
+            tr += mv.re * uv.re - mv.im * uv.im;
+            ti += mv.re * uv.im + mv.im * uv.re;
+        }
+        Ob[(size_t)i * n + j] = mk<double>(tr, ti);
+    }
+}
+
+__global__ void msp_basis_change_col2_kernel(const cx<double> *__restrict__ U, long long u_stride,
+                                             int n, int adjoint, int b0,
+                                             cx<double> *__restrict__ out) {
+    extern __shared__ __align__(16) char smem[];
+    cx<double> *col = reinterpret_cast<cx<double> *>(smem);
+    const int j = blockIdx.x, b = b0 + blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+    const cx<double> *Ub = U + (size_t)b * u_stride;
+    cx<double> *Ob = out + (size_t)b * n * n;
+    for (int k = tid; k < n; k += nt) col[k] = Ob[(size_t)k * n + j];
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+        double tr = 0, ti = 0;
+        for (int k = 0; k < n; ++k) {
+            // row i of U^dag = conj(U_ki); row i of U = U_ik
+            const cx<double> uv = adjoint ? Ub[(size_t)i * n + k] : conj(Ub[(size_t)k * n + i]);
+            const cx<double> tv = col[k];
+            tr += uv.re * tv.re - uv.im * tv.im;
+            ti += uv.re * tv.im + uv.im * tv.re;
+        }
+        Ob[(size_t)i * n + j] = mk<double>(tr, ti);
+    }
+}
+
 cudaError_t launch_basis_change(const double *U, long long u_stride, const double *M,
                                 long long m_stride, int n, int batch, int adjoint, double *out,
                                 cudaStream_t st) {
+    if (n > MSP_MAX_DIM) {
+        const size_t smem = (size_t)n * sizeof(cx<double>);
+        const cx<double> *Uc = reinterpret_cast<const cx<double> *>(U);
+        cx<double> *Oc = reinterpret_cast<cx<double> *>(out);
+        for (int b0 = 0; b0 < batch; b0 += 65535) {
+            const dim3 grid(n, batch - b0 < 65535 ? batch - b0 : 65535);
+            msp_basis_change_col1_kernel<<<grid, 256, smem, st>>>(
+                Uc, u_stride, reinterpret_cast<const cx<double> *>(M), m_stride, n, adjoint, b0,
+                Oc);
+            msp_basis_change_col2_kernel<<<grid, 256, smem, st>>>(Uc, u_stride, n, adjoint, b0,
+                                                                  Oc);
+        }
+        return cudaGetLastError();
+    }
     const size_t smem = (size_t)3 * n * n * sizeof(cx<double>);
     cudaError_t e = cudaFuncSetAttribute(msp_basis_change_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -167,3 +167,46 @@ def test_run_single_matches_batched():
     for snap in er.config:
         acc += er.run_single(snap) / er.config.avg_N
     assert np.abs(acc - batched).max() <= FP64_TOL
+
+
+# ---- n > 64 (Householder + QL; global-memory basis changes)
+
+def test_direct_api_large_against_oracle():
+    """Hamiltonian.evolve / integrate_decaying / fast_evolve at n = 96
+    (mu, e, 1H x 3, 14N dimensions) against the oracle's numpy
+    restatement."""
+    from oracle import port
+    from muspinsim_gb300.hamiltonian import Hamiltonian
+    from muspinsim_gb300.spinop import DensityOperator, SpinOperator
+    from tests.helpers import random_hermitian
+
+    rng = np.random.default_rng(960)
+    dims = (2, 2, 2, 2, 2, 3)
+    n = int(np.prod(dims))
+    # spectral width ~ 60 MHz and unit-norm operators, as for spin systems
+    Hm = random_hermitian(rng, n)
+    Hm *= 30.0 / np.abs(np.linalg.eigvalsh(Hm)).max()
+    R = random_hermitian(rng, n)
+    rho = R @ R.conj().T
+    rho /= np.trace(rho).real
+    ops = [o / np.abs(np.linalg.eigvalsh(o)).max()
+           for o in (random_hermitian(rng, n), random_hermitian(rng, n))]
+    t = np.linspace(0.0, 2.0, 37)
+    H = Hamiltonian(Hm, dim=dims)
+    rho0 = DensityOperator(rho, dims)
+    sops = [SpinOperator(o, dim=dims) for o in ops]
+    ev = H.evolve(rho0, t, sops)
+    assert ev.shape == (len(t), 2)
+    assert np.abs(ev - port.evolve(Hm, rho, t, ops)).max() <= FP64_TOL
+    dens = H.evolve(rho0, t[:3])
+    assert len(dens) == 3
+    evals, U = np.linalg.eigh(Hm)
+    for k in range(3):
+        ph = np.exp(-2j * np.pi * np.subtract.outer(evals, evals) * t[k])
+        want = U @ ((U.conj().T @ rho @ U) * ph) @ U.conj().T
+        assert np.abs(dens[k].matrix.toarray() - want).max() <= FP64_TOL
+    integ = H.integrate_decaying(rho0, 2.19703, sops)
+    assert np.abs(integ - port.integrate_decaying(Hm, rho, 2.19703, ops)).max() <= FP64_TOL
+    sig = port.sigma_mu([0.3, 0.4, np.sqrt(0.75)])
+    fast = H.fast_evolve(sig, t, n // 2)
+    assert np.abs(fast - port.fast_evolve(Hm, sig, t, n // 2)).max() <= FP64_TOL

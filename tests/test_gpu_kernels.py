@@ -456,3 +456,34 @@ def test_assemble_rotated_vs_host_and_field_rotation(K):
         lam_rot = np.linalg.eigvalsh(H[s] + np.einsum("a,aij->ij", B, Z))
         lam_fld = np.linalg.eigvalsh(Hsys + np.einsum("a,aij->ij", Rs[s].T @ B, Z))
         assert np.abs(lam_rot - lam_fld).max() <= 1e-10 * np.abs(lam_fld).max()
+
+
+def test_powder_general_path_large():
+    """The n > 64 general path (finite temperature, muon not first, decay
+    integrals) at n = 96 in both precisions against the oracle."""
+    from muspinsim_gb300 import workloads
+
+    wl = _large_workload(n_orient=3, n_times=200)
+    ref = oracle_powder(wl, temperature=5.0)
+    assert np.abs(_gpu_powder(wl, temperature=5.0) - ref).max() <= FP64_TOL
+    assert np.abs(_gpu_powder(wl, "mixed", temperature=5.0) - ref).max() <= MIXED_TOL
+    # electron first, muon second: the general path at T = inf
+    rng = np.random.default_rng(97)
+    coup = [("hyperfine", {"i": 2, "j": 1}, workloads.random_hyperfine(rng))]
+    for i in (3, 4, 5):
+        coup.append(("dipolar", {"i": 2, "j": i}, workloads.random_vector(rng, 1.0, 2.0)))
+    coup.append(("quadrupolar", {"i": 6}, workloads.random_efg(rng)))
+    wl2 = workloads.Workload(
+        name="e_mu_3H_N_dim96", spins=["e", "mu", "H", "H", "H", "N"], couplings=coup,
+        orientations=workloads.zcw_gen(3), fields=np.array([[0.0, 0.0, 0.005]]),
+        polarization=np.array([1.0, 0.0, 0.0]), times=np.linspace(0, 5, 150))
+    ref2 = oracle_powder(wl2)
+    assert np.abs(_gpu_powder(wl2) - ref2).max() <= FP64_TOL
+    assert np.abs(_gpu_powder(wl2, "mixed") - ref2).max() <= MIXED_TOL
+    # decay integrals over a field scan
+    for B in ([0.0, 0.0, 0.02], [0.0, 0.0, 0.3]):
+        refi = oracle_powder(wl, field=np.array(B), y_axis="integral")
+        got = _gpu_powder(wl, field=np.array(B), y_axis="integral")
+        assert abs(got - refi) <= FP64_TOL
+        got_m = _gpu_powder(wl, "mixed", field=np.array(B), y_axis="integral")
+        assert abs(got_m - refi) <= MIXED_TOL

@@ -297,11 +297,12 @@ def test_capi_library_exports_header():
     nbytes = ctypes.c_size_t(0)
     assert lib.msp_powder_workspace(ctypes.byref(a), ctypes.byref(nbytes)) == _lib.MSP_ERR_UNSUPPORTED
     assert "exceeds" in _lib.last_error()
-    # n > 64 runs the fast path only
+    # n > 64 takes every mode: the size passes, the next check (no output
+    # rows) fails
     a.n = 200
     a.mode = _lib.MODE_EVOLVE
-    assert lib.msp_powder_workspace(ctypes.byref(a), ctypes.byref(nbytes)) == _lib.MSP_ERR_UNSUPPORTED
-    assert "fast path only" in _lib.last_error()
+    assert lib.msp_powder_workspace(ctypes.byref(a), ctypes.byref(nbytes)) == _lib.MSP_ERR_ARG
+    assert "num_slots" in _lib.last_error()
     assert ctypes.sizeof(_lib.PowderArgs) > 0
 
 
