@@ -487,3 +487,25 @@ def test_powder_general_path_large():
         assert abs(got - refi) <= FP64_TOL
         got_m = _gpu_powder(wl, "mixed", field=np.array(B), y_axis="integral")
         assert abs(got_m - refi) <= MIXED_TOL
+
+
+def test_powder_fast_large_dim512():
+    """mu, e and seven protons (n = 512): the large-n kernels well above the
+    heterogeneous batch's sizes (32 tridiagonalisation panels and
+    reflector blocks, 16 x 32 refinement tiles), both precisions."""
+    from muspinsim_gb300 import workloads
+
+    rng = np.random.default_rng(512)
+    spins = ["mu", "e"] + ["H"] * 7
+    coup = [("hyperfine", {"i": 1}, workloads.random_hyperfine(rng))]
+    for i in range(3, 10):
+        coup.append(("hyperfine", {"i": i}, workloads.random_hyperfine(rng) * 0.05))
+        coup.append(("dipolar", {"i": 1, "j": i}, workloads.random_vector(rng, 1.0, 3.0)))
+    wl = workloads.Workload(
+        name="mu_e_7H_dim512", spins=spins, couplings=coup, orientations=workloads.zcw_gen(2),
+        fields=np.array([[0.0, 0.0, 0.01]]), polarization=np.array([0.0, 0.0, 1.0]),
+        times=np.linspace(0.0, 10.0, 60))
+    assert int(np.prod(wl.system().dimension)) == 512
+    ref = oracle_powder(wl)
+    assert np.abs(_gpu_powder(wl) - ref).max() <= FP64_TOL
+    assert np.abs(_gpu_powder(wl, "mixed") - ref).max() <= MIXED_TOL
