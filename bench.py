@@ -71,6 +71,10 @@ def parse_args():
                         "5: dim 65536 from global memory)")
     p.add_argument("--celio-states", type=int, default=19,
                    help="celio workload: random states per orientation")
+    p.add_argument("--c4-systems", type=int, default=512,
+                   help="config4: systems (the full configuration: 4096)")
+    p.add_argument("--c4-orientations", type=int, default=32,
+                   help="config4: orientations per system (the full configuration: 256)")
     p.add_argument("--workload", default="config2",
                    choices=["config1", "config2", "config3", "config4", "config5", "lindblad",
                             "celio"],
@@ -635,20 +639,22 @@ def run_config3(args, world, rank, local):
 def run_config4(args, world, rank, local):
     """Heterogeneous batch: spin systems of dimension 4 ... 192, one output
     row each, through msp_multi_run (size buckets, persistent launches,
-    concurrent streams, CUDA graph).  Scaled to 512 systems x 32
-    orientations (the 4,096 x 256 configuration has the same per-snapshot
-    mix; its n = 192 FP64 eigensolves alone take about two minutes)."""
+    concurrent streams, CUDA graph).  Scaled by default to 512 systems x 32
+    orientations (the 4,096 x 256 configuration, --c4-systems 4096
+    --c4-orientations 256, has the same per-snapshot mix: about 11 s per
+    step in mixed precision, two minutes in FP64; --fp64-steps 0 skips the
+    FP64 comparison)."""
     import torch
 
     from muspinsim_gb300 import workloads
     from muspinsim_gb300.multi import MultiSystemBatch
 
-    n_sys, n_or = 512, 32
+    n_sys, n_or = args.c4_systems, args.c4_orientations
     wls = workloads.config4(n_systems=n_sys, n_orient=n_or)
     systems = [w.system() for w in wls]
     T = len(wls[0].times)
     out = {}
-    for prec in ("mixed", "fp64"):
+    for prec in ("mixed", "fp64") if args.fp64_steps > 0 else ("mixed",):
         b = MultiSystemBatch(systems, wls[0].orientations, wls[0].fields[0],
                              wls[0].polarization, wls[0].times, precision=prec)
         b.run(graph=True)
@@ -658,17 +664,20 @@ def run_config4(args, world, rank, local):
         b.plan.close()
     ms, res, info = out["mixed"]
     samples = n_sys * n_or * T
-    dP = float((res - out["fp64"][1]).abs().max().item())
+    dP = float((res - out["fp64"][1]).abs().max().item()) if "fp64" in out else None
     buckets = [{k: bi[k] for k in ("n", "num_systems", "num_snap", "num_chunks",
                                     "snap_threads", "grid")} for bi in info]
+    cfg = {"systems": n_sys, "orientations": n_or, "times": T,
+           "dims": [4, 8, 12, 24, 48, 96, 192], "graph": True}
+    if (n_sys, n_or) != (4096, 256):
+        cfg["scaled_from"] = "4096 systems x 256"
     return _line("heterogeneous-batch P(t) samples/s, mixed precision", samples / (ms * 1e-3),
-                 "samples/s", ms, args, world, "4_to_192_dim_systems_512x32_orient_2048_t",
-                 {"systems": n_sys, "orientations": n_or, "times": T,
-                  "dims": [4, 8, 12, 24, 48, 96, 192], "scaled_from": "4096 systems x 256",
-                  "graph": True},
+                 "samples/s", ms, args, world,
+                 f"4_to_192_dim_systems_{n_sys}x{n_or}_orient_{T}_t", cfg,
                  dtype="f32 (Jacobi for n <= 64, Householder + QL for n > 64; double-word "
                        "refinement; phase sum)",
-                 fp64={"value": samples / (out["fp64"][0] * 1e-3), "ms_per_step": out["fp64"][0]},
+                 fp64=({"value": samples / (out["fp64"][0] * 1e-3),
+                        "ms_per_step": out["fp64"][0]} if "fp64" in out else None),
                  max_abs_dP_mixed_vs_fp64=dP, buckets=buckets)
 
 

@@ -20,6 +20,12 @@ from muspinsim_gb300.hamiltonian import Hamiltonian
 from muspinsim_gb300.spinop import Clonable, SpinOperator
 
 
+# Kronecker-embedded operators keyed by (quantum numbers, include_only_given,
+# axes per spin): many systems of a batch share their spins' structure.
+_EMBED_CACHE = {}
+_EMBED_CACHE_MAX = 65536
+
+
 class InteractionTerm(Clonable):
     """T_{ab...} S^a_i S^b_j ... (muspinsim/spinsys.py:22-92)."""
 
@@ -285,9 +291,23 @@ class SpinSystem(Clonable):
     def operator(self, terms=None, include_only_given=False):
         """Kronecker embedding of single-spin operators, spin 0 slowest
         (muspinsim/spinsys.py:545-592).  A list of axes for one index is
-        multiplied in order."""
+        multiplied in order.  The embedding depends only on the spins'
+        quantum numbers and the requested axes, so it is cached across
+        terms and systems (a copy is returned)."""
         if terms is None:
             terms = {}
+        key = (tuple(float(x) for x in self._Is), bool(include_only_given),
+               tuple(sorted((int(i), tuple(v) if isinstance(v, list) else v)
+                            for i, v in terms.items())))
+        hit = _EMBED_CACHE.get(key)
+        if hit is not None:
+            return hit.clone()
+        M = self._embed(terms, include_only_given)
+        if len(_EMBED_CACHE) < _EMBED_CACHE_MAX:
+            _EMBED_CACHE[key] = M.clone()
+        return M
+
+    def _embed(self, terms, include_only_given):
         ops = []
         for i in range(len(self)):
             spec = terms.get(i, None if include_only_given else "0")
