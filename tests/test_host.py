@@ -325,3 +325,44 @@ def test_rotation_basis_reproduces_rotated_hamiltonians():
         H = np.einsum("k,kij->ij", coef, B)
         ref = sy.rotate(R).hamiltonian_matrix()
         assert np.abs(H - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_capi_large_n_workspace_sizes():
+    """Workspace sizing of msp_powder_run for 64 < n through the C ABI (no
+    device needed: the occupancy query falls back to one CTA per SM): the
+    fast path's FP64 and mixed working sets, and the general path's (two
+    more n x n complex matrices per CTA) for EVOLVE and INTEGRAL."""
+    from muspinsim_gb300 import _lib
+
+    lib = _lib.load()
+    n = 96
+    a = _lib.PowderArgs()
+    a.n = n
+    a.num_spins = 6
+    a.mu_index = 0
+    for k, d in enumerate((2, 2, 2, 2, 2, 3)):
+        a.dims[k] = d
+    a.num_snap = 10
+    a.num_slots = 1
+    a.num_times = 8
+    a.uniform = 1
+    a.dt = 0.1
+    a.tau = 2.19703
+
+    def size(mode, prec):
+        a.mode, a.precision = mode, prec
+        nbytes = ctypes.c_size_t(0)
+        assert lib.msp_powder_workspace(ctypes.byref(a), ctypes.byref(nbytes)) == _lib.MSP_OK, \
+            _lib.last_error()
+        return nbytes.value
+
+    fast64 = size(_lib.MODE_FAST, _lib.PREC_FP64)
+    fastmx = size(_lib.MODE_FAST, _lib.PREC_MIXED)
+    evolve = size(_lib.MODE_EVOLVE, _lib.PREC_FP64)
+    integ = size(_lib.MODE_INTEGRAL, _lib.PREC_FP64)
+    per_fp64 = 5 * n * n * 8  # A, U (complex) and Zt per CTA
+    assert fast64 >= 10 * per_fp64
+    assert fastmx >= 10 * 56 * n * n  # double-word H and Y, X, X2, SR per CTA
+    # the general path adds two complex n x n matrices per CTA
+    assert evolve >= fast64 + 10 * 4 * n * n * 8 - 10 * 4096
+    assert integ >= 10 * (9 * n * n * 8)
