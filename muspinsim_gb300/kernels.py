@@ -327,6 +327,20 @@ class PowderPlan:
         a.wscale, a.slot = self.W.data_ptr(), self.Sl.data_ptr()
         return self
 
+    def fetch(self):
+        """The output and the per-snapshot status on the host after one
+        synchronisation: asynchronous copies into pinned staging buffers
+        kept with the plan.  Returns two numpy arrays (copies)."""
+        if getattr(self, "_host", None) is None:
+            self._host = (torch.empty(tuple(self.out.shape), dtype=torch.float64, pin_memory=True),
+                          torch.empty(tuple(self.status.shape), dtype=torch.int32,
+                                      pin_memory=True))
+        ho, hs = self._host
+        ho.copy_(self.out, non_blocking=True)
+        hs.copy_(self.status, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return ho.numpy().copy(), hs.numpy()[:self.num_snap].copy()
+
     def run(self, timer=None):
         """Enqueue the batch on the current stream; returns the output tensor."""
         self.args.stream = torch.cuda.current_stream().cuda_stream

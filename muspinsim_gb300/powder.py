@@ -70,16 +70,19 @@ def _cached_plan(system, Hs, Zd, n, F, Pl, W, slot, num_slots, times, mode, prec
             _PLANS[key] = plan
         return plan
     plan.rebind(F, Pl, W, slot)
-    uni, t0, dt = kernels.uniform_grid(th)
-    plan.T.copy_(torch.as_tensor(th), non_blocking=False)
-    a = plan.args
-    a.uniform, a.t0, a.dt = (1 if uni else 0), t0, dt
+    last = getattr(plan, "_times_host", None)
+    if last is None or not np.array_equal(last, th):  # the grid only moves when it changed
+        uni, t0, dt = kernels.uniform_grid(th)
+        plan.T.copy_(torch.as_tensor(th), non_blocking=False)
+        a = plan.args
+        a.uniform, a.t0, a.dt = (1 if uni else 0), t0, dt
+        plan._times_host = th.copy()
     return plan
 
 
 def run_snapshots(system, B_lab, p_lab, T, wscale, slot, num_slots, times,
                   y_axis="asymmetry", precision="fp64", max_sweeps=0, Hsys=None, Z=None,
-                  fast_mask=None):
+                  fast_mask=None, host_out=False):
     """Evaluate and reduce a batch of snapshots on the GPU.
 
     B_lab, p_lab: (S, 3) lab-frame field (incl. intrinsic) and muon
@@ -90,7 +93,9 @@ def run_snapshots(system, B_lab, p_lab, T, wscale, slot, num_slots, times,
 
     ``fast_mask``: a precomputed fast-path decision (bool, one for all
     snapshots); B_lab, p_lab and wscale may then be device tensors and
-    ``slot`` None (every snapshot in row 0)."""
+    ``slot`` None (every snapshot in row 0).  ``host_out``: return the
+    output as a host numpy array (on that path fetched together with the
+    status after a single synchronisation)."""
     prec = precision_code(precision)
     dev = kernels.device()
     if fast_mask is not None and isinstance(B_lab, torch.Tensor):
@@ -123,6 +128,8 @@ def run_snapshots(system, B_lab, p_lab, T, wscale, slot, num_slots, times,
         plan = _cached_plan(system, Hs, Zd, n, B_lab, p_lab, wscale, slot, num_slots, times, mode,
                             prec, dims, mu, None if mode == _lib.MODE_FAST else Tarr, max_sweeps)
         out = plan.run()
+        if host_out:
+            return plan.fetch()
         return out, plan.status[:S].cpu().numpy()
 
     if y_axis == "integral":
@@ -149,6 +156,8 @@ def run_snapshots(system, B_lab, p_lab, T, wscale, slot, num_slots, times,
         else:
             out += res
         status[idx] = st.cpu().numpy()
+    if host_out:
+        return out.cpu().numpy(), status
     return out, status
 
 
@@ -202,18 +211,17 @@ def powder_average(system, orientations, field=(0.0, 0.0, 0.0), polarization=(1.
         N = len(rows)
         wnorm = 1.0 / float(rows[:, 3].sum()) if (rows.shape[1] == 4 and N > 1) else 1.0 / N
         F, Pl, W = kernels.orient_snapshots(rows, f, p, intr, mode, wnorm)
-        out, status = run_snapshots(system, F, Pl, temperature, W, None, 1, times, y_axis,
-                                    precision, max_sweeps, fast_mask=fast)
+        res, status = run_snapshots(system, F, Pl, temperature, W, None, 1, times, y_axis,
+                                    precision, max_sweeps, fast_mask=fast, host_out=True)
     else:
         qs, ws = orientation_rows_to_quats(orientations, mode)
         N = len(qs)
         ws = ws * (N / ws.sum()) if N > 1 else np.ones(1)
         B_lab = Q.rotate(qs, f) + intr
         p_lab = Q.rotate(qs, p)
-        out, status = run_snapshots(system, B_lab, p_lab, temperature, ws / N,
+        res, status = run_snapshots(system, B_lab, p_lab, temperature, ws / N,
                                     np.zeros(N, np.int64), 1, times, y_axis, precision,
-                                    max_sweeps)
-    res = out.cpu().numpy()
+                                    max_sweeps, host_out=True)
     if np.any(status & _lib.MSP_ITEM_BAD_SLOT):
         raise RuntimeError("powder_average: invalid output rows")
     return res[0]
