@@ -133,3 +133,19 @@ def test_autotune_caches_choices(tmp_path, monkeypatch, batch):
     b2 = MultiSystemBatch(*args, precision="mixed", tuning="auto")
     assert os.path.getmtime(path) == mtime
     assert b2.tuning == b.tuning
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_multi_with_dim192_systems(precision, tol):
+    """Two 192-dimensional systems (the blocked FP32 reduction of the mixed
+    large-n kernel) between smaller ones, as multi-system segments."""
+    from muspinsim_gb300.multi import powder_average_multi
+
+    wls = _batch(seed=192, n_orient=3, n_times=200, dims=(192, 24, 192, 96))[:4]
+    refs = [oracle_powder(w) for w in wls]
+    got = powder_average_multi([w.system() for w in wls], wls[0].orientations,
+                               field=wls[0].fields[0], polarization=wls[0].polarization,
+                               times=wls[0].times, precision=precision)
+    for k, (w, ref) in enumerate(zip(wls, refs)):
+        err = np.abs(got[k] - ref).max()
+        assert err <= tol, (k, w.name, err)
