@@ -162,6 +162,11 @@ int large_threads(int n);
 size_t large_scratch_bytes(int n, int grid, int precision = MSP_PREC_FP64);
 int large_ctas_per_sm(int n, int precision = MSP_PREC_FP64);
 int large_grid(int batch, int n, int precision = MSP_PREC_FP64);
+// The MIXED fast path's kernel (msp_large_mixed.cu).
+cudaError_t launch_large_fast_mixed(const SnapArgs &a, double *scratch, int grid,
+                                    cudaStream_t st, int threads);
+size_t large_mixed_scratch_per_cta(int n);
+int large_mixed_occupancy(int n, int threads);
 // General path for n > 64 (EVOLVE / INTEGRAL, FP64 in both precisions).
 cudaError_t launch_large_rho(const SnapArgs &a, double *scratch, int grid, cudaStream_t st,
                              int integral);
