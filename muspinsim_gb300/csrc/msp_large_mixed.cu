@@ -74,8 +74,9 @@ constexpr int LM_KT = 16;  // k depth of a GEMM slab
 
 struct LmVec {
     double *lam, *sd, *rd;
+    unsigned long long *best;  // most strongly coupled near-degenerate partner per level
     float *lamf, *corr, *ed, *rn, *cn, *yn;
-    int *step;
+    int *step;  // [0]: largest correction, [1]: largest |l_i| (float bits)
     char *slab;  // two stages of GEMM slabs (A: TR x LM_KT, B: LM_KT x 32)
 };
 
@@ -87,7 +88,7 @@ __host__ __device__ inline size_t lm_stage_bytes(int threads) {
 // Bytes of the refinement vectors (also the back-transformation's two
 // LM_KT x LM_KT complex matrices).
 __host__ __device__ inline size_t lm_vec_bytes(int n) {
-    size_t b = 48 * (size_t)n + 16;
+    size_t b = 56 * (size_t)n + 16;
     if (b < 2 * LM_KT * LM_KT * 8) b = 2 * LM_KT * LM_KT * 8;
     return (b + 15) & ~size_t(15);
 }
@@ -110,7 +111,8 @@ __device__ __forceinline__ LmVec lm_vec(char *smem, int n) {
     v.lam = reinterpret_cast<double *>(smem);
     v.sd = v.lam + n;
     v.rd = v.sd + n;
-    v.lamf = reinterpret_cast<float *>(v.rd + n);
+    v.best = reinterpret_cast<unsigned long long *>(v.rd + n);
+    v.lamf = reinterpret_cast<float *>(v.best + n);
     v.corr = v.lamf + n;
     v.ed = v.corr + n;
     v.rn = v.ed + n;
@@ -512,37 +514,74 @@ __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
     const int tid = threadIdx.x, nt = blockDim.x;
     cx<float> *__restrict__ SR = s.SR;
     lm_colnorms(reinterpret_cast<const float *>(X), 2, n, v.cn);
-    if (tid == 0) *v.step = 0;
+    if (tid == 0) {
+        v.step[0] = 0;  // largest correction (float bits)
+        v.step[1] = 0;  // largest |l_i| (float bits): the degeneracy scale
+    }
     __syncthreads();
     lm_gemm<LM_HX>(s, X, X2, v, n);
     lm_colnorms(reinterpret_cast<const float *>(s.Y), 4, n, v.yn);
     __syncthreads();
     lm_gemm<LM_S>(s, X, X2, v, n);
     lm_gemm<LM_G>(s, X, X2, v, n);
+    float lmax = 0.f;
     for (int i = tid; i < n; i += nt) {
         const double l = v.sd[i] / (1.0 - v.rd[i]);
         v.lam[i] = l;
         v.lamf[i] = (float)l;
         v.corr[i] = 0.f;
         v.ed[i] = 0.f;
+        lmax = fmaxf(lmax, fabsf((float)l));
     }
+    atomicMax(&v.step[1], __float_as_int(lmax));  // non-negative: int order = float order
     __syncthreads();
-    // E (both triangles) in place of S / R, second-order eigenvalue terms;
-    // only the gap l_j - l_i needs FP64
+    // pairs closer than rounding form one degenerate level, and
+    // near-degenerate pairs rotate only as disjoint mutual-best pairs per
+    // step (see the n <= 64 refinement): orthonormalised otherwise
+    const float lscale = __int_as_float(v.step[1]);
+    const float deg = 1e-11f * lscale;
     const int nup = n * (n - 1) / 2;
-    float emax = 0.f;
-    for (int e = tid; e < nup; e += nt) {
-        int j = (int)((sqrtf(8.0f * (float)e + 1.0f) + 1.0f) * 0.5f);
+    auto pair_of = [&](int e, int &i, int &j) {
+        j = (int)((sqrtf(8.0f * (float)e + 1.0f) + 1.0f) * 0.5f);
         while (j * (j - 1) / 2 > e) --j;
         while ((j + 1) * j / 2 <= e) ++j;
-        const int i = e - j * (j - 1) / 2;  // 0 <= i < j
+        i = e - j * (j - 1) / 2;  // 0 <= i < j
+    };
+    for (int i = tid; i < n; i += nt) v.best[i] = 0ull;
+    __syncthreads();
+    for (int e = tid; e < nup; e += nt) {
+        int i, j;
+        pair_of(e, i, j);
+        const cx<float> S = SR[(size_t)i * n + j], R = SR[(size_t)j * n + i];
+        const float dl = (float)(v.lam[j] - v.lam[i]);
+        const float lj_f = v.lamf[j], li_f = v.lamf[i];
+        const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;
+        const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;
+        if (fabsf(dl) <= deg ||
+            fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) < 1e-2f * fabsf(dl))
+            continue;
+        const float cr = 0.5f * (ar + br), ci = 0.5f * (ai + bi);
+        const unsigned long long key = (unsigned long long)__float_as_uint(sqrtf(cr * cr + ci * ci))
+                                       << 32;
+        atomicMax(&v.best[i], key | (unsigned)(j + 1));
+        atomicMax(&v.best[j], key | (unsigned)(i + 1));
+    }
+    __syncthreads();
+    float emax = 0.f;
+    for (int e = tid; e < nup; e += nt) {
+        int i, j;
+        pair_of(e, i, j);
         const cx<float> S = SR[(size_t)i * n + j], R = SR[(size_t)j * n + i];
         const float dl = (float)(v.lam[j] - v.lam[i]);
         const float lj_f = v.lamf[j], li_f = v.lamf[i];
         const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;  // S_ij + l_j R_ij
         const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;  // S_ij + l_i R_ij
         cx<float> Eij, Eji;
-        if (fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) < 1e-2f * fabsf(dl)) {
+        if (fabsf(dl) <= deg) {
+            Eij = mk<float>(0.5f * R.re, 0.5f * R.im);
+            Eji = mk<float>(0.5f * R.re, -0.5f * R.im);
+        } else if (fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) <
+                   1e-2f * fabsf(dl)) {
             const float inv = 1.0f / dl;
             Eij = mk<float>(br * inv, bi * inv);
             Eji = mk<float>(-ar * inv, ai * inv);
@@ -551,7 +590,8 @@ __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
             emax = fmaxf(emax, fmaxf(fmaxf(fabsf(Eij.re), fabsf(Eij.im)),
                                      fmaxf(fabsf(Eji.re), fabsf(Eji.im))));
         } else {
-            // near-degenerate pair: exact rotation of the orthonormalised 2 x 2 block
+            const bool mutual = (unsigned)(v.best[i] & 0xffffffffull) == (unsigned)(j + 1) &&
+                                (unsigned)(v.best[j] & 0xffffffffull) == (unsigned)(i + 1);
             const float cr = 0.5f * (ar + br), ci = 0.5f * (ai + bi);
             const float mag = sqrtf(cr * cr + ci * ci);
             float sr = 0.f, si = 0.f;
@@ -562,17 +602,19 @@ __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
                                     : copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
                 const float qq = sqrtf(1.0f + t * t);  // 1 / k
                 const float f = t / (qq * mag);
-                sr = f * cr;
-                si = f * ci;
-                atomicAdd(&v.corr[i], -t * mag);
-                atomicAdd(&v.corr[j], t * mag);
-                const float km1 = -t * t / (qq * (1.0f + qq));  // k - 1 without cancellation
-                atomicAdd(&v.ed[i], km1);
-                atomicAdd(&v.ed[j], km1);
+                emax = fmaxf(emax, fmaxf(fabsf(f * cr), fabsf(f * ci)));
+                if (mutual) {
+                    sr = f * cr;
+                    si = f * ci;
+                    atomicAdd(&v.corr[i], -t * mag);
+                    atomicAdd(&v.corr[j], t * mag);
+                    const float km1 = -t * t / (qq * (1.0f + qq));  // k - 1 without cancellation
+                    atomicAdd(&v.ed[i], km1);
+                    atomicAdd(&v.ed[j], km1);
+                }
             }
             Eij = mk<float>(sr + 0.5f * R.re, si + 0.5f * R.im);
             Eji = mk<float>(-sr + 0.5f * R.re, si - 0.5f * R.im);
-            emax = fmaxf(emax, fmaxf(fabsf(sr), fabsf(si)));
         }
         SR[(size_t)i * n + j] = Eij;
         SR[(size_t)j * n + i] = Eji;

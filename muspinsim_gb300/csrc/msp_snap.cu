@@ -222,7 +222,10 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1;
     cx<float> *X = s.w.U;
     cx<float> *Yh = s.w.H;  // Jacobi work matrix is free now
-    if (tid == 0) s.rank[0] = 0;
+    if (tid == 0) {
+        s.rank[0] = 0;  // largest correction (float bits)
+        s.rank[1] = 0;  // largest |l_i| (float bits): the degeneracy scale
+    }
     // Y = H X
     for (int e = tid; e < n * n; e += nt) {
         const int i = FastDiv(n).div(e), j = e - i * n;
@@ -275,26 +278,72 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         }
     }
     __syncthreads();
+    float lmax = 0.f;
     for (int i = tid; i < n; i += nt) {
         const double l = s.sd[i] / (1.0 - s.rd[i]);
         s.lam[i] = l;
         s.lamf[i] = (float)l;
         s.corr[i] = 0.f;
         s.ed[i] = 0.f;
+        lmax = fmaxf(lmax, fabsf((float)l));
     }
+    atomicMax(&s.rank[1], __float_as_int(lmax));  // non-negative: int order = float order
     __syncthreads();
+    // Levels closer than rounding (gap <= 1e-11 max|l|: the Rayleigh
+    // quotients carry ~1e-13) are one degenerate level, e.g. the Zeeman
+    // multiplets of uncoupled spins: any orthonormal basis of it is exact,
+    // so such pairs are only orthonormalised.  Rotating them as
+    // near-degenerate pairs would apply overlapping 2 x 2 rotations inside
+    // a multiplet of three or more at once, which is not a rotation.
+    const float lscale = __int_as_float(s.rank[1]);
+    const float deg = 1e-11f * lscale;
     // E in place of S/R; second-order eigenvalue terms.  Only the gap
     // l_j - l_i needs FP64 (a difference of nearly equal large numbers);
     // E, S, R and the second-order terms are small corrections, FP32 is
     // ample for them.
+    //
+    // Near-degenerate pairs are rotated exactly, but only disjoint ones in
+    // a step: a pair rotates when each of its levels is the other's most
+    // strongly coupled near-degenerate partner (key |c| << 32 | partner + 1,
+    // 64-bit atomic max), so the step's rotations compose into a unitary
+    // factor.  Other near-degenerate pairs are orthonormalised only and
+    // keep the iteration going (cyclic Jacobi inside a cluster of levels;
+    // within an exactly degenerate multiplet any orthonormal basis is
+    // exact).  Overlapping rotations applied at once in X + X E are not a
+    // rotation and destroyed orthogonality in multiplets of three.
+    unsigned long long *best = reinterpret_cast<unsigned long long *>(s.w.rot);  // free now
+    for (int i = tid; i < n; i += nt) best[i] = 0ull;
+    __syncthreads();
     const int nup = n * (n - 1) / 2;
-    float emax = 0.f;
-    for (int e = tid; e < nup; e += nt) {
+    auto pair_of = [&](int e, int &i, int &j) {
         // strict upper pairs (i < j): j = row of the packed strict triangle
-        int j = (int)((sqrtf(8.0f * (float)e + 1.0f) + 1.0f) * 0.5f);
+        j = (int)((sqrtf(8.0f * (float)e + 1.0f) + 1.0f) * 0.5f);
         while (j * (j - 1) / 2 > e) --j;
         while ((j + 1) * j / 2 <= e) ++j;
-        const int i = e - j * (j - 1) / 2;  // 0 <= i < j
+        i = e - j * (j - 1) / 2;  // 0 <= i < j
+    };
+    for (int e = tid; e < nup; e += nt) {
+        int i, j;
+        pair_of(e, i, j);
+        const cx<float> S = s.SR[i * ld + j], R = s.SR[j * ld + i];
+        const float dl = (float)(s.lam[j] - s.lam[i]);
+        const float lj_f = s.lamf[j], li_f = s.lamf[i];
+        const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;
+        const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;
+        if (fabsf(dl) <= deg ||
+            fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) < 1e-2f * fabsf(dl))
+            continue;
+        const float cr = 0.5f * (ar + br), ci = 0.5f * (ai + bi);
+        const unsigned long long key = (unsigned long long)__float_as_uint(sqrtf(cr * cr + ci * ci))
+                                       << 32;
+        atomicMax(&best[i], key | (unsigned)(j + 1));
+        atomicMax(&best[j], key | (unsigned)(i + 1));
+    }
+    __syncthreads();
+    float emax = 0.f;
+    for (int e = tid; e < nup; e += nt) {
+        int i, j;
+        pair_of(e, i, j);
         const cx<float> S = s.SR[i * ld + j], R = s.SR[j * ld + i];
         // only the gap needs FP64 (a difference of nearly equal large numbers)
         const float dl = (float)(s.lam[j] - s.lam[i]);
@@ -302,7 +351,11 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;  // S_ij + l_j R_ij
         const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;  // S_ij + l_i R_ij
         cx<float> Eij, Eji;
-        if (fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) < 1e-2f * fabsf(dl)) {
+        if (fabsf(dl) <= deg) {
+            Eij = mk<float>(0.5f * R.re, 0.5f * R.im);
+            Eji = mk<float>(0.5f * R.re, -0.5f * R.im);
+        } else if (fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) <
+                   1e-2f * fabsf(dl)) {
             // separated pair: E_ij = (S_ij + l_j R_ij) / (l_j - l_i),
             // E_ji = (S_ji + l_i R_ji) / (l_i - l_j)
             const float inv = 1.0f / dl;
@@ -314,7 +367,10 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
             emax = fmaxf(emax, fmaxf(fmaxf(fabsf(Eij.re), fabsf(Eij.im)),
                                      fmaxf(fabsf(Eji.re), fabsf(Eji.im))));
         } else {
-            // near-degenerate pair: exact rotation of the orthonormalised 2x2 block
+            // near-degenerate pair: exact rotation of the orthonormalised 2x2
+            // block when the pair is mutual best, else orthonormalisation only
+            const bool mutual = (unsigned)(best[i] & 0xffffffffull) == (unsigned)(j + 1) &&
+                                (unsigned)(best[j] & 0xffffffffull) == (unsigned)(i + 1);
             const float cr = 0.5f * (ar + br), ci = 0.5f * (ai + bi);
             const float mag = sqrtf(cr * cr + ci * ci);
             float sr = 0.f, si = 0.f;
@@ -325,17 +381,19 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
                                     : copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
                 const float q = sqrtf(1.0f + t * t);  // 1 / k
                 const float f = t / (q * mag);
-                sr = f * cr;
-                si = f * ci;
-                atomicAdd(&s.corr[i], -t * mag);
-                atomicAdd(&s.corr[j], t * mag);
-                const float km1 = -t * t / (q * (1.0f + q));  // k - 1 without cancellation
-                atomicAdd(&s.ed[i], km1);
-                atomicAdd(&s.ed[j], km1);
+                emax = fmaxf(emax, fmaxf(fabsf(f * cr), fabsf(f * ci)));
+                if (mutual) {
+                    sr = f * cr;
+                    si = f * ci;
+                    atomicAdd(&s.corr[i], -t * mag);
+                    atomicAdd(&s.corr[j], t * mag);
+                    const float km1 = -t * t / (q * (1.0f + q));  // k - 1 without cancellation
+                    atomicAdd(&s.ed[i], km1);
+                    atomicAdd(&s.ed[j], km1);
+                }
             }
             Eij = mk<float>(sr + 0.5f * R.re, si + 0.5f * R.im);
             Eji = mk<float>(-sr + 0.5f * R.re, si - 0.5f * R.im);
-            emax = fmaxf(emax, fmaxf(fabsf(sr), fabsf(si)));
         }
         s.SR[i * ld + j] = Eij;
         s.SR[j * ld + i] = Eji;
