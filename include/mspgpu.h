@@ -37,6 +37,10 @@ extern "C" {
 #define MSP_ITEM_OK 0
 #define MSP_ITEM_NOT_CONVERGED 1 /* Jacobi reached max_sweeps */
 #define MSP_ITEM_BAD_SLOT 2      /* slot index out of range / not sorted */
+#define MSP_ITEM_REFINE_LIMIT 4  /* MIXED: the last eigenvector refinement step
+                                    allowed (max_refine) still corrected by more
+                                    than 2e-4; the snapshot may miss the 1e-6
+                                    accuracy of the mixed form */
 
 /* precision of the eigensolve and phase sum */
 #define MSP_PREC_FP64 0  /* all-FP64: bit-faithful drop-in (max|dP| <= 1e-10) */
@@ -230,6 +234,8 @@ typedef struct msp_powder_args {
     size_t workspace_bytes;
     void *stream;             /* cudaStream_t */
     msp_timer *timer;         /* optional stage timer (NULL: none) */
+    int max_refine;           /* MIXED: eigenvector refinement step cap, <= 0
+                                 selects 4 (MSP_ITEM_REFINE_LIMIT when used up) */
 } msp_powder_args;
 
 /* Scratch bytes msp_powder_run needs for these arguments (no pointer is

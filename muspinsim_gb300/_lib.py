@@ -21,6 +21,7 @@ MSP_ERR_UNSUPPORTED = 4
 MSP_ITEM_OK = 0
 MSP_ITEM_NOT_CONVERGED = 1
 MSP_ITEM_BAD_SLOT = 2
+MSP_ITEM_REFINE_LIMIT = 4
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -71,6 +72,7 @@ class PowderArgs(ctypes.Structure):
         ("workspace_bytes", ctypes.c_size_t),
         ("stream", _c_dp),
         ("timer", _c_dp),
+        ("max_refine", ctypes.c_int),
     ]
 
 

@@ -272,7 +272,7 @@ static cudaEvent_t *timer_slot(msp_timer *t) {
 // ---------------------------------------------------------------- powder pipeline
 
 struct Layout {
-    size_t coef, omega, snap_const, slot_first, item_first, partial, large, total;
+    size_t coef, omega, snap_const, slot_first, item_first, partial, large, evec, total;
     int P, IP, max_items, T;
     bool phase_records;
 };
@@ -356,6 +356,8 @@ static Layout powder_layout(const msp_powder_args *a) {
     off += align256((size_t)(a->num_slots + 1) * 4);
     L.partial = off;
     off += align256((size_t)L.max_items * L.T * (L.phase_records ? 4 : 8));
+    L.evec = off;
+    off += align256(snap_evec_bytes(a->n, a->num_snap, a->precision));
     L.large = off;
     if (a->n > MSP_MAX_DIM) {
         if (a->mode == MSP_MODE_FAST)
@@ -406,6 +408,7 @@ int msp_powder_run(const msp_powder_args *a) {
     sa.n = a->n;
     sa.num_snap = a->num_snap;
     sa.max_sweeps = a->max_sweeps > 0 ? a->max_sweeps : 40;
+    sa.max_refine = a->max_refine > 0 ? a->max_refine : 4;
     sa.Hsys = reinterpret_cast<const cx<double> *>(a->Hsys);
     sa.Z = reinterpret_cast<const cx<double> *>(a->Z);
     sa.field = a->field;
@@ -435,6 +438,7 @@ int msp_powder_run(const msp_powder_args *a) {
     sa.snap_const = reinterpret_cast<double *>(ws + L.snap_const);
     sa.status = a->status;
     sa.coef_f32 = a->precision == MSP_PREC_MIXED;
+    sa.evec = snap_evec_bytes(a->n, a->num_snap, a->precision) > 0 ? ws + L.evec : NULL;
 
     const bool large = a->n > MSP_MAX_DIM;
     if (!large) {

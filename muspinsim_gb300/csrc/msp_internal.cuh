@@ -27,6 +27,7 @@ struct SnapArgs {
     int n;
     int num_snap;
     int max_sweeps;
+    int max_refine;  // MIXED refinement step cap
     const cx<double> *Hsys;
     const cx<double> *Z;
     const double *field;
@@ -53,6 +54,9 @@ struct SnapArgs {
     double *snap_const;  // num_snap
     int *status;         // num_snap
     int coef_f32;        // n > 64 kernels: pair_coef holds float2 (MIXED) instead of double2
+    void *evec;          // MIXED, n <= 32: num_snap * n * n FP32 complex eigenvectors
+                         // (row-major) from the warp Jacobi stage; NULL runs the
+                         // single-kernel form
     // Heterogeneous batches (msp_multi_*): when num_seg > 0 the launch's
     // snapshots form num_seg segments; snapshot sn of segment j
     // (seg_first[j] <= sn < seg_first[j + 1]) reads its field, polarisation
@@ -114,6 +118,13 @@ struct PhaseArgs {
 };
 
 size_t snap_smem_bytes(int n, int mode, int precision, int fac_len);
+// Two-stage MIXED snapshots (n <= 32): the warp-per-matrix FP32 Jacobi
+// (msp_jacobi_warp.cu) writes eigenvectors to SnapArgs::evec; the snapshot
+// kernels refine them.  Bytes of that scratch for num_snap snapshots (0 when
+// the form does not apply).
+bool jacobi_warp_supported(int n);
+size_t snap_evec_bytes(int n, long long num_snap, int precision);
+cudaError_t launch_jacobi_warp(const SnapArgs &a, cudaStream_t st);
 cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStream_t st,
                              int threads = 0, int grid = 0);
 // Threads per CTA of the snapshot kernels when the caller gives none.

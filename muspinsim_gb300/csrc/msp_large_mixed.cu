@@ -3,6 +3,7 @@
 // shared-memory tile engine (see the section comment below).
 #include <type_traits>
 
+#include "msp_cluster.cuh"
 #include "msp_dw.cuh"
 #include "msp_large.cuh"
 
@@ -74,9 +75,9 @@ constexpr int LM_KT = 16;  // k depth of a GEMM slab
 
 struct LmVec {
     double *lam, *sd, *rd;
-    unsigned long long *best;  // most strongly coupled near-degenerate partner per level
-    float *lamf, *corr, *ed, *rn, *cn, *yn;
-    int *step;  // [0]: largest correction, [1]: largest |l_i| (float bits)
+    int *rank, *order, *cstart;  // refinement clusters (msp_cluster.cuh)
+    float *lamf, *corr, *rn, *cn, *yn;
+    int *step;  // [0]: largest correction, [1]: largest |l_i|, [2]: amax (float bits)
     char *slab;  // two stages of GEMM slabs (A: TR x LM_KT, B: LM_KT x 32)
 };
 
@@ -111,11 +112,12 @@ __device__ __forceinline__ LmVec lm_vec(char *smem, int n) {
     v.lam = reinterpret_cast<double *>(smem);
     v.sd = v.lam + n;
     v.rd = v.sd + n;
-    v.best = reinterpret_cast<unsigned long long *>(v.rd + n);
-    v.lamf = reinterpret_cast<float *>(v.best + n);
+    v.rank = reinterpret_cast<int *>(v.rd + n);
+    v.order = v.rank + n;
+    v.cstart = v.order + n;
+    v.lamf = reinterpret_cast<float *>(v.cstart + n);
     v.corr = v.lamf + n;
-    v.ed = v.corr + n;
-    v.rn = v.ed + n;
+    v.rn = v.corr + n;
     v.cn = v.rn + n;
     v.yn = v.cn + n;
     v.step = reinterpret_cast<int *>(v.yn + n);
@@ -507,17 +509,15 @@ __device__ __forceinline__ void lm_colnorms(const float *M, int stride, int n, f
 }
 
 // One refinement step of the eigenvector columns X into X2 and of the
-// eigenvalues v.lam.  Returns the largest first-order |E_ij| or rotation
-// |s| (the size of the correction just applied).
+// eigenvalues v.lam, clusters resolved as in the n <= 64 refinement
+// (msp_cluster.cuh; T in the Y buffer, free once S is formed).  Returns the
+// step's largest correction.
 __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
                            cx<float> *__restrict__ X2, const LmVec &v, int n) {
     const int tid = threadIdx.x, nt = blockDim.x;
     cx<float> *__restrict__ SR = s.SR;
     lm_colnorms(reinterpret_cast<const float *>(X), 2, n, v.cn);
-    if (tid == 0) {
-        v.step[0] = 0;  // largest correction (float bits)
-        v.step[1] = 0;  // largest |l_i| (float bits): the degeneracy scale
-    }
+    if (tid < 4) v.step[tid] = 0;  // step, max|l|, amax (float bits)
     __syncthreads();
     lm_gemm<LM_HX>(s, X, X2, v, n);
     lm_colnorms(reinterpret_cast<const float *>(s.Y), 4, n, v.yn);
@@ -530,102 +530,33 @@ __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
         v.lam[i] = l;
         v.lamf[i] = (float)l;
         v.corr[i] = 0.f;
-        v.ed[i] = 0.f;
         lmax = fmaxf(lmax, fabsf((float)l));
     }
     atomicMax(&v.step[1], __float_as_int(lmax));  // non-negative: int order = float order
     __syncthreads();
-    // pairs closer than rounding form one degenerate level, and
-    // near-degenerate pairs rotate only as disjoint mutual-best pairs per
-    // step (see the n <= 64 refinement): orthonormalised otherwise
-    const float lscale = __int_as_float(v.step[1]);
-    const float deg = 1e-11f * lscale;
-    const int nup = n * (n - 1) / 2;
-    auto pair_of = [&](int e, int &i, int &j) {
-        j = (int)((sqrtf(8.0f * (float)e + 1.0f) + 1.0f) * 0.5f);
-        while (j * (j - 1) / 2 > e) --j;
-        while ((j + 1) * j / 2 <= e) ++j;
-        i = e - j * (j - 1) / 2;  // 0 <= i < j
-    };
-    for (int i = tid; i < n; i += nt) v.best[i] = 0ull;
-    __syncthreads();
-    for (int e = tid; e < nup; e += nt) {
-        int i, j;
-        pair_of(e, i, j);
-        const cx<float> S = SR[(size_t)i * n + j], R = SR[(size_t)j * n + i];
-        const float dl = (float)(v.lam[j] - v.lam[i]);
-        const float lj_f = v.lamf[j], li_f = v.lamf[i];
-        const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;
-        const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;
-        if (fabsf(dl) <= deg ||
-            fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) < 1e-2f * fabsf(dl))
-            continue;
-        const float cr = 0.5f * (ar + br), ci = 0.5f * (ai + bi);
-        const unsigned long long key = (unsigned long long)__float_as_uint(sqrtf(cr * cr + ci * ci))
-                                       << 32;
-        atomicMax(&v.best[i], key | (unsigned)(j + 1));
-        atomicMax(&v.best[j], key | (unsigned)(i + 1));
-    }
-    __syncthreads();
+    OaCluster cl;
+    cl.rank = v.rank;
+    cl.order = v.order;
+    cl.cstart = v.cstart;
+    cl.scal = v.step + 2;
+    cl.T = reinterpret_cast<cx<float> *>(s.Y);
+    cl.ldt = n;
+    oa_clusters(SR, n, v.lam, v.lamf, n, cl);
     float emax = 0.f;
+    const int nup = n * (n - 1) / 2;
     for (int e = tid; e < nup; e += nt) {
         int i, j;
-        pair_of(e, i, j);
-        const cx<float> S = SR[(size_t)i * n + j], R = SR[(size_t)j * n + i];
-        const float dl = (float)(v.lam[j] - v.lam[i]);
-        const float lj_f = v.lamf[j], li_f = v.lamf[i];
-        const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;  // S_ij + l_j R_ij
-        const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;  // S_ij + l_i R_ij
-        cx<float> Eij, Eji;
-        if (fabsf(dl) <= deg) {
-            Eij = mk<float>(0.5f * R.re, 0.5f * R.im);
-            Eji = mk<float>(0.5f * R.re, -0.5f * R.im);
-        } else if (fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) <
-                   1e-2f * fabsf(dl)) {
-            const float inv = 1.0f / dl;
-            Eij = mk<float>(br * inv, bi * inv);
-            Eji = mk<float>(-ar * inv, ai * inv);
-            atomicAdd(&v.corr[i], -(ar * ar + ai * ai) * inv);
-            atomicAdd(&v.corr[j], (br * br + bi * bi) * inv);
-            emax = fmaxf(emax, fmaxf(fmaxf(fabsf(Eij.re), fabsf(Eij.im)),
-                                     fmaxf(fabsf(Eji.re), fabsf(Eji.im))));
-        } else {
-            const bool mutual = (unsigned)(v.best[i] & 0xffffffffull) == (unsigned)(j + 1) &&
-                                (unsigned)(v.best[j] & 0xffffffffull) == (unsigned)(i + 1);
-            const float cr = 0.5f * (ar + br), ci = 0.5f * (ai + bi);
-            const float mag = sqrtf(cr * cr + ci * ci);
-            float sr = 0.f, si = 0.f;
-            if (mag > 0.f) {
-                const float zeta = dl / (2.0f * mag);
-                const float t = fabsf(zeta) > 1e18f
-                                    ? 0.5f / zeta
-                                    : copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
-                const float qq = sqrtf(1.0f + t * t);  // 1 / k
-                const float f = t / (qq * mag);
-                emax = fmaxf(emax, fmaxf(fabsf(f * cr), fabsf(f * ci)));
-                if (mutual) {
-                    sr = f * cr;
-                    si = f * ci;
-                    atomicAdd(&v.corr[i], -t * mag);
-                    atomicAdd(&v.corr[j], t * mag);
-                    const float km1 = -t * t / (qq * (1.0f + qq));  // k - 1 without cancellation
-                    atomicAdd(&v.ed[i], km1);
-                    atomicAdd(&v.ed[j], km1);
-                }
-            }
-            Eij = mk<float>(sr + 0.5f * R.re, si + 0.5f * R.im);
-            Eji = mk<float>(-sr + 0.5f * R.re, si - 0.5f * R.im);
-        }
-        SR[(size_t)i * n + j] = Eij;
-        SR[(size_t)j * n + i] = Eji;
+        oa_pair_of(e, i, j);
+        oa_pair_correction(SR, n, v.lam, v.lamf, cl, v.corr, i, j, emax);
     }
-    atomicMax(v.step, __float_as_int(emax));  // non-negative: int order = float order
     __syncthreads();
-    for (int j = tid; j < n; j += nt)
-        SR[(size_t)j * n + j] = mk<float>((float)(0.5 * v.rd[j]) + v.ed[j], 0.f);
+    oa_cluster_diagonal(v.lam, v.corr, n, cl);
+    for (int j = tid; j < n; j += nt) SR[(size_t)j * n + j] = mk<float>((float)(0.5 * v.rd[j]), 0.f);
     __syncthreads();
     lm_gemm<LM_XE>(s, X, X2, v, n);
-    for (int i = tid; i < n; i += nt) v.lam[i] += (double)v.corr[i];
+    emax = fmaxf(emax, oa_resolve_clusters(X2, n, n, v.lam, v.corr, n, cl,
+                                           __int_as_float(v.step[1])));
+    atomicMax(v.step, __float_as_int(emax));  // non-negative: int order = float order
     __syncthreads();
     const float step = __int_as_float(*v.step);
     __syncthreads();
@@ -850,12 +781,17 @@ __global__ void __maxnreg__(96) msp_large_fast_mixed_kernel(SnapArgs a, char *sc
         }
         __syncthreads();
         cx<float> *X = s.X, *X2 = s.X2;
-        for (int it = 0; it < 4; ++it) {
+        const int max_refine = a.max_refine > 0 ? a.max_refine : 4;
+        st |= MSP_ITEM_REFINE_LIMIT;
+        for (int it = 0; it < max_refine; ++it) {
             const float step = lm_refine(s, X, X2, v, n);
             cx<float> *t = X;
             X = X2;
             X2 = t;
-            if (step <= 2e-4f) break;
+            if (step <= 2e-4f) {
+                st &= ~MSP_ITEM_REFINE_LIMIT;
+                break;
+            }
         }
         // W = (sigma_p (x) 1_d) X into X2
         const float px = (float)a.pol[3 * g], py = (float)a.pol[3 * g + 1],

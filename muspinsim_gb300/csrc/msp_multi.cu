@@ -77,7 +77,7 @@ struct MultiBucket {
     std::vector<int> systems;  // global system ids, ascending
     std::vector<MultiChunk> chunks;
     int max_items;
-    size_t off_coef, off_phase, off_const, off_partial, off_large, bytes;
+    size_t off_coef, off_phase, off_const, off_partial, off_evec, off_large, bytes;
     cudaStream_t stream;
     cudaEvent_t done;
 };
@@ -254,6 +254,8 @@ static int plan_layout(msp_multi_plan *p, const msp_multi_desc *d) {
         off += al256(S * 8);
         b.off_partial = off;
         off += al256((size_t)b.max_items * T * (records ? 4 : 8));
+        b.off_evec = off;
+        off += al256(b.large ? 0 : snap_evec_bytes(b.n, (long long)S, p->precision));
         b.off_large = off;
         if (b.large) {
             int g = p->sms * b.ctas_per_sm;
@@ -366,6 +368,7 @@ static int plan_enqueue(msp_multi_plan *p, const msp_multi_io *io, cudaStream_t 
             sa.n = b.n;
             sa.num_snap = cs;
             sa.max_sweeps = p->max_sweeps > 0 ? p->max_sweeps : 40;
+            sa.max_refine = 4;
             sa.Hsys = reinterpret_cast<const cx<double> *>(io->Hsys_all);
             sa.Z = reinterpret_cast<const cx<double> *>(io->Z_all);
             sa.field = io->field;
@@ -379,6 +382,8 @@ static int plan_enqueue(msp_multi_plan *p, const msp_multi_io *io, cudaStream_t 
             sa.snap_const = reinterpret_cast<double *>(ws + b.off_const);
             sa.status = io->status;
             sa.coef_f32 = mixed;
+            sa.evec = (!b.large && snap_evec_bytes(b.n, 1, p->precision) > 0) ? ws + b.off_evec
+                                                                               : NULL;
             sa.num_seg = c.num_seg;
             sa.seg_first = reinterpret_cast<const int *>(ws + c.seg_first);
             sa.seg_g0 = reinterpret_cast<const int *>(ws + c.seg_g0);

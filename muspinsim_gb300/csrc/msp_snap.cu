@@ -15,6 +15,7 @@
 //            ~60x its FP64 rate, so this costs about as much as the FP32
 //            sweeps themselves instead of dominating as FP64 would.
 #include "msp_internal.cuh"
+#include "msp_cluster.cuh"
 #include "msp_jacobi.cuh"
 #include "msp_rho.cuh"
 
@@ -29,7 +30,7 @@ static_assert(sizeof(JRot<float>) == 16 && sizeof(JRot<double>) == 32, "JRot lay
 struct SnapLayout {
     size_t H, U, rot, dia, red, tab, diag;     // Jacobi work
     size_t lam, acc, rank;                     // eigenvalues, reductions, sort
-    size_t Hh, Hl, Yl, SR, sd, corr, rd, ed, lamf;  // refinement (MIXED)
+    size_t Hh, Hl, Yl, SR, sd, corr, rd, lamf, rk, ord, cst, scal;  // refinement (MIXED)
     size_t fac, B2;                            // general path
     size_t total;
 };
@@ -62,7 +63,8 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
     L.lam = lay_take(off, m * 8);
     L.acc = lay_take(off, 2 * 8);
     L.rank = lay_take(off, m * 4);
-    L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = L.ed = L.lamf = 0;
+    L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = L.lamf = 0;
+    L.rk = L.ord = L.cst = L.scal = 0;
     if (refine) {
         L.Hh = lay_take(off, mm * 8);
         L.Hl = lay_take(off, mm * 8);
@@ -71,8 +73,11 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
         L.sd = lay_take(off, m * 8);
         L.corr = lay_take(off, m * 4);
         L.rd = lay_take(off, m * 8);
-        L.ed = lay_take(off, m * 4);
         L.lamf = lay_take(off, m * 4);
+        L.rk = lay_take(off, m * 4);
+        L.ord = lay_take(off, m * 4);
+        L.cst = lay_take(off, m * 4);
+        L.scal = lay_take(off, 4 * 4);
     }
     L.fac = L.B2 = 0;
     if (rho) {
@@ -106,7 +111,8 @@ struct SnapSmem {
     int *rank;
     cx<float> *Hh, *Hl, *Yl, *SR;
     double *sd, *rd;
-    float *corr, *ed, *lamf;
+    float *corr, *lamf;
+    int *rk, *ord, *cst, *scal;  // refinement clusters
     cx<double> *fac;
     cx<T> *B2;
 };
@@ -133,8 +139,11 @@ __device__ __forceinline__ SnapSmem<T> snap_carve(char *base, int n, bool rho, i
     s.sd = REFINE ? reinterpret_cast<double *>(base + L.sd) : nullptr;
     s.corr = REFINE ? reinterpret_cast<float *>(base + L.corr) : nullptr;
     s.rd = REFINE ? reinterpret_cast<double *>(base + L.rd) : nullptr;
-    s.ed = REFINE ? reinterpret_cast<float *>(base + L.ed) : nullptr;
     s.lamf = REFINE ? reinterpret_cast<float *>(base + L.lamf) : nullptr;
+    s.rk = REFINE ? reinterpret_cast<int *>(base + L.rk) : nullptr;
+    s.ord = REFINE ? reinterpret_cast<int *>(base + L.ord) : nullptr;
+    s.cst = REFINE ? reinterpret_cast<int *>(base + L.cst) : nullptr;
+    s.scal = REFINE ? reinterpret_cast<int *>(base + L.scal) : nullptr;
     s.fac = rho ? reinterpret_cast<cx<double> *>(base + L.fac) : nullptr;
     s.B2 = rho ? reinterpret_cast<cx<T> *>(base + L.B2) : nullptr;
     return s;
@@ -170,7 +179,7 @@ __device__ __forceinline__ void store_frequency(const SnapArgs &a, size_t o, dou
 
 // H = Hsys + b . Z (FP64) into the Jacobi buffer (precision T, padded to m);
 // in MIXED mode also its exact split H = Hh + Hl into two FP32 matrices.
-template <typename T, bool REFINE>
+template <typename T, bool REFINE, bool PRE = false>
 __device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
                                  const double *b, int n, int m, SnapSmem<T> &s) {
     const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1, ldh = jacobi_ldh(m);
@@ -185,7 +194,7 @@ __device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
             h.re = hs.re + bx * z0.re + by * z1.re + bz * z2.re;
             h.im = hs.im + bx * z0.im + by * z1.im + bz * z2.im;
         }
-        s.w.H[i * ldh + j] = mk<T>((T)h.re, (T)h.im);
+        if (!PRE) s.w.H[i * ldh + j] = mk<T>((T)h.re, (T)h.im);
         if (REFINE) {
             const float hr = (float)h.re, hi = (float)h.im;
             s.Hh[i * ld + j] = mk<float>(hr, hi);
@@ -193,6 +202,25 @@ __device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
         }
     }
     __syncthreads();
+}
+
+// The eigensolve of a snapshot: FP64 or FP32 Jacobi in this CTA, or (PRE)
+// the FP32 eigenvectors the warp Jacobi stage left in a.evec, with the
+// status it wrote.  Leaves the eigenvectors in s.w.U (row stride m + 1).
+template <typename T, bool PRE>
+__device__ __forceinline__ int snap_eigvecs(const SnapArgs &a, int sn, int g, int n, int m,
+                                            SnapSmem<T> &s) {
+    if (!PRE) return jacobi_sweeps<T>(s.w, m, a.max_sweeps);
+    const float2 *X = reinterpret_cast<const float2 *>(a.evec) + (size_t)sn * n * n;
+    const int ld = m + 1;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = FastDiv(n).div(e), j = e - i * n;
+        const float2 x = X[e];
+        s.w.U[i * ld + j] = mk<T>((T)x.x, (T)x.y);
+    }
+    const int st = a.status[g];
+    __syncthreads();
+    return st;
 }
 
 // One Ogita-Aishima refinement step of the FP32 eigenvector matrix X
@@ -205,27 +233,14 @@ __device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
 // sum_j |S_ij + l_i R_ij|^2 / (l_i - l_j).  H X, X^H H X and X^H X use
 // double-word FP32 accumulation, 1 - R_ii and l_i are FP64; E, the
 // second-order terms and X E are FP32 (they are small corrections).
-//
-// Near-degenerate pairs: FP32 Jacobi leaves levels whose gap is within a
-// few FP32 resolutions of |H| mixed by angles up to ~0.5, where the
-// first-order E is no longer accurate and the iteration stalls or
-// diverges.  A pair whose first-order |E_ij| would exceed 1e-2 is instead
-// rotated exactly: the 2x2 Hermitian block [[l_i, c], [conj(c), l_j]],
-// c = S_ij + (l_i + l_j) / 2 R_ij (the coupling after first-order
-// orthonormalisation), is diagonalised by the Jacobi rotation
-// [[k, s], [-conj(s), k]], which enters E as E_ij = s + R_ij / 2,
-// E_ji = -conj(s) + conj(R_ij) / 2 and k - 1 on both diagonal entries;
-// the eigenvalues move by -/+ t |c|.
-// Returns the largest first-order |E_ij| or rotation |s| (the size of the
-// correction just applied); s.rank[0] is its scratch.
+// Levels too close for the first-order E (near-degenerate clusters, e.g.
+// at level anticrossings, and exactly degenerate multiplets) are resolved
+// as clusters (msp_cluster.cuh).  Returns this step's largest correction.
 __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1;
     cx<float> *X = s.w.U;
     cx<float> *Yh = s.w.H;  // Jacobi work matrix is free now
-    if (tid == 0) {
-        s.rank[0] = 0;  // largest correction (float bits)
-        s.rank[1] = 0;  // largest |l_i| (float bits): the degeneracy scale
-    }
+    if (tid < 4) s.scal[tid] = 0;  // [0]: amax, [1]: max|l|, [2]: step (float bits)
     // Y = H X
     for (int e = tid; e < n * n; e += nt) {
         const int i = FastDiv(n).div(e), j = e - i * n;
@@ -284,127 +299,33 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         s.lam[i] = l;
         s.lamf[i] = (float)l;
         s.corr[i] = 0.f;
-        s.ed[i] = 0.f;
         lmax = fmaxf(lmax, fabsf((float)l));
     }
-    atomicMax(&s.rank[1], __float_as_int(lmax));  // non-negative: int order = float order
+    atomicMax(&s.scal[1], __float_as_int(lmax));  // non-negative: int order = float order
     __syncthreads();
-    // Levels closer than rounding (gap <= 1e-11 max|l|: the Rayleigh
-    // quotients carry ~1e-13) are one degenerate level, e.g. the Zeeman
-    // multiplets of uncoupled spins: any orthonormal basis of it is exact,
-    // so such pairs are only orthonormalised.  Rotating them as
-    // near-degenerate pairs would apply overlapping 2 x 2 rotations inside
-    // a multiplet of three or more at once, which is not a rotation.
-    const float lscale = __int_as_float(s.rank[1]);
-    const float deg = 1e-11f * lscale;
-    // E in place of S/R; second-order eigenvalue terms.  Only the gap
-    // l_j - l_i needs FP64 (a difference of nearly equal large numbers);
-    // E, S, R and the second-order terms are small corrections, FP32 is
-    // ample for them.
-    //
-    // Near-degenerate pairs are rotated exactly, but only disjoint ones in
-    // a step: a pair rotates when each of its levels is the other's most
-    // strongly coupled near-degenerate partner (key |c| << 32 | partner + 1,
-    // 64-bit atomic max), so the step's rotations compose into a unitary
-    // factor.  Other near-degenerate pairs are orthonormalised only and
-    // keep the iteration going (cyclic Jacobi inside a cluster of levels;
-    // within an exactly degenerate multiplet any orthonormal basis is
-    // exact).  Overlapping rotations applied at once in X + X E are not a
-    // rotation and destroyed orthogonality in multiplets of three.
-    unsigned long long *best = reinterpret_cast<unsigned long long *>(s.w.rot);  // free now
-    for (int i = tid; i < n; i += nt) best[i] = 0ull;
-    __syncthreads();
-    const int nup = n * (n - 1) / 2;
-    auto pair_of = [&](int e, int &i, int &j) {
-        // strict upper pairs (i < j): j = row of the packed strict triangle
-        j = (int)((sqrtf(8.0f * (float)e + 1.0f) + 1.0f) * 0.5f);
-        while (j * (j - 1) / 2 > e) --j;
-        while ((j + 1) * j / 2 <= e) ++j;
-        i = e - j * (j - 1) / 2;  // 0 <= i < j
-    };
-    for (int e = tid; e < nup; e += nt) {
-        int i, j;
-        pair_of(e, i, j);
-        const cx<float> S = s.SR[i * ld + j], R = s.SR[j * ld + i];
-        const float dl = (float)(s.lam[j] - s.lam[i]);
-        const float lj_f = s.lamf[j], li_f = s.lamf[i];
-        const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;
-        const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;
-        if (fabsf(dl) <= deg ||
-            fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) < 1e-2f * fabsf(dl))
-            continue;
-        const float cr = 0.5f * (ar + br), ci = 0.5f * (ai + bi);
-        const unsigned long long key = (unsigned long long)__float_as_uint(sqrtf(cr * cr + ci * ci))
-                                       << 32;
-        atomicMax(&best[i], key | (unsigned)(j + 1));
-        atomicMax(&best[j], key | (unsigned)(i + 1));
-    }
-    __syncthreads();
+    // clusters; T in Yl (free now)
+    OaCluster cl;
+    cl.rank = s.rk;
+    cl.order = s.ord;
+    cl.cstart = s.cst;
+    cl.scal = s.scal;
+    cl.T = s.Yl;
+    cl.ldt = ld;
+    oa_clusters(s.SR, ld, s.lam, s.lamf, n, cl);
     float emax = 0.f;
+    const int nup = n * (n - 1) / 2;
     for (int e = tid; e < nup; e += nt) {
         int i, j;
-        pair_of(e, i, j);
-        const cx<float> S = s.SR[i * ld + j], R = s.SR[j * ld + i];
-        // only the gap needs FP64 (a difference of nearly equal large numbers)
-        const float dl = (float)(s.lam[j] - s.lam[i]);
-        const float lj_f = s.lamf[j], li_f = s.lamf[i];
-        const float br = S.re + lj_f * R.re, bi = S.im + lj_f * R.im;  // S_ij + l_j R_ij
-        const float ar = S.re + li_f * R.re, ai = S.im + li_f * R.im;  // S_ij + l_i R_ij
-        cx<float> Eij, Eji;
-        if (fabsf(dl) <= deg) {
-            Eij = mk<float>(0.5f * R.re, 0.5f * R.im);
-            Eji = mk<float>(0.5f * R.re, -0.5f * R.im);
-        } else if (fmaxf(fmaxf(fabsf(br), fabsf(bi)), fmaxf(fabsf(ar), fabsf(ai))) <
-                   1e-2f * fabsf(dl)) {
-            // separated pair: E_ij = (S_ij + l_j R_ij) / (l_j - l_i),
-            // E_ji = (S_ji + l_i R_ji) / (l_i - l_j)
-            const float inv = 1.0f / dl;
-            Eij = mk<float>(br * inv, bi * inv);
-            Eji = mk<float>(-ar * inv, ai * inv);
-            // second order: |S_ij + l_i R_ij|^2 / (l_i - l_j) for l_i, and the mirror
-            atomicAdd(&s.corr[i], -(ar * ar + ai * ai) * inv);
-            atomicAdd(&s.corr[j], (br * br + bi * bi) * inv);
-            emax = fmaxf(emax, fmaxf(fmaxf(fabsf(Eij.re), fabsf(Eij.im)),
-                                     fmaxf(fabsf(Eji.re), fabsf(Eji.im))));
-        } else {
-            // near-degenerate pair: exact rotation of the orthonormalised 2x2
-            // block when the pair is mutual best, else orthonormalisation only
-            const bool mutual = (unsigned)(best[i] & 0xffffffffull) == (unsigned)(j + 1) &&
-                                (unsigned)(best[j] & 0xffffffffull) == (unsigned)(i + 1);
-            const float cr = 0.5f * (ar + br), ci = 0.5f * (ai + bi);
-            const float mag = sqrtf(cr * cr + ci * ci);
-            float sr = 0.f, si = 0.f;
-            if (mag > 0.f) {
-                const float zeta = dl / (2.0f * mag);
-                const float t = fabsf(zeta) > 1e18f
-                                    ? 0.5f / zeta
-                                    : copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
-                const float q = sqrtf(1.0f + t * t);  // 1 / k
-                const float f = t / (q * mag);
-                emax = fmaxf(emax, fmaxf(fabsf(f * cr), fabsf(f * ci)));
-                if (mutual) {
-                    sr = f * cr;
-                    si = f * ci;
-                    atomicAdd(&s.corr[i], -t * mag);
-                    atomicAdd(&s.corr[j], t * mag);
-                    const float km1 = -t * t / (q * (1.0f + q));  // k - 1 without cancellation
-                    atomicAdd(&s.ed[i], km1);
-                    atomicAdd(&s.ed[j], km1);
-                }
-            }
-            Eij = mk<float>(sr + 0.5f * R.re, si + 0.5f * R.im);
-            Eji = mk<float>(-sr + 0.5f * R.re, si - 0.5f * R.im);
-        }
-        s.SR[i * ld + j] = Eij;
-        s.SR[j * ld + i] = Eji;
+        oa_pair_of(e, i, j);
+        oa_pair_correction(s.SR, ld, s.lam, s.lamf, cl, s.corr, i, j, emax);
     }
-    atomicMax(&s.rank[0], __float_as_int(emax));  // non-negative: int order = float order
     __syncthreads();
-    // X' = X + X E  (into Yh), E_ii = R_ii / 2 plus the rotations' k - 1
+    oa_cluster_diagonal(s.lam, s.corr, n, cl);
+    // X' = X + X E  (into Yh), E_ii = R_ii / 2
     for (int e = tid; e < n * n; e += nt) {
         const int k = FastDiv(n).div(e), j = e - k * n;
         const cx<float> xkj = X[k * ld + j];
-        const float hr = (float)(0.5 * s.rd[j]) + s.ed[j];
+        const float hr = (float)(0.5 * s.rd[j]);
         float ar = xkj.re + hr * xkj.re, ai = xkj.im + hr * xkj.im;
         for (int i = 0; i < n; ++i) {
             if (i == j) continue;
@@ -419,31 +340,40 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         const int k = FastDiv(n).div(e), j = e - k * n;
         X[k * ld + j] = Yh[k * ld + j];
     }
-    for (int i = tid; i < n; i += nt) s.lam[i] += (double)s.corr[i];
     __syncthreads();
-    const float step = __int_as_float(s.rank[0]);
+    emax = fmaxf(emax, oa_resolve_clusters(X, ld, n, s.lam, s.corr, n, cl,
+                                           __int_as_float(s.scal[1])));
+    atomicMax(&s.scal[2], __float_as_int(emax));  // non-negative: int order = float order
+    __syncthreads();
+    const float step = __int_as_float(s.scal[2]);
     __syncthreads();
     return step;
 }
 
 // Eigenvalues into lam[0..n): the Jacobi diagonal (FP64), or the refined
 // values (MIXED; also refines the eigenvectors in place).
+// Returns status bits (MSP_ITEM_REFINE_LIMIT when the refinement ran out of
+// steps).
 template <typename T, bool REFINE>
-__device__ void eigenpairs(SnapSmem<T> &s, int n, int m);
+__device__ int eigenpairs(SnapSmem<T> &s, int n, int m, int max_refine);
 
 template <>
-__device__ void eigenpairs<double, false>(SnapSmem<double> &s, int n, int m) {
+__device__ int eigenpairs<double, false>(SnapSmem<double> &s, int n, int m, int) {
     for (int j = threadIdx.x; j < n; j += blockDim.x) s.lam[j] = s.w.diag[j];
     __syncthreads();
+    return MSP_ITEM_OK;
 }
 
 // One refinement step leaves an error of order E^2; a step whose largest
-// correction exceeds 2e-4 (a pair within ~1e3 FP32 resolutions, as at a
-// level anticrossing) is followed by another, at most four in all.
+// correction exceeds 2e-4 (clusters resolved by large rotations, levels
+// within ~1e3 FP32 resolutions) is followed by another, at most max_refine
+// in all; a last step still above 2e-4 sets MSP_ITEM_REFINE_LIMIT.
 template <>
-__device__ void eigenpairs<float, true>(SnapSmem<float> &s, int n, int m) {
-    for (int it = 0; it < 4; ++it)
-        if (oa_refine(s, n, m) <= 2e-4f) break;
+__device__ int eigenpairs<float, true>(SnapSmem<float> &s, int n, int m, int max_refine) {
+    if (max_refine <= 0) max_refine = 4;
+    for (int it = 0; it < max_refine; ++it)
+        if (oa_refine(s, n, m) <= 2e-4f) return MSP_ITEM_OK;
+    return MSP_ITEM_REFINE_LIMIT;
 }
 
 // ------------------------------------------------------------------ eigh
@@ -470,8 +400,8 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
             }
         }
         __syncthreads();
-        const int st = jacobi_sweeps<T>(s.w, m, max_sweeps);
-        eigenpairs<T, REFINE>(s, n, m);
+        int st = jacobi_sweeps<T>(s.w, m, max_sweeps);
+        st |= eigenpairs<T, REFINE>(s, n, m, 4);
         // ascending order, ties by index (stable)
         for (int j = tid; j < n; j += nt) {
             int r = 0;
@@ -501,7 +431,7 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
 // 166-217): A = |U^dag (sigma_p (x) 1_d) U|^2 and omega_jk = 2 pi (l_j - l_k)
 // for j > k, scaled by 0.5 * w / (d * N_avg), plus the constant
 // 0.5 * sum_j A_jj part.
-template <typename T, bool REFINE>
+template <typename T, bool REFINE, bool PRE = false>
 __global__ void msp_snap_fast_kernel(SnapArgs a) {
     extern __shared__ __align__(16) char smem[];
     const int n = a.n, m = n + (n & 1), ld = m + 1, d = n / 2;
@@ -514,9 +444,9 @@ __global__ void msp_snap_fast_kernel(SnapArgs a) {
     for (int sn = blockIdx.x; sn < a.num_snap; sn += gridDim.x) {
         const SnapSource src = snap_source(a, sn);
         const size_t g = (size_t)src.g;
-        load_hamiltonian<T, REFINE>(src.Hsys, src.Z, a.field + 3 * g, n, m, s);
-        const int st = jacobi_sweeps<T>(s.w, m, a.max_sweeps);
-        eigenpairs<T, REFINE>(s, n, m);
+        load_hamiltonian<T, REFINE, PRE>(src.Hsys, src.Z, a.field + 3 * g, n, m, s);
+        int st = snap_eigvecs<T, PRE>(a, sn, (int)g, n, m, s);
+        st |= eigenpairs<T, REFINE>(s, n, m, a.max_refine);
 
         // sigma_p = p . sigma (Pauli), applied on the muon (slowest) digit
         const double px = a.pol[3 * g], py = a.pol[3 * g + 1], pz = a.pol[3 * g + 2];
@@ -595,7 +525,7 @@ __device__ void apply_digit(const cx<double> *F, int dim, int stride, const cx<T
 // pair coefficients of <O>(t) = sum_ij rho'_ij O'_ji exp(-i w_ij t)
 // (muspinsim/hamiltonian.py:80-107); INTEGRAL writes the decaying integral
 // divided by tau (muspinsim/hamiltonian.py:150-164, experiment.py:492-496).
-template <typename T, bool REFINE, bool INTEGRAL>
+template <typename T, bool REFINE, bool INTEGRAL, bool PRE = false>
 __global__ void msp_snap_rho_kernel(SnapArgs a) {
     extern __shared__ __align__(16) char smem[];
     const int n = a.n, m = n + (n & 1), ld = m + 1;
@@ -613,9 +543,9 @@ __global__ void msp_snap_rho_kernel(SnapArgs a) {
         } else {
             build_rho_factors(a, sn, s.fac);
         }
-        load_hamiltonian<T, REFINE>(a.Hsys, a.Z, a.field + 3 * (size_t)sn, n, m, s);
-        const int st = jacobi_sweeps<T>(s.w, m, a.max_sweeps);
-        eigenpairs<T, REFINE>(s, n, m);
+        load_hamiltonian<T, REFINE, PRE>(a.Hsys, a.Z, a.field + 3 * (size_t)sn, n, m, s);
+        int st = snap_eigvecs<T, PRE>(a, sn, sn, n, m, s);
+        st |= eigenpairs<T, REFINE>(s, n, m, a.max_refine);
         const cx<T> *U = s.w.U;
 
         // T1 = rho0 U by Kronecker factors: X ping-pongs between H and B2
@@ -752,10 +682,18 @@ int snap_occupancy(int n, int mode, int precision, int threads) {
     if (threads <= 0) threads = snap_default_threads(n);
     const size_t smem = snap_smem_threads(n, mode, precision, 0, threads);
     const bool mixed = precision == MSP_PREC_MIXED;
-    if (mode == MSP_MODE_FAST)
+    if (mode == MSP_MODE_FAST) {
+        if (mixed && jacobi_warp_supported(n))
+            return occupancy_of(msp_snap_fast_kernel<float, true, true>, threads, smem);
         return mixed ? occupancy_of(msp_snap_fast_kernel<float, true>, threads, smem)
                      : occupancy_of(msp_snap_fast_kernel<double, false>, threads, smem);
+    }
     return 1;
+}
+
+size_t snap_evec_bytes(int n, long long num_snap, int precision) {
+    if (precision != MSP_PREC_MIXED || !jacobi_warp_supported(n) || num_snap <= 0) return 0;
+    return (size_t)num_snap * (size_t)n * (size_t)n * sizeof(float2);
 }
 
 // threads = 0: jacobi_threads(m); grid = 0: one CTA per snapshot.  Any
@@ -767,6 +705,17 @@ cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStr
     const size_t smem = snap_smem_threads(a.n, mode, precision, a.fac_len, threads);
     if (grid <= 0 || grid > a.num_snap) grid = a.num_snap;
     const bool mixed = precision == MSP_PREC_MIXED;
+    if (mixed && a.evec != nullptr && jacobi_warp_supported(a.n)) {
+        // two stages: warp Jacobi, then refinement and eigenbasis products
+        const cudaError_t e = launch_jacobi_warp(a, st);
+        if (e != cudaSuccess) return e;
+        if (mode == MSP_MODE_FAST)
+            return launch_snap(msp_snap_fast_kernel<float, true, true>, a, grid, threads, smem, st);
+        if (mode == MSP_MODE_EVOLVE)
+            return launch_snap(msp_snap_rho_kernel<float, true, false, true>, a, grid, threads, smem,
+                               st);
+        return launch_snap(msp_snap_rho_kernel<float, true, true, true>, a, grid, threads, smem, st);
+    }
     if (mode == MSP_MODE_FAST) {
         return mixed ? launch_snap(msp_snap_fast_kernel<float, true>, a, grid, threads, smem, st)
                      : launch_snap(msp_snap_fast_kernel<double, false>, a, grid, threads, smem, st);

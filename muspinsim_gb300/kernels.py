@@ -248,7 +248,8 @@ class PowderPlan:
 
     def __init__(self, n, Hsys, Z, field, pol, wscale, slot, num_slots, times,
                  mode=_lib.MODE_FAST, precision=_lib.PREC_FP64, dims=None, mu_index=0,
-                 gammas=None, temperature=None, rho_fac=None, tau=1.0, max_sweeps=0):
+                 gammas=None, temperature=None, rho_fac=None, tau=1.0, max_sweeps=0,
+                 max_refine=0):
         d = device()
         a = _lib.PowderArgs()
         a.n = int(n)
@@ -300,6 +301,7 @@ class PowderPlan:
         a.mode = int(mode)
         a.precision = int(precision)
         a.max_sweeps = int(max_sweeps)
+        a.max_refine = int(max_refine)
         self.out = torch.empty(shape, dtype=torch.float64, device=d)
         self.status = torch.zeros((max(S, 1),), dtype=torch.int32, device=d)
         a.out = self.out.data_ptr()
@@ -351,10 +353,10 @@ class PowderPlan:
 
 def powder_run(n, Hsys, Z, field, pol, wscale, slot, num_slots, times, mode=_lib.MODE_FAST,
                precision=_lib.PREC_FP64, dims=None, mu_index=0, gammas=None, temperature=None,
-               rho_fac=None, tau=1.0, max_sweeps=0):
+               rho_fac=None, tau=1.0, max_sweeps=0, max_refine=0):
     """One msp_powder_run on fresh device buffers; returns (out, status)."""
     plan = PowderPlan(n, Hsys, Z, field, pol, wscale, slot, num_slots, times, mode, precision,
-                      dims, mu_index, gammas, temperature, rho_fac, tau, max_sweeps)
+                      dims, mu_index, gammas, temperature, rho_fac, tau, max_sweeps, max_refine)
     out = plan.run()
     return out, plan.status[:plan.num_snap]
 
