@@ -65,4 +65,72 @@ __device__ __forceinline__ float pow2_above(float b) {
     return __uint_as_float((e + 1u) << 23);
 }
 
+// ---- anchored double-word product sums (shared by the refinement kernels)
+//
+// A sum of products starts at an anchor K, a power of two >= 4.01 times a
+// bound on the sum's magnitude (|row| |column| by Cauchy-Schwarz), so every
+// partial sum stays within a factor of two of K: s - fl(s + p) is then
+// exact, and fma(a, b, s - t) is the rounding error of t = fl(s + a b).
+// Errors accumulate in a compensation term; the anchor is subtracted
+// exactly at the end.
+
+__device__ __forceinline__ u64 lm_anchor(float bound) {
+    const float K = pow2_above(4.01f * bound);
+    return f32x2(K, K);
+}
+
+// Anchored double-word product-sum step for one complex product a b:
+// ah = (a.re, a.im) as stored (one 64-bit register pair), bx = (b.re,
+// b.re), by = (b.im, b.im) (duplicated once per k and shared by a
+// thread's four outputs):
+//   S1 += ah bx = (a.re b.re, a.im b.re),  S2 += ah by = (a.re b.im, a.im b.im),
+// so that a b = S1 + i S2 (lane-wise: re = S1.x - S2.y, im = S1.y + S2.x)
+// and conj(a) b = conj(S1) + i conj(S2); rounding errors into c1, c2.  The
+// lo parts: al (A's, ALO) times bx, by; ah times blx, bly (B's, BLO).
+template <bool ALO, bool BLO>
+__device__ __forceinline__ void lm_step(u64 &s1, u64 &c1, u64 &s2, u64 &c2, u64 ah, u64 al, u64 bx,
+                                        u64 by, u64 blx, u64 bly) {
+    const u64 t1 = fma_f32x2(ah, bx, s1);
+    const u64 t2 = fma_f32x2(ah, by, s2);
+    c1 = add2(c1, fma_f32x2(ah, bx, sub2(s1, t1)));
+    c2 = add2(c2, fma_f32x2(ah, by, sub2(s2, t2)));
+    s1 = t1;
+    s2 = t2;
+    if (BLO) {
+        c1 = fma_f32x2(ah, blx, c1);
+        c2 = fma_f32x2(ah, bly, c2);
+    }
+    if (ALO) {
+        c1 = fma_f32x2(al, bx, c1);
+        c2 = fma_f32x2(al, by, c2);
+    }
+}
+
+// (re, im) -> (re, -im) on a lane pair: the sign bit of the upper lane
+__device__ __forceinline__ u64 lm_conj2(u64 v) { return v ^ 0x8000000000000000ull; }
+
+// The double-word value of an anchored sum pair (a b, or conj(a) b when
+// CONJ), anchor K removed: (re_hi, im_hi, re_lo, im_lo).
+template <bool CONJ>
+__device__ __forceinline__ float4 lm_dw(u64 s1, u64 c1, u64 s2, u64 c2, u64 K) {
+    s1 = sub2(s1, K);  // exact
+    s2 = sub2(s2, K);
+    if (CONJ) {
+        s1 = lm_conj2(s1);
+        c1 = lm_conj2(c1);
+        s2 = lm_conj2(s2);
+        c2 = lm_conj2(c2);
+    }
+    return dw_finish(s1, c1, s2, c2);
+}
+
+// The FP32 value of a plain sum pair (a b, or conj(a) b when CONJ).
+template <bool CONJ>
+__device__ __forceinline__ cx<float> lm_plain(u64 s1, u64 s2) {
+    float ax, ay, bx, by;
+    split_f32x2(s1, ax, ay);
+    split_f32x2(s2, bx, by);
+    return CONJ ? mk<float>(ax + by, bx - ay) : mk<float>(ax - by, ay + bx);
+}
+
 }  // namespace msp

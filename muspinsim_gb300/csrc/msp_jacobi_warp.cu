@@ -18,20 +18,24 @@
 // steps and a full sweep returns every index to its own position.  The
 // permutation is folded into where each updated element is stored.
 //   * H, upper triangle, as h (h + 1) / 2 blocks of 2 x 2 complex (block
-//     (X, Y), X <= Y, holds rows 2X..2X+1 and columns 2Y..2Y+1); a diagonal
+//     (X, Y), X <= Y, holds rows 2X..2X+1 and columns 2Y..2Y+1; first rows
+//     and second rows in two separate arrays, jw_slot); a diagonal
 //     block keeps only its coupling (2X, 2X+1), the diagonal entries are
 //     tracked separately.  Double-buffered: step s reads one buffer and
 //     writes the permuted result into the other.
 //   * The eigenvector matrix U (U <- U G): lane r keeps row r in registers;
 //     the rotations of a step act on register pairs (2k, 2k+1), then the
 //     row is permuted like the positions.
-// A step: each lane updates whole 2 x 2 blocks, B' = G_k1^H B G_k2, and
-// stores every element at its permuted place (conjugated when it lands in
-// the lower triangle).  The element that becomes the coupling of a next-step
-// pair is stored in that pair's diagonal block, and the lane that produced
-// it also computes the next step's rotation from it and the new diagonal
-// entries (known from this step's rotations), so one __syncwarp ends a
-// step.  Rotation, convergence test and tolerances are those of
+// A step: each lane updates whole off-diagonal 2 x 2 blocks,
+// B' = G_k1^H B G_k2, and stores every element at its permuted place
+// (conjugated when it lands in the lower triangle); the elements that
+// become next-step couplings land in the diagonal blocks.  After a
+// __syncwarp, lane X computes next-step pair X's rotation from its coupling
+// and the two diagonal entries (this step's rotated diagonal, moved), and
+// stores the zero left by this step's pair X at its new place.  The
+// rotation arithmetic uses the hardware reciprocal square root: a rotation
+// only has to stay unitary to FP32 rounding, and the refinement stage
+// restores full accuracy.  Convergence test and tolerances are those of
 // msp_jacobi.cuh (FP32: off-diagonal norm <= 4e-7 of the total, or a
 // rounding floor of 2e-5 that a sweep no longer shrinks).
 #include "msp_internal.cuh"
@@ -50,21 +54,55 @@ __host__ __device__ constexpr int jw_next(int p, int h) {
                              : ((p >> 1) == h - 1 ? p + 1 : p + 2));
 }
 
+// Previous position of the element now at position p (the inverse of
+// jw_next).
+__host__ __device__ constexpr int jw_prev(int p, int h) {
+    return p == 0 ? 0
+                  : (p == 2 ? 1
+                            : ((p & 1) == 0 ? p - 2 : (p == 2 * h - 1 ? p - 1 : p + 2)));
+}
+
 // Storage index of block (X, Y), X <= Y: diagonal blocks first.
 __host__ __device__ constexpr int jw_blk(int X, int Y, int h) {
     return X == Y ? X : h + X * (2 * h - X - 1) / 2 + (Y - X - 1);
 }
 
-// Route code of one updated element: destination float2 index (block * 4
-// + slot, 10 bits), conjugate flag (bit 10), producer flag (bit 11: the
-// element is a next-step pair coupling; when the conjugate flag is set the
-// element's row position becomes the pair's second member).
+// float2 index of slot s (row-in-pair * 2 + column-in-pair) of block b:
+// slots 0, 1 of every block in one array and slots 2, 3 in another, so that
+// a lane reads its block's two rows with two conflict-free 16-byte loads.
+__host__ __device__ constexpr int jw_slot(int b, int s, int h) {
+    return (s >> 1) * (h * (h + 1)) + 2 * b + (s & 1);
+}
+
+// Route code of one updated element: destination float2 index (15 bits)
+// and a conjugate flag (bit 15) when the element lands in the lower
+// triangle.  A next-step coupling (both positions in pair X) goes to slot 1
+// of diagonal block X as element (2X, 2X+1).
 __device__ __forceinline__ unsigned jw_route(int x0, int y0, int h) {
     const int x = jw_next(x0, h), y = jw_next(y0, h);
     const int X = x >> 1, Y = y >> 1;
-    if (X < Y) return (unsigned)(jw_blk(X, Y, h) * 4 + (x & 1) * 2 + (y & 1));
-    if (X > Y) return (unsigned)(jw_blk(Y, X, h) * 4 + (y & 1) * 2 + (x & 1)) | (1u << 10);
-    return (unsigned)(X * 4 + 1) | ((unsigned)(x & 1) << 10) | (1u << 11);
+    if (X < Y) return (unsigned)jw_slot(jw_blk(X, Y, h), (x & 1) * 2 + (y & 1), h);
+    if (X > Y) return (unsigned)jw_slot(jw_blk(Y, X, h), (y & 1) * 2 + (x & 1), h) | (1u << 15);
+    return (unsigned)jw_slot(X, 1, h) | ((unsigned)(x & 1) << 15);
+}
+
+// Rotation [[c, s], [-conj(s), c]] zeroing apq (diagonal app, aqq) and the
+// new diagonal entries, couplings at or below `skip` left alone; float4
+// (c, s.re, s.im, 0).
+__device__ __forceinline__ float4 jw_rotation(float app, float aqq, float2 apq, float skip,
+                                              float &na, float &nb) {
+    const float mag2 = fmaf(apq.x, apq.x, apq.y * apq.y);
+    na = app;
+    nb = aqq;
+    if (!(mag2 > skip * skip)) return make_float4(1.f, 0.f, 0.f, 0.f);
+    const float rinv = rsqrtf(mag2), mag = mag2 * rinv;
+    const float zeta = 0.5f * (aqq - app) * rinv;
+    const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
+    const float c = rsqrtf(fmaf(t, t, 1.f));
+    const float f = t * c * rinv;
+    na = app - t * mag;
+    nb = aqq + t * mag;
+    return make_float4(c, f * apq.x, f * apq.y, 0.f);
 }
 
 template <int M>
@@ -72,7 +110,6 @@ struct JwShape {
     static constexpr int H = M / 2;
     static constexpr int NB = H * (H + 1) / 2;  // blocks
     static constexpr int NOFF = NB - H;         // off-diagonal blocks
-    static constexpr int NTASK = H + NOFF;      // zero stores + block updates
 };
 
 // Per-warp shared memory (floats): two H buffers, two rotation tables, two
@@ -104,7 +141,7 @@ __device__ __forceinline__ void jw_rotate(float4 R, cx<float> &x, cx<float> &y) 
 }  // namespace
 
 template <int M>
-__global__ void __launch_bounds__(JW_WARPS * 32) msp_jacobi_warp_kernel(SnapArgs a) {
+__global__ void __launch_bounds__(JW_WARPS * 32, 4) msp_jacobi_warp_kernel(SnapArgs a) {
     using S = JwShape<M>;
     constexpr int H = S::H, NB = S::NB, NOFF = S::NOFF;
     extern __shared__ __align__(16) char smem[];
@@ -123,27 +160,21 @@ __global__ void __launch_bounds__(JW_WARPS * 32) msp_jacobi_warp_kernel(SnapArgs
     auto rbuf = [&](int b) { return rot0 + b * H; };
     auto dbuf = [&](int b) { return dia0 + b * M; };
 
-    // route tables: producer blocks first, so that the rotation arithmetic
-    // spreads over different lanes
-    if (threadIdx.x == 0) {
-        int pos = 0;
-        for (int pass = 0; pass < 2; ++pass)
-            for (int k1 = 0; k1 < H; ++k1)
-                for (int k2 = k1 + 1; k2 < H; ++k2) {
-                    unsigned c[4];
-                    bool prod = false;
-                    for (int r = 0; r < 2; ++r)
-                        for (int q = 0; q < 2; ++q) {
-                            c[r * 2 + q] = jw_route(2 * k1 + r, 2 * k2 + q, H);
-                            prod |= (c[r * 2 + q] >> 11) & 1u;
-                        }
-                    if (prod != (pass == 0)) continue;
-                    route[pos] = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
-                    kk[pos] = (unsigned)k1 | ((unsigned)k2 << 8);
-                    ++pos;
-                }
-        for (int k = 0; k < H; ++k) zroute[k] = jw_route(2 * k, 2 * k + 1, H);
+    // route tables
+    for (int o = threadIdx.x; o < NOFF; o += blockDim.x) {
+        int k1 = 0, rem = o;
+        while (rem >= H - 1 - k1) {
+            rem -= H - 1 - k1;
+            ++k1;
+        }
+        const int k2 = k1 + 1 + rem;  // o = jw_blk(k1, k2) - H
+        unsigned c[4];
+        for (int r = 0; r < 2; ++r)
+            for (int q = 0; q < 2; ++q) c[r * 2 + q] = jw_route(2 * k1 + r, 2 * k2 + q, H);
+        route[o] = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+        kk[o] = (unsigned)k1 | ((unsigned)k2 << 8);
     }
+    for (int k = threadIdx.x; k < H; k += blockDim.x) zroute[k] = jw_route(2 * k, 2 * k + 1, H);
     __syncthreads();
 
     const int n = a.n;
@@ -175,7 +206,7 @@ __global__ void __launch_bounds__(JW_WARPS * 32) msp_jacobi_warp_kernel(SnapArgs
                 fro += hr * hr;
             } else {
                 const int X = j >> 1, Y = i >> 1;
-                Hbuf(0)[jw_blk(X, Y, H) * 4 + (j & 1) * 2 + (i & 1)] = make_float2(hr, hi);
+                Hbuf(0)[jw_slot(jw_blk(X, Y, H), (j & 1) * 2 + (i & 1), H)] = make_float2(hr, hi);
                 fro += 2.f * (hr * hr + hi * hi);
             }
         }
@@ -185,12 +216,9 @@ __global__ void __launch_bounds__(JW_WARPS * 32) msp_jacobi_warp_kernel(SnapArgs
         const float skip = tol * sqrtf(fro) / (float)M;
         // rotations of step 0
         if (lane < H) {
-            const float2 apq = Hbuf(0)[lane * 4 + 1];
-            JRot<float> R;
             float na, nb;
-            jacobi_rotation<float>(dbuf(1)[2 * lane], dbuf(1)[2 * lane + 1], mk<float>(apq.x, apq.y),
-                                   skip, 0, 0, R, na, nb);
-            rbuf(0)[lane] = make_float4(R.c, R.sr, R.si, 0.f);
+            rbuf(0)[lane] = jw_rotation(dbuf(1)[2 * lane], dbuf(1)[2 * lane + 1],
+                                        Hbuf(0)[jw_slot(lane, 1, H)], skip, na, nb);
             dbuf(0)[2 * lane] = na;
             dbuf(0)[2 * lane + 1] = nb;
         }
@@ -208,12 +236,12 @@ __global__ void __launch_bounds__(JW_WARPS * 32) msp_jacobi_warp_kernel(SnapArgs
             float off = 0.f;
             for (int t = lane; t < NB; t += 32) {
                 if (t < H) {
-                    const float2 v = Hbuf(cur)[t * 4 + 1];
+                    const float2 v = Hbuf(cur)[jw_slot(t, 1, H)];
                     off += 2.f * (v.x * v.x + v.y * v.y);
                 } else {
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        const float2 v = Hbuf(cur)[t * 4 + q];
+                        const float2 v = Hbuf(cur)[jw_slot(t, q, H)];
                         off += 2.f * (v.x * v.x + v.y * v.y);
                     }
                 }
@@ -245,18 +273,12 @@ __global__ void __launch_bounds__(JW_WARPS * 32) msp_jacobi_warp_kernel(SnapArgs
 #pragma unroll
                     for (int p = 0; p < M; ++p) u[p] = w[p];
                 }
-                for (int t = lane; t < S::NTASK; t += 32) {
-                    if (t < H) {
-                        // the zeroed coupling of pair t moves to its new place
-                        Hn[zroute[t] & 1023u] = make_float2(0.f, 0.f);
-                        continue;
-                    }
-                    const int o = t - H;
+                for (int o = lane; o < NOFF; o += 32) {
                     const unsigned k12 = kk[o];
                     const int k1 = (int)(k12 & 255u), k2 = (int)(k12 >> 8);
-                    const float2 *B = Hbuf(cur) + (size_t)jw_blk(k1, k2, H) * 4;
-                    const float4 bA = *reinterpret_cast<const float4 *>(B);
-                    const float4 bB = *reinterpret_cast<const float4 *>(B + 2);
+                    const float2 *B = Hbuf(cur);
+                    const float4 bA = *reinterpret_cast<const float4 *>(B + jw_slot(H + o, 0, H));
+                    const float4 bB = *reinterpret_cast<const float4 *>(B + jw_slot(H + o, 2, H));
                     const cx<float> b00 = mk<float>(bA.x, bA.y), b01 = mk<float>(bA.z, bA.w);
                     const cx<float> b10 = mk<float>(bB.x, bB.y), b11 = mk<float>(bB.z, bB.w);
                     const float4 R1 = rc[k1], R2 = rc[k2];
@@ -277,24 +299,20 @@ __global__ void __launch_bounds__(JW_WARPS * 32) msp_jacobi_warp_kernel(SnapArgs
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         const unsigned code = ((q < 2 ? rt.x : rt.y) >> (16 * (q & 1))) & 0xffffu;
-                        const bool cj = (code >> 10) & 1u;
-                        const cx<float> v = cj ? conj(nv[q]) : nv[q];
-                        Hn[code & 1023u] = make_float2(v.re, v.im);
-                        if (code & (1u << 11)) {
-                            // next-step pair X = dest / 4: (2X, 2X+1) takes the
-                            // element's row position first unless conjugated
-                            const int pr = 2 * k1 + (q >> 1), pc = 2 * k2 + (q & 1);
-                            const float app = cj ? dc[pc] : dc[pr];
-                            const float aqq = cj ? dc[pr] : dc[pc];
-                            const int X = (int)((code & 1023u) >> 2);
-                            JRot<float> Rn;
-                            float na, nb;
-                            jacobi_rotation<float>(app, aqq, v, skip, 0, 0, Rn, na, nb);
-                            rbuf(nxt)[X] = make_float4(Rn.c, Rn.sr, Rn.si, 0.f);
-                            dbuf(nxt)[2 * X] = na;
-                            dbuf(nxt)[2 * X + 1] = nb;
-                        }
+                        const float sg = (code & 0x8000u) ? -1.f : 1.f;
+                        Hn[code & 0x7fffu] = make_float2(nv[q].re, sg * nv[q].im);
                     }
+                }
+                __syncwarp();
+                // next-step rotations; this step's zeroed couplings moved
+                if (lane < H) {
+                    Hn[zroute[lane] & 0x7fffu] = make_float2(0.f, 0.f);
+                    float na, nb;
+                    rbuf(nxt)[lane] = jw_rotation(dc[jw_prev(2 * lane, H)],
+                                                  dc[jw_prev(2 * lane + 1, H)],
+                                                  Hn[jw_slot(lane, 1, H)], skip, na, nb);
+                    dbuf(nxt)[2 * lane] = na;
+                    dbuf(nxt)[2 * lane + 1] = nb;
                 }
                 __syncwarp();
                 cur = nxt;

@@ -16,6 +16,7 @@
 //            sweeps themselves instead of dominating as FP64 would.
 #include "msp_internal.cuh"
 #include "msp_cluster.cuh"
+#include "msp_dw.cuh"
 #include "msp_jacobi.cuh"
 #include "msp_rho.cuh"
 
@@ -30,7 +31,7 @@ static_assert(sizeof(JRot<float>) == 16 && sizeof(JRot<double>) == 32, "JRot lay
 struct SnapLayout {
     size_t H, U, rot, dia, red, tab, diag;     // Jacobi work
     size_t lam, acc, rank;                     // eigenvalues, reductions, sort
-    size_t Hh, Hl, Yl, SR, sd, corr, rd, lamf, rk, ord, cst, scal;  // refinement (MIXED)
+    size_t Hh, Hl, Yl, SR, sd, corr, rd, lamf, rk, ord, cst, scal, rn, cn, yn;  // refinement (MIXED)
     size_t fac, B2;                            // general path
     size_t total;
 };
@@ -64,7 +65,7 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
     L.acc = lay_take(off, 2 * 8);
     L.rank = lay_take(off, m * 4);
     L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = L.lamf = 0;
-    L.rk = L.ord = L.cst = L.scal = 0;
+    L.rk = L.ord = L.cst = L.scal = L.rn = L.cn = L.yn = 0;
     if (refine) {
         L.Hh = lay_take(off, mm * 8);
         L.Hl = lay_take(off, mm * 8);
@@ -78,6 +79,9 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
         L.ord = lay_take(off, m * 4);
         L.cst = lay_take(off, m * 4);
         L.scal = lay_take(off, 4 * 4);
+        L.rn = lay_take(off, m * 4);
+        L.cn = lay_take(off, m * 4);
+        L.yn = lay_take(off, m * 4);
     }
     L.fac = L.B2 = 0;
     if (rho) {
@@ -113,6 +117,7 @@ struct SnapSmem {
     double *sd, *rd;
     float *corr, *lamf;
     int *rk, *ord, *cst, *scal;  // refinement clusters
+    float *rn, *cn, *yn;         // norms: rows of H, columns of X and of Y
     cx<double> *fac;
     cx<T> *B2;
 };
@@ -144,6 +149,9 @@ __device__ __forceinline__ SnapSmem<T> snap_carve(char *base, int n, bool rho, i
     s.ord = REFINE ? reinterpret_cast<int *>(base + L.ord) : nullptr;
     s.cst = REFINE ? reinterpret_cast<int *>(base + L.cst) : nullptr;
     s.scal = REFINE ? reinterpret_cast<int *>(base + L.scal) : nullptr;
+    s.rn = REFINE ? reinterpret_cast<float *>(base + L.rn) : nullptr;
+    s.cn = REFINE ? reinterpret_cast<float *>(base + L.cn) : nullptr;
+    s.yn = REFINE ? reinterpret_cast<float *>(base + L.yn) : nullptr;
     s.fac = rho ? reinterpret_cast<cx<double> *>(base + L.fac) : nullptr;
     s.B2 = rho ? reinterpret_cast<cx<T> *>(base + L.B2) : nullptr;
     return s;
@@ -177,6 +185,21 @@ __device__ __forceinline__ void store_frequency(const SnapArgs &a, size_t o, dou
     }
 }
 
+// Row norms of H's hi part (bounds of the refinement's anchored sums).
+template <typename T>
+__device__ void hamiltonian_row_norms(SnapSmem<T> &s, int n, int m) {
+    const int ld = m + 1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        float acc = 0.f;
+        for (int k = 0; k < n; ++k) {
+            const cx<float> h = s.Hh[i * ld + k];
+            acc = fmaf(h.re, h.re, fmaf(h.im, h.im, acc));
+        }
+        s.rn[i] = sqrtf(acc);
+    }
+    __syncthreads();
+}
+
 // H = Hsys + b . Z (FP64) into the Jacobi buffer (precision T, padded to m);
 // in MIXED mode also its exact split H = Hh + Hl into two FP32 matrices.
 template <typename T, bool REFINE, bool PRE = false>
@@ -202,6 +225,7 @@ __device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
         }
     }
     __syncthreads();
+    if (REFINE) hamiltonian_row_norms(s, n, m);
 }
 
 // The eigensolve of a snapshot: FP64 or FP32 Jacobi in this CTA, or (PRE)
@@ -241,55 +265,64 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     cx<float> *X = s.w.U;
     cx<float> *Yh = s.w.H;  // Jacobi work matrix is free now
     if (tid < 4) s.scal[tid] = 0;  // [0]: amax, [1]: max|l|, [2]: step (float bits)
-    // Y = H X
-    for (int e = tid; e < n * n; e += nt) {
-        const int i = FastDiv(n).div(e), j = e - i * n;
-        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-        for (int k = 0; k < n; ++k) {
-            const cx<float> h = s.Hh[i * ld + k], hl = s.Hl[i * ld + k], x = X[k * ld + j];
-            dw_acc(rh, rl, h.re, x.re);
-            dw_acc(rh, rl, -h.im, x.im);
-            dw_acc(ih, il, h.re, x.im);
-            dw_acc(ih, il, h.im, x.re);
-            rl = fmaf(hl.re, x.re, rl);
-            rl = fmaf(-hl.im, x.im, rl);
-            il = fmaf(hl.re, x.im, il);
-            il = fmaf(hl.im, x.re, il);
-        }
-        Yh[i * ld + j] = mk<float>(rh, ih);
-        s.Yl[i * ld + j] = mk<float>(rl, il);
+    // anchored double-word products (msp_dw.cuh): column norms of X bound
+    // every partial sum
+    for (int j = tid; j < n; j += nt) {
+        float acc = 0.f;
+        for (int k = 0; k < n; ++k) acc = fmaf(X[k * ld + j].re, X[k * ld + j].re,
+                                               fmaf(X[k * ld + j].im, X[k * ld + j].im, acc));
+        s.cn[j] = sqrtf(acc);
     }
     __syncthreads();
-    // S_ij (i <= j) into SR upper triangle / sd; R_ij (i < j) into SR lower
-    // triangle at (j, i); R_ii into rd
+    // Y = H X (H as hi + lo)
+    for (int e = tid; e < n * n; e += nt) {
+        const int i = FastDiv(n).div(e), j = e - i * n;
+        const u64 K = lm_anchor(s.rn[i] * s.cn[j]);
+        u64 s1 = K, s2 = K, c1 = 0ull, c2 = 0ull;
+        const u64 *hh = reinterpret_cast<const u64 *>(s.Hh + i * ld);
+        const u64 *hl = reinterpret_cast<const u64 *>(s.Hl + i * ld);
+        for (int k = 0; k < n; ++k) {
+            const cx<float> x = X[k * ld + j];
+            lm_step<true, false>(s1, c1, s2, c2, hh[k], hl[k], f32x2(x.re, x.re),
+                                 f32x2(x.im, x.im), 0ull, 0ull);
+        }
+        const float4 r = lm_dw<false>(s1, c1, s2, c2, K);
+        Yh[i * ld + j] = mk<float>(r.x, r.y);
+        s.Yl[i * ld + j] = mk<float>(r.z, r.w);
+    }
+    __syncthreads();
+    for (int j = tid; j < n; j += nt) {
+        float acc = 0.f;
+        for (int k = 0; k < n; ++k) acc = fmaf(Yh[k * ld + j].re, Yh[k * ld + j].re,
+                                               fmaf(Yh[k * ld + j].im, Yh[k * ld + j].im, acc));
+        s.yn[j] = sqrtf(acc);
+    }
+    __syncthreads();
+    // S_ij = X_i^H Y_j (i <= j) into SR upper triangle / sd; R_ij = -X_i^H X_j
+    // (i < j) into SR lower triangle at (j, i); R_ii into rd
     const int ntri = n * (n + 1) / 2;
     for (int e = tid; e < ntri; e += nt) {
         int j, i;
         tri_index(e, j, i);  // j >= i
-        float sr = 0.f, srl = 0.f, si = 0.f, sil = 0.f;
-        float gr = 0.f, grl = 0.f, gi = 0.f, gil = 0.f;
+        const u64 KS = lm_anchor(s.cn[i] * s.yn[j]), KG = lm_anchor(s.cn[i] * s.cn[j]);
+        u64 a1 = KS, a2 = KS, ac1 = 0ull, ac2 = 0ull;
+        u64 g1 = KG, g2 = KG, gc1 = 0ull, gc2 = 0ull;
         for (int k = 0; k < n; ++k) {
-            const cx<float> xi = X[k * ld + i], xj = X[k * ld + j];
-            const cx<float> yh = Yh[k * ld + j], yl = s.Yl[k * ld + j];
-            // conj(xi) * (yh + yl)
-            dw_acc(sr, srl, xi.re, yh.re);
-            dw_acc(sr, srl, xi.im, yh.im);
-            dw_acc(si, sil, xi.re, yh.im);
-            dw_acc(si, sil, -xi.im, yh.re);
-            srl = fmaf(xi.re, yl.re, fmaf(xi.im, yl.im, srl));
-            sil = fmaf(xi.re, yl.im, fmaf(-xi.im, yl.re, sil));
-            // conj(xi) * xj
-            dw_acc(gr, grl, xi.re, xj.re);
-            dw_acc(gr, grl, xi.im, xj.im);
-            dw_acc(gi, gil, xi.re, xj.im);
-            dw_acc(gi, gil, -xi.im, xj.re);
+            const u64 xi = *reinterpret_cast<const u64 *>(X + k * ld + i);
+            const cx<float> y = Yh[k * ld + j], yl = s.Yl[k * ld + j], xj = X[k * ld + j];
+            lm_step<false, true>(a1, ac1, a2, ac2, xi, 0ull, f32x2(y.re, y.re), f32x2(y.im, y.im),
+                                 f32x2(yl.re, yl.re), f32x2(yl.im, yl.im));
+            lm_step<false, false>(g1, gc1, g2, gc2, xi, 0ull, f32x2(xj.re, xj.re),
+                                  f32x2(xj.im, xj.im), 0ull, 0ull);
         }
+        const float4 S = lm_dw<true>(a1, ac1, a2, ac2, KS);
+        const float4 G = lm_dw<true>(g1, gc1, g2, gc2, KG);
         if (i == j) {
-            s.sd[i] = (double)sr + (double)srl;
-            s.rd[i] = (1.0 - (double)gr) - (double)grl;  // R_ii = 1 - G_ii
+            s.sd[i] = (double)S.x + (double)S.z;
+            s.rd[i] = (1.0 - (double)G.x) - (double)G.z;  // R_ii = 1 - G_ii
         } else {
-            s.SR[i * ld + j] = mk<float>(sr + srl, si + sil);
-            s.SR[j * ld + i] = mk<float>(-(gr + grl), -(gi + gil));  // R_ij = -G_ij
+            s.SR[i * ld + j] = mk<float>(S.x + S.z, S.y + S.w);
+            s.SR[j * ld + i] = mk<float>(-(G.x + G.z), -(G.y + G.w));  // R_ij = -G_ij
         }
     }
     __syncthreads();
@@ -400,6 +433,7 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
             }
         }
         __syncthreads();
+        if (REFINE) hamiltonian_row_norms(s, n, m);
         int st = jacobi_sweeps<T>(s.w, m, max_sweeps);
         st |= eigenpairs<T, REFINE>(s, n, m, 4);
         // ascending order, ties by index (stable)

@@ -41,7 +41,7 @@ class Lindbladian(SuperOperator):
         Ld = gamma * (SuperOperator.bracket(A) - 0.5 * SuperOperator.anticommutator(AA))
         if Ld.dimension != self.dimension:
             raise ValueError("Invalid dissipation operator for this Lindbladian")
-        self._matrix = self._matrix + Ld.matrix
+        self._mat = self._mat + Ld.matrix
 
     def _checked(self, rho0, operators):
         dim = rho0.dimension

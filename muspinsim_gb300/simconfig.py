@@ -38,13 +38,31 @@ _CDICT = {
     "orientation": "orient",
     "temperature": "T",
 }
-_CSDICT = {
-    "zeeman": "zmn",
-    "dipolar": "dip",
-    "quadrupolar": "quad",
-    "hyperfine": "hfc",
-    "dissipation": "dsp",
+# Coupling kinds: the shape of the value and how a term enters the spin
+# system (i, j 0-based; j may be None).  Dissipation terms are collected
+# per spin instead, for the runner's Lindbladian.
+_COUPLINGS = {
+    "zeeman": ((3,), lambda sy, i, j, v: sy.add_zeeman_term(i, v)),
+    "dipolar": ((3,), lambda sy, i, j, v: sy.add_dipolar_term(i, j, v)),
+    "hyperfine": ((3, 3), lambda sy, i, j, v: sy.add_hyperfine_term(i, v, j)),
+    "quadrupolar": ((3, 3), lambda sy, i, j, v: sy.add_quadrupolar_term(i, v)),
+    "dissipation": ((1,), None),
 }
+
+
+def _index_grid(ranges):
+    """Every index combination of an ordered set of ranges (a time range is
+    kept whole: its index is slice(None)), first range slowest."""
+    return list(product(*[[slice(None)] if k == "t" else range(len(v))
+                          for k, v in ranges.items()]))
+
+
+def _exposed(attr, view=None):
+    """Read-only property returning attribute `attr` (through `view`, which
+    returns a copy where callers must not alias the state)."""
+    if view is None:
+        return property(lambda self: getattr(self, attr))
+    return property(lambda self: view(getattr(self, attr)))
 
 ConfigSnapshot = namedtuple("ConfigSnapshot", ["id", "y"] + list(_CDICT.values()))
 MuSpinInputValue = namedtuple("MuSpinInputValue", ["name", "args", "value"])
@@ -126,7 +144,14 @@ class ParamsInput:
 
 class MuSpinConfig:
     """Ranges, snapshots and result accumulation of one simulation
-    (muspinsim/simconfig.py:78-647)."""
+    (muspinsim/simconfig.py:78-647).
+
+    Every axis keyword is validated into a list of values and then takes
+    one role: a constant (one value), the x axis, an averaged axis or a
+    file range (several values; _axis_role).  The snapshots are the index
+    grid file x averaged x x, and results[file, x] accumulates the averaged
+    snapshots' signal.
+    """
 
     def __init__(self, params={}, use_experimental_x_axis=True):
         self._constants = {}
@@ -140,102 +165,108 @@ class MuSpinConfig:
         self._celio = self._validate_celio(params["celio"].value[0])
         self._y_axis = self.validate("y", params["y_axis"].value[0])[0]
         self._results_function = params["results_function"]
-        try:
-            x = _CDICT[params["x_axis"].value[0][0]]
-        except KeyError as exc:
-            raise MuSpinConfigError("Invalid x axis name in input file") from exc
-        self._x_range[x] = None
-        for a in np.asarray(params["average_axes"].value).reshape((-1,)):
-            if str(a).lower() == "none":
-                continue
-            try:
-                self._avg_ranges[_CDICT[a]] = None
-            except KeyError as exc:
-                raise MuSpinConfigError("Invalid average axis name in input file") from exc
+        x_axis, averaged = self._declared_axes(params)
+        self._time_isavg = "t" in averaged
         self._time_N = 0
-        self._time_isavg = "t" in self._avg_ranges
+        avg_values = OrderedDict((a, None) for a in averaged)
+        x_values = None
         for iname, cname in _CDICT.items():
-            try:
-                p = params[iname]
-            except KeyError as exc:
+            if iname not in params:
                 raise MuSpinConfigError(
-                    f"Invalid params object passed to MuSpinConfig: missing {iname}") from exc
-            v = self.validate(cname, p.value, p.args)
-            if cname == "t":
-                if self._y_axis == "integral":
-                    logging.warning("Ignoring time axis since Y = integral")
-                    v = [np.inf]
-                self._time_N = len(v)
-            elif cname == "orient":
-                if cname in self._avg_ranges:
-                    norm = len(v) / np.sum(np.array([w for (q, w) in v]))
-                    v = [(q, w * norm) for (q, w) in v]
-                else:
-                    v = [(q, 1.0) for (q, w) in v]
-            if len(v) > 1:
-                if cname in self._x_range:
-                    self._x_range[cname] = v
-                elif cname in self._avg_ranges:
-                    self._avg_ranges[cname] = v
-                else:
-                    self._file_ranges[cname] = v
+                    f"Invalid params object passed to MuSpinConfig: missing {iname}")
+            values = self._axis_values(cname, params[iname], averaged)
+            role = self._axis_role(cname, len(values), x_axis, averaged)
+            if role == "const":
+                self._constants[cname] = values[0]
+            elif role == "x":
+                x_values = values
+            elif role == "avg":
+                avg_values[cname] = values
             else:
-                self._constants[cname] = v[0]
-        if self._y_axis == "integral" and "t" in self._x_range:
+                self._file_ranges[cname] = values
+        if self._y_axis == "integral" and x_axis == "t":
             raise MuSpinConfigError("Can not use time as X axis when evaluating integral of signal")
         if params["fitting_info"].get("fit"):
             raise MuSpinConfigError("Fitting configurations are not supported by muspinsim_gb300")
-        if list(self._x_range.values())[0] is None:
+        if x_values is None:
             raise MuSpinConfigError("Specified x axis is not a range")
-        self._avg_ranges = OrderedDict((k, v) for k, v in self._avg_ranges.items() if v is not None)
+        self._x_range[x_axis] = x_values
+        # averaged axes in the order they were declared, ranges only
+        self._avg_ranges = OrderedDict((k, v) for k, v in avg_values.items() if v is not None)
+        self._system, self._dissip_terms = self._build_system(params["couplings"])
+        self._results = np.zeros([len(v) for v in self._file_ranges.values()]
+                                 + [len(x_values)])
+        grids = [_index_grid(r) for r in (self._file_ranges, self._avg_ranges, self._x_range)]
+        self._configurations = list(product(*grids))
+        self._avg_N = len(grids[1])
 
-        self._system = MuonSpinSystem(self._spins, self.celio_k)
-        self._dissip_terms = {}
-        for iid, idata in params["couplings"].items():
-            try:
-                cname = _CSDICT[idata.name]
-            except KeyError as exc:
+    @staticmethod
+    def _declared_axes(params):
+        """The x axis and the averaged axes (declaration order), as config
+        keys."""
+        try:
+            x_axis = _CDICT[params["x_axis"].value[0][0]]
+        except KeyError as exc:
+            raise MuSpinConfigError("Invalid x axis name in input file") from exc
+        averaged = []
+        for a in np.asarray(params["average_axes"].value).reshape((-1,)):
+            if str(a).lower() == "none":
+                continue
+            if a not in _CDICT:
+                raise MuSpinConfigError("Invalid average axis name in input file")
+            if _CDICT[a] not in averaged:
+                averaged.append(_CDICT[a])
+        return x_axis, averaged
+
+    def _axis_values(self, cname, pvalue, averaged):
+        """Validated values of one axis keyword.  Time: a single infinite
+        time when the y axis is the integral.  Orientations: weights scaled
+        to sum to the count when averaged, else all 1."""
+        values = self.validate(cname, pvalue.value, pvalue.args)
+        if cname == "t":
+            if self._y_axis == "integral":
+                logging.warning("Ignoring time axis since Y = integral")
+                values = [np.inf]
+            self._time_N = len(values)
+        elif cname == "orient":
+            if cname in averaged:
+                scale = len(values) / np.sum([w for (_, w) in values])
+                values = [(q, w * scale) for (q, w) in values]
+            else:
+                values = [(q, 1.0) for (q, _) in values]
+        return values
+
+    @staticmethod
+    def _axis_role(cname, count, x_axis, averaged):
+        if count <= 1:
+            return "const"
+        if cname == x_axis:
+            return "x"
+        return "avg" if cname in averaged else "file"
+
+    def _build_system(self, couplings):
+        """The MuonSpinSystem of the coupling terms, and the dissipation
+        rates by spin."""
+        system = MuonSpinSystem(self._spins, self.celio_k)
+        dissipation = {}
+        nspins = len(self._spins)
+        for term in couplings.values():
+            if term.name not in _COUPLINGS:
                 raise MuSpinConfigError(
-                    f"Invalid params object passed to MuSpinConfig: unknown {idata.name} coupling"
-                ) from exc
-            args = idata.args
-            ij = np.array([v for v in args.values() if v is not None])
-            if (ij < 1).any() or (ij > len(self._spins)).any():
+                    f"Invalid params object passed to MuSpinConfig: unknown {term.name} coupling")
+            shape, add = _COUPLINGS[term.name]
+            indices = [v for v in term.args.values() if v is not None]
+            if any(k < 1 or k > nspins for k in indices):
                 raise MuSpinConfigError("Out of range indices for coupling")
-            cval = np.asarray(idata.value[0], dtype=float)
-            shape = {"zmn": (3,), "dip": (3,), "hfc": (3, 3), "quad": (3, 3), "dsp": (1,)}[cname]
-            if cval.shape != shape:
-                raise MuSpinConfigError(f"Invalid shape for {idata.name} coupling term")
-            i = args.get("i")
-            j = args.get("j")
-            i = i - 1 if i is not None else None
-            j = j - 1 if j is not None else None
-            if cname == "zmn":
-                self._system.add_zeeman_term(i, cval)
-            elif cname == "dip":
-                self._system.add_dipolar_term(i, j, cval)
-            elif cname == "hfc":
-                self._system.add_hyperfine_term(i, cval, j)
-            elif cname == "quad":
-                self._system.add_quadrupolar_term(i, cval)
-            elif cname == "dsp":
-                self._dissip_terms[i] = cval[0]
-
-        res_shape = [len(v) for v in self._file_ranges.values()]
-        res_shape += [len(v) for v in self._x_range.values()]
-        self._results = np.zeros(res_shape)
-
-        def make_configs(od):
-            cfg = []
-            for k, v in od.items():
-                cfg.append([slice(None)] if k == "t" else np.arange(len(v)))
-            return list(product(*cfg))
-
-        fconfigs = make_configs(self._file_ranges)
-        aconfigs = make_configs(self._avg_ranges)
-        xconfigs = make_configs(self._x_range)
-        self._configurations = list(product(*[fconfigs, aconfigs, xconfigs]))
-        self._avg_N = len(aconfigs)
+            value = np.asarray(term.value[0], dtype=float)
+            if value.shape != shape:
+                raise MuSpinConfigError(f"Invalid shape for {term.name} coupling term")
+            i, j = (None if k is None else k - 1 for k in (term.args.get("i"), term.args.get("j")))
+            if add is None:
+                dissipation[i] = value[0]
+            else:
+                add(system, i, j, value)
+        return system, dissipation
 
     # -------------------------------------------------------------- validators
     def validate(self, name, value, args=None):
@@ -347,33 +378,23 @@ class MuSpinConfig:
         return "[ZYZ] a = {0:.1f} deg, b = {1:.1f} deg, c = {2:.1f} deg, weight = {3}".format(*abc, w)
 
     # -------------------------------------------------------------- properties
-    @property
-    def name(self):
-        return self._name
-
-    @property
-    def spins(self):
-        return list(self._spins)
-
-    @property
-    def celio_k(self):
-        return self._celio[0]
-
-    @property
-    def celio_averages(self):
-        return self._celio[1]
-
-    @property
-    def system(self):
-        return self._system.clone()
-
-    @property
-    def constants(self):
-        return {**self._constants}
-
-    @property
-    def dissipation_terms(self):
-        return {**self._dissip_terms}
+    name = _exposed("_name")
+    spins = _exposed("_spins", list)
+    celio_k = property(lambda self: self._celio[0])
+    celio_averages = property(lambda self: self._celio[1])
+    system = _exposed("_system", lambda sy: sy.clone())
+    constants = _exposed("_constants", dict)
+    dissipation_terms = _exposed("_dissip_terms", dict)
+    x_axis = property(lambda self: next(iter(self._x_range)))
+    x_axis_values = property(lambda self: np.array(next(iter(self._x_range.values()))))
+    y_axis = _exposed("_y_axis")
+    results_function = _exposed("_results_function")
+    file_ranges = _exposed("_file_ranges", OrderedDict)
+    avg_ranges = _exposed("_avg_ranges", OrderedDict)
+    x_range = _exposed("_x_range", OrderedDict)
+    avg_N = _exposed("_avg_N")
+    time_N = _exposed("_time_N")
+    time_is_averaged = _exposed("_time_isavg")
 
     @property
     def results(self):
@@ -385,46 +406,6 @@ class MuSpinConfig:
         if r.shape != self._results.shape:
             raise ValueError("Trying to set an invalid results array")
         self._results = r
-
-    @property
-    def x_axis(self):
-        return [*self._x_range.keys()][0]
-
-    @property
-    def x_axis_values(self):
-        return np.array([*self._x_range.values()][0])
-
-    @property
-    def y_axis(self):
-        return self._y_axis
-
-    @property
-    def results_function(self):
-        return self._results_function
-
-    @property
-    def file_ranges(self):
-        return OrderedDict(self._file_ranges)
-
-    @property
-    def avg_ranges(self):
-        return OrderedDict(self._avg_ranges)
-
-    @property
-    def x_range(self):
-        return OrderedDict(self._x_range)
-
-    @property
-    def avg_N(self):
-        return self._avg_N
-
-    @property
-    def time_N(self):
-        return self._time_N
-
-    @property
-    def time_is_averaged(self):
-        return self._time_isavg
 
     @property
     def configurations(self):

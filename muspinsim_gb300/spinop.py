@@ -67,184 +67,192 @@ class Clonable:
 
 
 class Hermitian:
-    """Mixin for Hermitian operators (muspinsim/spinop.py:44-82)."""
+    """Mixin marking operators that must be Hermitian (the reference's
+    Hermitian, muspinsim/spinop.py:44-82): construction checks it, and the
+    eigendecomposition runs on the GPU."""
 
-    def __init__(self):
-        if not self.is_hermitian:
-            raise ValueError("Operator must be hermitian")
+    _must_be_hermitian = True
 
     def diag(self):
         """Eigenvalues (ascending) and eigenvector matrix (columns), as
         numpy.linalg.eigh returns them, computed by the GPU Jacobi solver in
         FP64.  The result is cached while the matrix is unchanged."""
-        M = _dense(self._matrix)
-        dd = getattr(self, "_diagdata", None)
-        if dd is not None and dd["matrix"].shape == M.shape and np.array_equal(dd["matrix"], M):
-            return dd["eigh"]
+        M = _dense(self.matrix)
+        cached = getattr(self, "_eigh_cache", None)
+        if cached is not None and cached[0].shape == M.shape and np.array_equal(cached[0], M):
+            return cached[1]
         evals, evecs, status = kernels.eigh(M[None])
         if int(status[0].item()) != 0:
             raise RuntimeError("Hermitian.diag: the Jacobi eigensolver did not converge")
         eigh = (evals[0].cpu().numpy(), evecs[0].cpu().numpy())
-        self._diagdata = {"matrix": M.copy(), "eigh": eigh}
+        self._eigh_cache = (M.copy(), eigh)
         return eigh
 
 
+def _as_storage(M, want_sparse):
+    """M as a CSR matrix or a dense ndarray."""
+    if want_sparse:
+        return M.tocsr() if sparse.issparse(M) else sparse.csr_matrix(M)
+    return M.toarray() if sparse.issparse(M) else np.array(M)
+
+
+# The binary matrix operations behind the operator algebra, with the
+# reference's message for operands on different spaces.
+_MATRIX_OPS = {
+    "+": (lambda a, b: a + b, "Can not add to Operators with different dimensions"),
+    "-": (lambda a, b: a - b, "Can not subtract to Operators with different dimensions"),
+    "@": (lambda a, b: a @ b, "Can not multiply to Operators with different dimensions"),
+}
+
+
 class Operator(Clonable):
-    """A spin-space operator (muspinsim/spinop.py:85-355)."""
+    """A matrix on a tensor-product spin space (the reference's Operator,
+    muspinsim/spinop.py:85-355).
+
+    State: the matrix in CSR or dense storage (``matrix``), the dimension of
+    each factor space (``dimension``) and the Hermiticity tolerance.  All
+    arithmetic goes through one path: the other operand is turned into a
+    matrix of the same space (a Number c stands for c times the identity
+    under + and -, for a plain scale under * and /), checked for the same
+    factor dimensions, and combined by one of _MATRIX_OPS into a copy of
+    this operator.
+    """
 
     def __init__(self, matrix, dim=None, herm_tol=1e-6, use_sparse=True):
-        self._sparse = use_sparse
-        if self._sparse:
-            self._matrix = sparse.csr_matrix(matrix)
-        else:
-            self._matrix = np.array(matrix)
-        if not matrix.shape[0] == matrix.shape[1]:
+        rows, cols = np.shape(matrix)[:2] if np.ndim(matrix) == 2 else (0, -1)
+        if rows != cols:
             raise ValueError("Matrix passed to Operator must be square")
-        if dim is None:
-            dim = (matrix.shape[0],)
-        elif np.prod(dim) != matrix.shape[0]:
+        factors = (rows,) if dim is None else tuple(dim)
+        if np.prod(factors) != rows:
             raise ValueError("Dimensions are not compatible with matrix")
-        self._dim = tuple(dim)
-        self._htol = herm_tol
-        super(Operator, self).__init__()
+        self._mat = _as_storage(matrix, use_sparse)
+        self._factors = factors
+        self._tol = herm_tol
+        # set by the Hermitian mixin, wherever it sits in the class's bases
+        if getattr(self, "_must_be_hermitian", False) and not self.is_hermitian:
+            raise ValueError("Operator must be hermitian")
 
+    # -- state
     @property
-    def Is(self):
-        return tuple((d - 1) / 2.0 for d in self._dim)
+    def matrix(self):
+        return self._mat
 
     @property
     def dimension(self):
-        return self._dim
+        return self._factors
+
+    @property
+    def Is(self):
+        return tuple((d - 1) / 2.0 for d in self._factors)
 
     @property
     def N(self):
-        return np.prod(self._dim)
-
-    @property
-    def matrix(self):
-        return self._matrix
-
-    @property
-    def is_hermitian(self):
-        x = self._matrix.conjugate().T
-        y = self._matrix
-        return np.abs(y - x).max() < self._htol
+        return np.prod(self._factors)
 
     @property
     def is_sparse(self):
-        return self._sparse
+        return sparse.issparse(self._mat)
 
-    def dagger(self):
-        cls = self.__class__
-        ans = cls.__new__(cls)
-        ans._dim = tuple(self._dim)
-        ans._matrix = self.matrix.conjugate().T
-        ans._sparse = self._sparse
-        ans._htol = getattr(self, "_htol", 1e-6)
-        return ans
+    @property
+    def is_hermitian(self):
+        return np.abs(self._mat - self._mat.conjugate().T).max() < self._tol
+
+    def _with_matrix(self, M):
+        """A copy of this operator (same class and space) holding M."""
+        out = self.clone()
+        out._mat = _as_storage(M, self.is_sparse)
+        return out
+
+    # -- algebra
+    def _operand(self, x, op):
+        """The matrix x stands for in `op` with self, or None."""
+        if isinstance(x, Number):
+            if op not in "+-":
+                return None
+            n = self._mat.shape[0]
+            return x * (sparse.identity(n, format="csr") if self.is_sparse else np.eye(n))
+        if isinstance(x, Operator) and self._accepts(x):
+            if x.dimension != self.dimension:
+                raise ArithmeticError(_MATRIX_OPS[op][1])
+            return x.matrix
+        return None
+
+    def _accepts(self, x):
+        """Whether an operator of x's type combines with this one."""
+        return True
+
+    _unsupported = "Unsupported operation for Operator"
+
+    def _binary(self, x, op):
+        M = self._operand(x, op)
+        if M is None:
+            raise TypeError(self._unsupported)
+        return self._with_matrix(_MATRIX_OPS[op][0](self._mat, M))
+
+    def _scaled(self, c):
+        return self._with_matrix(self._mat * c)
 
     def __add__(self, x):
-        if isinstance(x, Operator):
-            if self.dimension != x.dimension:
-                raise ArithmeticError("Can not add to Operators with different dimensions")
-            ans = self.clone()
-            ans._matrix = ans._matrix + x._matrix
-            return ans
-        elif isinstance(x, Number):
-            ans = self.clone()
-            if self._sparse:
-                ans._matrix = ans._matrix + sparse.eye(ans._matrix.shape[0]) * x
-            else:
-                ans._matrix = ans._matrix + np.eye(ans._matrix.shape[0]) * x
-            return ans
-        raise TypeError("Unsupported operation for Operator")
+        return self._binary(x, "+")
 
     def __sub__(self, x):
-        if isinstance(x, Operator):
-            if self.dimension != x.dimension:
-                raise ArithmeticError("Can not subtract to Operators with different dimensions")
-            ans = self.clone()
-            ans._matrix = ans._matrix - x._matrix
-            return ans
-        elif isinstance(x, Number):
-            return self + (-x)
-        raise TypeError("Unsupported operation for Operator")
+        return self._binary(x, "-")
 
     def __mul__(self, x):
-        if isinstance(x, Operator):
-            if self.dimension != x.dimension:
-                raise ArithmeticError("Can not multiply to Operators with different dimensions")
-            ans = self.clone()
-            if self._sparse:
-                ans._matrix = ans._matrix.dot(x._matrix)
-            else:
-                ans._matrix = ans._matrix @ x._matrix
-            return ans
-        elif isinstance(x, Number):
-            ans = self.clone()
-            if self._sparse:
-                ans._matrix = ans._matrix.multiply(x).tocsr()
-            else:
-                ans._matrix = ans._matrix * x
-            return ans
-        raise TypeError("Unsupported operation for Operator")
+        if isinstance(x, Number):
+            return self._scaled(x)
+        return self._binary(x, "@")
 
     def __rmul__(self, x):
         if isinstance(x, Number):
-            return self.__mul__(x)
-        elif isinstance(x, Operator):
-            return x * self
+            return self._scaled(x)
+        if isinstance(x, Operator):
+            return x.__mul__(self)
         raise TypeError("Unsupported operation for Operator")
 
     def __truediv__(self, x):
-        if isinstance(x, Number):
-            return self * (1.0 / x)
-        raise TypeError("Unsupported operation for Operator")
+        if not isinstance(x, Number):
+            raise TypeError("Unsupported operation for Operator")
+        return self._scaled(1.0 / x)
 
     def __eq__(self, x):
-        if not isinstance(x, Operator):
-            return False
-        if self.dimension != x.dimension:
-            return False
-        return bool(np.array_equal(_dense(self._matrix), _dense(x._matrix)))
+        return (isinstance(x, Operator) and self.dimension == x.dimension
+                and bool(np.array_equal(_dense(self._mat), _dense(x.matrix))))
 
     __hash__ = None
 
+    def dagger(self):
+        """The adjoint (conjugate transpose), same class and space."""
+        return self._with_matrix(self._mat.conjugate().T)
+
     def kron(self, x):
-        """Tensor product (muspinsim/spinop.py:266-295)."""
+        """Tensor product (muspinsim/spinop.py:266-295): the factor spaces
+        of self followed by those of x."""
         if not isinstance(x, Operator):
             raise ValueError("Can only perform Kronecker product with another Operator")
-        ans = self.__class__.__new__(self.__class__)
-        ans._dim = self._dim + x._dim
-        ans._sparse = self._sparse
-        ans._htol = getattr(self, "_htol", 1e-6)
-        if self._sparse:
-            ans._matrix = sparse.kron(self._matrix, x._matrix, format="csr")
-        else:
-            ans._matrix = np.kron(self._matrix, x._matrix)
-        return ans
+        out = self._with_matrix(
+            sparse.kron(self._mat, x.matrix, format="csr") if self.is_sparse
+            else np.kron(_dense(self._mat), _dense(x.matrix)))
+        out._factors = self._factors + x.dimension
+        return out
 
     def hilbert_schmidt(self, x):
         """tr(A^dag B) (muspinsim/spinop.py:297-328)."""
         if not isinstance(x, Operator):
             raise ValueError("Can only perform Hilbert-Schmidt product with another Operator")
-        if not x.dimension == self.dimension:
+        if x.dimension != self.dimension:
             raise ValueError(
                 "Operators must have the same dimension to perform Hilbert-Schmidt product"
             )
-        A = self.matrix
-        B = x.matrix
-        return A.conjugate().T.dot(B).trace().item()
+        # tr(A^dag B) = sum_ij conj(A_ij) B_ij
+        return complex(np.sum(np.conj(_dense(self._mat)) * _dense(x.matrix)))
 
     def basis_change(self, basis, use_sparse=False):
         """basis^dag M basis, computed on the GPU (muspinsim/spinop.py:330-355)."""
+        M = _dense(self._mat).astype(complex)
+        out = kernels.basis_change(np.asarray(basis, dtype=complex), M)[0].cpu().numpy()
         ans = self.clone()
-        M = _dense(ans._matrix)
-        out = kernels.basis_change(np.asarray(basis, dtype=complex), M.astype(complex))[0]
-        ans._matrix = out.cpu().numpy()
-        if use_sparse:
-            ans._matrix = sparse.csr_matrix(ans._matrix)
-        ans._sparse = use_sparse
+        ans._mat = _as_storage(out, use_sparse)
         return ans
 
 
@@ -271,15 +279,14 @@ class SpinOperator(Operator):
 
 
 class DensityOperator(Operator):
-    """Trace-one Hermitian operator (muspinsim/spinop.py:414-600)."""
+    """Trace-one Hermitian operator (muspinsim/spinop.py:414-600): the
+    matrix is normalised to unit trace on construction."""
 
     def __init__(self, matrix, dim=None, use_sparse=True):
         super(DensityOperator, self).__init__(matrix, dim, use_sparse=use_sparse)
-        tr = self._matrix.trace()
-        if tr == 0:
+        if self.trace == 0:
             raise ValueError("Can not define a DensityOperator with zero trace")
-        else:
-            self.normalize()
+        self.normalize()
         if not self.is_hermitian:
             raise ValueError("DensityOperator must be hermitian!")
 
@@ -314,34 +321,31 @@ class DensityOperator(Operator):
 
     @property
     def trace(self):
-        return self._matrix.trace()
+        return self._mat.trace()
 
     def clone_sparse(self):
         """Copy with CSR storage (what basis_change(..., use_sparse=True)
         returns in the reference)."""
         ans = self.clone()
-        ans._matrix = sparse.csr_matrix(_dense(ans._matrix))
-        ans._sparse = True
+        ans._mat = _as_storage(ans._mat, True)
         return ans
 
     def normalize(self):
-        if self._sparse:
-            self._matrix = self._matrix.multiply(1 / self.trace).tocsr()
-        else:
-            self._matrix = np.multiply(self._matrix, 1 / self.trace)
+        """Rescale to unit trace in place."""
+        self._mat = _as_storage(self._mat * (1 / self.trace), self.is_sparse)
 
     def partial_trace(self, trace_dim=None):
         """Trace out the listed subsystems (muspinsim/spinop.py:543-572)."""
         if trace_dim is None:
             trace_dim = []
-        dim = list(self._dim)
+        dim = list(self._factors)
         tdim = list(sorted(trace_dim))
-        m = _dense(self._matrix).reshape(dim + dim)
+        m = _dense(self._mat).reshape(dim + dim)
         while len(tdim) > 0:
             td = tdim.pop(-1)
             m = np.trace(m, axis1=td, axis2=td + len(dim))
             dim.pop(td)
-        return DensityOperator(m, dim, use_sparse=self._sparse)
+        return DensityOperator(m, dim, use_sparse=self.is_sparse)
 
     def expectation(self, operator):
         """tr(rho O) (muspinsim/spinop.py:574-600)."""
@@ -395,36 +399,26 @@ class SuperOperator(Operator):
         m = operator.matrix
         return cls(sparse.kron(m, m.conjugate()), operator.dimension + operator.dimension)
 
-    def __add__(self, x):
-        if isinstance(x, (SuperOperator, Number)):
-            return super(SuperOperator, self).__add__(x)
-        raise TypeError("Unsupported operation for SuperOperator")
+    # algebra: + and - only with other superoperators (or numbers); a
+    # product with a plain Operator applies the map to it
+    def _accepts(self, x):
+        return isinstance(x, SuperOperator)
 
-    def __sub__(self, x):
-        if isinstance(x, (SuperOperator, Number)):
-            return super(SuperOperator, self).__sub__(x)
-        raise TypeError("Unsupported operation for SuperOperator")
+    def _binary(self, x, op):
+        if op in "+-" and not isinstance(x, (SuperOperator, Number)):
+            raise TypeError("Unsupported operation for SuperOperator")
+        return super(SuperOperator, self)._binary(x, op)
 
     def __mul__(self, x):
-        if isinstance(x, (SuperOperator, Number)):
-            return super(SuperOperator, self).__mul__(x)
-        elif isinstance(x, Operator):
-            m = _dense(x.matrix)
-            v = self.matrix.dot(m.reshape((-1,))).reshape(m.shape)
-            return Operator(v, x.dimension)
-        raise TypeError("Unsupported operation for Operator")
+        if isinstance(x, Operator) and not isinstance(x, SuperOperator):
+            rho = _dense(x.matrix)
+            return Operator(self.matrix.dot(rho.reshape(-1)).reshape(rho.shape), x.dimension)
+        return super(SuperOperator, self).__mul__(x)
 
     def __rmul__(self, x):
-        if isinstance(x, Number):
-            return self.__mul__(x)
-        elif isinstance(x, SuperOperator):
-            return x * self
-        raise TypeError("Unsupported operation for Operator")
-
-    def __truediv__(self, x):
-        if isinstance(x, Number):
-            return self * (1.0 / x)
-        raise TypeError("Unsupported operation for Operator")
+        if isinstance(x, Operator) and not isinstance(x, SuperOperator):
+            raise TypeError("Unsupported operation for Operator")
+        return super(SuperOperator, self).__rmul__(x)
 
 
 def spin_projectors(I, axis):

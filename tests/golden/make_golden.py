@@ -188,10 +188,144 @@ def save_celio():
                     [(0.0, 0.0, 0.0)], (0.0, 1.0, 0.0), celio=(5, 0))
 
 
+CONFIG_LAYOUTS = [
+    # (times, orientations, fields, temperatures, y axis, x axis, averaged axes)
+    (np.linspace(0, 5, 7).tolist(), [(0, 0, 0, 1.0), (0.3, 0.2, 0.1, 2.0), (1, 2, 0.5, 1.0)],
+     [(0, 0, 0.01), (0, 0, 0.02)], [np.inf], "asymmetry", "time", ["orientation"]),
+    ([0.0], [(0, 0, 0), (0.3, 0.2, 0.1)], [(0, 0, 0.01), (0, 0, 0.02), (0, 0, 0.03)],
+     [np.inf, 10.0], "integral", "field", ["orientation", "temperature"]),
+    (np.linspace(0, 1, 5).tolist(), [(0, 0, 0)], [(0, 0, 0.01), (0, 0, 0.02)], [np.inf],
+     "asymmetry", "field", ["time"]),
+    (np.linspace(0, 1, 5).tolist(), [(0, 0, 0)], [(0, 0, 0.01), (0.005, 0, 0.01)],
+     [np.inf, 5.0], "asymmetry", "time", ["none"]),
+]
+CONFIG_SPINS = ["mu", "e", "H"]
+CONFIG_COUPLINGS = [("hyperfine", {"i": 1}, 100.0 * np.eye(3)),
+                    ("dipolar", {"i": 1, "j": 3}, [0.0, 0.0, 1.5]),
+                    ("zeeman", {"i": 3}, [0.0, 0.0, 0.01])]
+
+
+def save_config_layouts(name):
+    """The reference MuSpinConfig's snapshot grid for four axis layouts: the
+    configuration indices, result shape, range keys in order, constants,
+    averaged count and per-snapshot orientation quaternions and weights
+    (muspinsim/simconfig.py:78-321); and the .dat files its save_output
+    writes for set results (muspinsim/simconfig.py:370-429), with the date
+    line blanked."""
+    import tempfile
+
+    from muspinsim.simconfig import MuSpinConfig
+
+    layouts = []
+    for times, orients, fields, temps, y, x, avg in CONFIG_LAYOUTS:
+        p = refshim.make_params(CONFIG_SPINS, CONFIG_COUPLINGS, times, orients, field=fields,
+                                polarization=(1.0, 0.0, 0.0), temperature=temps, y_axis=y,
+                                x_axis=x, average_axes=avg)
+        cfg = MuSpinConfig(p)
+        cfgs = [[[None if isinstance(i, slice) else int(i) for i in part] for part in c]
+                for c in cfg._configurations]
+        snaps = []
+        for k in range(len(cfg)):
+            o = cfg[k].orient
+            snaps.append([list(map(float, o[0].q)), float(o[1])])
+        cfg.results = np.arange(cfg.results.size, dtype=float).reshape(cfg.results.shape) * 0.25
+        files = {}
+        with tempfile.TemporaryDirectory() as d:
+            cfg.save_output(name="out", path=d)
+            for fn in sorted(os.listdir(d)):
+                with open(os.path.join(d, fn)) as f:
+                    lines = f.read().splitlines()
+                files[fn] = [("# Output file written on <date>" if ln.startswith(
+                    "# Output file written on") else ln) for ln in lines]
+        layouts.append({
+            "layout": [times, [list(o) for o in orients], [list(f) for f in fields],
+                       [float(t) for t in temps], y, x, avg],
+            "configurations": cfgs, "shape": list(cfg.results.shape),
+            "file_ranges": list(cfg._file_ranges.keys()),
+            "avg_ranges": list(cfg._avg_ranges.keys()), "x": list(cfg._x_range.keys())[0],
+            "avg_N": int(cfg._avg_N), "time_N": int(cfg._time_N),
+            "constants": sorted(cfg._constants.keys()), "orient": snaps, "files": files})
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
+        json.dump({"spins": CONFIG_SPINS, "couplings": _jsonable_couplings(CONFIG_COUPLINGS),
+                   "layouts": layouts}, f, indent=0, default=float)
+    print(f"{name}: {len(layouts)} layouts")
+
+
+def _reference_system(wl):
+    from muspinsim.spinsys import MuonSpinSystem
+
+    sy = MuonSpinSystem(list(wl.spins))
+    for kind, args, val in wl.couplings:
+        i, j = args["i"] - 1, args.get("j")
+        j = None if j is None else j - 1
+        {"hyperfine": lambda: sy.add_hyperfine_term(i, val, j),
+         "dipolar": lambda: sy.add_dipolar_term(i, j, val),
+         "quadrupolar": lambda: sy.add_quadrupolar_term(i, val)}[kind]()
+    return sy
+
+
+def save_rotated(name):
+    """SpinSystem.rotate(R).hamiltonian of the dim-24 system for seeded
+    rotation matrices (muspinsim/spinsys.py:103-135, 594-626)."""
+    from muspinsim_gb300 import quaternion as Q
+    from muspinsim_gb300 import workloads
+
+    wl = workloads.config2(n_orient=1, n_times=8)
+    sy = _reference_system(wl)
+    rng = np.random.default_rng(4242)
+    qs = Q.from_euler(*rng.uniform(0, 2 * np.pi, (3, 6)), "zyz")
+    Rs = Q.rotation_matrix(qs)
+    H0 = sy.hamiltonian.matrix.toarray()
+    HR = np.array([sy.rotate(R).hamiltonian.matrix.toarray() for R in Rs])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), R=Rs, H=H0, HR=HR,
+                        meta=np.array(json.dumps({"spins": list(wl.spins),
+                                                  "couplings": _jsonable_couplings(wl.couplings)})))
+    print(f"{name}: {len(Rs)} rotations of a dim-{H0.shape[0]} system")
+
+
+def save_fast_binding(name):
+    """The arguments Hamiltonian.fast_evolve passes to its native kernel
+    parallel_fast_time_evolve (muspinsim/hamiltonian.py:195-217), that
+    kernel's output and fast_evolve's result, for the dim-24 system in a
+    field: what a GPU stub bound at muspinsim/hamiltonian.py:10 receives."""
+    import muspinsim.hamiltonian as hm
+
+    from muspinsim_gb300 import workloads
+
+    wl = workloads.config2(n_orient=1, n_times=8)
+    sy = _reference_system(wl)
+    sy.add_zeeman_term(0, [0.002, -0.001, 0.01])
+    sy.add_zeeman_term(1, [0.002, -0.001, 0.01])
+    calls = []
+    native = hm.parallel_fast_time_evolve
+
+    def spy(times, other_dimension, A, W):
+        out = native(times, other_dimension, A, W)
+        calls.append((np.array(times), int(other_dimension), np.array(A), np.array(W),
+                      np.array(out)))
+        return out
+
+    hm.parallel_fast_time_evolve = spy
+    try:
+        t = np.linspace(0.0, 10.0, 777)
+        fast = sy.hamiltonian.fast_evolve(sy.sigma_mu([0.3, -0.4, 0.866]), t, 12)
+    finally:
+        hm.parallel_fast_time_evolve = native
+    times, d, A, W, kout = calls[0]
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), times=times, d=d, A=A, W=W,
+                        kernel=kout, fast=fast)
+    print(f"{name}: n = {A.shape[0]}, {len(times)} times")
+
+
 def main(only=None):
     refshim.install()
     if only == "celio":
         save_celio()
+        return
+    if only == "boundary":
+        save_config_layouts("config_layouts")
+        save_rotated("rotated_dim24")
+        save_fast_binding("fast_binding_dim24")
         return
     from muspinsim_gb300 import workloads
 
@@ -237,6 +371,9 @@ def main(only=None):
                     dissipation={2: 1.5})
     save_lindblad_direct("lindblad_direct")
     save_celio()
+    save_config_layouts("config_layouts")
+    save_rotated("rotated_dim24")
+    save_fast_binding("fast_binding_dim24")
 
 
 if __name__ == "__main__":
