@@ -75,6 +75,12 @@ def parse_args():
                    help="config4: systems (the full configuration: 4096)")
     p.add_argument("--c4-orientations", type=int, default=32,
                    help="config4: orientations per system (the full configuration: 256)")
+    p.add_argument("--c3-fields", type=int, default=2000,
+                   help="config3 workload: fields of the ALC scan (a smaller scan for profiling)")
+    p.add_argument("--c4-graph", choices=["on", "off"], default="on",
+                   help="config4 workload: replay the batch from a CUDA graph")
+    p.add_argument("--c4-dims", default="4,8,12,24,48,96,192",
+                   help="config4 workload: dimensions drawn for the systems")
     p.add_argument("--workload", default="config2",
                    choices=["config1", "config2", "config3", "config4", "config5", "lindblad",
                             "celio"],
@@ -116,6 +122,25 @@ def max_over_ranks(world, x):
                      device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def cpu_model():
+    """Host CPU model name (lscpu / /proc/cpuinfo), or None."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return None
 
 
 # ---------------------------------------------------------------- workload
@@ -257,12 +282,14 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- CPU reference
 
-def cpu_reference_rate(sy, B_lab, p_lab, times, n_orient, threads):
+def cpu_reference_rate(sy, B_lab, p_lab, times, n_orient, threads, wscale=None):
     """Samples/s of the reference's fast path on the host: per orientation
     H = Hsys + b.Z, numpy eigh, A = |U^dag (sigma (x) 1) U|^2, W, and the
     reference's own Cython cosine sum compiled from its sources
     (oracle/_ref), with all host threads; the C restatement
-    (oracle/fast_cos_sum.c) when the reference kernel is absent."""
+    (oracle/fast_cos_sum.c) when the reference kernel is absent.  Also
+    returns the weighted average P(t) of those orientations (weights
+    wscale, renormalised over the sample), for the parity check."""
     os.environ["OMP_NUM_THREADS"] = str(threads)
     from oracle import build as obuild
     from oracle import port
@@ -286,6 +313,7 @@ def cpu_reference_rate(sy, B_lab, p_lab, times, n_orient, threads):
     Z = sy.zeeman_operators()
     d = Hsys.shape[0] // 2
     t = np.ascontiguousarray(times, dtype=np.float64)
+    w = np.ones(n_orient) if wscale is None else np.asarray(wscale[:n_orient], dtype=float)
     t0 = time.perf_counter()
     acc = np.zeros(len(t))
     for k in range(n_orient):
@@ -295,9 +323,33 @@ def cpu_reference_rate(sy, B_lab, p_lab, times, n_orient, threads):
             r = np.asarray(kernel(t, d, np.ascontiguousarray(A), np.ascontiguousarray(W)))
         else:
             r = port.fast_cos_sum(t, d, A, W, threads)
-        acc += 0.5 * r
+        acc += w[k] * 0.5 * r
     dt = time.perf_counter() - t0
-    return n_orient * len(t) / dt, dt, kind
+    return n_orient * len(t) / dt, dt, kind, acc / w.sum()
+
+
+def cpu_evolve_rate(spins, sy, B_lab, p_lab, times, n_orient):
+    """Samples/s of the reference's general evolve on the host, per
+    orientation: numpy eigh, rho0' and O' basis changes and the per-time loop
+    of Hamiltonian.evolve (oracle.port.evolve_per_time restates it,
+    muspinsim/hamiltonian.py:40-117), with numpy's default threads; and the
+    largest deviation from the fast path's P(t) on the same orientations."""
+    from oracle import port
+    from tests.helpers import oracle_system
+
+    osy = oracle_system(list(spins), [])
+    Hsys, Z = sy.hamiltonian_matrix(), sy.zeeman_operators()
+    t = np.asarray(times, dtype=float)
+    Smu = [port.embed(osy.Is, {0: a}) for a in "xyz"]
+    dt = 0.0
+    for k in range(n_orient):
+        H = Hsys + np.einsum("a,aij->ij", B_lab[k], Z)
+        rho = port.rho0(osy, B_lab[k], p_lab[k], np.inf)
+        O = sum(p_lab[k][a] * Smu[a] for a in range(3))
+        t0 = time.perf_counter()
+        port.evolve_per_time(H, rho, t, [O])
+        dt += time.perf_counter() - t0
+    return n_orient * len(t) / dt, dt
 
 
 # ---------------------------------------------------------------- main arms
@@ -310,12 +362,14 @@ def run_reference(args, world, rank):
     n = min(args.ref_orientations, len(B_lab))
     rates = []
     for step in range(args.warmup + args.steps):
-        rate, dt, kind = cpu_reference_rate(sy, B_lab, p_lab, wl.times, n, threads)
+        rate, dt, kind, _ = cpu_reference_rate(sy, B_lab, p_lab, wl.times, n, threads)
         if step >= args.warmup:
             rates.append((rate, dt))
     value = statistics.median([r for r, _ in rates])
     ms = statistics.median([d for _, d in rates]) * 1e3
     sample = f"{n} of {len(B_lab)} orientations x {len(wl.times)} times per step"
+    ev_n = 4
+    ev_rate, ev_dt = cpu_evolve_rate(wl.spins, sy, B_lab, p_lab, wl.times, ev_n)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -324,7 +378,11 @@ def run_reference(args, world, rank):
         "config": {"workload": WORKLOAD, "orientations": len(B_lab), "times": len(wl.times),
                    "dim": 24, "l2": "n/a (host)"},
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": kind,
-                         "sample": sample},
+                         "cpu_model": cpu_model(), "sample": sample},
+        "evolve": {"value": ev_rate, "unit": "samples/s", "seconds": ev_dt,
+                   "sample": f"{ev_n} orientations x {len(wl.times)} times",
+                   "path": "Hamiltonian.evolve restated per time step (oracle.port."
+                           "evolve_per_time), numpy default threads"},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -401,10 +459,11 @@ def run_gb300(args, world, rank, local):
         if k >= args.warmup:
             e2e_ms.append((t1 - t0) * 1e3)
     dP_e2e = float(np.abs(r - res_fp64[0].cpu().numpy()).max())
-    # per call: the orientation rows and the time grid go up (the system's
-    # Hsys and Z stay on the device after the first call, like a model's
-    # weights), the powder average and the per-snapshot status come back
-    h2d = int(np.asarray(wl.orientations).nbytes) + T * 8
+    # per call: the orientation rows go up (the system's Hsys and Z stay on
+    # the device after the first call, like a model's weights, and the time
+    # grid is re-uploaded only when it changes, which it does not here); the
+    # powder average and the per-snapshot status come back
+    h2d = int(np.asarray(wl.orientations).nbytes)
     d2h = T * 8 + S * 4
 
     t_mixed = statistics.median(ms_mixed)
@@ -414,23 +473,43 @@ def run_gb300(args, world, rank, local):
     samples = S * T
     value = world * samples / (t_mixed_max * 1e-3)
 
-    # roofline of the dominant kernel (live CUDA-event stage times)
+    # roofline per stage (live CUDA-event stage times; each stage is one
+    # kernel on this path) and of the dominant one
     per_run = {k: v / max(runs, 1) for k, v in stages.items()}
-    dom = max(per_run, key=per_run.get)
-    flops = {"snapshots": 68.0 * n**3 * S, "phase": (4.0 * n * n + 2.0) * samples,
-             "schedule": 0.0, "reduce": 2.0 * samples}
-    kname = {"snapshots": "msp_snap_fast_kernel<float,true>",
-             "phase": "msp_phase_uniform_kernel<float>",
-             "schedule": "msp_schedule_kernel", "reduce": "msp_reduce_kernel"}[dom]
-    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
-    fp32_peak = SMS * FP32_FMA_PER_SM * 2 * 2070e6 / 1e12
-    achieved = flops[dom] / (per_run[dom] * 1e-3) / 1e12
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             peaks = json.load(f)
     except OSError:
         pass
+    fp32_peak = SMS * FP32_FMA_PER_SM * 2 * 2070e6 / 1e12
+    bf16 = peaks.get("bf16_tflops")
+    tf32_peak = (bf16 if bf16 else 1900.0) / 2.0  # dense TF32 runs at half the bf16 rate
+    tf32_src = ("measured bf16 burst / 2 (MEASURED_PEAKS.json)" if bf16
+                else "fallback 1.9 PF/s bf16 / 2")
+    # algorithmic work: eigensolve 36 n^3 and eigenbasis products 32 n^3 per
+    # snapshot, 4 n^2 + 2 per time sample (phase sum + accumulation)
+    kernels_rl = {
+        "eigensolve": ("msp_jacobi_warp_kernel<24>", 36.0 * n**3 * S, "fp32-pipe", fp32_peak,
+                       "nominal FP32 FMA pipe (152 x 128 x 2 x 2070 MHz)"),
+        "snapshots": ("msp_snap_fast_kernel<float,true,true> (refinement + amplitudes)",
+                      32.0 * n**3 * S, "fp32-pipe", fp32_peak,
+                      "nominal FP32 FMA pipe (152 x 128 x 2 x 2070 MHz)"),
+        "phase": ("msp_phase_tc_kernel<32> (tcgen05 kind::tf32, 3xTF32)",
+                  (4.0 * n * n) * samples, "tensor", tf32_peak, tf32_src),
+        "reduce": ("msp_reduce_kernel", 2.0 * samples, "fp32-pipe", fp32_peak,
+                   "nominal FP32 FMA pipe"),
+    }
+    rl_all = {}
+    for k, (kn, fl, bound, pk, src) in kernels_rl.items():
+        if per_run.get(k, 0.0) > 0.0:
+            ach = fl / (per_run[k] * 1e-3) / 1e12
+            rl_all[k] = {"kernel": kn, "ms": per_run[k], "achieved_tflops": ach,
+                         "peak_tflops": pk, "frac": ach / pk, "bound": bound,
+                         "peak_source": src}
+    dom = max(rl_all, key=lambda k: rl_all[k]["ms"])
+    kn, fl, bound, pk, src = kernels_rl[dom]
+    achieved = rl_all[dom]["achieved_tflops"]
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed_max,
@@ -448,30 +527,92 @@ def run_gb300(args, world, rank, local):
         "e2e": {"value": world * samples / (max_over_ranks(world, t_e2e) * 1e-3),
                 "unit": "samples/s", "ms_per_step": t_e2e, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "api": "muspinsim_gb300.powder_average",
-                "max_abs_dP_vs_fp64": dP_e2e},
+                "max_abs_dP_vs_fp64": dP_e2e,
+                "h2d": "orientation rows (time grid cached on the device)"},
         "stage_ms_per_step": per_run,
         "roofline": {
-            "bound": "fp32-pipe", "kernel": kname, "achieved": achieved,
-            "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+            "bound": bound, "kernel": kn, "achieved": achieved, "peak": pk, "unit": "TFLOP/s",
+            "frac": achieved / pk,
             "traffic": TRAFFIC_PER_SNAPSHOT.get(dom, 0.0) * S or None,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, scaled per snapshot",
-            "algorithmic": f"{'68 n^3 per snapshot' if dom == 'snapshots' else '(4 n^2 + 2) per sample'}",
-            "peak_source": "nominal FP32 FMA pipe at sm_max_mhz (152 x 128 x 2 x 2070 MHz)",
-            "tensor_frac_of_measured_bf16": achieved / peaks["bf16_tflops"] if peaks else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                              "scaled per snapshot",
+            "algorithmic": {"eigensolve": "36 n^3 per snapshot",
+                            "snapshots": "32 n^3 per snapshot",
+                            "phase": "4 n^2 per sample", "reduce": "2 per sample"}[dom],
+            "peak_source": src,
+            "stages": rl_all,
         },
         "clocks": clk,
-        "gpu_launches": 4 * args.steps,
+        # warp Jacobi, refinement, schedule, phase sum, reduction
+        "gpu_launches": 5 * args.steps,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         nc = min(args.cpu_orientations, S)
-        rate, dt, kind = cpu_reference_rate(sy, B_lab, p_lab, wl.times, nc, threads)
+        rate, dt, kind, ref_avg = cpu_reference_rate(sy, B_lab, p_lab, wl.times, nc, threads,
+                                                     wscale)
         line["cpu_baseline"] = {"value": rate, "unit": "samples/s", "cores": threads,
-                                "kind": kind, "seconds": dt,
+                                "kind": kind, "cpu_model": cpu_model(), "seconds": dt,
                                 "sample": f"{nc} of {S} orientations x {T} times"}
+        # parity at the benchmark's size: both GPU forms on the same sample of
+        # orientations (weights renormalised over it) against the reference's
+        # own P(t), on the full time grid
+        sub_w = wscale[:nc] / wscale[:nc].sum()
+        par = {}
+        for name, prec in (("mixed", _lib.PREC_MIXED), ("fp64", _lib.PREC_FP64)):
+            pl = kernels.PowderPlan(n, Hsys, Z, B_lab[:nc], p_lab[:nc], sub_w,
+                                    np.zeros(nc, dtype=np.int32), 1, wl.times,
+                                    mode=_lib.MODE_FAST, precision=prec)
+            got = pl.run()[0].cpu().numpy()
+            par[name] = float(np.abs(got - ref_avg).max())
+        line["max_abs_dP_vs_reference"] = {
+            **par, "sample": f"{nc} of {S} orientations x {T} times", "reference": kind,
+            "gates": {"mixed": 1e-6, "fp64": 1e-10}}
     if rank == 0:
         print(json.dumps(line))
     return 0
+
+
+# ---------------------------------------------------------------- CPU pools
+
+def _pool_init():
+    # one BLAS / OpenMP thread per worker process: the pool supplies the
+    # parallelism
+    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[k] = "1"
+
+
+def _snapshot_task(task):
+    """Worker: the oracle's per-snapshot path (numpy eigh + the reference's
+    arithmetic) for a chunk of (spins, couplings, orientation row, field,
+    polarisation, times, y) items; returns the weighted sum of results."""
+    from oracle import port
+    from tests.helpers import oracle_system
+
+    spins, couplings, rows, fields, pol, times, y, weights = task
+    osy = oracle_system(spins, couplings)
+    Hn, Zn = osy.hamiltonian(), osy.zeeman_operators()
+    acc = 0.0
+    for row, B, w in zip(rows, fields, weights):
+        q = port.orientation_quat(row)[0]
+        r = port.snapshot(osy, Hn, Zn, q, 1.0, np.asarray(B, float), pol, np.inf, np.zeros(3),
+                          times, y=y)
+        acc = acc + w * np.asarray(r)
+    return acc
+
+
+def cpu_pool_map(tasks, threads):
+    """Run _snapshot_task over tasks in a spawn pool of `threads` processes
+    (spawn: no process is forked from one that holds a CUDA context)."""
+    import multiprocessing as mp
+
+    with mp.get_context("spawn").Pool(threads, initializer=_pool_init) as pool:
+        return pool.map(_snapshot_task, tasks)
+
+
+def _chunks(items, k):
+    n = len(items)
+    return [items[i * n // k:(i + 1) * n // k] for i in range(k) if i * n // k < (i + 1) * n // k]
 
 
 # ---------------------------------------------------------------- other workloads
@@ -552,15 +693,15 @@ def run_config1(args, world, rank, local):
         from oracle import port
         from tests.helpers import oracle_system
 
-        osy = oracle_system(wl.spins, wl.couplings)
-        t0 = time.perf_counter()
-        reps = 200
+        threads = os.cpu_count() or 1
+        reps, total, kind = 200, 0.0, "port"
         for _ in range(reps):
-            port.powder_average(osy, wl.orientations, wl.fields[0], wl.polarization, np.inf,
-                                wl.times)
-        dt = (time.perf_counter() - t0) / reps
-        line["cpu_baseline"] = {"value": T / dt, "unit": "samples/s", "cores": 1, "kind": "port",
-                                "sample": f"{reps} full runs (numpy eigh + C cosine sum)"}
+            _, dt, kind, _ = cpu_reference_rate(sy, B, p, wl.times, 1, threads)
+            total += dt
+        line["cpu_baseline"] = {"value": reps * T / total, "unit": "samples/s", "cores": threads,
+                                "kind": kind, "cpu_model": cpu_model(),
+                                "sample": f"{reps} runs of the fast path (numpy eigh + the "
+                                          "reference's OpenMP cosine sum)"}
     return line
 
 
@@ -575,7 +716,7 @@ def run_config3(args, world, rank, local):
     from muspinsim_gb300.constants import MU_TAU
     from muspinsim_gb300.orientations import orientation_rows_to_quats
 
-    wl = workloads.config3()
+    wl = workloads.config3(n_fields=args.c3_fields)
     sy = wl.system()
     qs, ws = orientation_rows_to_quats(wl.orientations)
     No = len(qs)
@@ -602,13 +743,13 @@ def run_config3(args, world, rank, local):
     for _ in range(args.warmup):
         mixed.run()
     ms = _events_ms(mixed.run, args.steps)
-    sub = 100  # FP64 on 100 fields x all orientations (5% of the scan)
+    sub = min(100, Nf)  # FP64 on 100 fields x all orientations (5% of the full scan)
     f64 = plan(_lib.PREC_FP64, sub)
     f64.run()
     ms64 = _events_ms(f64.run, max(1, args.fp64_steps))
     dP = float((mixed.out[:sub] - f64.out).abs().max().item())
     line = _line("ALC (field, orientation) integrals/s, mixed precision", units / (ms * 1e-3),
-                 "integrals/s", ms, args, world, "mu_e_3H_dim32_alc_2000_fields_1000_orient",
+                 "integrals/s", ms, args, world, f"mu_e_3H_dim32_alc_{Nf}_fields_{No}_orient",
                  {"fields": Nf, "orientations": No, "dim": 32, "tau_us": MU_TAU,
                   "l2": "inputs (96 MB of field/polarisation) resident; not flushed"},
                  dtype="f32 Jacobi + df32 refinement + f64 integral",
@@ -621,18 +762,20 @@ def run_config3(args, world, rank, local):
         from oracle import port
         from tests.helpers import oracle_system
 
-        osy = oracle_system(wl.spins, wl.couplings)
-        Hn, Zn = osy.hamiltonian(), osy.zeeman_operators()
-        nsamp = 200
+        threads = os.cpu_count() or 1
+        nsamp = 200 * threads
+        items = [((k * 10) % Nf, (k * 37) % No) for k in range(nsamp)]
+        tasks = [(list(wl.spins), wl.couplings, [wl.orientations[o] for _, o in c],
+                  [wl.fields[f] for f, _ in c], wl.polarization, np.array([np.inf]),
+                  "integral", np.ones(len(c))) for c in _chunks(items, threads)]
+        cpu_pool_map(tasks[:1], threads)  # start-up and imports outside the timing
         t0 = time.perf_counter()
-        for k in range(nsamp):
-            f, o = (k * 10) % Nf, (k * 37) % No
-            q = port.orientation_quat(wl.orientations[o])[0]
-            port.snapshot(osy, Hn, Zn, q, 1.0, wl.fields[f], wl.polarization, np.inf,
-                          np.zeros(3), np.array([np.inf]), y="integral")
+        cpu_pool_map(tasks, threads)
         dt = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": nsamp / dt, "unit": "integrals/s", "cores": 1,
-                                "kind": "port", "sample": f"{nsamp} (field, orientation) units"}
+        line["cpu_baseline"] = {"value": nsamp / dt, "unit": "integrals/s", "cores": threads,
+                                "kind": "port", "cpu_model": cpu_model(),
+                                "sample": f"{nsamp} (field, orientation) units over {threads} "
+                                          "processes (numpy eigh + the reference's integral)"}
     return line
 
 
@@ -650,16 +793,18 @@ def run_config4(args, world, rank, local):
     from muspinsim_gb300.multi import MultiSystemBatch
 
     n_sys, n_or = args.c4_systems, args.c4_orientations
-    wls = workloads.config4(n_systems=n_sys, n_orient=n_or)
+    dims = tuple(int(x) for x in args.c4_dims.split(","))
+    graph = args.c4_graph == "on"
+    wls = workloads.config4(n_systems=n_sys, n_orient=n_or, dims=dims)
     systems = [w.system() for w in wls]
     T = len(wls[0].times)
     out = {}
     for prec in ("mixed", "fp64") if args.fp64_steps > 0 else ("mixed",):
         b = MultiSystemBatch(systems, wls[0].orientations, wls[0].fields[0],
                              wls[0].polarization, wls[0].times, precision=prec)
-        b.run(graph=True)
+        b.run(graph=graph)
         torch.cuda.synchronize()
-        ms = _events_ms(lambda: b.run(graph=True), max(1, args.steps // 10))
+        ms = _events_ms(lambda: b.run(graph=graph), max(1, args.steps // 10))
         out[prec] = (ms, b.plan.out.clone(), b.plan.info())
         b.plan.close()
     ms, res, info = out["mixed"]
@@ -667,13 +812,13 @@ def run_config4(args, world, rank, local):
     dP = float((res - out["fp64"][1]).abs().max().item()) if "fp64" in out else None
     buckets = [{k: bi[k] for k in ("n", "num_systems", "num_snap", "num_chunks",
                                     "snap_threads", "grid")} for bi in info]
-    cfg = {"systems": n_sys, "orientations": n_or, "times": T,
-           "dims": [4, 8, 12, 24, 48, 96, 192], "graph": True}
+    cfg = {"systems": n_sys, "orientations": n_or, "times": T, "dims": list(dims),
+           "graph": graph}
     if (n_sys, n_or) != (4096, 256):
         cfg["scaled_from"] = "4096 systems x 256"
     return _line("heterogeneous-batch P(t) samples/s, mixed precision", samples / (ms * 1e-3),
                  "samples/s", ms, args, world,
-                 f"4_to_192_dim_systems_{n_sys}x{n_or}_orient_{T}_t", cfg,
+                 f"{min(dims)}_to_{max(dims)}_dim_systems_{n_sys}x{n_or}_orient_{T}_t", cfg,
                  dtype="f32 (Jacobi for n <= 64, Householder + QL for n > 64; double-word "
                        "refinement; phase sum)",
                  fp64=({"value": samples / (out["fp64"][0] * 1e-3),
@@ -747,14 +892,21 @@ def run_config5(args, world, rank, local):
         from oracle import port
         from tests.helpers import oracle_system
 
-        osy = oracle_system(wl.spins, wl.couplings)
+        threads = os.cpu_count() or 1
+        rows = list(wl.orientations)
+        tasks = [(list(wl.spins), wl.couplings, c, [np.zeros(3)] * len(c), wl.polarization,
+                  wl.times, "asymmetry", np.ones(len(c)) / len(rows))
+                 for c in _chunks(rows, threads)]
+        cpu_pool_map(tasks[:1], threads)  # start-up and imports outside the timing
         t0 = time.perf_counter()
-        port.powder_average(osy, wl.orientations, np.zeros(3), wl.polarization, np.inf, wl.times)
+        cpu_pool_map(tasks, threads)
         dt = time.perf_counter() - t0
         # a central-difference gradient in 2 parameters costs 5 forward runs
-        line["cpu_baseline"] = {"value": 1.0 / (5 * dt), "unit": "evaluations/s", "cores": 1,
-                                "kind": "port",
-                                "sample": "one forward run; loss + central-FD gradient = 5 runs"}
+        line["cpu_baseline"] = {"value": 1.0 / (5 * dt), "unit": "evaluations/s",
+                                "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+                                "sample": "one forward run over all orientations in "
+                                          f"{threads} processes; loss + central-FD gradient = "
+                                          "5 runs"}
     return line
 
 

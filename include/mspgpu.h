@@ -168,15 +168,41 @@ int msp_orient_snapshots(const double *rows, int num_rows, int row_len, int eule
                          double weight_norm, double *field, double *pol, double *weight,
                          void *stream);
 
+/* Orientation grids generated on the device (the input keywords
+ * `orientation zcw(N)` / `eulrange(N)`: muspinsim/utils.py:34-50,
+ * muspinsim/input/keyword.py:38), expanded as the Cartesian product of a
+ * field list and the grid (MuSpinConfig's snapshot product,
+ * muspinsim/simconfig.py:299-321, for a field axis or file range with
+ * averaged orientations).  Snapshot s = f * num_orient + o gets the
+ * lab-frame field R_o fields[f] + B_intr, polarisation R_o p, weight
+ * w_o * weight_norm (w_o = 1 for ZCW, sin(beta) for eulrange; 1 when the
+ * grid has one point) and, when slot is not NULL, output row f.  ZCW point
+ * j of N: polar angles theta = arccos(c1 (c2 j / N - 1)), phi = 2 pi
+ * frac(j g / N) (c = (1, 2) sphere, (-1, 1) hemisphere; g = zcw_generator,
+ * coprime with N), rotated like a (theta, phi) row; eulrange: N^3 ZYZ (or
+ * ZXZ, euler_mode 1) angles a, c = linspace(0, 2 pi, N), b = interior of
+ * linspace(0, pi, N + 2), in the reference's meshgrid order.  fields is a
+ * DEVICE array of num_fields x 3; p and B_intr are host 3-vectors; the
+ * outputs are device arrays of num_fields * num_orient snapshots. */
+#define MSP_GRID_ZCW_SPHERE 0
+#define MSP_GRID_ZCW_HEMISPHERE 1
+#define MSP_GRID_EULRANGE 2
+int msp_orient_grid_snapshots(int grid_kind, int grid_n, int zcw_generator, int euler_mode,
+                              const double *fields, int num_fields, const double *p,
+                              const double *B_intr, double weight_norm, double *field,
+                              double *pol, double *weight, int *slot, void *stream);
+
 /* ---- stage timer ---------------------------------------------------------- */
 
 /* Opaque set of CUDA events that msp_powder_run records around its stages
- * when msp_powder_args.timer is set: snapshots (assembly, eigensolve,
- * eigenbasis amplitudes), schedule, phase sum, reduction.  No counterpart in
+ * when msp_powder_args.timer is set: eigensolve (the warp-per-matrix FP32
+ * Jacobi of the two-stage MIXED form, n <= 32; empty otherwise), snapshots
+ * (assembly, eigensolve or refinement, eigenbasis amplitudes), schedule,
+ * phase sum, reduction.  No counterpart in
  * the reference, which has no timing beyond wall-clock logging
  * (muspinsim/__main__.py:124, 163-165). */
 typedef struct msp_timer msp_timer;
-#define MSP_TIMER_STAGES 4
+#define MSP_TIMER_STAGES 5
 #define MSP_TIMER_CAPACITY 512 /* runs recorded between two reads */
 
 int msp_timer_create(msp_timer **timer);
@@ -260,7 +286,9 @@ int msp_powder_run(const msp_powder_args *args);
  * until exit, and a batch needing more returns MSP_ERR_WORKSPACE with the
  * sizes in msp_last_error.  Nothing is allocated.  The first call on each
  * device (with it current) looks up the array's device address; make that
- * call before any stream capture.  All calls share the array: calls that
+ * call before any stream capture.  That address is not valid across
+ * cudaDeviceReset: do not call this entry point on a device after resetting
+ * it.  All calls share the array: calls that
  * overlap on the GPU race and must be serialised by the caller.  Same
  * results as msp_powder_run. */
 int msp_powder_run_static(const msp_powder_args *args);

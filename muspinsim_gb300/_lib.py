@@ -23,6 +23,10 @@ MSP_ITEM_NOT_CONVERGED = 1
 MSP_ITEM_BAD_SLOT = 2
 MSP_ITEM_REFINE_LIMIT = 4
 
+GRID_ZCW_SPHERE = 0
+GRID_ZCW_HEMISPHERE = 1
+GRID_EULRANGE = 2
+
 PREC_FP64 = 0
 PREC_MIXED = 1
 
@@ -245,8 +249,8 @@ class CelioArgs(ctypes.Structure):
     ]
 
 
-TIMER_STAGES = 4
-TIMER_STAGE_NAMES = ("snapshots", "schedule", "phase", "reduce")
+TIMER_STAGES = 5
+TIMER_STAGE_NAMES = ("eigensolve", "snapshots", "schedule", "phase", "reduce")
 
 
 # name -> (restype, argtypes)
@@ -273,6 +277,11 @@ _SIGNATURES = {
         ctypes.c_int,
         [_c_dp, ctypes.c_longlong, _c_dp, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
          ctypes.c_int, _c_dp, _c_dp],
+    ),
+    "msp_orient_grid_snapshots": (
+        ctypes.c_int,
+        [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp, ctypes.c_int, _c_dp,
+         _c_dp, ctypes.c_double, _c_dp, _c_dp, _c_dp, _c_dp, _c_dp],
     ),
     "msp_fast_cos_sum": (
         ctypes.c_int,

@@ -450,7 +450,16 @@ int msp_powder_run(const msp_powder_args *a) {
 
     cudaEvent_t *ev = timer_slot(a->timer);
     if (ev) cudaEventRecord(ev[0], st);
-    if (large && a->num_snap > 0 && a->mode == MSP_MODE_FAST)
+    // two-stage MIXED snapshots (n <= 32): the warp Jacobi is its own stage
+    const bool two_stage = !large && sa.evec != NULL && a->num_snap > 0;
+    if (two_stage) {
+        rc = cuda_check(launch_jacobi_warp(sa, st), "msp_jacobi_warp");
+        if (rc != MSP_OK) return rc;
+    }
+    if (ev) cudaEventRecord(ev[1], st);
+    if (two_stage)
+        rc = cuda_check(launch_snapshots_refine(sa, a->mode, st), "msp_snap");
+    else if (large && a->num_snap > 0 && a->mode == MSP_MODE_FAST)
         rc = cuda_check(launch_large_fast(sa, reinterpret_cast<double *>(ws + L.large),
                                           large_grid(a->num_snap, a->n, a->precision), st, 0,
                                           a->precision),
@@ -463,7 +472,7 @@ int msp_powder_run(const msp_powder_args *a) {
     else
         rc = cuda_check(launch_snapshots(sa, a->mode, a->precision, st), "msp_snap");
     if (rc != MSP_OK) return rc;
-    if (ev) cudaEventRecord(ev[1], st);
+    if (ev) cudaEventRecord(ev[2], st);
 
     PhaseArgs pa;
     memset(&pa, 0, sizeof(pa));
@@ -488,15 +497,15 @@ int msp_powder_run(const msp_powder_args *a) {
                                     reinterpret_cast<int *>(ws + L.item_first), a->status, st),
                     "msp_schedule");
     if (rc != MSP_OK) return rc;
-    if (ev) cudaEventRecord(ev[2], st);
+    if (ev) cudaEventRecord(ev[3], st);
     if (a->mode != MSP_MODE_INTEGRAL) {
         rc = cuda_check(launch_phase(pa, a->precision, L.max_items, a->uniform, st), "msp_phase");
         if (rc != MSP_OK) return rc;
     }
-    if (ev) cudaEventRecord(ev[3], st);
+    if (ev) cudaEventRecord(ev[4], st);
     rc = cuda_check(launch_reduce(pa, sa.snap_const, a->out, L.T, st), "msp_reduce");
     if (rc != MSP_OK) return rc;
-    if (ev) cudaEventRecord(ev[4], st);
+    if (ev) cudaEventRecord(ev[5], st);
     return MSP_OK;
 }
 

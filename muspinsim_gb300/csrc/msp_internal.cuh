@@ -125,6 +125,8 @@ size_t snap_smem_bytes(int n, int mode, int precision, int fac_len);
 bool jacobi_warp_supported(int n);
 size_t snap_evec_bytes(int n, long long num_snap, int precision);
 cudaError_t launch_jacobi_warp(const SnapArgs &a, cudaStream_t st);
+cudaError_t launch_snapshots_refine(const SnapArgs &a, int mode, cudaStream_t st, int threads = 0,
+                                    int grid = 0);
 cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStream_t st,
                              int threads = 0, int grid = 0);
 // Threads per CTA of the snapshot kernels when the caller gives none.

@@ -88,6 +88,70 @@ __global__ void msp_orient_kernel(OrientArgs a) {
     }
 }
 
+// Generated grids times a field list: snapshot s = f * num_orient + o.
+struct GridArgs {
+    int kind, n, gen, euler_axis;  // kind: MSP_GRID_*; gen: ZCW generator g
+    int num_orient, num_fields;
+    const double *B;               // num_fields x 3 (device)
+    double p[3], Bi[3];
+    double wnorm;
+    double *field, *pol, *weight;
+    int *slot;
+};
+
+// Euler angles (a, b, c) in the grid's convention and the row weight of
+// grid point o: ZCW (theta, phi) rows as polar angles (Euler (phi, theta,
+// phi), 'zyz'), eulrange (a, b, c, sin b).
+__device__ __forceinline__ void grid_point(const GridArgs &g, int o, double &ea, double &eb,
+                                           double &ec, double &w, int &bax) {
+    const double twopi = 6.283185307179586476925;
+    if (g.kind == MSP_GRID_EULRANGE) {
+        const int N = g.n;
+        const int k = o % N, j = (o / N) % N, i = o / (N * N);
+        const double da = N > 1 ? twopi / (double)(N - 1) : 0.0;
+        ea = j == N - 1 && N > 1 ? twopi : (double)j * da;
+        eb = (double)(i + 1) * (3.14159265358979323846 / (double)(N + 1));
+        ec = k == N - 1 && N > 1 ? twopi : (double)k * da;
+        w = sin(eb);
+        bax = g.euler_axis;
+    } else {
+        // beta = arccos(c1 (c2 j / N - 1)), alpha = 2 pi frac(j g / N)
+        const double c1 = g.kind == MSP_GRID_ZCW_HEMISPHERE ? -1.0 : 1.0;
+        const double c2 = g.kind == MSP_GRID_ZCW_HEMISPHERE ? 1.0 : 2.0;
+        double x = c1 * (c2 * ((double)o / (double)g.n) - 1.0);
+        x = fmin(1.0, fmax(-1.0, x));
+        const double theta = acos(x);
+        const long long jg = ((long long)o * (long long)g.gen) % (long long)g.n;
+        const double phi = twopi * ((double)jg / (double)g.n);
+        ea = phi;
+        eb = theta;
+        ec = phi;
+        w = 1.0;
+        bax = 1;
+    }
+}
+
+__global__ void msp_orient_grid_kernel(GridArgs g) {
+    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)g.num_orient * g.num_fields;
+    if (s >= total) return;
+    const int f = (int)(s / g.num_orient), o = (int)(s - (long long)f * g.num_orient);
+    double ea, eb, ec, w;
+    int bax;
+    grid_point(g, o, ea, eb, ec, w, bax);
+    const Quat q = qmul(qmul(qaxis(2, ec), qaxis(bax, eb)), qaxis(2, ea));
+    const Quat qs = {q.w, -q.x, -q.y, -q.z};  // the stored conjugate
+    double b[3], p[3];
+    qrotate(qs, g.B + 3 * (size_t)f, b);
+    qrotate(qs, g.p, p);
+    for (int i = 0; i < 3; ++i) {
+        g.field[3 * s + i] = b[i] + g.Bi[i];
+        g.pol[3 * s + i] = p[i];
+    }
+    g.weight[s] = (g.num_orient > 1 ? w : 1.0) * g.wnorm;
+    if (g.slot) g.slot[s] = f;
+}
+
 }  // namespace msp
 
 using namespace msp;
@@ -122,6 +186,52 @@ extern "C" int msp_orient_snapshots(const double *rows, int num_rows, int row_le
     a.pol = pol;
     a.weight = weight;
     msp_orient_kernel<<<(num_rows + 255) / 256, 256, 0, (cudaStream_t)stream>>>(a);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return record_error(MSP_ERR_CUDA, cudaGetErrorString(e));
+    return MSP_OK;
+}
+
+extern "C" int msp_orient_grid_snapshots(int grid_kind, int grid_n, int zcw_generator,
+                                         int euler_mode, const double *fields, int num_fields,
+                                         const double *p, const double *B_intr,
+                                         double weight_norm, double *field, double *pol,
+                                         double *weight, int *slot, void *stream) {
+    if (grid_kind < MSP_GRID_ZCW_SPHERE || grid_kind > MSP_GRID_EULRANGE || grid_n < 1 ||
+        num_fields < 0 || (euler_mode != 0 && euler_mode != 1))
+        return record_error(MSP_ERR_ARG,
+                            "msp_orient_grid_snapshots: unknown grid kind, grid_n < 1, "
+                            "num_fields < 0 or euler_mode not 0 / 1");
+    long long num_orient = grid_kind == MSP_GRID_EULRANGE
+                               ? (long long)grid_n * grid_n * grid_n : (long long)grid_n;
+    if (grid_kind != MSP_GRID_EULRANGE &&
+        (zcw_generator < 1 || (grid_n > 1 && zcw_generator >= grid_n)))
+        return record_error(MSP_ERR_ARG,
+                            "msp_orient_grid_snapshots: ZCW generator outside 1 .. grid_n - 1");
+    if (num_orient * (long long)num_fields > (1LL << 31) - 1)
+        return record_error(MSP_ERR_UNSUPPORTED,
+                            "msp_orient_grid_snapshots: more than 2^31 - 1 snapshots");
+    if (num_fields == 0) return MSP_OK;
+    if (fields == NULL || p == NULL || field == NULL || pol == NULL || weight == NULL)
+        return record_error(MSP_ERR_ARG, "msp_orient_grid_snapshots: a required pointer is NULL");
+    GridArgs g;
+    g.kind = grid_kind;
+    g.n = grid_n;
+    g.gen = zcw_generator;
+    g.euler_axis = euler_mode == 0 ? 1 : 0;
+    g.num_orient = (int)num_orient;
+    g.num_fields = num_fields;
+    g.B = fields;
+    for (int i = 0; i < 3; ++i) {
+        g.p[i] = p[i];
+        g.Bi[i] = B_intr ? B_intr[i] : 0.0;
+    }
+    g.wnorm = weight_norm;
+    g.field = field;
+    g.pol = pol;
+    g.weight = weight;
+    g.slot = slot;
+    const long long total = num_orient * num_fields;
+    msp_orient_grid_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(g);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return record_error(MSP_ERR_CUDA, cudaGetErrorString(e));
     return MSP_OK;

@@ -728,6 +728,254 @@ __global__ void __launch_bounds__(MSP_TC_THREADS) msp_phase_tc_kernel(PhaseArgs 
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
 }
 
+// ---------------------------------------------------------------- warp-specialised form
+//
+// The same GEMM and numerics as msp_phase_tc_kernel, with the per-stage
+// CTA barrier replaced by mbarriers so that table building, operand
+// building, MMA issue and accumulator draining overlap:
+//   * warps 0..7 (producers): drain the accumulator block of stage s - 2
+//     (when its MMAs have completed), build stage s's operands from its
+//     tables, then arrive on op_full[b] and tab_empty[t];
+//   * warps 8..10 (tables): build the power tables of stage s into one of
+//     three table buffers once tab_empty says the stage that used it is
+//     built, then arrive on tab_full[t];
+//   * warp 11, one lane (MMA): waits on op_full[b], issues the stage's 12
+//     MMAs into accumulator block b and commits them to mma_done[b].
+// Every wait polls a bounded number of times and also gives up when another
+// thread has recorded a failure (s_fail), so a failure ends every loop
+// quickly; the tile's partials are then NaN and the tensor memory is
+// released only after the last committed MMAs have completed (waited for,
+// bounded).
+#define MSP_TCW_PRODUCERS 256
+#define MSP_TCW_TABLE_THREADS 96
+#define MSP_TCW_THREADS (MSP_TCW_PRODUCERS + MSP_TCW_TABLE_THREADS + 32)
+#define MSP_TCW_TABLES 3
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Bounded wait that also stops when *fail is set (checked every 256 polls).
+__device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity,
+                                                  volatile int *fail) {
+    for (int it = 0; it < MSP_TC_WAIT; ++it) {
+        uint32_t done = 0;
+        asm volatile(
+            "{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;"
+            " selp.b32 %0, 1, 0, p;}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 255) == 255 && *fail) return false;
+    }
+    *fail = 1;
+    return false;
+}
+
+template <int N>
+__global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArgs a) {
+    typedef TcLayout<N> L;
+    constexpr int PS = MSP_TC_PS, NH = N / 2;
+    extern __shared__ __align__(1024) char tsm[];
+    __shared__ __align__(16) TcTables<N> tabs[MSP_TCW_TABLES];
+    __shared__ __align__(8) uint64_t tab_full[MSP_TCW_TABLES], tab_empty[MSP_TCW_TABLES];
+    __shared__ __align__(8) uint64_t op_full[2], mma_done[2];
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_range[2];
+    __shared__ int s_issued;
+    __shared__ volatile int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        item_range(a, blockIdx.x, &s_range[0], &s_range[1]);
+        for (int t = 0; t < MSP_TCW_TABLES; ++t) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tab_full[t])),
+                         "r"(MSP_TCW_TABLE_THREADS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tab_empty[t])),
+                         "r"(MSP_TCW_PRODUCERS));
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&op_full[b])),
+                         "r"(MSP_TCW_PRODUCERS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mma_done[b])));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        s_issued = 0;
+        s_fail = 0;
+    }
+    __syncthreads();
+    const int pbeg = s_range[0], pend = s_range[1];
+    if (pbeg < 0) return;
+    const long long tile_base = (long long)blockIdx.y * (128 * N);
+    const float tile_steps = (float)tile_base;  // exact: < 2^24
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(
+            smem_u32(&s_tmem)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = s_tmem;
+    const int nstage = (pend - pbeg + PS - 1) / PS;
+
+    float acc[NH];
+#pragma unroll
+    for (int j = 0; j < NH; ++j) acc[j] = 0.f;
+
+    if (tid < MSP_TCW_PRODUCERS) {
+        // ------------------------------------------------------------ producers
+        const int half = warp >> 2;
+        const uint32_t my_tmem =
+            tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(half * NH);
+        uint32_t r[32];
+        // waits decided warp-uniformly: tcgen05.ld is a whole-warp instruction
+        for (int s = 0; s < nstage && !s_fail; ++s) {
+            const int b = s & 1, t = s % MSP_TCW_TABLES;
+            if (!__all_sync(0xffffffffu, mbar_wait_or_fail(smem_u32(&tab_full[t]),
+                                                            (s / MSP_TCW_TABLES) & 1, &s_fail)))
+                break;
+            if (s >= 2) {
+                if (!__all_sync(0xffffffffu, mbar_wait_or_fail(smem_u32(&mma_done[b]),
+                                                                ((s >> 1) - 1) & 1, &s_fail)))
+                    break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                tmem_load<NH>(my_tmem + 32u * b, r);
+#pragma unroll
+                for (int j = 0; j < NH; ++j) acc[j] += __uint_as_float(r[j]);
+            }
+            char *A_hi = tsm + b * L::STAGE;
+            char *A_lo = A_hi + L::A_BYTES;
+            char *B_hi = A_lo + L::A_BYTES;
+            char *B_lo = B_hi + L::B_BYTES;
+            const TcTables<N> &tb = tabs[t];
+            {
+                const int k1 = tid & 127, h0 = tid >> 7;
+                const int off = (k1 >> 3) * 128 + (k1 & 7) * 16;
+#pragma unroll 2
+                for (int gi = 0; gi < PS / 4; ++gi) {
+                    const int g = h0 + 2 * gi;
+                    const cx<float> x0 = cmul(tb.xhi[k1 >> 3][2 * g], tb.xlo[k1 & 7][2 * g]);
+                    const cx<float> x1 =
+                        cmul(tb.xhi[k1 >> 3][2 * g + 1], tb.xlo[k1 & 7][2 * g + 1]);
+                    const float4 v = make_float4(x0.re, -x0.im, x1.re, -x1.im);
+                    const float4 hh =
+                        make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+                    const float4 lo = make_float4(v.x - hh.x, v.y - hh.y, v.z - hh.z, v.w - hh.w);
+                    *reinterpret_cast<float4 *>(A_hi + g * L::CA + off) = hh;
+                    *reinterpret_cast<float4 *>(A_lo + g * L::CA + off) = lo;
+                }
+            }
+            for (int e = tid; e < N * (PS / 2); e += MSP_TCW_PRODUCERS) {
+                const int k0 = e % N, g = e / N;
+                const cx<float> y0 = cmul(tb.yhi[k0 >> 3][2 * g], tb.ylo[k0 & 7][2 * g]);
+                const cx<float> y1 = cmul(tb.yhi[k0 >> 3][2 * g + 1], tb.ylo[k0 & 7][2 * g + 1]);
+                const float4 v = make_float4(y0.re, y0.im, y1.re, y1.im);
+                const float4 hh =
+                    make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+                const float4 lo = make_float4(v.x - hh.x, v.y - hh.y, v.z - hh.z, v.w - hh.w);
+                const int off = g * L::CB + (k0 >> 3) * 128 + (k0 & 7) * 16;
+                *reinterpret_cast<float4 *>(B_hi + off) = hh;
+                *reinterpret_cast<float4 *>(B_lo + off) = lo;
+            }
+            mbar_arrive(smem_u32(&tab_empty[t]));
+            // operands written by the generic proxy, read by the tensor core;
+            // this thread's tensor-memory reads ordered before the next MMAs
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(smem_u32(&op_full[b]));
+        }
+        // the blocks of the last two stages
+        for (int st = nstage >= 2 ? nstage - 2 : 0; st < nstage && !s_fail; ++st) {
+            if (!__all_sync(0xffffffffu, mbar_wait_or_fail(smem_u32(&mma_done[st & 1]),
+                                                            (st >> 1) & 1, &s_fail)))
+                break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            tmem_load<NH>(my_tmem + 32u * (st & 1), r);
+#pragma unroll
+            for (int j = 0; j < NH; ++j) acc[j] += __uint_as_float(r[j]);
+        }
+    } else if (tid < MSP_TCW_PRODUCERS + MSP_TCW_TABLE_THREADS) {
+        // ------------------------------------------------------------ tables
+        const int tt = tid - MSP_TCW_PRODUCERS;
+        for (int s = 0; s < nstage && !s_fail; ++s) {
+            const int t = s % MSP_TCW_TABLES;
+            if (s >= MSP_TCW_TABLES &&
+                !mbar_wait_or_fail(smem_u32(&tab_empty[t]), ((s / MSP_TCW_TABLES) - 1) & 1,
+                                   &s_fail))
+                break;
+            const int pb = pbeg + s * PS;
+            tc_build_tables<N>(a, tabs[t], pb, (pend - pb) < PS ? (pend - pb) : PS, tile_steps,
+                               tt);
+            mbar_arrive(smem_u32(&tab_full[t]));
+        }
+    } else if (lane == 0) {
+        // ------------------------------------------------------------ MMA issue
+        const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) |
+                               ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+        int issued = 0;
+        for (int s = 0; s < nstage && !s_fail; ++s) {
+            const int b = s & 1;
+            if (!mbar_wait_or_fail(smem_u32(&op_full[b]), (s >> 1) & 1, &s_fail)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            char *A_hi = tsm + b * L::STAGE;
+            const uint32_t ah = smem_u32(A_hi), al = ah + L::A_BYTES;
+            const uint32_t bh = al + L::A_BYTES, bl = bh + L::B_BYTES;
+            const uint32_t d = tmem + 32u * b;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+                const uint32_t ao = ks * 2 * L::CA, bo = ks * 2 * L::CB;
+                const uint64_t dah = tc_desc(ah + ao, L::CA, 128), dal = tc_desc(al + ao, L::CA, 128);
+                const uint64_t dbh = tc_desc(bh + bo, L::CB, 128), dbl = tc_desc(bl + bo, L::CB, 128);
+                // the small products first, the block restarts at each stage
+                tc_mma(d, dal, dbh, idesc, ks > 0 ? 1u : 0u);
+                tc_mma(d, dah, dbl, idesc, 1u);
+                tc_mma(d, dah, dbh, idesc, 1u);
+            }
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    smem_u32(&mma_done[b]))
+                : "memory");
+            issued = s + 1;
+        }
+        s_issued = issued;
+    }
+    // epilogue: every MMA committed has completed before the tensor memory
+    // goes (waited for, bounded, even after a failure)
+    __syncthreads();
+    const int issued = s_issued;
+    if (tid == 0 && issued > 0) {
+        const int last = issued - 1;
+        volatile int never = 0;
+        if (!mbar_wait_or_fail(smem_u32(&mma_done[last & 1]), (last >> 1) & 1, &never))
+            s_fail = 1;
+    }
+    if (tid == 0 && issued < nstage) s_fail = 1;
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const bool ok = !s_fail;
+    float *tile = reinterpret_cast<float *>(tsm);  // operand buffers are free now
+    if (tid < MSP_TCW_PRODUCERS) {
+        const int half = warp >> 2;
+        const int k1 = 32 * (warp & 3) + lane;  // this thread's TMEM lane
+#pragma unroll
+        for (int j = 0; j < NH; ++j)
+            tile[k1 * (N + 1) + half * NH + j] = ok ? acc[j] : __int_as_float(0x7fc00000);
+    }
+    __syncthreads();
+    float *out = a.partial_f32 + (size_t)blockIdx.x * a.num_times;
+    for (int e = tid; e < 128 * N; e += MSP_TCW_THREADS) {
+        const long long t = tile_base + e;
+        if (t < a.num_times) out[t] = tile[(e / N) * (N + 1) + (e % N)];
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+}
+
 // Arbitrary time grids: one thread per sample, every pair's phase reduced in
 // FP64 and evaluated with sincos.
 template <typename T>
@@ -873,6 +1121,31 @@ bool phase_use_tensor_cores() {
     return !(v != NULL && v[0] == '1');
 }
 
+// The tensor-core phase sum runs in its warp-specialised form unless
+// MSP_PHASE_TC_BARRIER=1 selects the one-barrier-per-stage form.
+static bool phase_tc_warp_specialised() {
+    const char *v = getenv("MSP_PHASE_TC_BARRIER");
+    return !(v != NULL && v[0] == '1');
+}
+
+template <int N>
+static cudaError_t launch_tc(const PhaseArgs &a, int max_items, cudaStream_t st) {
+    const int smem = TcLayout<N>::SMEM;
+    const dim3 grid(max_items, (a.num_times + 128 * N - 1) / (128 * N));
+    if (phase_tc_warp_specialised()) {
+        cudaError_t e = cudaFuncSetAttribute(msp_phase_tcw_kernel<N>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        msp_phase_tcw_kernel<N><<<grid, MSP_TCW_THREADS, smem, st>>>(a);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(msp_phase_tc_kernel<N>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        msp_phase_tc_kernel<N><<<grid, MSP_TC_THREADS, smem, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
 int phase_snaps_per_item(int num_snap, int P, int precision) {
     if (P <= 0) return 1;
     // about 1500 items for load balance; FP32 accumulates at most
@@ -906,21 +1179,8 @@ cudaError_t launch_phase(const PhaseArgs &a, int precision, int max_items, int u
                          cudaStream_t st) {
     if (max_items <= 0 || a.num_times <= 0) return cudaSuccess;
     if (uniform && precision == MSP_PREC_MIXED && phase_use_tensor_cores()) {
-        if (a.num_times > 2048) {
-            const int smem = TcLayout<32>::SMEM;
-            cudaError_t e = cudaFuncSetAttribute(msp_phase_tc_kernel<32>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            if (e != cudaSuccess) return e;
-            dim3 grid(max_items, (a.num_times + 4095) / 4096);
-            msp_phase_tc_kernel<32><<<grid, MSP_TC_THREADS, smem, st>>>(a);
-        } else {
-            const int smem = TcLayout<16>::SMEM;
-            cudaError_t e = cudaFuncSetAttribute(msp_phase_tc_kernel<16>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            if (e != cudaSuccess) return e;
-            dim3 grid(max_items, (a.num_times + 2047) / 2048);
-            msp_phase_tc_kernel<16><<<grid, MSP_TC_THREADS, smem, st>>>(a);
-        }
+        return a.num_times > 2048 ? launch_tc<32>(a, max_items, st)
+                                  : launch_tc<16>(a, max_items, st);
     } else if (uniform) {
         dim3 grid(max_items, (a.num_times + 4095) / 4096);
         if (precision == MSP_PREC_MIXED)

@@ -730,6 +730,22 @@ size_t snap_evec_bytes(int n, long long num_snap, int precision) {
     return (size_t)num_snap * (size_t)n * (size_t)n * sizeof(float2);
 }
 
+// Second stage of the two-stage MIXED form: refinement and eigenbasis
+// products from the eigenvectors the warp Jacobi left in a.evec.
+cudaError_t launch_snapshots_refine(const SnapArgs &a, int mode, cudaStream_t st, int threads,
+                                    int grid) {
+    if (a.num_snap <= 0) return cudaSuccess;
+    if (threads <= 0) threads = snap_default_threads(a.n);
+    const size_t smem = snap_smem_threads(a.n, mode, MSP_PREC_MIXED, a.fac_len, threads);
+    if (grid <= 0 || grid > a.num_snap) grid = a.num_snap;
+    if (mode == MSP_MODE_FAST)
+        return launch_snap(msp_snap_fast_kernel<float, true, true>, a, grid, threads, smem, st);
+    if (mode == MSP_MODE_EVOLVE)
+        return launch_snap(msp_snap_rho_kernel<float, true, false, true>, a, grid, threads, smem,
+                           st);
+    return launch_snap(msp_snap_rho_kernel<float, true, true, true>, a, grid, threads, smem, st);
+}
+
 // threads = 0: jacobi_threads(m); grid = 0: one CTA per snapshot.  Any
 // other grid runs persistent CTAs that stride over the snapshots.
 cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStream_t st,
@@ -743,12 +759,7 @@ cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStr
         // two stages: warp Jacobi, then refinement and eigenbasis products
         const cudaError_t e = launch_jacobi_warp(a, st);
         if (e != cudaSuccess) return e;
-        if (mode == MSP_MODE_FAST)
-            return launch_snap(msp_snap_fast_kernel<float, true, true>, a, grid, threads, smem, st);
-        if (mode == MSP_MODE_EVOLVE)
-            return launch_snap(msp_snap_rho_kernel<float, true, false, true>, a, grid, threads, smem,
-                               st);
-        return launch_snap(msp_snap_rho_kernel<float, true, true, true>, a, grid, threads, smem, st);
+        return launch_snapshots_refine(a, mode, st, threads, grid);
     }
     if (mode == MSP_MODE_FAST) {
         return mixed ? launch_snap(msp_snap_fast_kernel<float, true>, a, grid, threads, smem, st)

@@ -16,7 +16,10 @@
 // code cannot use the array's name as a device address, so the first call
 // on each device -- with that device current -- looks the address up with
 // cudaGetSymbolAddress and caches it; make that first call before any
-// stream capture.  Every call shares the one array and finds the previous
+// stream capture.  The cached address belongs to the device's primary
+// context: cudaDeviceReset destroys that context (and the array with it),
+// after which the cached address is stale, so a process that resets a
+// device must not call this entry point on it again.  Every call shares the one array and finds the previous
 // call's contents in it: the pipeline writes every scratch byte before
 // reading it, so nothing has to be cleared, but two calls that overlap on
 // the GPU (different streams, or different host threads) race on the array

@@ -194,6 +194,41 @@ def orient_snapshots(rows, B, p, B_intr=(0.0, 0.0, 0.0), mode="zyz", weight_norm
     return field, pol, w
 
 
+def orient_grid_snapshots(kind, n, fields, p, B_intr=(0.0, 0.0, 0.0), mode="zyz",
+                          generator=None):
+    """Snapshots of a device-generated orientation grid times a field list
+    (msp_orient_grid_snapshots): kind 'zcw', 'zcw-hemisphere' or 'eulrange'
+    with n points (n^3 for eulrange), fields (F, 3).  Returns device tensors
+    field (F*No, 3), pol (F*No, 3), weight (F*No,) (weights normalised over
+    the grid) and slot (F*No,) int32 (the field index)."""
+    from muspinsim_gb300.orientations import zcw_generator
+
+    d = device()
+    code = {"zcw": _lib.GRID_ZCW_SPHERE, "zcw-hemisphere": _lib.GRID_ZCW_HEMISPHERE,
+            "eulrange": _lib.GRID_EULRANGE}[kind]
+    n = int(n)
+    No = n**3 if code == _lib.GRID_EULRANGE else n
+    if code == _lib.GRID_EULRANGE:
+        b = np.linspace(0, np.pi, n + 2)[1:-1]
+        wsum = float(np.sin(b).sum()) * n * n
+        wnorm = 1.0 / wsum if No > 1 else 1.0
+        gen = 1
+    else:
+        wnorm = 1.0 / No
+        gen = zcw_generator(n) if generator is None else int(generator)
+    F = dev(np.atleast_2d(np.asarray(fields, dtype=float)), torch.float64).reshape(-1, 3)
+    nf = int(F.shape[0])
+    field = torch.empty((nf * No, 3), dtype=torch.float64, device=d)
+    pol = torch.empty((nf * No, 3), dtype=torch.float64, device=d)
+    w = torch.empty((nf * No,), dtype=torch.float64, device=d)
+    slot = torch.empty((nf * No,), dtype=torch.int32, device=d)
+    vec = ctypes.c_double * 3
+    _lib.call("msp_orient_grid_snapshots", code, n, gen, 0 if mode == "zyz" else 1, ptr(F), nf,
+              vec(*np.asarray(p, dtype=float)), vec(*np.asarray(B_intr, dtype=float)),
+              float(wnorm), ptr(field), ptr(pol), ptr(w), ptr(slot), stream())
+    return field, pol, w, slot
+
+
 def uniform_grid(times, rtol=1e-12):
     """(is_uniform, t0, dt) for a 1-D time array."""
     t = np.asarray(times, dtype=np.float64)

@@ -23,6 +23,12 @@ import numpy as np
 from muspinsim_gb300 import quaternion as Q
 
 
+def zcw_generator(N):
+    """The ZCW generator g used for N points (coprime with N, nearest
+    N / phi^2)."""
+    return _generator(int(N))
+
+
 def _generator(N):
     phi2 = ((1.0 + 5**0.5) / 2.0) ** 2
     g0 = max(1, int(round(N / phi2)))
@@ -44,10 +50,13 @@ def zcw_gen(N, mode="sphere"):
         c1, c2, c3 = -1.0, 1.0, 1.0
     else:
         raise ValueError(f"Unknown ZCW mode {mode}")
-    j = np.arange(N)
+    j = np.arange(N, dtype=np.int64)
     g = _generator(N)
-    beta = np.arccos(np.clip(c1 * (c2 * np.mod(j / N, 1.0) - 1.0), -1.0, 1.0))
-    alpha = 2.0 * np.pi / c3 * np.mod(j * g / N, 1.0)
+    # frac(j / N) = j / N for j < N; frac(j g / N) from the exact integer
+    # remainder (the device grid generator, msp_orient_grid_snapshots, uses
+    # the same two expressions)
+    beta = np.arccos(np.clip(c1 * (c2 * (j / N) - 1.0), -1.0, 1.0))
+    alpha = 2.0 * np.pi / c3 * (((j * g) % N) / N)
     return np.stack([beta, alpha], axis=1)
 
 

@@ -176,6 +176,78 @@ def _fast_rule_uniform(field, intrinsic_field, temperature, mu_index):
     return bool(t_inf_speedup(np.atleast_2d(field), float(T), mu_index)[0])
 
 
+class OrientationGrid:
+    """A powder grid the GPU generates itself: the input language's
+    ``orientation zcw(N)`` / ``eulrange(N)`` (muspinsim/utils.py:34-50).
+    ``kind``: 'zcw', 'zcw-hemisphere' or 'eulrange' (n^3 points, sin(beta)
+    weights); ``mode``: Euler convention of eulrange rows."""
+
+    def __init__(self, kind, n, mode="zyz"):
+        if kind not in ("zcw", "zcw-hemisphere", "eulrange"):
+            raise ValueError(f"Unknown orientation grid {kind}")
+        self.kind, self.n, self.mode = kind, int(n), mode
+
+    def __len__(self):
+        return self.n**3 if self.kind == "eulrange" else self.n
+
+    def rows(self):
+        """The same grid as host rows (for host-side code and the oracle)."""
+        from muspinsim_gb300.orientations import eulrange_gen, zcw_gen
+
+        if self.kind == "eulrange":
+            return eulrange_gen(self.n)
+        return zcw_gen(self.n, "hemisphere" if self.kind == "zcw-hemisphere" else "sphere")
+
+
+def powder_scan(system, orientations, fields, polarization=(1.0, 0.0, 0.0), times=None,
+                temperature=np.inf, intrinsic_field=(0.0, 0.0, 0.0), y_axis="asymmetry",
+                precision="fp64", max_sweeps=0):
+    """One orientation-averaged result per field: a field scan (the field as
+    x axis or file range, orientations averaged; MuSpinConfig's snapshot
+    product, muspinsim/simconfig.py:299-321, run by ExperimentRunner,
+    muspinsim/experiment.py:358-498) in one msp_powder_run.
+
+    ``orientations``: an :class:`OrientationGrid` (points and the field x
+    orientation product generated on the device, msp_orient_grid_snapshots)
+    or explicit rows (product built on the host).  ``fields``: (F, 3) or
+    scalars along z (T).  Returns (F, len(times)), or (F,) for 'integral'."""
+    F = np.asarray(fields, dtype=float)
+    F = np.stack([np.zeros_like(F), np.zeros_like(F), F], axis=1) if F.ndim == 1 else F
+    p = np.asarray(polarization, dtype=float)
+    p = p / np.linalg.norm(p)
+    intr = np.atleast_1d(np.asarray(intrinsic_field, dtype=float))
+    if intr.size == 1:
+        intr = np.array([0.0, 0.0, intr[0]])
+    if y_axis == "integral":
+        times = np.array([np.inf])
+    times = np.asarray(times, dtype=float)
+    nf = len(F)
+    T = float(temperature)
+    # T = inf: the fast path wherever the muon comes first; a finite
+    # temperature: the general path, exact for every field
+    fast = bool(np.isinf(T) and system.muon_index == 0)
+    if isinstance(orientations, OrientationGrid):
+        B_lab, p_lab, W, slot = kernels.orient_grid_snapshots(
+            orientations.kind, orientations.n, F, p, intr, orientations.mode)
+        res, status = run_snapshots(system, B_lab, p_lab, T, W, slot, nf, times, y_axis,
+                                    precision, max_sweeps, fast_mask=fast, host_out=True)
+    else:
+        qs, ws = orientation_rows_to_quats(orientations)
+        N = len(qs)
+        ws = ws * (N / ws.sum()) if N > 1 else np.ones(1)
+        B_lab = np.concatenate([Q.rotate(qs, f) + intr for f in F])
+        p_lab = np.tile(Q.rotate(qs, p), (nf, 1))
+        W = np.tile(ws / N, nf)
+        slot = np.repeat(np.arange(nf), N)
+        res, status = run_snapshots(system, B_lab, p_lab, T, W, slot, nf, times, y_axis,
+                                    precision, max_sweeps, host_out=True)
+    if np.any(status & _lib.MSP_ITEM_NOT_CONVERGED):
+        raise RuntimeError("powder_scan: an eigensolve reached its sweep cap")
+    if np.any(status & _lib.MSP_ITEM_BAD_SLOT):
+        raise RuntimeError("powder_scan: invalid output rows")
+    return res
+
+
 def powder_average(system, orientations, field=(0.0, 0.0, 0.0), polarization=(1.0, 0.0, 0.0),
                    times=None, temperature=np.inf, intrinsic_field=(0.0, 0.0, 0.0),
                    y_axis="asymmetry", precision="fp64", mode="zyz", max_sweeps=0):
@@ -190,6 +262,11 @@ def powder_average(system, orientations, field=(0.0, 0.0, 0.0), polarization=(1.
     A regular grid of rows is rotated on the device (msp_orient_snapshots)
     and the system's matrices stay on the device between calls, so a call
     moves the rows, the time grid and the result across the bus."""
+    if isinstance(orientations, OrientationGrid):
+        f = np.atleast_1d(np.asarray(field, dtype=float))
+        f = np.array([0.0, 0.0, f[0]]) if f.size == 1 else f
+        return powder_scan(system, orientations, f[None, :], polarization, times, temperature,
+                           intrinsic_field, y_axis, precision, max_sweeps)[0]
     f = np.atleast_1d(np.asarray(field, dtype=float))
     if f.size == 1:
         f = np.array([0.0, 0.0, f[0]])

@@ -186,8 +186,9 @@ class MuSpinConfig:
                 self._file_ranges[cname] = values
         if self._y_axis == "integral" and x_axis == "t":
             raise MuSpinConfigError("Can not use time as X axis when evaluating integral of signal")
-        if params["fitting_info"].get("fit"):
-            raise MuSpinConfigError("Fitting configurations are not supported by muspinsim_gb300")
+        finfo = params["fitting_info"]
+        if finfo.get("fit"):
+            x_values = self._fit_x_axis(finfo, x_axis, x_values, use_experimental_x_axis)
         if x_values is None:
             raise MuSpinConfigError("Specified x axis is not a range")
         self._x_range[x_axis] = x_values
@@ -235,6 +236,41 @@ class MuSpinConfig:
             else:
                 values = [(q, 1.0) for (q, _) in values]
         return values
+
+    def _fit_x_axis(self, finfo, x_axis, x_values, use_experimental):
+        """Fitting (muspinsim/simconfig.py:180-233): no file ranges; the x axis
+        becomes the experimental data's first column (fields along z) when
+        asked, or when the x keyword holds a single value; the declared x
+        axis is then only used for the output file."""
+        if len(self._file_ranges) > 0:
+            raise MuSpinConfigError("Can not have file ranges when fitting")
+        self._constants.pop(x_axis, None)
+        if x_values is None:
+            use_experimental = True
+            finfo["evaluate_x_axis"] = False
+        if not use_experimental:
+            return x_values
+        data_x = np.asarray(finfo["data"])[:, 0]
+        if x_axis in ("B", "intrinsic_B"):
+            exp_x = np.array([[0.0, 0.0, v] for v in data_x])
+        else:
+            exp_x = data_x
+        if finfo.get("evaluate_x_axis") and x_values is not None:
+            logging.info("Fitting will be performed on experimental data-points, specified "
+                         "'x_axis' will only be used to generate final .dat file")
+            xv = np.asarray(x_values, dtype=float)
+            lo, hi = xv < exp_x[0], xv > exp_x[-1]
+            if np.all(hi) or np.all(lo):
+                logging.warning("All points on specified 'x_axis' are outside the experimental "
+                                "range, fitted parameters may not be appropriate for "
+                                "extrapolation")
+            elif np.any(hi) or np.any(lo):
+                logging.info("Some points on specified 'x_axis' are outside the experimental "
+                             "range, fitted parameters may not be appropriate for "
+                             "extrapolation")
+        if x_axis == "t":
+            self._time_N = len(exp_x)
+        return list(exp_x)
 
     @staticmethod
     def _axis_role(cname, count, x_axis, averaged):

@@ -265,6 +265,26 @@ def evolve(H, rho, times, operators):
     return out
 
 
+def evolve_per_time(H, rho, times, operators):
+    """The same <O>(t) computed the way the reference's Hamiltonian.evolve
+    does it, for CPU-baseline timing (muspinsim/hamiltonian.py:76-107): per
+    time, the n x n phase matrix exp(ll t) times rho', an elementwise
+    product-sum with each O'^T, and the row appended to the result with
+    np.concatenate (quadratic in the number of times, as there)."""
+    evals, evecs = np.linalg.eigh(H)
+    U = evecs
+    rp = U.conj().T @ rho @ U
+    opsT = np.array([(U.conj().T @ O @ U).T for O in operators])
+    ll = -2.0j * np.pi * (evals[:, None] - evals[None, :])
+    times = np.asarray(times, dtype=float)
+    result = None
+    for i in range(times.shape[0]):
+        r = np.exp(ll[None, :, :] * times[i, None, None]) * rp[None, :, :]
+        single = np.sum(r[0, None, :, :] * opsT[None, :, :, :], axis=(2, 3))
+        result = single if result is None else np.concatenate(([result, single]), axis=0)
+    return result
+
+
 def integrate_decaying(H, rho, tau, operators):
     """int_0^inf <O>(t) exp(-t/tau) dt = sum_ij rho'_ij [-O'/(2 pi i (l_i -
     l_j) - 1/tau)]^T_ij (muspinsim/hamiltonian.py:119-164)."""

@@ -317,8 +317,84 @@ def save_fast_binding(name):
     print(f"{name}: n = {A.shape[0]}, {len(times)} times")
 
 
+FIT_TIMES = np.linspace(0.0, 10.0, 150)
+FIT_TRUE = {"r1": 1.18, "r2": 1.25}
+FIT_START = {"r1": 1.10, "r2": 1.32}
+
+
+def fit_params(make_params, r1, r2):
+    """The F-mu-F fit problem's evaluated parameters (as a function of the two
+    mu-F distances, Angstrom): the config-5 geometry with its dipolar
+    directions kept and lengths set; 12 orientations; 150 times.  Used with
+    the reference's refshim.make_params here and with the package's
+    simconfig.make_params in the tests."""
+    from muspinsim_gb300 import workloads
+
+    wl = workloads.config5(n_orient=12, n_times=150)
+    (k1, a1, v1), (k2, a2, v2), third = wl.couplings
+    u1, u2 = np.asarray(v1) / np.linalg.norm(v1), np.asarray(v2) / np.linalg.norm(v2)
+    coup = [(k1, a1, u1 * r1), (k2, a2, u2 * r2), third]
+    return make_params(wl.spins, coup, FIT_TIMES, wl.orientations, wl.fields[0],
+                       wl.polarization)
+
+
+def save_fit(name):
+    """The reference's FittingRunner on the F-mu-F problem
+    (muspinsim/fitting.py:15-179): target = its own P(t) at FIT_TRUE plus
+    N(0, 0.01^2) noise; L-BFGS-B (its scipy difference quotients) and
+    Nelder-Mead results from FIT_START, the objective there and its central
+    differences (h = 1e-6)."""
+    from muspinsim.experiment import ExperimentRunner
+    from muspinsim.fitting import FittingRunner
+    from muspinsim.input.variables import FittingVariable
+
+    def mk(spins, coup, times, orients, field, pol):
+        return refshim.make_params(spins, coup, times, orients, field=[field],
+                                   polarization=pol)
+
+    truth = np.array(ExperimentRunner(refshim.ParamsInput(fit_params(mk, **FIT_TRUE))).run())
+    rng = np.random.default_rng(5151)
+    data = np.stack([FIT_TIMES, truth + rng.normal(0.0, 0.01, truth.shape)], axis=1)
+
+    class FitIn:
+        def __init__(self, method):
+            self.fitting_info = {"fit": True, "data": data, "method": method, "rtol": 1e-8,
+                                 "function": None, "single_simulation": False,
+                                 "evaluate_x_axis": False}
+            self.variables = {k: FittingVariable(k, v, 0.8, 2.0) for k, v in FIT_START.items()}
+
+        def evaluate(self, **v):
+            p = fit_params(mk, **v)
+            p["fitting_info"] = dict(self.fitting_info)
+            return p
+
+    out = {}
+    for method in ("lbfgs", "nelder-mead"):
+        fr = FittingRunner(FitIn(method))
+        sol = fr.run()
+        out[method] = (np.asarray(sol["x"], dtype=float), float(sol["fun"]), int(sol["nfev"]))
+    fr = FittingRunner(FitIn("lbfgs"))
+    x0 = np.array([FIT_START[k] for k in sorted(FIT_START)])
+    f0 = fr._targfun_minimise(x0)
+    g0 = np.zeros(2)
+    for k in range(2):
+        up, dn = x0.copy(), x0.copy()
+        up[k] += 1e-6
+        dn[k] -= 1e-6
+        g0[k] = (fr._targfun_minimise(up) - fr._targfun_minimise(dn)) / 2e-6
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), data=data, truth=truth, x0=x0, f0=f0,
+                        g0=g0, x_lbfgs=out["lbfgs"][0], f_lbfgs=out["lbfgs"][1],
+                        nfev_lbfgs=out["lbfgs"][2], x_nm=out["nelder-mead"][0],
+                        f_nm=out["nelder-mead"][1], nfev_nm=out["nelder-mead"][2])
+    print(f"{name}: lbfgs x={out['lbfgs'][0]} f={out['lbfgs'][1]:.6g} nfev={out['lbfgs'][2]}; "
+          f"nelder-mead x={out['nelder-mead'][0]} f={out['nelder-mead'][1]:.6g}")
+
+
 def main(only=None):
     refshim.install()
+    if only == "fit":
+        save_fit("fit_fmuf")
+        return
     if only == "celio":
         save_celio()
         return
@@ -374,6 +450,7 @@ def main(only=None):
     save_config_layouts("config_layouts")
     save_rotated("rotated_dim24")
     save_fast_binding("fast_binding_dim24")
+    save_fit("fit_fmuf")
 
 
 if __name__ == "__main__":

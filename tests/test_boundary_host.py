@@ -86,3 +86,33 @@ def test_rotate_host_matches_reference():
     assert np.abs(sy.hamiltonian_matrix() - z["H"]).max() <= 1e-12 * scale
     for R, HR in zip(z["R"], z["HR"]):
         assert np.abs(sy.rotate(R).hamiltonian_matrix() - HR).max() <= 1e-12 * scale
+
+
+def test_fit_config_uses_experimental_axis():
+    """Fitting (muspinsim/simconfig.py:180-233): the x axis becomes the
+    data's first column; file ranges are refused; FittingVariable checks
+    its bounds (muspinsim/input/variables.py:4-40)."""
+    import pytest
+
+    from muspinsim_gb300.fitting import FitInput, FittingVariable
+    from muspinsim_gb300.simconfig import MuSpinConfig, MuSpinConfigError, make_params
+
+    data = np.stack([np.linspace(0, 5, 11), np.zeros(11)], axis=1)
+
+    def build(a):
+        return make_params(spins=["mu", "e"], couplings=[("hyperfine", {"i": 1}, a * np.eye(3))],
+                           time=np.linspace(0, 1, 3))
+
+    inp = FitInput(build, [FittingVariable("a", 10.0, 0.0, 50.0)], data)
+    cfg = MuSpinConfig(inp.evaluate(a=10.0))
+    assert np.allclose(cfg.x_axis_values, data[:, 0]) and cfg.time_N == 11
+    bad = dict(inp.evaluate(a=10.0))
+    bad.update(make_params(spins=["mu", "e"], time=np.linspace(0, 1, 3),
+                           field=[0.0, 0.01]))  # a field file range
+    bad["fitting_info"] = inp.fitting_info
+    with pytest.raises(MuSpinConfigError, match="file ranges"):
+        MuSpinConfig(bad)
+    with pytest.raises(ValueError, match="invalid range"):
+        FittingVariable("b", 1.0, 2.0, 1.0)
+    with pytest.raises(ValueError, match="starting value"):
+        FittingVariable("b", 3.0, 0.0, 1.0)
