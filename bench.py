@@ -495,7 +495,7 @@ def run_gb300(args, world, rank, local):
         "snapshots": ("msp_snap_fast_kernel<float,true,true> (refinement + amplitudes)",
                       32.0 * n**3 * S, "fp32-pipe", fp32_peak,
                       "nominal FP32 FMA pipe (152 x 128 x 2 x 2070 MHz)"),
-        "phase": ("msp_phase_tc_kernel<32> (tcgen05 kind::tf32, 3xTF32)",
+        "phase": ("msp_phase_tcw_kernel<32> (tcgen05 kind::tf32, 3xTF32, warp-specialised)",
                   (4.0 * n * n) * samples, "tensor", tf32_peak, tf32_src),
         "reduce": ("msp_reduce_kernel", 2.0 * samples, "fp32-pipe", fp32_peak,
                    "nominal FP32 FMA pipe"),
