@@ -272,7 +272,7 @@ static cudaEvent_t *timer_slot(msp_timer *t) {
 // ---------------------------------------------------------------- powder pipeline
 
 struct Layout {
-    size_t coef, omega, snap_const, slot_first, item_first, partial, large, evec, total;
+    size_t coef, omega, snap_const, slot_first, item_first, partial, large, evec, hdw, total;
     int P, IP, max_items, T;
     bool phase_records;
 };
@@ -358,6 +358,11 @@ static Layout powder_layout(const msp_powder_args *a) {
     off += align256((size_t)L.max_items * L.T * (L.phase_records ? 4 : 8));
     L.evec = off;
     off += align256(snap_evec_bytes(a->n, a->num_snap, a->precision));
+    // MIXED, n <= MSP_MAX_DIM: Hsys and Z as double-words (no FP64 in the
+    // snapshot kernels)
+    L.hdw = off;
+    if (a->precision == MSP_PREC_MIXED && a->n <= MSP_MAX_DIM && a->num_snap > 0)
+        off += align256((size_t)4 * a->n * a->n * 16);
     L.large = off;
     if (a->n > MSP_MAX_DIM) {
         if (a->mode == MSP_MODE_FAST)
@@ -435,6 +440,7 @@ int msp_powder_run(const msp_powder_args *a) {
     sa.pair_phase = L.phase_records ? reinterpret_cast<float4 *>(ws + L.omega) : NULL;
     sa.t0 = a->t0;
     sa.dt = a->dt;
+    snap_time_constants(sa);
     sa.snap_const = reinterpret_cast<double *>(ws + L.snap_const);
     sa.status = a->status;
     sa.coef_f32 = a->precision == MSP_PREC_MIXED;
@@ -450,6 +456,14 @@ int msp_powder_run(const msp_powder_args *a) {
 
     cudaEvent_t *ev = timer_slot(a->timer);
     if (ev) cudaEventRecord(ev[0], st);
+    if (a->precision == MSP_PREC_MIXED && !large && a->num_snap > 0) {
+        const size_t nn = (size_t)a->n * a->n;
+        float4 *hdw = reinterpret_cast<float4 *>(ws + L.hdw);
+        rc = cuda_check(launch_split_dw(a->Hsys, nn, a->Z, 3 * nn, hdw, st), "msp_split_dw");
+        if (rc != MSP_OK) return rc;
+        sa.Hsys_dw = hdw;
+        sa.Z_dw = hdw + nn;
+    }
     // two-stage MIXED snapshots (n <= 32): the warp Jacobi is its own stage
     const bool two_stage = !large && sa.evec != NULL && a->num_snap > 0;
     if (two_stage) {

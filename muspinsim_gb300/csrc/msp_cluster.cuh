@@ -34,6 +34,7 @@
 // the clusters are disjoint diagonal blocks of one n x n buffer.
 #pragma once
 
+#include "msp_dw.cuh"
 #include "msp_jacobi.cuh"
 
 namespace msp {
@@ -62,11 +63,12 @@ __device__ __forceinline__ bool oa_in_cluster(const int *cstart, int n, int r) {
 
 // Clusters of the refinement step: amax, the sort, the cluster starts and
 // the off-diagonal entries of T.  SR holds S_ij (i < j) at [i][j] and R_ij
-// at [j][i] (row stride ld); lam / lamf are the Rayleigh quotients.
+// at [j][i] (row stride ld); lam / lamf are the Rayleigh quotients (lam as
+// double-words, msp_dw.cuh; lamf their high words).
 // c.scal[0] must be zero on entry (made visible by a barrier).  All threads
 // of the CTA call it; it ends with a barrier.
-static __device__ void oa_clusters(const cx<float> *SR, int ld, const double *lam, const float *lamf,
-                            int n, const OaCluster &c) {
+static __device__ void oa_clusters(const cx<float> *SR, int ld, const float2 *lam,
+                                   const float *lamf, int n, const OaCluster &c) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int nup = n * (n - 1) / 2;
     float amax = 0.f;
@@ -81,11 +83,11 @@ static __device__ void oa_clusters(const cx<float> *SR, int ld, const double *la
     atomicMax(&c.scal[0], __float_as_int(amax));  // non-negative: int order = float order
     // ascending order, ties by index
     for (int i = tid; i < n; i += nt) {
-        const double li = lam[i];
+        const float2 li = lam[i];
         int r = 0;
         for (int k = 0; k < n; ++k) {
-            const double lk = lam[k];
-            r += (lk < li) || (lk == li && k < i);
+            const float2 lk = lam[k];
+            r += dw_less(lk, li) || (dw_equal(lk, li) && k < i);
         }
         c.rank[i] = r;
         c.order[r] = i;
@@ -99,7 +101,7 @@ static __device__ void oa_clusters(const cx<float> *SR, int ld, const double *la
         const int q0 = lane * per, q1 = min(q0 + per, n);
         int run = -1;
         for (int q = q0; q < q1; ++q) {
-            const bool brk = q == 0 || (float)(lam[c.order[q]] - lam[c.order[q - 1]]) > gamma;
+            const bool brk = q == 0 || dw_sub_f(lam[c.order[q]], lam[c.order[q - 1]]) > gamma;
             if (brk) run = q;
             c.cstart[q] = run;  // -1: continues a run from an earlier chunk
         }
@@ -131,7 +133,7 @@ static __device__ void oa_clusters(const cx<float> *SR, int ld, const double *la
 
 // E for the pair (i < j) in place of S_ij / R_ij, with the second-order
 // eigenvalue terms (cross-cluster pairs) and the step size.
-__device__ __forceinline__ void oa_pair_correction(cx<float> *SR, int ld, const double *lam,
+__device__ __forceinline__ void oa_pair_correction(cx<float> *SR, int ld, const float2 *lam,
                                                    const float *lamf, const OaCluster &c,
                                                    float *corr, int i, int j, float &emax) {
     const cx<float> S = SR[(size_t)i * ld + j], R = SR[(size_t)j * ld + i];
@@ -140,8 +142,9 @@ __device__ __forceinline__ void oa_pair_correction(cx<float> *SR, int ld, const 
         Eij = mk<float>(0.5f * R.re, 0.5f * R.im);
         Eji = mk<float>(0.5f * R.re, -0.5f * R.im);
     } else {
-        // only the gap needs FP64 (a difference of nearly equal large numbers)
-        const float dl = (float)(lam[j] - lam[i]);
+        // only the gap needs the double-words (a difference of nearly equal
+        // large numbers)
+        const float dl = dw_sub_f(lam[j], lam[i]);
         const float br = S.re + lamf[j] * R.re, bi = S.im + lamf[j] * R.im;  // S_ij + l_j R_ij
         const float ar = S.re + lamf[i] * R.re, ai = S.im + lamf[i] * R.im;  // S_ij + l_i R_ij
         const float inv = 1.0f / dl;
@@ -158,13 +161,13 @@ __device__ __forceinline__ void oa_pair_correction(cx<float> *SR, int ld, const 
 
 // Diagonal of T (after the pair corrections, so the second-order terms are
 // in corr).  Ends with a barrier.
-static __device__ void oa_cluster_diagonal(const double *lam, const float *corr, int n,
-                                    const OaCluster &c) {
+static __device__ void oa_cluster_diagonal(const float2 *lam, const float *corr, int n,
+                                           const OaCluster &c) {
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         if (!oa_in_cluster(c.cstart, n, r)) continue;
         const int i = c.order[r];
-        const double lref = lam[c.order[c.cstart[r]]];
-        c.T[(size_t)r * c.ldt + r] = mk<float>((float)(lam[i] - lref) + corr[i], 0.f);
+        const float2 lref = lam[c.order[c.cstart[r]]];
+        c.T[(size_t)r * c.ldt + r] = mk<float>(dw_sub_f(lam[i], lref) + corr[i], 0.f);
     }
     __syncthreads();
 }
@@ -173,7 +176,7 @@ static __device__ void oa_cluster_diagonal(const double *lam, const float *corr,
 // the corrected eigenvector matrix X (nrows x n, row stride ldx), and sets
 // the clusters' eigenvalues; the other levels get l_i + corr_i.  Returns
 // this thread's share of the step size.  Ends with a barrier.
-static __device__ float oa_resolve_clusters(cx<float> *X, int ldx, int nrows, double *lam,
+static __device__ float oa_resolve_clusters(cx<float> *X, int ldx, int nrows, float2 *lam,
                                      const float *corr, int n, const OaCluster &c,
                                      float lscale) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -185,7 +188,7 @@ static __device__ float oa_resolve_clusters(cx<float> *X, int ldx, int nrows, do
         if (c.cstart[q0] != q0 || q0 + 1 >= n || c.cstart[q0 + 1] != q0) continue;
         int k = 2;
         while (q0 + k < n && c.cstart[q0 + k] == q0) ++k;
-        const double lref = lam[c.order[q0]];
+        const float2 lref = lam[c.order[q0]];
         cx<float> *T = c.T + (size_t)q0 * c.ldt + q0;
         const int ldt = c.ldt;
         for (int sweep = 0; sweep < 16; ++sweep) {
@@ -233,12 +236,13 @@ static __device__ float oa_resolve_clusters(cx<float> *X, int ldx, int nrows, do
             if (nrot == 0) break;
         }
         for (int p = lane; p < k; p += 32)
-            lam[c.order[q0 + p]] = lref + (double)T[(size_t)p * ldt + p].re;
+            lam[c.order[q0 + p]] = dw_add_f(lref, T[(size_t)p * ldt + p].re);
         __syncwarp();
     }
     __syncthreads();
     for (int r = threadIdx.x; r < n; r += blockDim.x)
-        if (!oa_in_cluster(c.cstart, n, r)) lam[c.order[r]] += (double)corr[c.order[r]];
+        if (!oa_in_cluster(c.cstart, n, r))
+            lam[c.order[r]] = dw_add_f(lam[c.order[r]], corr[c.order[r]]);
     __syncthreads();
     return emax;
 }

@@ -133,4 +133,132 @@ __device__ __forceinline__ cx<float> lm_plain(u64 s1, u64 s2) {
     return CONJ ? mk<float>(ax + by, bx - ay) : mk<float>(ax - by, ay + bx);
 }
 
+// ---- double-word scalars: a value hi + lo as a float2 (x = hi, y = lo),
+// normalised (|lo| <= half an ulp of hi) unless stated otherwise.  About
+// 2^-48 relative accuracy: eigenvalues and phase increments of the
+// mixed-precision paths are kept in this form so that those paths need no
+// FP64 arithmetic (FP64 runs at a small fraction of the FP32 rate here).
+
+#define MSP_TWOPI_HI 6.28318548202514648f      // fl32(2 pi)
+#define MSP_TWOPI_LO (-1.7484555314695172e-07f)  // 2 pi - MSP_TWOPI_HI
+
+// (h, l) <- (h + l) reduced modulo 2 pi, then renormalised (|l| <= half an
+// ulp of h).  k * MSP_TWOPI_HI is split exactly by an FMA and h - p is
+// exact (Sterbenz), so only the low-word sum rounds; the _rn intrinsics keep
+// the compiler from contracting the split.
+__device__ __forceinline__ void dw_reduce_2pi(float &h, float &l) {
+    const float k = rintf(h * 0.15915494309189535f);
+    const float p = __fmul_rn(k, MSP_TWOPI_HI);
+    const float e = fmaf(k, MSP_TWOPI_HI, -p);
+    const float t = __fsub_rn(h, p);
+    const float lo = (l - e) - k * MSP_TWOPI_LO;
+    const float s = __fadd_rn(t, lo);
+    const float bb = __fsub_rn(s, t);
+    l = __fadd_rn(__fsub_rn(t, __fsub_rn(s, bb)), __fsub_rn(lo, bb));
+    h = s;
+}
+
+// (h, l) += (h2, l2), the high sum split exactly (TwoSum).
+__device__ __forceinline__ void dw_add(float &h, float &l, float h2, float l2) {
+    const float s = __fadd_rn(h, h2);
+    const float bb = __fsub_rn(s, h);
+    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+    h = s;
+    l = l + l2 + err;
+}
+
+// a + b exactly as hi + lo (TwoSum, Knuth)
+__device__ __forceinline__ float2 dw_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+
+// a + b (double-word plus float), normalised
+__device__ __forceinline__ float2 dw_add_f(float2 a, float b) {
+    const float2 t = dw_two_sum(a.x, b);
+    return dw_two_sum(t.x, __fadd_rn(t.y, a.y));
+}
+
+// a - b as a double-word
+__device__ __forceinline__ float2 dw_sub(float2 a, float2 b) {
+    const float2 t = dw_two_sum(a.x, -b.x);
+    return dw_two_sum(t.x, __fadd_rn(t.y, __fsub_rn(a.y, b.y)));
+}
+
+// a - b rounded to FP32 (the high words' difference is exact when they are
+// within a factor of two of each other, and FP32-accurate otherwise)
+__device__ __forceinline__ float dw_sub_f(float2 a, float2 b) {
+    return __fadd_rn(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
+}
+
+// a < b for normalised double-words
+__device__ __forceinline__ bool dw_less(float2 a, float2 b) {
+    return a.x < b.x || (a.x == b.x && a.y < b.y);
+}
+
+__device__ __forceinline__ bool dw_equal(float2 a, float2 b) { return a.x == b.x && a.y == b.y; }
+
+__host__ __device__ __forceinline__ float2 dw_of(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+
+__device__ __forceinline__ double dw_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
+// Rayleigh quotient S / (1 + g) of a refinement step for double-words S
+// and g = G - 1 (|g| << 1: X^H X close to I), as S - S g + S g^2 / (1 + g)
+// with S.hi g.hi split exactly by an FMA and every smaller term summed in
+// FP32: ~2e-14 relative for |g| <= 3e-5, 3e-13 at |g| = 1e-3 (an FP32
+// quotient would lose |g| 2^-24 relative: 1e-12 of l at |g| ~ 1e-5).
+__device__ __forceinline__ float2 dw_rayleigh(float2 S, float2 g) {
+    const float p = __fmul_rn(S.x, g.x);
+    const float pe = fmaf(S.x, g.x, -p);
+    const float gs = g.x + g.y;
+    const float q2 = gs * gs / (1.0f + gs);
+    const float c = S.y - pe - S.x * g.y - S.y * g.x + S.x * q2;
+    const float2 t = dw_two_sum(S.x, -p);
+    return dw_two_sum(t.x, __fadd_rn(t.y, c));
+}
+
+// d * c reduced modulo 2 pi (double-words d, c): the phase step of a level
+// pair, d the level gap and c = 2 pi dt.
+__device__ __forceinline__ float2 dw_phase_mod2pi(float2 d, float2 c) {
+    float h = __fmul_rn(d.x, c.x);
+    float l = fmaf(d.x, c.y, fmaf(d.y, c.x, fmaf(d.x, c.x, -h)));
+    dw_reduce_2pi(h, l);
+    return make_float2(h, l);
+}
+
+// Warp sum of double-words (every lane gets the total).
+__device__ __forceinline__ float2 dw_warp_sum(float2 v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h = __shfl_xor_sync(0xffffffffu, v.x, o);
+        const float l = __shfl_xor_sync(0xffffffffu, v.y, o);
+        const float2 t = dw_two_sum(v.x, h);
+        v = dw_two_sum(t.x, __fadd_rn(t.y, __fadd_rn(v.y, l)));
+    }
+    return v;
+}
+
+// CTA sum of every thread's double-word v; red holds one float2 per warp.
+// All threads call it; the result is valid in every thread.  Begins and
+// ends with a barrier (red may be reused right after).
+__device__ __forceinline__ double dw_block_sum(float2 v, float2 *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    v = dw_warp_sum(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    float2 t = make_float2(0.f, 0.f);
+    for (int w = 0; w < nw; ++w) {
+        const float2 u = dw_two_sum(t.x, red[w].x);
+        t = dw_two_sum(u.x, __fadd_rn(u.y, __fadd_rn(t.y, red[w].y)));
+    }
+    __syncthreads();
+    return dw_to_double(t);
+}
+
 }  // namespace msp

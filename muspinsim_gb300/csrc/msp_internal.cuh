@@ -2,6 +2,7 @@
 #pragma once
 
 #include "msp_common.cuh"
+#include "msp_dw.cuh"
 
 namespace msp {
 
@@ -30,6 +31,11 @@ struct SnapArgs {
     int max_refine;  // MIXED refinement step cap
     const cx<double> *Hsys;
     const cx<double> *Z;
+    // MIXED (optional): Hsys and Z pre-split into double-words, one float4
+    // (re_hi, im_hi, re_lo, im_lo) per entry, same indexing; NULL: the
+    // kernels split the FP64 matrices themselves
+    const float4 *Hsys_dw;
+    const float4 *Z_dw;
     const double *field;
     const double *pol;
     const double *wscale;
@@ -43,8 +49,12 @@ struct SnapArgs {
     double gammas[MSP_MAX_SPINS];
     int fac_len;
     double tau;
-    // time grid (uniform grids: t_k = t0 + k dt)
+    // time grid (uniform grids: t_k = t0 + k dt); c_dt, c_t0 = 2 pi dt and
+    // 2 pi t0 as double-words (hi, lo) for the mixed path's phase records,
+    // and t0_zero = (t0 == 0)
     double t0, dt;
+    float2 c_dt, c_t0;
+    int t0_zero;
     // outputs
     void *pair_coef;     // num_snap * P of float2 / double2: (a_c, a_s)
     double *pair_omega;  // num_snap * P angular frequencies (FP64 path, arbitrary grids)
@@ -70,10 +80,18 @@ struct SnapArgs {
     const long long *seg_hoff;
 };
 
+// Sets c_dt, c_t0 and t0_zero from t0 and dt.
+inline void snap_time_constants(SnapArgs &a) {
+    a.c_dt = dw_of(6.283185307179586476925 * a.dt);
+    a.c_t0 = dw_of(6.283185307179586476925 * a.t0);
+    a.t0_zero = a.t0 == 0.0;
+}
+
 // Global snapshot index and system matrices of launch-local snapshot sn.
 struct SnapSource {
     int g;
     const cx<double> *Hsys, *Z;
+    const float4 *Hdw, *Zdw;
 };
 
 __device__ __forceinline__ SnapSource snap_source(const SnapArgs &a, int sn) {
@@ -81,6 +99,8 @@ __device__ __forceinline__ SnapSource snap_source(const SnapArgs &a, int sn) {
     r.g = sn;
     r.Hsys = a.Hsys;
     r.Z = a.Z;
+    r.Hdw = a.Hsys_dw;
+    r.Zdw = a.Z_dw;
     if (a.num_seg > 0) {
         int lo = 0, hi = a.num_seg - 1;
         while (lo < hi) {
@@ -94,6 +114,10 @@ __device__ __forceinline__ SnapSource snap_source(const SnapArgs &a, int sn) {
         const long long o = a.seg_hoff[lo];
         r.Hsys = a.Hsys + o;
         r.Z = a.Z + 3 * o;
+        if (a.Hsys_dw) {
+            r.Hdw = a.Hsys_dw + o;
+            r.Zdw = a.Z_dw + 3 * o;
+        }
     }
     return r;
 }
@@ -118,6 +142,10 @@ struct PhaseArgs {
 };
 
 size_t snap_smem_bytes(int n, int mode, int precision, int fac_len);
+// Hsys (nh entries) and Z (nz entries) split into double-words into dst
+// (nh + nz float4: Hsys first), for SnapArgs::Hsys_dw / Z_dw.
+cudaError_t launch_split_dw(const double *Hsys, size_t nh, const double *Z, size_t nz,
+                            float4 *dst, cudaStream_t st);
 // Two-stage MIXED snapshots (n <= 32): the warp-per-matrix FP32 Jacobi
 // (msp_jacobi_warp.cu) writes eigenvectors to SnapArgs::evec; the snapshot
 // kernels refine them.  Bytes of that scratch for num_snap snapshots (0 when

@@ -185,8 +185,11 @@ __global__ void __launch_bounds__(JW_WARPS * 32, 4) msp_jacobi_warp_kernel(SnapA
         const SnapSource src = snap_source(a, sn);
         const double bx = a.field[3 * (size_t)src.g], by = a.field[3 * (size_t)src.g + 1],
                      bz = a.field[3 * (size_t)src.g + 2];
-        // H = Hsys + b . Z (FP64) into the blocks of buffer 0, diagonal into
-        // dia[1] (free until step 0's producers write it)
+        const float bxf = (float)bx, byf = (float)by, bzf = (float)bz;
+        // H = Hsys + b . Z (FP32 from the double-word high parts when the
+        // caller pre-split the matrices, else FP64) into the blocks of
+        // buffer 0, diagonal into dia[1] (free until step 0's producers
+        // write it)
         float fro = 0.f;
         for (int e = lane; e < M * (M + 1) / 2; e += 32) {
             int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);  // e = i (i + 1) / 2 + j
@@ -196,10 +199,17 @@ __global__ void __launch_bounds__(JW_WARPS * 32, 4) msp_jacobi_warp_kernel(SnapA
             float hr = 0.f, hi = 0.f;
             if (i < n) {
                 const size_t o = (size_t)j * n + i;
-                const cx<double> hs = src.Hsys[o], z0 = src.Z[o], z1 = src.Z[nn + o],
-                                 z2 = src.Z[2 * (size_t)nn + o];
-                hr = (float)(hs.re + bx * z0.re + by * z1.re + bz * z2.re);
-                hi = (float)(hs.im + bx * z0.im + by * z1.im + bz * z2.im);
+                if (src.Hdw != nullptr) {
+                    const float4 hs = src.Hdw[o], z0 = src.Zdw[o], z1 = src.Zdw[nn + o],
+                                 z2 = src.Zdw[2 * (size_t)nn + o];
+                    hr = fmaf(bzf, z2.x, fmaf(byf, z1.x, fmaf(bxf, z0.x, hs.x)));
+                    hi = fmaf(bzf, z2.y, fmaf(byf, z1.y, fmaf(bxf, z0.y, hs.y)));
+                } else {
+                    const cx<double> hs = src.Hsys[o], z0 = src.Z[o], z1 = src.Z[nn + o],
+                                     z2 = src.Z[2 * (size_t)nn + o];
+                    hr = (float)(hs.re + bx * z0.re + by * z1.re + bz * z2.re);
+                    hi = (float)(hs.im + bx * z0.im + by * z1.im + bz * z2.im);
+                }
             }
             if (i == j) {
                 dbuf(1)[i] = hr;

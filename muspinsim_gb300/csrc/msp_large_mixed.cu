@@ -74,7 +74,8 @@ __host__ __device__ inline size_t lm_scratch_bytes(int n) { return lm_layout(n, 
 constexpr int LM_KT = 16;  // k depth of a GEMM slab
 
 struct LmVec {
-    double *lam, *sd, *rd;
+    float2 *lam, *sd;  // eigenvalues and S_ii as double-words (msp_dw.cuh)
+    float2 *gd;        // x_i^H x_i - 1 (double-word)
     int *rank, *order, *cstart;  // refinement clusters (msp_cluster.cuh)
     float *lamf, *corr, *rn, *cn, *yn;
     int *step;  // [0]: largest correction, [1]: largest |l_i|, [2]: amax (float bits)
@@ -109,10 +110,10 @@ __host__ __device__ inline size_t lm_smem_bytes(int n, int threads) {
 
 __device__ __forceinline__ LmVec lm_vec(char *smem, int n) {
     LmVec v;
-    v.lam = reinterpret_cast<double *>(smem);
+    v.lam = reinterpret_cast<float2 *>(smem);
     v.sd = v.lam + n;
-    v.rd = v.sd + n;
-    v.rank = reinterpret_cast<int *>(v.rd + n);
+    v.gd = v.sd + n;
+    v.rank = reinterpret_cast<int *>(v.gd + n);
     v.order = v.rank + n;
     v.cstart = v.order + n;
     v.lamf = reinterpret_cast<float *>(v.cstart + n);
@@ -313,7 +314,7 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
                 const u64 K = lm_anchor(bound(i, j));
                 const float4 r = lm_dw<true>(s1, c1, s2, c2, K);
                 if (i == j)
-                    v.sd[i] = (double)r.x + (double)r.z;
+                    v.sd[i] = make_float2(r.x, r.z);
                 else if (i < j)
                     s.SR[(size_t)i * n + j] = mk<float>(r.x + r.z, r.y + r.w);
             });
@@ -328,7 +329,7 @@ __device__ void lm_gemm(const LargeMixed &s, const cx<float> *__restrict__ X,
                 const u64 K = lm_anchor(bound(i, j));
                 const float4 r = lm_dw<true>(s1, c1, s2, c2, K);
                 if (i == j)
-                    v.rd[i] = (1.0 - (double)r.x) - (double)r.z;
+                    v.gd[i] = make_float2(r.x - 1.0f, r.z);  // r.x - 1 exact
                 else if (i < j)
                     s.SR[(size_t)j * n + i] = mk<float>(-(r.x + r.z), -(r.y + r.w));
             });
@@ -467,11 +468,11 @@ __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
     lm_gemm<LM_G>(s, X, X2, v, n);
     float lmax = 0.f;
     for (int i = tid; i < n; i += nt) {
-        const double l = v.sd[i] / (1.0 - v.rd[i]);
+        const float2 l = dw_rayleigh(v.sd[i], v.gd[i]);
         v.lam[i] = l;
-        v.lamf[i] = (float)l;
+        v.lamf[i] = l.x;
         v.corr[i] = 0.f;
-        lmax = fmaxf(lmax, fabsf((float)l));
+        lmax = fmaxf(lmax, fabsf(l.x));
     }
     atomicMax(&v.step[1], __float_as_int(lmax));  // non-negative: int order = float order
     __syncthreads();
@@ -492,7 +493,8 @@ __device__ float lm_refine(const LargeMixed &s, const cx<float> *__restrict__ X,
     }
     __syncthreads();
     oa_cluster_diagonal(v.lam, v.corr, n, cl);
-    for (int j = tid; j < n; j += nt) SR[(size_t)j * n + j] = mk<float>((float)(0.5 * v.rd[j]), 0.f);
+    for (int j = tid; j < n; j += nt)  // E_jj = R_jj / 2
+        SR[(size_t)j * n + j] = mk<float>(-0.5f * (v.gd[j].x + v.gd[j].y), 0.f);
     __syncthreads();
     lm_gemm<LM_XE>(s, X, X2, v, n);
     emax = fmaxf(emax, oa_resolve_clusters(X2, n, n, v.lam, v.corr, n, cl,
@@ -679,6 +681,20 @@ __device__ void lm_tridiag(const LargeMixed &s, const LmVec &vv, char *smem, int
 // correction drops below 2e-4 (at most four; one step leaves an error of
 // order E^2); M = U^H (sigma_p (x) 1_d) U in FP32; pair records with FP64
 // frequencies from the refined eigenvalues.
+// Pair record of the mixed kernel: FP32 coefficient and, from the level gap
+// d (double-word), the double-word phases on a uniform grid or the FP64
+// frequency otherwise.
+__device__ __forceinline__ void lm_store_pair(const SnapArgs &a, size_t o, float cA, float2 d) {
+    reinterpret_cast<float2 *>(a.pair_coef)[o] = make_float2(cA, 0.f);
+    if (a.pair_phase) {
+        const float2 psi = dw_phase_mod2pi(d, a.c_dt);
+        const float2 ph0 = a.t0_zero ? make_float2(0.f, 0.f) : dw_phase_mod2pi(d, a.c_t0);
+        a.pair_phase[o] = make_float4(psi.x, psi.y, ph0.x, ph0.y);
+    } else {
+        a.pair_omega[o] = 6.283185307179586476925 * dw_to_double(d);
+    }
+}
+
 __global__ void __maxnreg__(96) msp_large_fast_mixed_kernel(SnapArgs a, char *scratch) {
     extern __shared__ __align__(16) char smem[];
     const int n = a.n, d = n / 2, P = n * (n - 1) / 2;
@@ -753,6 +769,7 @@ __global__ void __maxnreg__(96) msp_large_fast_mixed_kernel(SnapArgs a, char *sc
         }
         __syncthreads();
         const double scale = 0.5 * a.wscale[g] / (double)d;
+        const float scale_f = (float)scale;
         double diag = 0.0;
         // G = X^H W (tiles with an entry j >= k only); A_jk = |G_jk|^2
         lm_tiles<LM_PLAIN_C, true>(
@@ -762,12 +779,12 @@ __global__ void __maxnreg__(96) msp_large_fast_mixed_kernel(SnapArgs a, char *sc
             [&](int j, int k, u64 s1, u64, u64 s2, u64) {
                 if (j < k) return;
                 const cx<float> G = lm_plain<true>(s1, s2);
-                const double Am = (double)(G.re * G.re + G.im * G.im);
+                const float Am = G.re * G.re + G.im * G.im;
                 if (j == k)
-                    diag += Am;
+                    diag += (double)Am;
                 else
-                    large_store_pair(a, (size_t)sn * P + (size_t)j * (j - 1) / 2 + k, scale * Am,
-                                     6.283185307179586476925 * (v.lam[j] - v.lam[k]));
+                    lm_store_pair(a, (size_t)sn * P + (size_t)j * (j - 1) / 2 + k, scale_f * Am,
+                                  dw_sub(v.lam[j], v.lam[k]));
             });
         diag = block_sum(diag, red);
         if (tid == 0) {

@@ -376,6 +376,7 @@ static int plan_enqueue(msp_multi_plan *p, const msp_multi_io *io, cudaStream_t 
             sa.wscale = io->wscale;
             sa.t0 = p->t0;
             sa.dt = p->dt;
+            snap_time_constants(sa);
             sa.pair_coef = ws + b.off_coef;
             sa.pair_omega = records ? NULL : reinterpret_cast<double *>(ws + b.off_phase);
             sa.pair_phase = records ? reinterpret_cast<float4 *>(ws + b.off_phase) : NULL;

@@ -20,6 +20,7 @@
 // value, which is the periodic resync.
 #include <stdlib.h>
 
+#include "msp_dw.cuh"
 #include "msp_internal.cuh"
 
 namespace msp {
@@ -198,33 +199,7 @@ __global__ void __launch_bounds__(128) msp_phase_uniform_kernel(PhaseArgs a) {
 //    (fma.rn.f32x2): two accumulators of adjacent time columns per
 //    instruction, half the issue slots of scalar FMAs.
 
-#define MSP_TWOPI_HI 6.28318548202514648f      // fl32(2 pi)
-#define MSP_TWOPI_LO (-1.7484555314695172e-07f)  // 2 pi - MSP_TWOPI_HI
-
-// (h, l) <- (h + l) reduced modulo 2 pi, then renormalised (|l| <= half an
-// ulp of h).  k * MSP_TWOPI_HI is split exactly by an FMA and h - p is
-// exact (Sterbenz), so only the low-word sum rounds; the _rn intrinsics keep
-// the compiler from contracting the split.
-__device__ __forceinline__ void dw_reduce_2pi(float &h, float &l) {
-    const float k = rintf(h * 0.15915494309189535f);
-    const float p = __fmul_rn(k, MSP_TWOPI_HI);
-    const float e = fmaf(k, MSP_TWOPI_HI, -p);
-    const float t = __fsub_rn(h, p);
-    const float lo = (l - e) - k * MSP_TWOPI_LO;
-    const float s = __fadd_rn(t, lo);
-    const float bb = __fsub_rn(s, t);
-    l = __fadd_rn(__fsub_rn(t, __fsub_rn(s, bb)), __fsub_rn(lo, bb));
-    h = s;
-}
-
-// (h, l) += (h2, l2), the high sum split exactly (TwoSum).
-__device__ __forceinline__ void dw_add(float &h, float &l, float h2, float l2) {
-    const float s = __fadd_rn(h, h2);
-    const float bb = __fsub_rn(s, h);
-    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
-    h = s;
-    l = l + l2 + err;
-}
+// MSP_TWOPI_HI / _LO, dw_reduce_2pi and dw_add: msp_dw.cuh.
 
 // e^{i (h + l)} for |l| <~ 1e-3: sincosf(h) turned by l, second order in l.
 __device__ __forceinline__ cx<float> dw_expi(float h, float l) {
@@ -516,19 +491,21 @@ struct TcTables {
         xhi[16][MSP_TC_PS + 1];
 };
 
+// rec / cf: the stage's first pair record and coefficient (global or
+// shared memory); np <= MSP_TC_PS of them are valid.
 template <int N>
-__device__ __forceinline__ void tc_build_tables(const PhaseArgs &a, TcTables<N> &tb, int pb,
-                                                int np, float tile_steps, int tid) {
+__device__ __forceinline__ void tc_build_tables(const float4 *rec_p, const float2 *cf_p,
+                                                TcTables<N> &tb, int np, float tile_steps,
+                                                int tid) {
     constexpr int PS = MSP_TC_PS, YH = N / 8;
     if (tid >= 5 * PS) return;
-    const float2 *coef = reinterpret_cast<const float2 *>(a.pair_coef);
     const int c = tid / PS, i = tid - c * PS;
     const int len = c == 1 ? YH : 8;
     cx<float> *dst = c == 0 ? &tb.ylo[0][i] : c == 1 ? &tb.yhi[0][i] : c == 2 ? &tb.xlo[0][i]
                                                 : c == 3 ? &tb.xhi[0][i] : &tb.xhi[8][i];
     cx<float> p = mk<float>(c >= 3 ? 0.f : 1.f, 0.f), base = mk<float>(1.f, 0.f);
     if (i < np) {
-        const float4 rec = a.pair_phase[pb + i];
+        const float4 rec = rec_p[i];
         const float sc = c == 0 ? 1.f : c == 1 ? 8.f : c == 2 ? (float)N : 8.f * N;
         float h = rec.x * sc, l = rec.y * sc;  // exact power-of-two scaling
         dw_reduce_2pi(h, l);
@@ -543,7 +520,7 @@ __device__ __forceinline__ void tc_build_tables(const PhaseArgs &a, TcTables<N> 
                 dw_add(th, tl, bh, bl);
                 dw_reduce_2pi(th, tl);
             }
-            const float2 cf = coef[pb + i];
+            const float2 cf = cf_p[i];
             p = mk<float>(cf.x, -cf.y);
             if (th != 0.f || tl != 0.f) p = cmul(p, dw_expi(th, tl));
         }
@@ -587,8 +564,9 @@ __global__ void __launch_bounds__(MSP_TC_THREADS) msp_phase_tc_kernel(PhaseArgs 
             smem_u32(&s_tmem)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    tc_build_tables<N>(a, tabs[0], pbeg, (pend - pbeg) < PS ? (pend - pbeg) : PS, tile_steps,
-                       tid);
+    const float2 *coef = reinterpret_cast<const float2 *>(a.pair_coef);
+    tc_build_tables<N>(a.pair_phase + pbeg, coef + pbeg, tabs[0],
+                       (pend - pbeg) < PS ? (pend - pbeg) : PS, tile_steps, tid);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
@@ -661,7 +639,8 @@ __global__ void __launch_bounds__(MSP_TC_THREADS) msp_phase_tc_kernel(PhaseArgs 
         // tables of the next stage (the buffer last read by stage s - 1)
         if (s + 1 < nstage) {
             const int pb1 = pbeg + (s + 1) * PS;
-            tc_build_tables<N>(a, tabs[buf ^ 1], pb1, (pend - pb1) < PS ? (pend - pb1) : PS,
+            tc_build_tables<N>(a.pair_phase + pb1, coef + pb1, tabs[buf ^ 1],
+                               (pend - pb1) < PS ? (pend - pb1) : PS,
                                tile_steps, tid);
         }
         // operands written by the generic proxy, read by the tensor core;
@@ -746,10 +725,61 @@ __global__ void __launch_bounds__(MSP_TC_THREADS) msp_phase_tc_kernel(PhaseArgs 
 // quickly; the tile's partials are then NaN and the tensor memory is
 // released only after the last committed MMAs have completed (waited for,
 // bounded).
+//
+// The A operands live in tensor memory rather than shared memory: each
+// producer thread stores its row's 16 K-columns of A hi and A lo with
+// tcgen05.st (row k1 = TMEM lane k1, K index = column, one tf32 per
+// column), and the MMAs read A from there.  Only B (N rows) is staged in
+// shared memory (a stage moves ~20 KB through it instead of ~100 KB), which
+// leaves room for the work item's pair records (at most MSP_F32_ITEM_PAIRS
+// x 24 B): the table warps copy them into shared memory once, so a stage's
+// tables start without a global-memory round trip -- the table warps'
+// per-stage latency was what paced the pipeline (the MMAs of a stage take
+// ~300 cycles, the producers ~900, the tables ~2000 with the loads).
+// Tensor memory per CTA (256 columns): accumulator blocks at columns 0 and
+// 32, A buffer b (hi, lo) at columns 64 + 64 b and 96 + 64 b.  The dynamic
+// shared memory is padded so that two CTAs share an SM (2 x 256 = 512
+// columns): a third would wait in tcgen05.alloc.
 #define MSP_TCW_PRODUCERS 256
 #define MSP_TCW_TABLE_THREADS 96
 #define MSP_TCW_THREADS (MSP_TCW_PRODUCERS + MSP_TCW_TABLE_THREADS + 32)
 #define MSP_TCW_TABLES 3
+#define MSP_TCW_TMEM_COLS 256
+#define MSP_TCW_A_COL 64u
+
+template <int N>
+struct TcwLayout {
+    static constexpr int CB = (N / 8) * 128;  // bytes of one B K-chunk
+    static constexpr int B_BYTES = 8 * CB;    // 8 K-chunks per stage (K = 32)
+    static constexpr int STAGE = 2 * B_BYTES; // hi and lo of B
+    static constexpr int REC = 40 * 1024;     // the item's pair records (24 B each)
+    static constexpr int SMEM = 80 * 1024;    // padded: two CTAs per SM
+    static_assert(2 * STAGE <= REC && 128 * (N + 1) * 4 <= REC &&
+                      REC + 24 * MSP_F32_ITEM_PAIRS <= SMEM,
+                  "TcwLayout");
+};
+
+// Stores r[0..16) into 16 consecutive columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_store16(uint32_t taddr, const uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+        "%13,%14,%15,%16};" ::"r"(taddr),
+        "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+        "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+        "r"(r[15])
+        : "memory");
+}
+
+// One MMA with A read from tensor memory (address a_tmem), B from shared
+// memory (descriptor bd).
+__device__ __forceinline__ void tc_mma_ta(uint32_t tmem, uint32_t a_tmem, uint64_t bd,
+                                          uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;}" ::"r"(tmem),
+        "r"(a_tmem), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
+}
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
@@ -775,7 +805,7 @@ __device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity,
 
 template <int N>
 __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArgs a) {
-    typedef TcLayout<N> L;
+    typedef TcwLayout<N> L;
     constexpr int PS = MSP_TC_PS, NH = N / 2;
     extern __shared__ __align__(1024) char tsm[];
     __shared__ __align__(16) TcTables<N> tabs[MSP_TCW_TABLES];
@@ -810,8 +840,9 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
     const long long tile_base = (long long)blockIdx.y * (128 * N);
     const float tile_steps = (float)tile_base;  // exact: < 2^24
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(
-            smem_u32(&s_tmem)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&s_tmem)),
+                     "n"(MSP_TCW_TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -845,27 +876,33 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
 #pragma unroll
                 for (int j = 0; j < NH; ++j) acc[j] += __uint_as_float(r[j]);
             }
-            char *A_hi = tsm + b * L::STAGE;
-            char *A_lo = A_hi + L::A_BYTES;
-            char *B_hi = A_lo + L::A_BYTES;
+            char *B_hi = tsm + b * L::STAGE;
             char *B_lo = B_hi + L::B_BYTES;
             const TcTables<N> &tb = tabs[t];
             {
+                // A row k1, K-columns 16 h0 .. 16 h0 + 15 (pairs 8 h0 .. 8 h0 + 7)
                 const int k1 = tid & 127, h0 = tid >> 7;
-                const int off = (k1 >> 3) * 128 + (k1 & 7) * 16;
-#pragma unroll 2
-                for (int gi = 0; gi < PS / 4; ++gi) {
-                    const int g = h0 + 2 * gi;
+                uint32_t rh[16], rl[16];
+#pragma unroll
+                for (int gi = 0; gi < 4; ++gi) {
+                    const int g = 4 * h0 + gi;
                     const cx<float> x0 = cmul(tb.xhi[k1 >> 3][2 * g], tb.xlo[k1 & 7][2 * g]);
                     const cx<float> x1 =
                         cmul(tb.xhi[k1 >> 3][2 * g + 1], tb.xlo[k1 & 7][2 * g + 1]);
-                    const float4 v = make_float4(x0.re, -x0.im, x1.re, -x1.im);
-                    const float4 hh =
-                        make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
-                    const float4 lo = make_float4(v.x - hh.x, v.y - hh.y, v.z - hh.z, v.w - hh.w);
-                    *reinterpret_cast<float4 *>(A_hi + g * L::CA + off) = hh;
-                    *reinterpret_cast<float4 *>(A_lo + g * L::CA + off) = lo;
+                    const float v[4] = {x0.re, -x0.im, x1.re, -x1.im};
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const float hh = tf32_rn(v[q]);
+                        // the tensor core reads lo as tf32 (truncated): |lo| <= 2^-11 |x|
+                        rh[4 * gi + q] = __float_as_uint(hh);
+                        rl[4 * gi + q] = __float_as_uint(v[q] - hh);
+                    }
                 }
+                const uint32_t ta = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + MSP_TCW_A_COL +
+                                    64u * b + 16u * h0;
+                tmem_store16(ta, rh);
+                tmem_store16(ta + 32u, rl);
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             }
             for (int e = tid; e < N * (PS / 2); e += MSP_TCW_PRODUCERS) {
                 const int k0 = e % N, g = e / N;
@@ -880,8 +917,8 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
                 *reinterpret_cast<float4 *>(B_lo + off) = lo;
             }
             mbar_arrive(smem_u32(&tab_empty[t]));
-            // operands written by the generic proxy, read by the tensor core;
-            // this thread's tensor-memory reads ordered before the next MMAs
+            // B written by the generic proxy, read by the tensor core; this
+            // thread's tensor-memory loads and stores ordered before the MMAs
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;");
             mbar_arrive(smem_u32(&op_full[b]));
@@ -899,6 +936,18 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
     } else if (tid < MSP_TCW_PRODUCERS + MSP_TCW_TABLE_THREADS) {
         // ------------------------------------------------------------ tables
         const int tt = tid - MSP_TCW_PRODUCERS;
+        // the item's pair records, once, into shared memory: a stage's
+        // tables then start without a global-memory round trip
+        float4 *rph = reinterpret_cast<float4 *>(tsm + L::REC);
+        float2 *rcf = reinterpret_cast<float2 *>(tsm + L::REC + 16 * MSP_F32_ITEM_PAIRS);
+        {
+            const float2 *coef = reinterpret_cast<const float2 *>(a.pair_coef);
+            for (int e = tt; e < pend - pbeg; e += MSP_TCW_TABLE_THREADS) {
+                rph[e] = a.pair_phase[pbeg + e];
+                rcf[e] = coef[pbeg + e];
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(MSP_TCW_TABLE_THREADS) : "memory");
+        }
         for (int s = 0; s < nstage && !s_fail; ++s) {
             const int t = s % MSP_TCW_TABLES;
             if (s >= MSP_TCW_TABLES &&
@@ -906,8 +955,8 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
                                    &s_fail))
                 break;
             const int pb = pbeg + s * PS;
-            tc_build_tables<N>(a, tabs[t], pb, (pend - pb) < PS ? (pend - pb) : PS, tile_steps,
-                               tt);
+            tc_build_tables<N>(rph + (pb - pbeg), rcf + (pb - pbeg), tabs[t],
+                               (pend - pb) < PS ? (pend - pb) : PS, tile_steps, tt);
             mbar_arrive(smem_u32(&tab_full[t]));
         }
     } else if (lane == 0) {
@@ -919,19 +968,17 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
             const int b = s & 1;
             if (!mbar_wait_or_fail(smem_u32(&op_full[b]), (s >> 1) & 1, &s_fail)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            char *A_hi = tsm + b * L::STAGE;
-            const uint32_t ah = smem_u32(A_hi), al = ah + L::A_BYTES;
-            const uint32_t bh = al + L::A_BYTES, bl = bh + L::B_BYTES;
+            const uint32_t bh = smem_u32(tsm + b * L::STAGE), bl = bh + L::B_BYTES;
+            const uint32_t ah = tmem + MSP_TCW_A_COL + 64u * b, al = ah + 32u;
             const uint32_t d = tmem + 32u * b;
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks) {
-                const uint32_t ao = ks * 2 * L::CA, bo = ks * 2 * L::CB;
-                const uint64_t dah = tc_desc(ah + ao, L::CA, 128), dal = tc_desc(al + ao, L::CA, 128);
+                const uint32_t bo = ks * 2 * L::CB;
                 const uint64_t dbh = tc_desc(bh + bo, L::CB, 128), dbl = tc_desc(bl + bo, L::CB, 128);
                 // the small products first, the block restarts at each stage
-                tc_mma(d, dal, dbh, idesc, ks > 0 ? 1u : 0u);
-                tc_mma(d, dah, dbl, idesc, 1u);
-                tc_mma(d, dah, dbh, idesc, 1u);
+                tc_mma_ta(d, al + 8u * ks, dbh, idesc, ks > 0 ? 1u : 0u);
+                tc_mma_ta(d, ah + 8u * ks, dbl, idesc, 1u);
+                tc_mma_ta(d, ah + 8u * ks, dbh, idesc, 1u);
             }
             asm volatile(
                 "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -973,7 +1020,8 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "n"(MSP_TCW_TMEM_COLS));
 }
 
 // Arbitrary time grids: one thread per sample, every pair's phase reduced in
@@ -1066,9 +1114,10 @@ __global__ void msp_schedule_kernel(const int *__restrict__ slot, int S, int num
 // in a fixed order (deterministic); heterogeneous batches map slots to
 // output rows (slot_row) and add to the row (accumulate) when a system's
 // snapshots are split over several launches.  A block covers 32 times of one slot:
-// warp w sums items w, w + 8, w + 16, ... (several loads in flight per
-// thread), then the 8 warp sums are added in warp order.
-#define MSP_REDUCE_WARPS 8
+// warp w sums items w, w + 32, w + 64, ... (eight loads in flight per
+// thread: a slot's partials are tens of MB that only many outstanding
+// loads stream at HBM rate), then the 32 warp sums are added in warp order.
+#define MSP_REDUCE_WARPS 32
 __global__ void __launch_bounds__(32 * MSP_REDUCE_WARPS)
     msp_reduce_kernel(PhaseArgs a, const double *__restrict__ snap_const,
                       double *__restrict__ out, int T) {
@@ -1088,12 +1137,12 @@ __global__ void __launch_bounds__(32 * MSP_REDUCE_WARPS)
         const int i0 = a.item_first[sl], i1 = a.item_first[sl + 1];
         if (a.partial_f32) {
             const float *p = a.partial_f32 + t;
-#pragma unroll 4
+#pragma unroll 8
             for (int it = i0 + warp; it < i1; it += MSP_REDUCE_WARPS)
                 v += (double)p[(size_t)it * T];
         } else {
             const double *p = a.partial + t;
-#pragma unroll 4
+#pragma unroll 8
             for (int it = i0 + warp; it < i1; it += MSP_REDUCE_WARPS) v += p[(size_t)it * T];
         }
     }
@@ -1130,14 +1179,15 @@ static bool phase_tc_warp_specialised() {
 
 template <int N>
 static cudaError_t launch_tc(const PhaseArgs &a, int max_items, cudaStream_t st) {
-    const int smem = TcLayout<N>::SMEM;
     const dim3 grid(max_items, (a.num_times + 128 * N - 1) / (128 * N));
     if (phase_tc_warp_specialised()) {
+        const int smem = TcwLayout<N>::SMEM;
         cudaError_t e = cudaFuncSetAttribute(msp_phase_tcw_kernel<N>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         msp_phase_tcw_kernel<N><<<grid, MSP_TCW_THREADS, smem, st>>>(a);
     } else {
+        const int smem = TcLayout<N>::SMEM;
         cudaError_t e = cudaFuncSetAttribute(msp_phase_tc_kernel<N>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;

@@ -31,8 +31,8 @@ static_assert(sizeof(JRot<float>) == 16 && sizeof(JRot<double>) == 32, "JRot lay
 struct SnapLayout {
     size_t H, U, rot, dia, red, tab, diag;     // Jacobi work
     size_t lam, acc, rank;                     // eigenvalues, reductions, sort
-    size_t Hh, Hl, Yl, SR, sd, corr, rd, lamf, rk, ord, cst, scal, rn, cn, yn;  // refinement (MIXED)
-    size_t fac, B2;                            // general path
+    size_t Hh, Hl, Yl, SR, corr, rd, lamf, rk, ord, cst, scal, rn, cn, yn;  // refinement (MIXED)
+    size_t fac, facf, B2;                      // general path
     size_t total;
 };
 
@@ -64,14 +64,13 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
     L.lam = lay_take(off, m * 8);
     L.acc = lay_take(off, 2 * 8);
     L.rank = lay_take(off, m * 4);
-    L.Hh = L.Hl = L.Yl = L.SR = L.sd = L.corr = L.rd = L.lamf = 0;
+    L.Hh = L.Hl = L.Yl = L.SR = L.corr = L.rd = L.lamf = 0;
     L.rk = L.ord = L.cst = L.scal = L.rn = L.cn = L.yn = 0;
     if (refine) {
         L.Hh = lay_take(off, mm * 8);
         L.Hl = lay_take(off, mm * 8);
         L.Yl = lay_take(off, mm * 8);
         L.SR = lay_take(off, mm * 8);
-        L.sd = lay_take(off, m * 8);
         L.corr = lay_take(off, m * 4);
         L.rd = lay_take(off, m * 8);
         L.lamf = lay_take(off, m * 4);
@@ -83,9 +82,10 @@ __host__ __device__ inline SnapLayout snap_layout(int n, int esize, bool refine,
         L.cn = lay_take(off, m * 4);
         L.yn = lay_take(off, m * 4);
     }
-    L.fac = L.B2 = 0;
+    L.fac = L.facf = L.B2 = 0;
     if (rho) {
         L.fac = lay_take(off, (size_t)fac_len * 16);
+        if (refine) L.facf = lay_take(off, (size_t)fac_len * 8);
         // MIXED: the second basis buffer reuses Hh (free after refinement)
         L.B2 = refine ? L.Hh : lay_take(off, mm * 2 * esize);
     }
@@ -111,14 +111,16 @@ size_t snap_smem_bytes(int n, int mode, int precision, int fac_len) {
 template <typename T>
 struct SnapSmem {
     JacobiWork<T> w;
-    double *lam, *acc;
+    double *lam, *acc;  // FP64 path: eigenvalues
+    float2 *lw;         // MIXED: eigenvalues as double-words (msp_dw.cuh), over lam
     int *rank;
     cx<float> *Hh, *Hl, *Yl, *SR;
-    double *sd, *rd;
+    float2 *gd;         // MIXED: x_i^H x_i - 1 of the refinement step (double-word)
     float *corr, *lamf;
     int *rk, *ord, *cst, *scal;  // refinement clusters
     float *rn, *cn, *yn;         // norms: rows of H, columns of X and of Y
     cx<double> *fac;
+    cx<float> *facf;    // MIXED: FP32 copy of fac
     cx<T> *B2;
 };
 
@@ -135,15 +137,15 @@ __device__ __forceinline__ SnapSmem<T> snap_carve(char *base, int n, bool rho, i
     s.w.tab = reinterpret_cast<uint2 *>(base + L.tab);
     s.w.diag = reinterpret_cast<T *>(base + L.diag);
     s.lam = reinterpret_cast<double *>(base + L.lam);
+    s.lw = REFINE ? reinterpret_cast<float2 *>(base + L.lam) : nullptr;
     s.acc = reinterpret_cast<double *>(base + L.acc);
     s.rank = reinterpret_cast<int *>(base + L.rank);
     s.Hh = REFINE ? reinterpret_cast<cx<float> *>(base + L.Hh) : nullptr;
     s.Hl = REFINE ? reinterpret_cast<cx<float> *>(base + L.Hl) : nullptr;
     s.Yl = REFINE ? reinterpret_cast<cx<float> *>(base + L.Yl) : nullptr;
     s.SR = REFINE ? reinterpret_cast<cx<float> *>(base + L.SR) : nullptr;
-    s.sd = REFINE ? reinterpret_cast<double *>(base + L.sd) : nullptr;
     s.corr = REFINE ? reinterpret_cast<float *>(base + L.corr) : nullptr;
-    s.rd = REFINE ? reinterpret_cast<double *>(base + L.rd) : nullptr;
+    s.gd = REFINE ? reinterpret_cast<float2 *>(base + L.rd) : nullptr;
     s.lamf = REFINE ? reinterpret_cast<float *>(base + L.lamf) : nullptr;
     s.rk = REFINE ? reinterpret_cast<int *>(base + L.rk) : nullptr;
     s.ord = REFINE ? reinterpret_cast<int *>(base + L.ord) : nullptr;
@@ -153,6 +155,7 @@ __device__ __forceinline__ SnapSmem<T> snap_carve(char *base, int n, bool rho, i
     s.cn = REFINE ? reinterpret_cast<float *>(base + L.cn) : nullptr;
     s.yn = REFINE ? reinterpret_cast<float *>(base + L.yn) : nullptr;
     s.fac = rho ? reinterpret_cast<cx<double> *>(base + L.fac) : nullptr;
+    s.facf = rho && REFINE ? reinterpret_cast<cx<float> *>(base + L.facf) : nullptr;
     s.B2 = rho ? reinterpret_cast<cx<T> *>(base + L.B2) : nullptr;
     return s;
 }
@@ -185,6 +188,20 @@ __device__ __forceinline__ void store_frequency(const SnapArgs &a, size_t o, dou
     }
 }
 
+// Frequency record of pair o on the mixed path from its level gap d
+// (double-word): the phases d (2 pi dt) and d (2 pi t0) reduced modulo 2 pi,
+// or the FP64 angular frequency for arbitrary grids.  No FP64 arithmetic on
+// a uniform grid.
+__device__ __forceinline__ void store_frequency_dw(const SnapArgs &a, size_t o, float2 d) {
+    if (a.pair_phase) {
+        const float2 psi = dw_phase_mod2pi(d, a.c_dt);
+        const float2 ph0 = a.t0_zero ? make_float2(0.f, 0.f) : dw_phase_mod2pi(d, a.c_t0);
+        a.pair_phase[o] = make_float4(psi.x, psi.y, ph0.x, ph0.y);
+    } else {
+        a.pair_omega[o] = 6.283185307179586476925 * dw_to_double(d);
+    }
+}
+
 // Row norms of H's hi part (bounds of the refinement's anchored sums).
 template <typename T>
 __device__ void hamiltonian_row_norms(SnapSmem<T> &s, int n, int m) {
@@ -200,28 +217,97 @@ __device__ void hamiltonian_row_norms(SnapSmem<T> &s, int n, int m) {
     __syncthreads();
 }
 
-// H = Hsys + b . Z (FP64) into the Jacobi buffer (precision T, padded to m);
-// in MIXED mode also its exact split H = Hh + Hl into two FP32 matrices.
+// (s, c) += b z for a double-word b and z = zh + zl: the product's high
+// part summed with its rounding error (TwoSum) and every low-order term
+// into c.
+__device__ __forceinline__ void dw_acc_prod(float &s, float &c, float2 b, float zh, float zl) {
+    const float p = __fmul_rn(b.x, zh);
+    const float e = fmaf(b.x, zh, -p);
+    const float t = __fadd_rn(s, p);
+    const float bb = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, __fadd_rn(e, fmaf(b.x, zl, b.y * zh))));
+}
+
+// v[0..3) in precision T; FP32: converted by lanes 0..2 and shared across
+// the warp (one FP64 conversion per warp instead of one per thread).
+template <typename T>
+__device__ __forceinline__ void load_vec3(const double *v, T &x, T &y, T &z) {
+    if constexpr (sizeof(T) == 8) {
+        x = v[0];
+        y = v[1];
+        z = v[2];
+    } else {
+        const int lane = threadIdx.x & 31;
+        const float f = lane < 3 ? (float)v[lane] : 0.f;
+        x = __shfl_sync(0xffffffffu, f, 0);
+        y = __shfl_sync(0xffffffffu, f, 1);
+        z = __shfl_sync(0xffffffffu, f, 2);
+    }
+}
+
+// b[0..3) as double-words, computed by lanes 0..2 of the warp and shared.
+__device__ __forceinline__ void field_dw(const double *b, float2 &bx, float2 &by, float2 &bz) {
+    const int lane = threadIdx.x & 31;
+    const float2 v = lane < 3 ? dw_of(b[lane]) : make_float2(0.f, 0.f);
+    bx = make_float2(__shfl_sync(0xffffffffu, v.x, 0), __shfl_sync(0xffffffffu, v.y, 0));
+    by = make_float2(__shfl_sync(0xffffffffu, v.x, 1), __shfl_sync(0xffffffffu, v.y, 1));
+    bz = make_float2(__shfl_sync(0xffffffffu, v.x, 2), __shfl_sync(0xffffffffu, v.y, 2));
+}
+
+// H = Hsys + b . Z into the Jacobi buffer (precision T, padded to m); in
+// MIXED mode also its split H = Hh + Hl into two FP32 matrices.  MIXED
+// with Hdw / Zdw (Hsys and Z pre-split into double-words, (re_hi, im_hi,
+// re_lo, im_lo) per entry) assembles in double-word FP32 (~2^-47 relative),
+// otherwise in FP64 (split exactly).  blockDim.x is a multiple of 32.
 template <typename T, bool REFINE, bool PRE = false>
-__device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z,
-                                 const double *b, int n, int m, SnapSmem<T> &s) {
+__device__ void load_hamiltonian(const cx<double> *Hsys, const cx<double> *Z, const float4 *Hdw,
+                                 const float4 *Zdw, const double *b, int n, int m,
+                                 SnapSmem<T> &s) {
     const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1, ldh = jacobi_ldh(m);
-    const double bx = b[0], by = b[1], bz = b[2];
     const size_t nn = (size_t)n * n;
-    for (int e = tid; e < m * m; e += nt) {
-        const int i = FastDiv(m).div(e), j = e - i * m;
-        cx<double> h = mk<double>(0.0, 0.0);
-        if (i < n && j < n) {
-            const size_t o = (size_t)i * n + j;
-            const cx<double> hs = Hsys[o], z0 = Z[o], z1 = Z[nn + o], z2 = Z[2 * nn + o];
-            h.re = hs.re + bx * z0.re + by * z1.re + bz * z2.re;
-            h.im = hs.im + bx * z0.im + by * z1.im + bz * z2.im;
+    if (REFINE && Hdw != nullptr) {
+        float2 bx, by, bz;
+        field_dw(b, bx, by, bz);
+        for (int e = tid; e < m * m; e += nt) {
+            const int i = FastDiv(m).div(e), j = e - i * m;
+            float2 hr = make_float2(0.f, 0.f), hi = hr;
+            if (i < n && j < n) {
+                const size_t o = (size_t)i * n + j;
+                const float4 hs = Hdw[o], z0 = Zdw[o], z1 = Zdw[nn + o], z2 = Zdw[2 * nn + o];
+                float sr = hs.x, cr = hs.z, si = hs.y, ci = hs.w;
+                dw_acc_prod(sr, cr, bx, z0.x, z0.z);
+                dw_acc_prod(si, ci, bx, z0.y, z0.w);
+                dw_acc_prod(sr, cr, by, z1.x, z1.z);
+                dw_acc_prod(si, ci, by, z1.y, z1.w);
+                dw_acc_prod(sr, cr, bz, z2.x, z2.z);
+                dw_acc_prod(si, ci, bz, z2.y, z2.w);
+                hr = dw_two_sum(sr, cr);
+                hi = dw_two_sum(si, ci);
+            }
+            if (!PRE) s.w.H[i * ldh + j] = mk<T>((T)hr.x, (T)hi.x);
+            s.Hh[i * ld + j] = mk<float>(hr.x, hi.x);
+            s.Hl[i * ld + j] = mk<float>(hr.y, hi.y);
         }
-        if (!PRE) s.w.H[i * ldh + j] = mk<T>((T)h.re, (T)h.im);
-        if (REFINE) {
-            const float hr = (float)h.re, hi = (float)h.im;
-            s.Hh[i * ld + j] = mk<float>(hr, hi);
-            s.Hl[i * ld + j] = mk<float>((float)(h.re - (double)hr), (float)(h.im - (double)hi));
+    } else {
+        const double bx = b[0], by = b[1], bz = b[2];
+        for (int e = tid; e < m * m; e += nt) {
+            const int i = FastDiv(m).div(e), j = e - i * m;
+            cx<double> h = mk<double>(0.0, 0.0);
+            if (i < n && j < n) {
+                const size_t o = (size_t)i * n + j;
+                const cx<double> hs = Hsys[o], z0 = Z[o], z1 = Z[nn + o], z2 = Z[2 * nn + o];
+                h.re = hs.re + bx * z0.re + by * z1.re + bz * z2.re;
+                h.im = hs.im + bx * z0.im + by * z1.im + bz * z2.im;
+            }
+            if (!PRE) s.w.H[i * ldh + j] = mk<T>((T)h.re, (T)h.im);
+            if (REFINE) {
+                const float hr = (float)h.re, hi = (float)h.im;
+                s.Hh[i * ld + j] = mk<float>(hr, hi);
+                s.Hl[i * ld + j] =
+                    mk<float>((float)(h.re - (double)hr), (float)(h.im - (double)hi));
+            }
         }
     }
     __syncthreads();
@@ -255,8 +341,9 @@ __device__ __forceinline__ int snap_eigvecs(const SnapArgs &a, int sn, int g, in
 //   E_ii = R_ii / 2,   X <- X + X E,
 // with eigenvalues l_i plus the second-order term
 // sum_j |S_ij + l_i R_ij|^2 / (l_i - l_j).  H X, X^H H X and X^H X use
-// double-word FP32 accumulation, 1 - R_ii and l_i are FP64; E, the
-// second-order terms and X E are FP32 (they are small corrections).
+// double-word FP32 accumulation and l_i is a double-word (S_ii over
+// 1 - R_ii = 1 + g_i as S_ii - S_ii g_i / (1 + g_i)); E, the second-order
+// terms and X E are FP32 (they are small corrections).  No FP64.
 // Levels too close for the first-order E (near-degenerate clusters, e.g.
 // at level anticrossings, and exactly degenerate multiplets) are resolved
 // as clusters (msp_cluster.cuh).  Returns this step's largest correction.
@@ -318,8 +405,8 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         const float4 S = lm_dw<true>(a1, ac1, a2, ac2, KS);
         const float4 G = lm_dw<true>(g1, gc1, g2, gc2, KG);
         if (i == j) {
-            s.sd[i] = (double)S.x + (double)S.z;
-            s.rd[i] = (1.0 - (double)G.x) - (double)G.z;  // R_ii = 1 - G_ii
+            s.gd[i] = make_float2(G.x - 1.0f, G.z);  // G_ii - 1 (G.x - 1 exact)
+            s.lw[i] = make_float2(S.x, S.z);         // S_ii until l_i replaces it
         } else {
             s.SR[i * ld + j] = mk<float>(S.x + S.z, S.y + S.w);
             s.SR[j * ld + i] = mk<float>(-(G.x + G.z), -(G.y + G.w));  // R_ij = -G_ij
@@ -328,11 +415,12 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     __syncthreads();
     float lmax = 0.f;
     for (int i = tid; i < n; i += nt) {
-        const double l = s.sd[i] / (1.0 - s.rd[i]);
-        s.lam[i] = l;
-        s.lamf[i] = (float)l;
+        const float2 lw = dw_rayleigh(s.lw[i], s.gd[i]);
+        const float l = lw.x;
+        s.lw[i] = lw;
+        s.lamf[i] = l;
         s.corr[i] = 0.f;
-        lmax = fmaxf(lmax, fabsf((float)l));
+        lmax = fmaxf(lmax, fabsf(l));
     }
     atomicMax(&s.scal[1], __float_as_int(lmax));  // non-negative: int order = float order
     __syncthreads();
@@ -344,21 +432,21 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     cl.scal = s.scal;
     cl.T = s.Yl;
     cl.ldt = ld;
-    oa_clusters(s.SR, ld, s.lam, s.lamf, n, cl);
+    oa_clusters(s.SR, ld, s.lw, s.lamf, n, cl);
     float emax = 0.f;
     const int nup = n * (n - 1) / 2;
     for (int e = tid; e < nup; e += nt) {
         int i, j;
         oa_pair_of(e, i, j);
-        oa_pair_correction(s.SR, ld, s.lam, s.lamf, cl, s.corr, i, j, emax);
+        oa_pair_correction(s.SR, ld, s.lw, s.lamf, cl, s.corr, i, j, emax);
     }
     __syncthreads();
-    oa_cluster_diagonal(s.lam, s.corr, n, cl);
+    oa_cluster_diagonal(s.lw, s.corr, n, cl);
     // X' = X + X E  (into Yh), E_ii = R_ii / 2
     for (int e = tid; e < n * n; e += nt) {
         const int k = FastDiv(n).div(e), j = e - k * n;
         const cx<float> xkj = X[k * ld + j];
-        const float hr = (float)(0.5 * s.rd[j]);
+        const float hr = -0.5f * (s.gd[j].x + s.gd[j].y);  // R_jj / 2
         float ar = xkj.re + hr * xkj.re, ai = xkj.im + hr * xkj.im;
         for (int i = 0; i < n; ++i) {
             if (i == j) continue;
@@ -374,7 +462,7 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         X[k * ld + j] = Yh[k * ld + j];
     }
     __syncthreads();
-    emax = fmaxf(emax, oa_resolve_clusters(X, ld, n, s.lam, s.corr, n, cl,
+    emax = fmaxf(emax, oa_resolve_clusters(X, ld, n, s.lw, s.corr, n, cl,
                                            __int_as_float(s.scal[1])));
     atomicMax(&s.scal[2], __float_as_int(emax));  // non-negative: int order = float order
     __syncthreads();
@@ -383,8 +471,9 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     return step;
 }
 
-// Eigenvalues into lam[0..n): the Jacobi diagonal (FP64), or the refined
-// values (MIXED; also refines the eigenvectors in place).
+// Eigenvalues: the Jacobi diagonal into lam[0..n) (FP64), or the refined
+// double-words into lw[0..n) (MIXED; also refines the eigenvectors in
+// place).
 // Returns status bits (MSP_ITEM_REFINE_LIMIT when the refinement ran out of
 // steps).
 template <typename T, bool REFINE>
@@ -439,13 +528,22 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
         // ascending order, ties by index (stable)
         for (int j = tid; j < n; j += nt) {
             int r = 0;
-            const double lj = s.lam[j];
-            for (int k = 0; k < n; ++k) {
-                const double lk = s.lam[k];
-                r += (lk < lj) || (lk == lj && k < j);
+            if constexpr (REFINE) {
+                const float2 lj = s.lw[j];
+                for (int k = 0; k < n; ++k) {
+                    const float2 lk = s.lw[k];
+                    r += dw_less(lk, lj) || (dw_equal(lk, lj) && k < j);
+                }
+                evals[(size_t)bidx * n + r] = dw_to_double(lj);
+            } else {
+                const double lj = s.lam[j];
+                for (int k = 0; k < n; ++k) {
+                    const double lk = s.lam[k];
+                    r += (lk < lj) || (lk == lj && k < j);
+                }
+                evals[(size_t)bidx * n + r] = lj;
             }
             s.rank[j] = r;
-            evals[(size_t)bidx * n + r] = lj;
         }
         __syncthreads();
         cx<double> *Vb = evecs + (size_t)bidx * n * n;
@@ -478,14 +576,16 @@ __global__ void msp_snap_fast_kernel(SnapArgs a) {
     for (int sn = blockIdx.x; sn < a.num_snap; sn += gridDim.x) {
         const SnapSource src = snap_source(a, sn);
         const size_t g = (size_t)src.g;
-        load_hamiltonian<T, REFINE, PRE>(src.Hsys, src.Z, a.field + 3 * g, n, m, s);
+        load_hamiltonian<T, REFINE, PRE>(src.Hsys, src.Z, src.Hdw, src.Zdw, a.field + 3 * g, n,
+                                         m, s);
         int st = snap_eigvecs<T, PRE>(a, sn, (int)g, n, m, s);
         st |= eigenpairs<T, REFINE>(s, n, m, a.max_refine);
 
         // sigma_p = p . sigma (Pauli), applied on the muon (slowest) digit
-        const double px = a.pol[3 * g], py = a.pol[3 * g + 1], pz = a.pol[3 * g + 2];
-        const cx<T> s00 = mk<T>((T)pz, T(0)), s01 = mk<T>((T)px, (T)(-py));
-        const cx<T> s10 = mk<T>((T)px, (T)py), s11 = mk<T>((T)(-pz), T(0));
+        T px, py, pz;
+        load_vec3<T>(a.pol + 3 * g, px, py, pz);
+        const cx<T> s00 = mk<T>(pz, T(0)), s01 = mk<T>(px, -py);
+        const cx<T> s10 = mk<T>(px, py), s11 = mk<T>(-pz, T(0));
         cx<T> *M = s.w.H;  // free buffer
         const cx<T> *U = s.w.U;
         for (int e = tid; e < n * n; e += nt) {
@@ -497,34 +597,63 @@ __global__ void msp_snap_fast_kernel(SnapArgs a) {
                 v = cadd(cmul(s10, U[(i - d) * ld + k]), cmul(s11, U[i * ld + k]));
             M[i * ld + k] = v;
         }
-        if (tid == 0) s.acc[0] = 0.0;
+        if (!REFINE && tid == 0) s.acc[0] = 0.0;
         __syncthreads();
-        const double scale = 0.5 * a.wscale[g] / (double)d;
         const int ntri = n * (n + 1) / 2;
-        double diag_local = 0.0;
-        for (int e = tid; e < ntri; e += nt) {
-            int j, k;
-            tri_index(e, j, k);
-            T gr = 0, gi = 0;
-            for (int i = 0; i < n; ++i) {
-                const cx<T> u = U[i * ld + j], mm = M[i * ld + k];
-                gr += u.re * mm.re + u.im * mm.im;
-                gi += u.re * mm.im - u.im * mm.re;
+        if constexpr (REFINE) {
+            // FP32 amplitudes, double-word level gaps and diagonal sum
+            const float scale = (float)a.wscale[g] * (0.5f / (float)d);
+            float2 diag = make_float2(0.f, 0.f);
+            for (int e = tid; e < ntri; e += nt) {
+                int j, k;
+                tri_index(e, j, k);
+                float gr = 0.f, gi = 0.f;
+                for (int i = 0; i < n; ++i) {
+                    const cx<float> u = U[i * ld + j], mm = M[i * ld + k];
+                    gr += u.re * mm.re + u.im * mm.im;
+                    gi += u.re * mm.im - u.im * mm.re;
+                }
+                const float A = gr * gr + gi * gi;
+                if (j == k) {
+                    diag = dw_add_f(diag, A);
+                } else {
+                    const size_t o = (size_t)sn * P + pair_index(j, k);
+                    reinterpret_cast<float2 *>(a.pair_coef)[o] = make_float2(scale * A, 0.f);
+                    store_frequency_dw(a, o, dw_sub(s.lw[j], s.lw[k]));
+                }
             }
-            const double A = (double)(gr * gr + gi * gi);
-            if (j == k) {
-                diag_local += A;
-            } else {
-                const size_t o = (size_t)sn * P + pair_index(j, k);
-                coef[o] = PairCoef<T>::make(scale * A, 0.0);
-                store_frequency(a, o, 6.283185307179586476925 * (s.lam[j] - s.lam[k]));
+            const double dsum = dw_block_sum(diag, reinterpret_cast<float2 *>(s.w.red));
+            if (tid == 0) {
+                a.snap_const[sn] = 0.25 * a.wscale[g] * dsum / (double)d;
+                a.status[g] = st;
             }
-        }
-        atomicAdd(&s.acc[0], diag_local);
-        __syncthreads();
-        if (tid == 0) {
-            a.snap_const[sn] = scale * 0.5 * s.acc[0];
-            a.status[g] = st;
+        } else {
+            const double scale = 0.5 * a.wscale[g] / (double)d;
+            double diag_local = 0.0;
+            for (int e = tid; e < ntri; e += nt) {
+                int j, k;
+                tri_index(e, j, k);
+                T gr = 0, gi = 0;
+                for (int i = 0; i < n; ++i) {
+                    const cx<T> u = U[i * ld + j], mm = M[i * ld + k];
+                    gr += u.re * mm.re + u.im * mm.im;
+                    gi += u.re * mm.im - u.im * mm.re;
+                }
+                const double A = (double)(gr * gr + gi * gi);
+                if (j == k) {
+                    diag_local += A;
+                } else {
+                    const size_t o = (size_t)sn * P + pair_index(j, k);
+                    coef[o] = PairCoef<T>::make(scale * A, 0.0);
+                    store_frequency(a, o, 6.283185307179586476925 * (s.lam[j] - s.lam[k]));
+                }
+            }
+            atomicAdd(&s.acc[0], diag_local);
+            __syncthreads();
+            if (tid == 0) {
+                a.snap_const[sn] = scale * 0.5 * s.acc[0];
+                a.status[g] = st;
+            }
         }
         __syncthreads();
     }
@@ -532,11 +661,12 @@ __global__ void msp_snap_fast_kernel(SnapArgs a) {
 
 // ------------------------------------------------------------------ general path
 
-// Applies the single-spin matrix F (dim x dim, complex128) on digit `stride`
-// of the row index of X (n x n, leading dim m) into Y: Y = (1 (x) F (x) 1) X.
-template <typename T>
-__device__ void apply_digit(const cx<double> *F, int dim, int stride, const cx<T> *X,
-                            cx<T> *Y, int n, int m) {
+// Applies the single-spin matrix F (dim x dim, complex FP64 or FP32) on
+// digit `stride` of the row index of X (n x n, leading dim m) into Y:
+// Y = (1 (x) F (x) 1) X.
+template <typename T, typename TF>
+__device__ void apply_digit(const cx<TF> *F, int dim, int stride, const cx<T> *X, cx<T> *Y, int n,
+                            int m) {
     const int ld = m + 1;
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
         const int i = FastDiv(n).div(e), k = e - i * n;
@@ -544,7 +674,7 @@ __device__ void apply_digit(const cx<double> *F, int dim, int stride, const cx<T
         const int base = i - di * stride;
         T yr = 0, yi = 0;
         for (int l = 0; l < dim; ++l) {
-            const cx<double> f = F[di * dim + l];
+            const cx<TF> f = F[di * dim + l];
             const cx<T> x = X[(base + l * stride) * ld + k];
             yr += (T)f.re * x.re - (T)f.im * x.im;
             yi += (T)f.re * x.im + (T)f.im * x.re;
@@ -569,6 +699,9 @@ __global__ void msp_snap_rho_kernel(SnapArgs a) {
     typedef typename PairCoef<T>::type coef_t;
     coef_t *coef = reinterpret_cast<coef_t *>(a.pair_coef);
     const double twopi = 6.283185307179586476925;
+    // MIXED constants (FP32)
+    const float tau_f = INTEGRAL ? (float)a.tau : 0.f;
+    const float itau_f = INTEGRAL ? (float)(1.0 / a.tau) : 0.f;
 
     for (int sn = blockIdx.x; sn < a.num_snap; sn += gridDim.x) {
         if (a.rho_fac) {
@@ -577,7 +710,11 @@ __global__ void msp_snap_rho_kernel(SnapArgs a) {
         } else {
             build_rho_factors(a, sn, s.fac);
         }
-        load_hamiltonian<T, REFINE, PRE>(a.Hsys, a.Z, a.field + 3 * (size_t)sn, n, m, s);
+        load_hamiltonian<T, REFINE, PRE>(a.Hsys, a.Z, a.Hsys_dw, a.Z_dw, a.field + 3 * (size_t)sn,
+                                         n, m, s);
+        if (REFINE)  // made visible by the eigensolve's barriers
+            for (int e = tid; e < a.fac_len; e += nt)
+                s.facf[e] = mk<float>((float)s.fac[e].re, (float)s.fac[e].im);
         int st = snap_eigvecs<T, PRE>(a, sn, sn, n, m, s);
         st |= eigenpairs<T, REFINE>(s, n, m, a.max_refine);
         const cx<T> *U = s.w.U;
@@ -589,7 +726,10 @@ __global__ void msp_snap_rho_kernel(SnapArgs a) {
             int off = 0;
             for (int sp = 0; sp < a.num_spins; ++sp) {
                 const int dim = a.dims[sp];
-                apply_digit<T>(s.fac + off, dim, a.strides[sp], X, Y, n, m);
+                if constexpr (REFINE)
+                    apply_digit<T>(s.facf + off, dim, a.strides[sp], X, Y, n, m);
+                else
+                    apply_digit<T>(s.fac + off, dim, a.strides[sp], X, Y, n, m);
                 off += dim * dim;
                 X = Y;
                 Y = (Y == s.w.H) ? s.B2 : s.w.H;
@@ -611,14 +751,15 @@ __global__ void msp_snap_rho_kernel(SnapArgs a) {
         __syncthreads();
         // O U into the buffer X (free now): O = sum_a p_a S^a on the muon digit
         cx<T> *OU = const_cast<cx<T> *>(X);
-        const double px = a.pol[3 * (size_t)sn], py = a.pol[3 * (size_t)sn + 1],
-                     pz = a.pol[3 * (size_t)sn + 2];
         {
+            T px, py, pz;
+            load_vec3<T>(a.pol + 3 * (size_t)sn, px, py, pz);
+            const T h = T(0.5);
             const int stride = a.strides[a.mu_index];
-            const cx<T> o00 = mk<T>((T)(0.5 * pz), T(0));
-            const cx<T> o01 = mk<T>((T)(0.5 * px), (T)(-0.5 * py));
-            const cx<T> o10 = mk<T>((T)(0.5 * px), (T)(0.5 * py));
-            const cx<T> o11 = mk<T>((T)(-0.5 * pz), T(0));
+            const cx<T> o00 = mk<T>(h * pz, T(0));
+            const cx<T> o01 = mk<T>(h * px, -h * py);
+            const cx<T> o10 = mk<T>(h * px, h * py);
+            const cx<T> o11 = mk<T>(-h * pz, T(0));
             for (int e = tid; e < n * n; e += nt) {
                 const int i = FastDiv(n).div(e), k = e - i * n;
                 const int di = (i / stride) & 1;
@@ -628,50 +769,95 @@ __global__ void msp_snap_rho_kernel(SnapArgs a) {
                                         : cadd(cmul(o10, x0), cmul(o11, x1));
             }
         }
-        if (tid == 0) s.acc[0] = 0.0;
+        if (!REFINE && tid == 0) s.acc[0] = 0.0;
         __syncthreads();
-        const double scale = a.wscale[sn];
-        double local = 0.0;
-        for (int e = tid; e < ntri; e += nt) {
-            int j, k;
-            tri_index(e, j, k);
-            // O'_kj = sum_i conj(U_ik) (O U)_ij
-            T orr = 0, oii = 0;
-            for (int i = 0; i < n; ++i) {
-                const cx<T> u = U[i * ld + k], x = OU[i * ld + j];
-                orr += u.re * x.re + u.im * x.im;
-                oii += u.re * x.im - u.im * x.re;
-            }
-            const cx<T> r = Y[j * ld + k];
-            // C_jk = rho'_jk O'_kj
-            const double cr = (double)r.re * (double)orr - (double)r.im * (double)oii;
-            const double ci = (double)r.re * (double)oii + (double)r.im * (double)orr;
-            if (INTEGRAL) {
-                // term = C_jk * (-1) / (2 pi i (l_k - l_j) - 1/tau); pairs count twice
-                const double inv_tau = 1.0 / a.tau;
-                if (j == k) {
-                    local += cr * a.tau;
-                } else {
-                    const double x = twopi * (s.lam[k] - s.lam[j]);
-                    // -C / (-1/tau + i x) = C (1/tau + i x) / (1/tau^2 + x^2)
-                    const double den = inv_tau * inv_tau + x * x;
-                    local += 2.0 * (cr * inv_tau - ci * x) / den;
+        if constexpr (REFINE) {
+            // FP32 terms, double-word level gaps and sums
+            const float scale2 = 2.0f * (float)a.wscale[sn];
+            float2 local = make_float2(0.f, 0.f);
+            for (int e = tid; e < ntri; e += nt) {
+                int j, k;
+                tri_index(e, j, k);
+                // O'_kj = sum_i conj(U_ik) (O U)_ij
+                float orr = 0.f, oii = 0.f;
+                for (int i = 0; i < n; ++i) {
+                    const cx<float> u = U[i * ld + k], x = OU[i * ld + j];
+                    orr += u.re * x.re + u.im * x.im;
+                    oii += u.re * x.im - u.im * x.re;
                 }
-            } else {
-                if (j == k) {
-                    local += cr;
+                const cx<float> r = Y[j * ld + k];
+                // C_jk = rho'_jk O'_kj
+                const float cr = r.re * orr - r.im * oii;
+                const float ci = r.re * oii + r.im * orr;
+                if (INTEGRAL) {
+                    if (j == k) {
+                        local = dw_add_f(local, cr * tau_f);
+                    } else {
+                        const float gap = dw_sub_f(s.lw[k], s.lw[j]);
+                        const float x = fmaf(gap, MSP_TWOPI_HI, gap * MSP_TWOPI_LO);
+                        const float den = fmaf(x, x, itau_f * itau_f);
+                        local = dw_add_f(local, 2.0f * (cr * itau_f - ci * x) / den);
+                    }
                 } else {
-                    const size_t o = (size_t)sn * P + pair_index(j, k);
-                    coef[o] = PairCoef<T>::make(2.0 * scale * cr, 2.0 * scale * ci);
-                    store_frequency(a, o, twopi * (s.lam[j] - s.lam[k]));
+                    if (j == k) {
+                        local = dw_add_f(local, cr);
+                    } else {
+                        const size_t o = (size_t)sn * P + pair_index(j, k);
+                        reinterpret_cast<float2 *>(a.pair_coef)[o] =
+                            make_float2(scale2 * cr, scale2 * ci);
+                        store_frequency_dw(a, o, dw_sub(s.lw[j], s.lw[k]));
+                    }
                 }
             }
-        }
-        atomicAdd(&s.acc[0], local);
-        __syncthreads();
-        if (tid == 0) {
-            a.snap_const[sn] = INTEGRAL ? scale * s.acc[0] / a.tau : scale * s.acc[0];
-            a.status[sn] = st;
+            const double sum = dw_block_sum(local, reinterpret_cast<float2 *>(s.w.red));
+            if (tid == 0) {
+                a.snap_const[sn] = INTEGRAL ? a.wscale[sn] * sum / a.tau : a.wscale[sn] * sum;
+                a.status[sn] = st;
+            }
+        } else {
+            const double scale = a.wscale[sn];
+            double local = 0.0;
+            for (int e = tid; e < ntri; e += nt) {
+                int j, k;
+                tri_index(e, j, k);
+                // O'_kj = sum_i conj(U_ik) (O U)_ij
+                T orr = 0, oii = 0;
+                for (int i = 0; i < n; ++i) {
+                    const cx<T> u = U[i * ld + k], x = OU[i * ld + j];
+                    orr += u.re * x.re + u.im * x.im;
+                    oii += u.re * x.im - u.im * x.re;
+                }
+                const cx<T> r = Y[j * ld + k];
+                // C_jk = rho'_jk O'_kj
+                const double cr = (double)r.re * (double)orr - (double)r.im * (double)oii;
+                const double ci = (double)r.re * (double)oii + (double)r.im * (double)orr;
+                if (INTEGRAL) {
+                    // term = C_jk * (-1) / (2 pi i (l_k - l_j) - 1/tau); pairs count twice
+                    const double inv_tau = 1.0 / a.tau;
+                    if (j == k) {
+                        local += cr * a.tau;
+                    } else {
+                        const double x = twopi * (s.lam[k] - s.lam[j]);
+                        // -C / (-1/tau + i x) = C (1/tau + i x) / (1/tau^2 + x^2)
+                        const double den = inv_tau * inv_tau + x * x;
+                        local += 2.0 * (cr * inv_tau - ci * x) / den;
+                    }
+                } else {
+                    if (j == k) {
+                        local += cr;
+                    } else {
+                        const size_t o = (size_t)sn * P + pair_index(j, k);
+                        coef[o] = PairCoef<T>::make(2.0 * scale * cr, 2.0 * scale * ci);
+                        store_frequency(a, o, twopi * (s.lam[j] - s.lam[k]));
+                    }
+                }
+            }
+            atomicAdd(&s.acc[0], local);
+            __syncthreads();
+            if (tid == 0) {
+                a.snap_const[sn] = INTEGRAL ? scale * s.acc[0] / a.tau : scale * s.acc[0];
+                a.status[sn] = st;
+            }
         }
         __syncthreads();
     }
@@ -773,6 +959,28 @@ cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStr
     return mixed ? launch_snap(msp_snap_rho_kernel<float, true, true>, a, grid, threads, smem, st)
                  : launch_snap(msp_snap_rho_kernel<double, false, true>, a, grid, threads, smem,
                                st);
+}
+
+__global__ void msp_split_dw_kernel(const cx<double> *__restrict__ Hsys, size_t nh,
+                                    const cx<double> *__restrict__ Z, size_t nz,
+                                    float4 *__restrict__ dst) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nh + nz; i += stride) {
+        const cx<double> v = i < nh ? Hsys[i] : Z[i - nh];
+        dst[i] = dw_split(make_double2(v.re, v.im));
+    }
+}
+
+cudaError_t launch_split_dw(const double *Hsys, size_t nh, const double *Z, size_t nz,
+                            float4 *dst, cudaStream_t st) {
+    const size_t total = nh + nz;
+    if (total == 0) return cudaSuccess;
+    size_t grid = (total + 255) / 256;
+    if (grid > 1024) grid = 1024;
+    msp_split_dw_kernel<<<(unsigned)grid, 256, 0, st>>>(
+        reinterpret_cast<const cx<double> *>(Hsys), nh, reinterpret_cast<const cx<double> *>(Z),
+        nz, dst);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_eigh(const double *H, int n, int batch, int precision, int max_sweeps,
