@@ -563,8 +563,10 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
 // 166-217): A = |U^dag (sigma_p (x) 1_d) U|^2 and omega_jk = 2 pi (l_j - l_k)
 // for j > k, scaled by 0.5 * w / (d * N_avg), plus the constant
 // 0.5 * sum_j A_jj part.
+// MIXED: at most 64 registers (no spills; ptxas would take ~88 and fit
+// 5 instead of 7-8 CTAs of 128 threads per SM).
 template <typename T, bool REFINE, bool PRE = false>
-__global__ void msp_snap_fast_kernel(SnapArgs a) {
+__global__ void __maxnreg__(REFINE ? 64 : 255) msp_snap_fast_kernel(SnapArgs a) {
     extern __shared__ __align__(16) char smem[];
     const int n = a.n, m = n + (n & 1), ld = m + 1, d = n / 2;
     SnapSmem<T> s = snap_carve<T, REFINE>(smem, n, false, 0);
@@ -689,8 +691,9 @@ __device__ void apply_digit(const cx<TF> *F, int dim, int stride, const cx<T> *X
 // pair coefficients of <O>(t) = sum_ij rho'_ij O'_ji exp(-i w_ij t)
 // (muspinsim/hamiltonian.py:80-107); INTEGRAL writes the decaying integral
 // divided by tau (muspinsim/hamiltonian.py:150-164, experiment.py:492-496).
+// MIXED: at most 72 registers (no spills).
 template <typename T, bool REFINE, bool INTEGRAL, bool PRE = false>
-__global__ void msp_snap_rho_kernel(SnapArgs a) {
+__global__ void __maxnreg__(REFINE ? 72 : 255) msp_snap_rho_kernel(SnapArgs a) {
     extern __shared__ __align__(16) char smem[];
     const int n = a.n, m = n + (n & 1), ld = m + 1;
     SnapSmem<T> s = snap_carve<T, REFINE>(smem, n, true, a.fac_len);
