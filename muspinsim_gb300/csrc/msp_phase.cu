@@ -531,6 +531,76 @@ __device__ __forceinline__ void tc_build_tables(const float4 *rec_p, const float
     }
 }
 
+// Seeds of one pair's power tables (the bases and starting values of
+// tc_build_tables' five chains), for the warp-specialised kernel, which
+// computes them for a whole work item at once: e^{i psi}, e^{i 8 psi},
+// e^{i N psi}, e^{i 8 N psi}, and c e^{i (phi0 + psi tile)},
+// c e^{i (phi0 + psi (tile + 64 N))} -- the same operations as
+// tc_build_tables, so the tables are identical.
+struct TcSeed {
+    cx<float> e1, e8, eN, e8N, p3, p4;
+};
+
+template <int N>
+__device__ __forceinline__ TcSeed tc_seed(float4 rec, float2 cf, float tile_steps) {
+    TcSeed sd;
+    const float sc[4] = {1.f, 8.f, (float)N, 8.f * N};
+    cx<float> e[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float h = rec.x * sc[c], l = rec.y * sc[c];  // exact power-of-two scaling
+        dw_reduce_2pi(h, l);
+        e[c] = dw_expi(h, l);
+    }
+    sd.e1 = e[0];
+    sd.e8 = e[1];
+    sd.eN = e[2];
+    sd.e8N = e[3];
+#pragma unroll
+    for (int c = 3; c < 5; ++c) {
+        float th = rec.z, tl = rec.w;
+        const float steps = tile_steps + (c == 4 ? 64.f * N : 0.f);  // exact
+        if (steps > 0.f) {
+            const float ph = rec.x * steps;
+            float bh = ph, bl = fmaf(rec.x, steps, -ph) + rec.y * steps;
+            dw_reduce_2pi(bh, bl);
+            dw_add(th, tl, bh, bl);
+            dw_reduce_2pi(th, tl);
+        }
+        cx<float> p = mk<float>(cf.x, -cf.y);
+        if (th != 0.f || tl != 0.f) p = cmul(p, dw_expi(th, tl));
+        if (c == 3)
+            sd.p3 = p;
+        else
+            sd.p4 = p;
+    }
+    return sd;
+}
+
+// The power tables of one stage from its pairs' seeds (np of them valid).
+template <int N>
+__device__ __forceinline__ void tc_chain_tables(const TcSeed *seed, TcTables<N> &tb, int np,
+                                                int tid) {
+    constexpr int PS = MSP_TC_PS, YH = N / 8;
+    if (tid >= 5 * PS) return;
+    const int c = tid / PS, i = tid - c * PS;
+    const int len = c == 1 ? YH : 8;
+    cx<float> *dst = c == 0 ? &tb.ylo[0][i] : c == 1 ? &tb.yhi[0][i] : c == 2 ? &tb.xlo[0][i]
+                                                : c == 3 ? &tb.xhi[0][i] : &tb.xhi[8][i];
+    cx<float> p = mk<float>(c >= 3 ? 0.f : 1.f, 0.f), base = mk<float>(1.f, 0.f);
+    if (i < np) {
+        const TcSeed &sd = seed[i];
+        base = c == 0 ? sd.e1 : c == 1 ? sd.e8 : c == 2 ? sd.eN : sd.e8N;
+        if (c == 3) p = sd.p3;
+        if (c == 4) p = sd.p4;
+    }
+    for (int q = 0; q < len; ++q) {
+        dst[q * (PS + 1)] = p;
+        p = cmul(p, base);
+    }
+}
+
+
 // 256 threads: warps w and w + 4 own the same 32 TMEM lanes (rows k1) and
 // drain the two column halves; operand generation is spread over all
 // threads (A: 4 K-chunks of one row each, B: one K-chunk each).  One
@@ -720,6 +790,11 @@ __global__ void __launch_bounds__(MSP_TC_THREADS) msp_phase_tc_kernel(PhaseArgs 
 //     built, then arrive on tab_full[t];
 //   * warp 11, one lane (MMA): waits on op_full[b], issues the stage's 12
 //     MMAs into accumulator block b and commits them to mma_done[b].
+// Producers and table warps arrive once per warp (lane 0, after a
+// __syncwarp that orders the other lanes' work before it): 8 + 8 + 3
+// arrivals a stage rather than one per thread.  Their waits and failure
+// checks are warp-uniform (__all_sync / __any_sync), so a warp never
+// splits around a __syncwarp or a tcgen05 instruction.
 // Every wait polls a bounded number of times and also gives up when another
 // thread has recorded a failure (s_fail), so a failure ends every loop
 // quickly; the tile's partials are then NaN and the tensor memory is
@@ -731,11 +806,12 @@ __global__ void __launch_bounds__(MSP_TC_THREADS) msp_phase_tc_kernel(PhaseArgs 
 // tcgen05.st (row k1 = TMEM lane k1, K index = column, one tf32 per
 // column), and the MMAs read A from there.  Only B (N rows) is staged in
 // shared memory (a stage moves ~20 KB through it instead of ~100 KB), which
-// leaves room for the work item's pair records (at most MSP_F32_ITEM_PAIRS
-// x 24 B): the table warps copy them into shared memory once, so a stage's
-// tables start without a global-memory round trip -- the table warps'
-// per-stage latency was what paced the pipeline (the MMAs of a stage take
-// ~300 cycles, the producers ~900, the tables ~2000 with the loads).
+// leaves room for the work item's table seeds (TcSeed, 48 B for each of at
+// most MSP_F32_ITEM_PAIRS pairs): all threads compute them at the start, so
+// a stage's tables are only short multiplication chains.  Built per stage
+// from the pair records, the tables' latency (~2000 cycles a stage, with
+// the loads and the sincosf calls) paced the pipeline; the MMAs of a stage
+// take ~300 cycles and the producers ~900.
 // Tensor memory per CTA (256 columns): accumulator blocks at columns 0 and
 // 32, A buffer b (hi, lo) at columns 64 + 64 b and 96 + 64 b.  The dynamic
 // shared memory is padded so that two CTAs share an SM (2 x 256 = 512
@@ -752,10 +828,11 @@ struct TcwLayout {
     static constexpr int CB = (N / 8) * 128;  // bytes of one B K-chunk
     static constexpr int B_BYTES = 8 * CB;    // 8 K-chunks per stage (K = 32)
     static constexpr int STAGE = 2 * B_BYTES; // hi and lo of B
-    static constexpr int REC = 40 * 1024;     // the item's pair records (24 B each)
+    static constexpr int REC = 16 * 1024;     // the item's table seeds (48 B per pair)
     static constexpr int SMEM = 80 * 1024;    // padded: two CTAs per SM
-    static_assert(2 * STAGE <= REC && 128 * (N + 1) * 4 <= REC &&
-                      REC + 24 * MSP_F32_ITEM_PAIRS <= SMEM,
+    // the epilogue's 128 x (N + 1) tile may overlap the seeds (dead by then)
+    static_assert(2 * STAGE <= REC && 128 * (N + 1) * 4 <= SMEM &&
+                      REC + 48 * MSP_F32_ITEM_PAIRS <= SMEM,
                   "TcwLayout");
 };
 
@@ -786,6 +863,8 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 }
 
 // Bounded wait that also stops when *fail is set (checked every 256 polls).
+// (A suspend-time hint on try_wait cut the polls from ~8 to ~1 a wait but
+// did not make the kernel faster.)
 __device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity,
                                                   volatile int *fail) {
     for (int it = 0; it < MSP_TC_WAIT; ++it) {
@@ -804,7 +883,7 @@ __device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity,
 }
 
 template <int N>
-__global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArgs a) {
+__global__ void __launch_bounds__(MSP_TCW_THREADS, 2) msp_phase_tcw_kernel(PhaseArgs a) {
     typedef TcwLayout<N> L;
     constexpr int PS = MSP_TC_PS, NH = N / 2;
     extern __shared__ __align__(1024) char tsm[];
@@ -821,13 +900,13 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
         item_range(a, blockIdx.x, &s_range[0], &s_range[1]);
         for (int t = 0; t < MSP_TCW_TABLES; ++t) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tab_full[t])),
-                         "r"(MSP_TCW_TABLE_THREADS));
+                         "r"(MSP_TCW_TABLE_THREADS / 32));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tab_empty[t])),
-                         "r"(MSP_TCW_PRODUCERS));
+                         "r"(MSP_TCW_PRODUCERS / 32));
         }
         for (int b = 0; b < 2; ++b) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&op_full[b])),
-                         "r"(MSP_TCW_PRODUCERS));
+                         "r"(MSP_TCW_PRODUCERS / 32));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mma_done[b])));
         }
         asm volatile("fence.mbarrier_init.release.cluster;");
@@ -850,6 +929,15 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = s_tmem;
     const int nstage = (pend - pbeg + PS - 1) / PS;
+    // every pair's table seeds, by all threads at once (the per-stage table
+    // work is then short multiplication chains)
+    TcSeed *seeds = reinterpret_cast<TcSeed *>(tsm + L::REC);
+    {
+        const float2 *coef = reinterpret_cast<const float2 *>(a.pair_coef);
+        for (int e = tid; e < pend - pbeg; e += MSP_TCW_THREADS)
+            seeds[e] = tc_seed<N>(a.pair_phase[pbeg + e], coef[pbeg + e], tile_steps);
+    }
+    __syncthreads();
 
     float acc[NH];
 #pragma unroll
@@ -862,7 +950,8 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
             tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(half * NH);
         uint32_t r[32];
         // waits decided warp-uniformly: tcgen05.ld is a whole-warp instruction
-        for (int s = 0; s < nstage && !s_fail; ++s) {
+        for (int s = 0; s < nstage; ++s) {
+            if (__any_sync(0xffffffffu, s_fail)) break;
             const int b = s & 1, t = s % MSP_TCW_TABLES;
             if (!__all_sync(0xffffffffu, mbar_wait_or_fail(smem_u32(&tab_full[t]),
                                                             (s / MSP_TCW_TABLES) & 1, &s_fail)))
@@ -916,15 +1005,18 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
                 *reinterpret_cast<float4 *>(B_hi + off) = hh;
                 *reinterpret_cast<float4 *>(B_lo + off) = lo;
             }
-            mbar_arrive(smem_u32(&tab_empty[t]));
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&tab_empty[t]));
             // B written by the generic proxy, read by the tensor core; this
             // thread's tensor-memory loads and stores ordered before the MMAs
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;");
-            mbar_arrive(smem_u32(&op_full[b]));
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&op_full[b]));
         }
         // the blocks of the last two stages
-        for (int st = nstage >= 2 ? nstage - 2 : 0; st < nstage && !s_fail; ++st) {
+        for (int st = nstage >= 2 ? nstage - 2 : 0; st < nstage; ++st) {
+            if (__any_sync(0xffffffffu, s_fail)) break;
             if (!__all_sync(0xffffffffu, mbar_wait_or_fail(smem_u32(&mma_done[st & 1]),
                                                             (st >> 1) & 1, &s_fail)))
                 break;
@@ -936,28 +1028,19 @@ __global__ void __launch_bounds__(MSP_TCW_THREADS) msp_phase_tcw_kernel(PhaseArg
     } else if (tid < MSP_TCW_PRODUCERS + MSP_TCW_TABLE_THREADS) {
         // ------------------------------------------------------------ tables
         const int tt = tid - MSP_TCW_PRODUCERS;
-        // the item's pair records, once, into shared memory: a stage's
-        // tables then start without a global-memory round trip
-        float4 *rph = reinterpret_cast<float4 *>(tsm + L::REC);
-        float2 *rcf = reinterpret_cast<float2 *>(tsm + L::REC + 16 * MSP_F32_ITEM_PAIRS);
-        {
-            const float2 *coef = reinterpret_cast<const float2 *>(a.pair_coef);
-            for (int e = tt; e < pend - pbeg; e += MSP_TCW_TABLE_THREADS) {
-                rph[e] = a.pair_phase[pbeg + e];
-                rcf[e] = coef[pbeg + e];
-            }
-            asm volatile("bar.sync 1, %0;" ::"n"(MSP_TCW_TABLE_THREADS) : "memory");
-        }
-        for (int s = 0; s < nstage && !s_fail; ++s) {
+        for (int s = 0; s < nstage; ++s) {
+            if (__any_sync(0xffffffffu, s_fail)) break;
             const int t = s % MSP_TCW_TABLES;
             if (s >= MSP_TCW_TABLES &&
-                !mbar_wait_or_fail(smem_u32(&tab_empty[t]), ((s / MSP_TCW_TABLES) - 1) & 1,
-                                   &s_fail))
+                !__all_sync(0xffffffffu,
+                            mbar_wait_or_fail(smem_u32(&tab_empty[t]),
+                                              ((s / MSP_TCW_TABLES) - 1) & 1, &s_fail)))
                 break;
             const int pb = pbeg + s * PS;
-            tc_build_tables<N>(rph + (pb - pbeg), rcf + (pb - pbeg), tabs[t],
-                               (pend - pb) < PS ? (pend - pb) : PS, tile_steps, tt);
-            mbar_arrive(smem_u32(&tab_full[t]));
+            tc_chain_tables<N>(seeds + (pb - pbeg), tabs[t], (pend - pb) < PS ? (pend - pb) : PS,
+                               tt);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&tab_full[t]));
         }
     } else if (lane == 0) {
         // ------------------------------------------------------------ MMA issue
