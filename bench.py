@@ -42,11 +42,14 @@ L2_BYTES = 129 * 1024 * 1024
 # tensor figures only.
 SMS, FP32_FMA_PER_SM = 152, 128
 # DRAM bytes (read + write) per snapshot of each stage's kernel, from an ncu
-# capture of the 10,000-orientation run (dram__bytes_read.sum +
-# dram__bytes_write.sum): 8.06 MB and 68.45 MB per launch over 10,000
-# snapshots.  Traffic scales with the
-# snapshot count (pair records and constants are per snapshot).
-TRAFFIC_PER_SNAPSHOT = {"snapshots": 8.06e6 / 1e4, "phase": 68.45e6 / 1e4}
+# --set full capture of the 2,000-orientation x 4,096-time case
+# (dram__bytes_read.sum + dram__bytes_write.sum per launch / 2,000): the
+# warp Jacobi reads the system matrices (L2-resident), the refinement its
+# eigenvectors (4.6 KB a snapshot), the phase sum the pair records (6.6 KB);
+# their outputs stay in the 129 MB L2.  Traffic scales with the snapshot
+# count.
+TRAFFIC_PER_SNAPSHOT = {"eigensolve": 0.0988e6 / 2000, "snapshots": 9.458e6 / 2000,
+                        "phase": 13.288e6 / 2000}
 
 
 def parse_args():
@@ -495,7 +498,8 @@ def run_gb300(args, world, rank, local):
         "snapshots": ("msp_snap_fast_kernel<float,true,true> (refinement + amplitudes)",
                       32.0 * n**3 * S, "fp32-pipe", fp32_peak,
                       "nominal FP32 FMA pipe (152 x 128 x 2 x 2070 MHz)"),
-        "phase": ("msp_phase_tcw_kernel<32> (tcgen05 kind::tf32, 3xTF32, warp-specialised)",
+        "phase": ("msp_phase_tcw_kernel<32> (tcgen05 kind::tf32, 3xTF32, A in tensor memory, "
+                  "warp-specialised)",
                   (4.0 * n * n) * samples, "tensor", tf32_peak, tf32_src),
         "reduce": ("msp_reduce_kernel", 2.0 * samples, "fp32-pipe", fp32_peak,
                    "nominal FP32 FMA pipe"),
@@ -514,7 +518,8 @@ def run_gb300(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed_max,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (Jacobi, phase sum) + df32/f64 (refinement, phase reduction, accumulation)",
+        "dtype": "f32 (Jacobi, 3xTF32 phase sum) + double-word f32 (refinement, eigenvalues, "
+                 "phase records); f64 only in the per-time reduction",
         "data": "synthetic (seeded couplings, ZCW-style grid)",
         "config": {"workload": WORKLOAD, "orientations": S, "times": T, "dim": n,
                    "precision": "mixed", "l2": "flushed between timed steps (258 MB write)",
@@ -543,8 +548,9 @@ def run_gb300(args, world, rank, local):
             "stages": rl_all,
         },
         "clocks": clk,
-        # warp Jacobi, refinement, schedule, phase sum, reduction
-        "gpu_launches": 5 * args.steps,
+        # double-word split of the system matrices, warp Jacobi, refinement,
+        # schedule, phase sum, reduction
+        "gpu_launches": 6 * args.steps,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -752,12 +758,14 @@ def run_config3(args, world, rank, local):
                  "integrals/s", ms, args, world, f"mu_e_3H_dim32_alc_{Nf}_fields_{No}_orient",
                  {"fields": Nf, "orientations": No, "dim": 32, "tau_us": MU_TAU,
                   "l2": "inputs (96 MB of field/polarisation) resident; not flushed"},
-                 dtype="f32 Jacobi + df32 refinement + f64 integral",
+                 dtype="f32 Jacobi + double-word f32 refinement and integral sums",
                  fp64={"value": sub * No / (ms64 * 1e-3), "unit": "integrals/s",
                        "ms_per_step": ms64, "sample": f"{sub} of {Nf} fields x {No} orientations"},
                  max_abs_dIntegral_mixed_vs_fp64=dP,
                  status_max=int(mixed.status[:units].max().item()),
-                 gpu_launches=3 * args.steps)
+                 # double-word split, warp Jacobi, refinement + integrals,
+                 # schedule, reduction
+                 gpu_launches=5 * args.steps)
     if not args.no_cpu_baseline:
         from oracle import port
         from tests.helpers import oracle_system
