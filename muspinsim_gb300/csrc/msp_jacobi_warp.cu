@@ -141,7 +141,7 @@ __device__ __forceinline__ void jw_rotate(float4 R, cx<float> &x, cx<float> &y) 
 }  // namespace
 
 template <int M>
-__global__ void __launch_bounds__(JW_WARPS * 32, 4) msp_jacobi_warp_kernel(SnapArgs a) {
+__global__ void __launch_bounds__(JW_WARPS * 32, M <= 24 ? 5 : 4) msp_jacobi_warp_kernel(SnapArgs a) {
     using S = JwShape<M>;
     constexpr int H = S::H, NB = S::NB, NOFF = S::NOFF;
     extern __shared__ __align__(16) char smem[];

@@ -310,9 +310,20 @@ static int plan_prepare(msp_multi_plan *p) {
         rc = mcuda(cudaMallocHost(&p->tab_pinned, p->tab_bytes > 0 ? p->tab_bytes : 256),
                    "msp_multi_run: pinned table copy");
     if (rc == MSP_OK) memcpy(p->tab_pinned, p->tab.data(), p->tab_bytes);
+    // bucket streams by priority in launch order (most work first): the
+    // long large-n kernel gets the SMs first and the small buckets fill in
+    // around it, in eager runs and in the graph (node priorities)
+    int prio_least = 0, prio_greatest = 0;
+    if (rc == MSP_OK)
+        rc = mcuda(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest),
+                   "msp_multi_run: stream priorities");
+    int rank = 0;
     for (MultiBucket &b : p->buckets) {
         if (rc != MSP_OK) break;
-        rc = mcuda(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking), "msp_multi_run");
+        int prio = prio_greatest + rank++;
+        if (prio > prio_least) prio = prio_least;
+        rc = mcuda(cudaStreamCreateWithPriority(&b.stream, cudaStreamNonBlocking, prio),
+                   "msp_multi_run");
         if (rc == MSP_OK)
             rc = mcuda(cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming), "msp_multi_run");
         if (rc == MSP_OK && !b.large) {
@@ -579,7 +590,8 @@ int msp_multi_run_graph(msp_multi_plan *p, const msp_multi_io *io, void *stream)
         }
         rc = mcuda(e, "msp_multi_run_graph: end capture");
         if (rc == MSP_OK)
-            rc = mcuda(cudaGraphInstantiate(&p->exec, graph, 0), "msp_multi_run_graph: instantiate");
+            rc = mcuda(cudaGraphInstantiate(&p->exec, graph, cudaGraphInstantiateFlagUseNodePriority),
+                       "msp_multi_run_graph: instantiate");
         if (graph) cudaGraphDestroy(graph);
         if (rc != MSP_OK) {
             p->exec = NULL;
