@@ -810,9 +810,13 @@ def run_config4(args, world, rank, local):
     for prec in ("mixed", "fp64") if args.fp64_steps > 0 else ("mixed",):
         b = MultiSystemBatch(systems, wls[0].orientations, wls[0].fields[0],
                              wls[0].polarization, wls[0].times, precision=prec)
-        b.run(graph=graph)
+        for _ in range(max(1, args.warmup if prec == "mixed" else 1)):
+            b.run(graph=graph)
         torch.cuda.synchronize()
-        ms = _events_ms(lambda: b.run(graph=graph), max(1, args.steps // 10))
+        # every timed step of the mixed batch; the FP64 batch (~1.8 s a step
+        # at 512 x 32) for --fp64-steps of them
+        nsteps = max(1, args.steps if prec == "mixed" else args.fp64_steps)
+        ms = _events_ms(lambda: b.run(graph=graph), nsteps)
         out[prec] = (ms, b.plan.out.clone(), b.plan.info())
         b.plan.close()
     ms, res, info = out["mixed"]
