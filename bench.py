@@ -607,13 +607,25 @@ def _snapshot_task(task):
     return acc
 
 
-def cpu_pool_map(tasks, threads):
-    """Run _snapshot_task over tasks in a spawn pool of `threads` processes
-    (spawn: no process is forked from one that holds a CUDA context)."""
+def _lindblad_task(task):
+    """Worker: the oracle's dissipative powder average (numpy eig of the
+    Lindbladian per snapshot) over a chunk of orientation rows."""
+    from oracle import port
+    from tests.helpers import oracle_system
+
+    spins, couplings, rows, field, pol, temperature, times, diss = task
+    osy = oracle_system(spins, couplings)
+    return port.powder_average(osy, rows, field, pol, temperature, times, dissipation=diss)
+
+
+def cpu_pool_map(tasks, threads, fn=None):
+    """Run fn (default _snapshot_task) over tasks in a spawn pool of
+    `threads` processes (spawn: no process is forked from one that holds a
+    CUDA context)."""
     import multiprocessing as mp
 
     with mp.get_context("spawn").Pool(threads, initializer=_pool_init) as pool:
-        return pool.map(_snapshot_task, tasks)
+        return pool.map(fn or _snapshot_task, tasks)
 
 
 def _chunks(items, k):
@@ -993,9 +1005,27 @@ def run_lindblad(args, world, rank, local):
                                      np.zeros(sample, np.int32), 1, wl.times,
                                      temperature=wl.temperature)[0].cpu().numpy()[0]
         line["max_abs_dP_vs_oracle_20_orient_fp64"] = float(np.abs(gpu20 - ref).max())
-        line["cpu_baseline"] = {"value": sample * T / dt, "unit": "samples/s", "cores": 1,
-                                "kind": "port",
-                                "sample": f"{sample} orientations (numpy eig of L per snapshot)"}
+        # the timed baseline: the same oracle path on every host core, ~5 s
+        # of work per process, timed after the (spawn) pool has started
+        import multiprocessing as mp
+
+        threads = os.cpu_count() or 1
+        per = max(1, int(round(sample / dt * 5.0)))
+        rows = [wl.orientations[k % N] for k in range(per * threads)]
+
+        def tasks_of(rs):
+            return [(list(wl.spins), wl.couplings, c, wl.fields[0], wl.polarization,
+                     wl.temperature, wl.times, diss) for c in _chunks(rs, threads)]
+
+        with mp.get_context("spawn").Pool(threads, initializer=_pool_init) as pool:
+            pool.map(_lindblad_task, tasks_of(rows[:threads]))  # start-up and imports
+            t0 = time.perf_counter()
+            pool.map(_lindblad_task, tasks_of(rows))
+            dtp = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(rows) * T / dtp, "unit": "samples/s",
+                                "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+                                "sample": f"{len(rows)} orientations over {threads} processes "
+                                          "(numpy eig of L per snapshot)"}
     del out
     return line
 

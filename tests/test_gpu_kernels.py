@@ -369,12 +369,15 @@ def test_powder_fast_large_mixed_dim192():
     assert np.abs(_gpu_powder(wl, "mixed") - ref).max() <= MIXED_TOL
 
 
-@pytest.mark.parametrize("n_times,t_end", [(4096, 20.0), (1500, 10.0), (9000, 30.0)])
+@pytest.mark.parametrize("n_times,t_end", [(4096, 20.0), (1500, 10.0), (9000, 30.0),
+                                           (256, 60.0)])
 def test_phase_tensor_cores_match_simt_and_oracle(monkeypatch, n_times, t_end):
     """Mixed precision on a uniform grid: the tcgen05 (3xTF32) phase sum
     against the FP32 SIMT kernel (same inputs, FP32-rounding agreement) and
     the oracle (1e-6).  4096 times use 128 x 32 tiles, 1500 one 128 x 16
-    tile, 9000 three 128 x 32 tiles."""
+    tile, 9000 three 128 x 32 tiles; 256 times over 60 us make the phase
+    steps psi = omega dt hundreds of radians (the double-word reduction
+    modulo 2 pi in the snapshot kernel)."""
     from muspinsim_gb300 import workloads
 
     wl = workloads.config2(n_orient=40, n_times=n_times)
