@@ -347,7 +347,11 @@ __device__ __forceinline__ int snap_eigvecs(const SnapArgs &a, int sn, int g, in
 // Levels too close for the first-order E (near-degenerate clusters, e.g.
 // at level anticrossings, and exactly degenerate multiplets) are resolved
 // as clusters (msp_cluster.cuh).  Returns this step's largest correction.
-__device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
+// NN > 0: n = NN at compile time (the product loops unroll with constant
+// shared-memory offsets); NN = 0: n from the argument.
+template <int NN>
+__device__ float oa_refine(SnapSmem<float> &s, int n_rt, int m_rt) {
+    const int n = NN > 0 ? NN : n_rt, m = NN > 0 ? NN + (NN & 1) : m_rt;
     const int tid = threadIdx.x, nt = blockDim.x, ld = m + 1;
     cx<float> *X = s.w.U;
     cx<float> *Yh = s.w.H;  // Jacobi work matrix is free now
@@ -356,6 +360,8 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     // every partial sum
     for (int j = tid; j < n; j += nt) {
         float acc = 0.f;
+        #pragma unroll
+
         for (int k = 0; k < n; ++k) acc = fmaf(X[k * ld + j].re, X[k * ld + j].re,
                                                fmaf(X[k * ld + j].im, X[k * ld + j].im, acc));
         s.cn[j] = sqrtf(acc);
@@ -368,6 +374,8 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         u64 s1 = K, s2 = K, c1 = 0ull, c2 = 0ull;
         const u64 *hh = reinterpret_cast<const u64 *>(s.Hh + i * ld);
         const u64 *hl = reinterpret_cast<const u64 *>(s.Hl + i * ld);
+        #pragma unroll
+
         for (int k = 0; k < n; ++k) {
             const cx<float> x = X[k * ld + j];
             lm_step<true, false>(s1, c1, s2, c2, hh[k], hl[k], f32x2(x.re, x.re),
@@ -380,6 +388,8 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
     __syncthreads();
     for (int j = tid; j < n; j += nt) {
         float acc = 0.f;
+        #pragma unroll
+
         for (int k = 0; k < n; ++k) acc = fmaf(Yh[k * ld + j].re, Yh[k * ld + j].re,
                                                fmaf(Yh[k * ld + j].im, Yh[k * ld + j].im, acc));
         s.yn[j] = sqrtf(acc);
@@ -394,6 +404,8 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         const u64 KS = lm_anchor(s.cn[i] * s.yn[j]), KG = lm_anchor(s.cn[i] * s.cn[j]);
         u64 a1 = KS, a2 = KS, ac1 = 0ull, ac2 = 0ull;
         u64 g1 = KG, g2 = KG, gc1 = 0ull, gc2 = 0ull;
+        #pragma unroll
+
         for (int k = 0; k < n; ++k) {
             const u64 xi = *reinterpret_cast<const u64 *>(X + k * ld + i);
             const cx<float> y = Yh[k * ld + j], yl = s.Yl[k * ld + j], xj = X[k * ld + j];
@@ -448,6 +460,8 @@ __device__ float oa_refine(SnapSmem<float> &s, int n, int m) {
         const cx<float> xkj = X[k * ld + j];
         const float hr = -0.5f * (s.gd[j].x + s.gd[j].y);  // R_jj / 2
         float ar = xkj.re + hr * xkj.re, ai = xkj.im + hr * xkj.im;
+        #pragma unroll
+
         for (int i = 0; i < n; ++i) {
             if (i == j) continue;
             const cx<float> x = X[k * ld + i], E = s.SR[i * ld + j];
@@ -493,8 +507,12 @@ __device__ int eigenpairs<double, false>(SnapSmem<double> &s, int n, int m, int)
 template <>
 __device__ int eigenpairs<float, true>(SnapSmem<float> &s, int n, int m, int max_refine) {
     if (max_refine <= 0) max_refine = 4;
-    for (int it = 0; it < max_refine; ++it)
-        if (oa_refine(s, n, m) <= 2e-4f) return MSP_ITEM_OK;
+    for (int it = 0; it < max_refine; ++it) {
+        const float step = n == 24   ? oa_refine<24>(s, n, m)
+                           : n == 32 ? oa_refine<32>(s, n, m)
+                                     : oa_refine<0>(s, n, m);
+        if (step <= 2e-4f) return MSP_ITEM_OK;
+    }
     return MSP_ITEM_REFINE_LIMIT;
 }
 
@@ -691,9 +709,10 @@ __device__ void apply_digit(const cx<TF> *F, int dim, int stride, const cx<T> *X
 // pair coefficients of <O>(t) = sum_ij rho'_ij O'_ji exp(-i w_ij t)
 // (muspinsim/hamiltonian.py:80-107); INTEGRAL writes the decaying integral
 // divided by tau (muspinsim/hamiltonian.py:150-164, experiment.py:492-496).
-// MIXED: at most 72 registers (no spills).
+// MIXED: at most 96 registers (shared memory limits these CTAs to ~4 per SM
+// at n = 32 anyway).
 template <typename T, bool REFINE, bool INTEGRAL, bool PRE = false>
-__global__ void __maxnreg__(REFINE ? 72 : 255) msp_snap_rho_kernel(SnapArgs a) {
+__global__ void __maxnreg__(REFINE ? 96 : 255) msp_snap_rho_kernel(SnapArgs a) {
     extern __shared__ __align__(16) char smem[];
     const int n = a.n, m = n + (n & 1), ld = m + 1;
     SnapSmem<T> s = snap_carve<T, REFINE>(smem, n, true, a.fac_len);
