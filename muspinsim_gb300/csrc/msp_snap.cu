@@ -577,6 +577,38 @@ __global__ void msp_eigh_kernel(const cx<double> *__restrict__ Hin, int n, int b
 
 // ------------------------------------------------------------------ fast path
 
+// Mixed fast path: A_jk = |(U^H M)_jk|^2 over the lower triangle j >= k
+// (FP32), pair records for j > k, and this thread's share of sum_j A_jj as
+// a double-word.  NN > 0: n = NN at compile time.
+template <int NN>
+__device__ __forceinline__ float2 amplitudes_mixed(const SnapArgs &a, const SnapSmem<float> &s,
+                                                   const cx<float> *U, const cx<float> *M,
+                                                   int n_rt, int sn, float scale) {
+    const int n = NN > 0 ? NN : n_rt, ld = n + (n & 1) + 1;
+    const int P = n * (n - 1) / 2, ntri = n * (n + 1) / 2;
+    float2 diag = make_float2(0.f, 0.f);
+    for (int e = threadIdx.x; e < ntri; e += blockDim.x) {
+        int j, k;
+        tri_index(e, j, k);
+        float gr = 0.f, gi = 0.f;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            const cx<float> u = U[i * ld + j], mm = M[i * ld + k];
+            gr += u.re * mm.re + u.im * mm.im;
+            gi += u.re * mm.im - u.im * mm.re;
+        }
+        const float A = gr * gr + gi * gi;
+        if (j == k) {
+            diag = dw_add_f(diag, A);
+        } else {
+            const size_t o = (size_t)sn * P + pair_index(j, k);
+            reinterpret_cast<float2 *>(a.pair_coef)[o] = make_float2(scale * A, 0.f);
+            store_frequency_dw(a, o, dw_sub(s.lw[j], s.lw[k]));
+        }
+    }
+    return diag;
+}
+
 // One snapshot of the muon-first T = inf shortcut (muspinsim/hamiltonian.py:
 // 166-217): A = |U^dag (sigma_p (x) 1_d) U|^2 and omega_jk = 2 pi (l_j - l_k)
 // for j > k, scaled by 0.5 * w / (d * N_avg), plus the constant
@@ -623,25 +655,9 @@ __global__ void __maxnreg__(REFINE ? 64 : 255) msp_snap_fast_kernel(SnapArgs a) 
         if constexpr (REFINE) {
             // FP32 amplitudes, double-word level gaps and diagonal sum
             const float scale = (float)a.wscale[g] * (0.5f / (float)d);
-            float2 diag = make_float2(0.f, 0.f);
-            for (int e = tid; e < ntri; e += nt) {
-                int j, k;
-                tri_index(e, j, k);
-                float gr = 0.f, gi = 0.f;
-                for (int i = 0; i < n; ++i) {
-                    const cx<float> u = U[i * ld + j], mm = M[i * ld + k];
-                    gr += u.re * mm.re + u.im * mm.im;
-                    gi += u.re * mm.im - u.im * mm.re;
-                }
-                const float A = gr * gr + gi * gi;
-                if (j == k) {
-                    diag = dw_add_f(diag, A);
-                } else {
-                    const size_t o = (size_t)sn * P + pair_index(j, k);
-                    reinterpret_cast<float2 *>(a.pair_coef)[o] = make_float2(scale * A, 0.f);
-                    store_frequency_dw(a, o, dw_sub(s.lw[j], s.lw[k]));
-                }
-            }
+            const float2 diag = n == 24   ? amplitudes_mixed<24>(a, s, U, M, n, sn, scale)
+                                : n == 32 ? amplitudes_mixed<32>(a, s, U, M, n, sn, scale)
+                                          : amplitudes_mixed<0>(a, s, U, M, n, sn, scale);
             const double dsum = dw_block_sum(diag, reinterpret_cast<float2 *>(s.w.red));
             if (tid == 0) {
                 a.snap_const[sn] = 0.25 * a.wscale[g] * dsum / (double)d;
@@ -704,6 +720,75 @@ __device__ void apply_digit(const cx<TF> *F, int dim, int stride, const cx<T> *X
     __syncthreads();
 }
 
+// Y[j][k] = sum_i conj(U_ij) X_ik for j >= k (row stride ld = n + (n & 1) + 1);
+// NN > 0: n = NN at compile time.
+template <typename T, int NN>
+__device__ __forceinline__ void tri_conj_products(const cx<T> *U, const cx<T> *X, cx<T> *Y,
+                                                  int n_rt) {
+    const int n = NN > 0 ? NN : n_rt, ld = n + (n & 1) + 1, ntri = n * (n + 1) / 2;
+    for (int e = threadIdx.x; e < ntri; e += blockDim.x) {
+        int j, k;
+        tri_index(e, j, k);
+        T gr = 0, gi = 0;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            const cx<T> u = U[i * ld + j], x = X[i * ld + k];
+            gr += u.re * x.re + u.im * x.im;
+            gi += u.re * x.im - u.im * x.re;
+        }
+        Y[j * ld + k] = mk<T>(gr, gi);
+    }
+}
+
+// Mixed general path: every term C_jk = rho'_jk O'_kj (j >= k, O'_kj =
+// sum_i conj(U_ik) (O U)_ij): pair records (EVOLVE) or the decaying-integral
+// terms (INTEGRAL); returns this thread's share of the constant / integral
+// as a double-word.  NN > 0: n = NN at compile time.
+template <bool INTEGRAL, int NN>
+__device__ __forceinline__ float2 rho_terms_mixed(const SnapArgs &a, const SnapSmem<float> &s,
+                                                  const cx<float> *U, const cx<float> *OU,
+                                                  const cx<float> *Y, int n_rt, int sn,
+                                                  float tau_f, float itau_f) {
+    const int n = NN > 0 ? NN : n_rt, ld = n + (n & 1) + 1;
+    const int P = n * (n - 1) / 2, ntri = n * (n + 1) / 2;
+    const float scale2 = 2.0f * (float)a.wscale[sn];
+    float2 local = make_float2(0.f, 0.f);
+    for (int e = threadIdx.x; e < ntri; e += blockDim.x) {
+        int j, k;
+        tri_index(e, j, k);
+        float orr = 0.f, oii = 0.f;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            const cx<float> u = U[i * ld + k], x = OU[i * ld + j];
+            orr += u.re * x.re + u.im * x.im;
+            oii += u.re * x.im - u.im * x.re;
+        }
+        const cx<float> r = Y[j * ld + k];
+        const float cr = r.re * orr - r.im * oii;
+        const float ci = r.re * oii + r.im * orr;
+        if (INTEGRAL) {
+            // term = C_jk (-1) / (2 pi i (l_k - l_j) - 1/tau); pairs count twice
+            if (j == k) {
+                local = dw_add_f(local, cr * tau_f);
+            } else {
+                const float gap = dw_sub_f(s.lw[k], s.lw[j]);
+                const float x = fmaf(gap, MSP_TWOPI_HI, gap * MSP_TWOPI_LO);
+                const float den = fmaf(x, x, itau_f * itau_f);
+                local = dw_add_f(local, 2.0f * (cr * itau_f - ci * x) / den);
+            }
+        } else {
+            if (j == k) {
+                local = dw_add_f(local, cr);
+            } else {
+                const size_t o = (size_t)sn * P + pair_index(j, k);
+                reinterpret_cast<float2 *>(a.pair_coef)[o] = make_float2(scale2 * cr, scale2 * ci);
+                store_frequency_dw(a, o, dw_sub(s.lw[j], s.lw[k]));
+            }
+        }
+    }
+    return local;
+}
+
 // One snapshot of the general path: rho' = U^dag rho0 U, O' = U^dag O U with
 // rho0 = (x)_s rho_s (Kronecker factors) and O = p . S_mu.  EVOLVE writes the
 // pair coefficients of <O>(t) = sum_ij rho'_ij O'_ji exp(-i w_ij t)
@@ -759,17 +844,12 @@ __global__ void __maxnreg__(REFINE ? 96 : 255) msp_snap_rho_kernel(SnapArgs a) {
         }
         // X holds rho0 U.  rho'_jk (j >= k) -> Y (the other buffer).
         const int ntri = n * (n + 1) / 2;
-        for (int e = tid; e < ntri; e += nt) {
-            int j, k;
-            tri_index(e, j, k);
-            T gr = 0, gi = 0;
-            for (int i = 0; i < n; ++i) {
-                const cx<T> u = U[i * ld + j], x = X[i * ld + k];
-                gr += u.re * x.re + u.im * x.im;
-                gi += u.re * x.im - u.im * x.re;
-            }
-            Y[j * ld + k] = mk<T>(gr, gi);
-        }
+        if (REFINE && n == 24)
+            tri_conj_products<T, 24>(U, X, Y, n);
+        else if (REFINE && n == 32)
+            tri_conj_products<T, 32>(U, X, Y, n);
+        else
+            tri_conj_products<T, 0>(U, X, Y, n);
         __syncthreads();
         // O U into the buffer X (free now): O = sum_a p_a S^a on the muon digit
         cx<T> *OU = const_cast<cx<T> *>(X);
@@ -795,42 +875,10 @@ __global__ void __maxnreg__(REFINE ? 96 : 255) msp_snap_rho_kernel(SnapArgs a) {
         __syncthreads();
         if constexpr (REFINE) {
             // FP32 terms, double-word level gaps and sums
-            const float scale2 = 2.0f * (float)a.wscale[sn];
-            float2 local = make_float2(0.f, 0.f);
-            for (int e = tid; e < ntri; e += nt) {
-                int j, k;
-                tri_index(e, j, k);
-                // O'_kj = sum_i conj(U_ik) (O U)_ij
-                float orr = 0.f, oii = 0.f;
-                for (int i = 0; i < n; ++i) {
-                    const cx<float> u = U[i * ld + k], x = OU[i * ld + j];
-                    orr += u.re * x.re + u.im * x.im;
-                    oii += u.re * x.im - u.im * x.re;
-                }
-                const cx<float> r = Y[j * ld + k];
-                // C_jk = rho'_jk O'_kj
-                const float cr = r.re * orr - r.im * oii;
-                const float ci = r.re * oii + r.im * orr;
-                if (INTEGRAL) {
-                    if (j == k) {
-                        local = dw_add_f(local, cr * tau_f);
-                    } else {
-                        const float gap = dw_sub_f(s.lw[k], s.lw[j]);
-                        const float x = fmaf(gap, MSP_TWOPI_HI, gap * MSP_TWOPI_LO);
-                        const float den = fmaf(x, x, itau_f * itau_f);
-                        local = dw_add_f(local, 2.0f * (cr * itau_f - ci * x) / den);
-                    }
-                } else {
-                    if (j == k) {
-                        local = dw_add_f(local, cr);
-                    } else {
-                        const size_t o = (size_t)sn * P + pair_index(j, k);
-                        reinterpret_cast<float2 *>(a.pair_coef)[o] =
-                            make_float2(scale2 * cr, scale2 * ci);
-                        store_frequency_dw(a, o, dw_sub(s.lw[j], s.lw[k]));
-                    }
-                }
-            }
+            const float2 local =
+                n == 24   ? rho_terms_mixed<INTEGRAL, 24>(a, s, U, OU, Y, n, sn, tau_f, itau_f)
+                : n == 32 ? rho_terms_mixed<INTEGRAL, 32>(a, s, U, OU, Y, n, sn, tau_f, itau_f)
+                          : rho_terms_mixed<INTEGRAL, 0>(a, s, U, OU, Y, n, sn, tau_f, itau_f);
             const double sum = dw_block_sum(local, reinterpret_cast<float2 *>(s.w.red));
             if (tid == 0) {
                 a.snap_const[sn] = INTEGRAL ? a.wscale[sn] * sum / a.tau : a.wscale[sn] * sum;
