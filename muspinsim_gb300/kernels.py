@@ -12,13 +12,21 @@ import torch
 
 from muspinsim_gb300 import _lib
 
+_CUDA_READY = False
+
+
 def device():
-    """The CUDA device the library runs on; raises when there is none."""
-    if not torch.cuda.is_available():
-        raise RuntimeError(
-            "muspinsim_gb300 needs a CUDA device: the polarisation kernels have no CPU path"
-        )
-    _lib.load()
+    """The CUDA device the library runs on; raises when there is none.  (The
+    availability check and the library load run once; both are slow enough
+    to show in a per-call profile.)"""
+    global _CUDA_READY
+    if not _CUDA_READY:
+        if not torch.cuda.is_available():
+            raise RuntimeError(
+                "muspinsim_gb300 needs a CUDA device: the polarisation kernels have no CPU path"
+            )
+        _lib.load()
+        _CUDA_READY = True
     return torch.device("cuda", torch.cuda.current_device())
 
 
@@ -169,12 +177,45 @@ def integrate_decaying(evals, rho, ops, tau):
     return out
 
 
-def orient_snapshots(rows, B, p, B_intr=(0.0, 0.0, 0.0), mode="zyz", weight_norm=None):
+class OrientBuffers:
+    """Reusable buffers of orient_snapshots for N rows of length L: a pinned
+    host copy of the rows (so the upload is asynchronous), the device rows
+    and the three outputs.  A caller that reuses them must not overwrite
+    the host rows while an upload from them may still run (the powder
+    path synchronises at the end of every call)."""
+
+    def __init__(self, N, L):
+        d = device()
+        self.host = torch.empty((N, L), dtype=torch.float64, pin_memory=True)
+        self.host_np = self.host.numpy()
+        self.rows = torch.empty((N, L), dtype=torch.float64, device=d)
+        self.field = torch.empty((N, 3), dtype=torch.float64, device=d)
+        self.pol = torch.empty((N, 3), dtype=torch.float64, device=d)
+        self.w = torch.empty((N,), dtype=torch.float64, device=d)
+        self.slot = torch.zeros((N,), dtype=torch.int32, device=d)
+        self.uploaded = None  # event after the last upload from `host`
+
+
+def orient_snapshots(rows, B, p, B_intr=(0.0, 0.0, 0.0), mode="zyz", weight_norm=None,
+                     buffers=None):
     """Lab-frame field, polarisation and weight/N of every orientation row on
     the device (msp_orient_snapshots).  ``rows``: (N, 2 | 3 | 4) array or
-    tensor.  Returns three device tensors: (N, 3), (N, 3), (N,)."""
+    tensor.  Returns three device tensors: (N, 3), (N, 3), (N,).
+    ``buffers``: an OrientBuffers of the same N and row length, whose
+    pinned copy, device rows and outputs are used instead of new ones (the
+    outputs are then overwritten by the next call with the same buffers)."""
     d = device()
-    R = dev(rows, torch.float64)
+    if buffers is not None and isinstance(rows, np.ndarray):
+        if buffers.uploaded is not None:
+            buffers.uploaded.synchronize()  # the previous upload has read `host`
+        np.copyto(buffers.host_np, rows)
+        buffers.rows.copy_(buffers.host, non_blocking=True)
+        if buffers.uploaded is None:
+            buffers.uploaded = torch.cuda.Event()
+        buffers.uploaded.record(torch.cuda.current_stream())
+        R = buffers.rows
+    else:
+        R = dev(rows, torch.float64)
     if R.dim() != 2 or R.shape[1] not in (2, 3, 4):
         raise ValueError("orientation rows must be (theta, phi), (a, b, c) or (a, b, c, w)")
     N, L = int(R.shape[0]), int(R.shape[1])
@@ -183,9 +224,14 @@ def orient_snapshots(rows, B, p, B_intr=(0.0, 0.0, 0.0), mode="zyz", weight_norm
             weight_norm = 1.0 / float(R[:, 3].sum().item())
         else:
             weight_norm = 1.0 / max(N, 1)
-    field = torch.empty((N, 3), dtype=torch.float64, device=d)
-    pol = torch.empty((N, 3), dtype=torch.float64, device=d)
-    w = torch.empty((N,), dtype=torch.float64, device=d)
+    if buffers is not None:
+        if tuple(buffers.field.shape) != (N, 3):
+            raise ValueError("orient_snapshots: buffers are for another row count")
+        field, pol, w = buffers.field, buffers.pol, buffers.w
+    else:
+        field = torch.empty((N, 3), dtype=torch.float64, device=d)
+        pol = torch.empty((N, 3), dtype=torch.float64, device=d)
+        w = torch.empty((N,), dtype=torch.float64, device=d)
     vec = ctypes.c_double * 3
     _lib.call("msp_orient_snapshots", ptr(R), N, L, 0 if mode == "zyz" else 1,
               vec(*np.asarray(B, dtype=float)), vec(*np.asarray(p, dtype=float)),
@@ -354,6 +400,10 @@ class PowderPlan:
     def rebind(self, field, pol, wscale, slot):
         """Point the plan at new per-snapshot inputs of the same sizes (device
         tensors), keeping its output, status and workspace."""
+        if all(isinstance(t, torch.Tensor) and t.is_cuda for t in (field, pol, wscale, slot)) and \
+                (field.data_ptr(), pol.data_ptr(), wscale.data_ptr(), slot.data_ptr()) == \
+                (self.F.data_ptr(), self.Pl.data_ptr(), self.W.data_ptr(), self.Sl.data_ptr()):
+            return self  # the same buffers as last time
         F = dev(field, torch.float64).reshape(-1, 3)
         if F.shape[0] != self.num_snap:
             raise ValueError("rebind: the snapshot count changed")

@@ -47,6 +47,20 @@ def _rows_sorted(slot):
 
 
 _PLANS = {}
+_ORIENT_BUFFERS = {}
+
+
+def _orient_buffers(N, L):
+    """OrientBuffers for N rows of length L on the current device, reused
+    across powder_average calls (every call synchronises before it returns,
+    so the pinned rows are free again by the next call)."""
+    key = (N, L, torch.cuda.current_device())
+    b = _ORIENT_BUFFERS.get(key)
+    if b is None:
+        if len(_ORIENT_BUFFERS) >= 8:
+            _ORIENT_BUFFERS.clear()
+        b = _ORIENT_BUFFERS[key] = kernels.OrientBuffers(N, L)
+    return b
 
 
 def _cached_plan(system, Hs, Zd, n, F, Pl, W, slot, num_slots, times, mode, prec, dims, mu, Tarr,
@@ -287,8 +301,9 @@ def powder_average(system, orientations, field=(0.0, 0.0, 0.0), polarization=(1.
     if rows is not None and fast is not None and len(rows) > 0:
         N = len(rows)
         wnorm = 1.0 / float(rows[:, 3].sum()) if (rows.shape[1] == 4 and N > 1) else 1.0 / N
-        F, Pl, W = kernels.orient_snapshots(rows, f, p, intr, mode, wnorm)
-        res, status = run_snapshots(system, F, Pl, temperature, W, None, 1, times, y_axis,
+        bufs = _orient_buffers(N, rows.shape[1])
+        F, Pl, W = kernels.orient_snapshots(rows, f, p, intr, mode, wnorm, buffers=bufs)
+        res, status = run_snapshots(system, F, Pl, temperature, W, bufs.slot, 1, times, y_axis,
                                     precision, max_sweeps, fast_mask=fast, host_out=True)
     else:
         qs, ws = orientation_rows_to_quats(orientations, mode)
