@@ -1196,15 +1196,21 @@ __global__ void msp_schedule_kernel(const int *__restrict__ slot, int S, int num
 // out[slot][t] = sum of the slot's snapshot constants + its items' partials,
 // in a fixed order (deterministic); heterogeneous batches map slots to
 // output rows (slot_row) and add to the row (accumulate) when a system's
-// snapshots are split over several launches.  A block covers 32 times of one slot:
-// warp w sums items w, w + 32, w + 64, ... (eight loads in flight per
-// thread: a slot's partials are tens of MB that only many outstanding
-// loads stream at HBM rate), then the 32 warp sums are added in warp order.
-#define MSP_REDUCE_WARPS 32
+// snapshots are split over several launches.  A block covers 8 times of
+// one slot (so that a 4096-time row gives 512 blocks: the slot's partials
+// are tens of MB that only many outstanding loads stream at HBM rate): lane
+// (g, tt) of warp w reads time tt of items 4 w + g, 4 w + g + 64, ...
+// (32-byte sectors of 4 items per load), summing FP32 partials as a
+// double-word (FP64 partials in FP64); the 64 stream sums are then added in
+// stream order in FP64.
+#define MSP_REDUCE_WARPS 16
+#define MSP_REDUCE_T 8
+#define MSP_REDUCE_STREAMS (MSP_REDUCE_WARPS * 32 / MSP_REDUCE_T)
 __global__ void __launch_bounds__(32 * MSP_REDUCE_WARPS)
     msp_reduce_kernel(PhaseArgs a, const double *__restrict__ snap_const,
                       double *__restrict__ out, int T) {
-    __shared__ double red[MSP_REDUCE_WARPS][33];
+    __shared__ double red[MSP_REDUCE_STREAMS][MSP_REDUCE_T + 1];
+    __shared__ double cred[MSP_REDUCE_WARPS];
     const int sl = blockIdx.y;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int s0 = a.slot_first[sl], s1 = a.slot_first[sl + 1];
@@ -1213,29 +1219,32 @@ __global__ void __launch_bounds__(32 * MSP_REDUCE_WARPS)
     // block reduction of the constants (fixed tree: deterministic)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if (lane == 0) red[warp][32] = c;
-    const int t = blockIdx.x * 32 + lane;
+    if (lane == 0) cred[warp] = c;
+    const int tt = lane & (MSP_REDUCE_T - 1), stream = warp * (32 / MSP_REDUCE_T) +
+                                                      lane / MSP_REDUCE_T;
+    const int t = blockIdx.x * MSP_REDUCE_T + tt;
     double v = 0.0;
     if (t < T) {
         const int i0 = a.item_first[sl], i1 = a.item_first[sl + 1];
         if (a.partial_f32) {
             const float *p = a.partial_f32 + t;
+            float2 acc = make_float2(0.f, 0.f);
 #pragma unroll 8
-            for (int it = i0 + warp; it < i1; it += MSP_REDUCE_WARPS)
-                v += (double)p[(size_t)it * T];
+            for (int it = i0 + stream; it < i1; it += MSP_REDUCE_STREAMS)
+                acc = dw_add_f(acc, p[(size_t)it * T]);
+            v = dw_to_double(acc);
         } else {
             const double *p = a.partial + t;
 #pragma unroll 8
-            for (int it = i0 + warp; it < i1; it += MSP_REDUCE_WARPS) v += p[(size_t)it * T];
+            for (int it = i0 + stream; it < i1; it += MSP_REDUCE_STREAMS) v += p[(size_t)it * T];
         }
     }
-    red[warp][lane] = v;
+    red[stream][tt] = v;
     __syncthreads();
-    if (warp == 0 && t < T) {
-        double cs = 0.0;
-        for (int w = 0; w < MSP_REDUCE_WARPS; ++w) cs += red[w][32];
-        double s = cs;
-        for (int w = 0; w < MSP_REDUCE_WARPS; ++w) s += red[w][lane];
+    if (tid < MSP_REDUCE_T && t < T) {
+        double s = 0.0;
+        for (int w = 0; w < MSP_REDUCE_WARPS; ++w) s += cred[w];
+        for (int q = 0; q < MSP_REDUCE_STREAMS; ++q) s += red[q][tid];
         const size_t o = (size_t)(a.slot_row ? a.slot_row[sl] : sl) * T + t;
         if (a.accumulate)
             out[o] += s;
@@ -1333,7 +1342,7 @@ cudaError_t launch_phase(const PhaseArgs &a, int precision, int max_items, int u
 cudaError_t launch_reduce(const PhaseArgs &a, const double *snap_const, double *out,
                           int num_times, cudaStream_t st) {
     if (a.num_slots <= 0) return cudaSuccess;
-    dim3 grid((num_times + 31) / 32, a.num_slots);
+    dim3 grid((num_times + MSP_REDUCE_T - 1) / MSP_REDUCE_T, a.num_slots);
     msp_reduce_kernel<<<grid, 32 * MSP_REDUCE_WARPS, 0, st>>>(a, snap_const, out, num_times);
     return cudaGetLastError();
 }
