@@ -519,7 +519,7 @@ def run_gb300(args, world, rank, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed_max,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (Jacobi, 3xTF32 phase sum) + double-word f32 (refinement, eigenvalues, "
-                 "phase records); f64 only in the per-time reduction",
+                 "phase records, item reduction); f64 only in the final per-time sums",
         "data": "synthetic (seeded couplings, ZCW-style grid)",
         "config": {"workload": WORKLOAD, "orientations": S, "times": T, "dim": n,
                    "precision": "mixed", "l2": "flushed between timed steps (258 MB write)",
