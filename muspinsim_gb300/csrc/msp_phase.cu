@@ -317,8 +317,8 @@ __global__ void __launch_bounds__(128, 4) msp_phase_uniform_f32_kernel(PhaseArgs
         __syncthreads();
     }
 
-    // combine the two groups, then write FP32 partials (the cross-item sum
-    // in msp_reduce_kernel is FP64)
+    // combine the two groups, then write FP32 partials (msp_reduce_kernel
+    // sums them across items as double-words)
     float *red = reinterpret_cast<float *>(&Xs[0][0]);  // K*K floats
     if (g == 1) {
 #pragma unroll

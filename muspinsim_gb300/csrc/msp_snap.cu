@@ -172,10 +172,10 @@ __device__ __forceinline__ void tri_index(int e, int &j, int &k) {
 
 __device__ __forceinline__ int pair_index(int j, int k) { return j * (j - 1) / 2 + k; }
 
-// Frequency record of pair o: the FP64 angular frequency w, or -- for the
-// mixed-precision phase kernel on a uniform grid -- the phases w dt and
-// w t0 reduced modulo 2 pi here in FP64 and stored as double-word floats,
-// so that the phase kernel needs no FP64 arithmetic.
+// Frequency record of pair o (FP64 snapshot kernels): the FP64 angular
+// frequency w, or -- on a uniform grid in mixed precision -- the phases
+// w dt and w t0 reduced modulo 2 pi in FP64 and stored as double-word
+// floats.  The mixed kernels use store_frequency_dw instead.
 __device__ __forceinline__ void store_frequency(const SnapArgs &a, size_t o, double w) {
     if (a.pair_phase) {
         const double psi = reduce_2pi(w * a.dt);
