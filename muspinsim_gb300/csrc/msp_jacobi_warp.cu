@@ -283,7 +283,12 @@ __global__ void __launch_bounds__(JW_WARPS * 32, M <= 24 ? 5 : 4) msp_jacobi_war
 #pragma unroll
                     for (int p = 0; p < M; ++p) u[p] = w[p];
                 }
-                for (int o = lane; o < NOFF; o += 32) {
+                // full rounds of whole blocks; a short last round (at most 8
+                // blocks, m = 24: 2 of 66) is split into single elements over
+                // four lanes per block instead of leaving 30 lanes idle
+                constexpr int FULL = (NOFF / 32) * 32, LEFT = NOFF - FULL;
+                constexpr bool SPLIT = LEFT > 0 && 4 * LEFT <= 32;
+                for (int o = lane; o < (SPLIT ? FULL : NOFF); o += 32) {
                     const unsigned k12 = kk[o];
                     const int k1 = (int)(k12 & 255u), k2 = (int)(k12 >> 8);
                     const float2 *B = Hbuf(cur);
@@ -312,6 +317,31 @@ __global__ void __launch_bounds__(JW_WARPS * 32, M <= 24 ? 5 : 4) msp_jacobi_war
                         const float sg = (code & 0x8000u) ? -1.f : 1.f;
                         Hn[code & 0x7fffu] = make_float2(nv[q].re, sg * nv[q].im);
                     }
+                }
+                if (SPLIT && lane < 4 * LEFT) {
+                    // element (r, cc) of B' = G1^H B G2 for block FULL + lane / 4
+                    const int o = FULL + (lane >> 2), q = lane & 3, r = q >> 1, cc = q & 1;
+                    const unsigned k12 = kk[o];
+                    const int k1 = (int)(k12 & 255u), k2 = (int)(k12 >> 8);
+                    const float2 *B = Hbuf(cur);
+                    const float4 bA = *reinterpret_cast<const float4 *>(B + jw_slot(H + o, 0, H));
+                    const float4 bB = *reinterpret_cast<const float4 *>(B + jw_slot(H + o, 2, H));
+                    const cx<float> b00 = mk<float>(bA.x, bA.y), b01 = mk<float>(bA.z, bA.w);
+                    const cx<float> b10 = mk<float>(bB.x, bB.y), b11 = mk<float>(bB.z, bB.w);
+                    const float4 R1 = rc[k1], R2 = rc[k2];
+                    const float c1 = R1.x, c2 = R2.x;
+                    const cx<float> s1 = mk<float>(R1.y, R1.z), s2 = mk<float>(R2.y, R2.z);
+                    // row r of T = G1^H B
+                    const cx<float> t0 = r == 0 ? cadd(cscale(c1, b00), cscale(-1.f, cmul(s1, b10)))
+                                                : cadd(cmulc(s1, b00), cscale(c1, b10));
+                    const cx<float> t1 = r == 0 ? cadd(cscale(c1, b01), cscale(-1.f, cmul(s1, b11)))
+                                                : cadd(cmulc(s1, b01), cscale(c1, b11));
+                    const cx<float> v = cc == 0 ? cadd(cscale(c2, t0), cscale(-1.f, cmulc(s2, t1)))
+                                                : cadd(cmul(s2, t0), cscale(c2, t1));
+                    const uint2 rt = route[o];
+                    const unsigned code = ((q < 2 ? rt.x : rt.y) >> (16 * (q & 1))) & 0xffffu;
+                    const float sg = (code & 0x8000u) ? -1.f : 1.f;
+                    Hn[code & 0x7fffu] = make_float2(v.re, sg * v.im);
                 }
                 __syncwarp();
                 // next-step rotations; this step's zeroed couplings moved

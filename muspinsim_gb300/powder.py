@@ -275,7 +275,10 @@ def powder_average(system, orientations, field=(0.0, 0.0, 0.0), polarization=(1.
 
     A regular grid of rows is rotated on the device (msp_orient_snapshots)
     and the system's matrices stay on the device between calls, so a call
-    moves the rows, the time grid and the result across the bus."""
+    moves the rows, the time grid and the result across the bus.  Plans and
+    orientation buffers are cached per process and reused by the next call
+    of the same sizes: calls from several host threads at once must be
+    serialised by the caller."""
     if isinstance(orientations, OrientationGrid):
         f = np.atleast_1d(np.asarray(field, dtype=float))
         f = np.array([0.0, 0.0, f[0]]) if f.size == 1 else f
