@@ -9,8 +9,9 @@ fast path.  Synthetic inputs stand in for a real material; see
 muspinsim_gb300/workloads.py.
 
 Metric: P(t) samples/s, one sample = one (orientation, time) value before the
-orientation average.  ``value`` is the mixed-precision pipeline (FP32 Jacobi +
-double-word refinement + FP32 phase sum) with inputs resident in HBM; the
+orientation average.  ``value`` is the mixed-precision pipeline (FP32
+Householder + QL eigensolve + double-word refinement + FP32 phase sum) with
+inputs resident in HBM; the
 all-FP64 pipeline is timed beside it (``fp64``) and the max |dP| between the
 two is reported.  ``e2e`` runs the public ``powder_average`` call on host
 inputs (host->device copies and the device->host result inside the timed
@@ -41,15 +42,19 @@ L2_BYTES = 129 * 1024 * 1024
 # 152 * 128 * 2 flop * SM clock.  MEASURED_PEAKS.json carries HBM and bf16
 # tensor figures only.
 SMS, FP32_FMA_PER_SM = 152, 128
-# DRAM bytes (read + write) per snapshot of each stage's kernel, from an ncu
-# --set full capture of the 2,000-orientation x 4,096-time case
+# DRAM bytes (read + write) per snapshot of each stage's kernel, from ncu
+# --set full captures of the 2,000-orientation x 4,096-time case
 # (dram__bytes_read.sum + dram__bytes_write.sum per launch / 2,000): the
-# warp Jacobi reads the system matrices (L2-resident), the refinement its
+# eigensolve reads the system matrices (L2-resident; its reflectors and
+# eigenvectors go through the L2-resident scratch), the refinement its
 # eigenvectors (4.6 KB a snapshot), the phase sum the pair records (6.6 KB);
 # their outputs stay in the 129 MB L2.  Traffic scales with the snapshot
 # count.
-TRAFFIC_PER_SNAPSHOT = {"eigensolve": 0.0988e6 / 2000, "snapshots": 9.458e6 / 2000,
+TRAFFIC_PER_SNAPSHOT = {"eigensolve": 0.117e6 / 2000, "snapshots": 9.458e6 / 2000,
                         "phase": 13.288e6 / 2000}
+# Batches of at least this many snapshots take the Householder + QL
+# eigensolve (smaller ones the warp Jacobi)
+QL_MIN_SNAPSHOTS = 4096
 
 
 def parse_args():
@@ -490,10 +495,15 @@ def run_gb300(args, world, rank, local):
     tf32_peak = (bf16 if bf16 else 1900.0) / 2.0  # dense TF32 runs at half the bf16 rate
     tf32_src = ("measured bf16 burst / 2 (MEASURED_PEAKS.json)" if bf16
                 else "fallback 1.9 PF/s bf16 / 2")
-    # algorithmic work: eigensolve 36 n^3 and eigenbasis products 32 n^3 per
-    # snapshot, 4 n^2 + 2 per time sample (phase sum + accumulation)
+    # algorithmic work per snapshot: eigensolve 36 n^3 (six Jacobi sweeps) or
+    # 19 n^3 (Householder 16/3 n^3, QL rotations 6 n^3 at ~n^2 rotations,
+    # back-transformation 8 n^3), eigenbasis products 32 n^3; per time
+    # sample 4 n^2 + 2 (phase sum + accumulation)
+    ql = S >= QL_MIN_SNAPSHOTS
     kernels_rl = {
-        "eigensolve": ("msp_jacobi_warp_kernel<24>", 36.0 * n**3 * S, "fp32-pipe", fp32_peak,
+        "eigensolve": (("msp_ql_warp_kernel<24,4> (Householder + QL, four matrices a warp)"
+                        if ql else "msp_jacobi_warp_kernel<24>"),
+                       (19.0 if ql else 36.0) * n**3 * S, "fp32-pipe", fp32_peak,
                        "nominal FP32 FMA pipe (152 x 128 x 2 x 2070 MHz)"),
         "snapshots": ("msp_snap_fast_kernel<float,true,true> (refinement + amplitudes)",
                       32.0 * n**3 * S, "fp32-pipe", fp32_peak,
@@ -518,8 +528,9 @@ def run_gb300(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed_max,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (Jacobi, 3xTF32 phase sum) + double-word f32 (refinement, eigenvalues, "
-                 "phase records, item reduction); f64 only in the final per-time sums",
+        "dtype": "f32 (Householder + QL eigensolve, 3xTF32 phase sum) + double-word f32 "
+                 "(refinement, eigenvalues, phase records, item reduction); f64 only in the "
+                 "final per-time sums",
         "data": "synthetic (seeded couplings, ZCW-style grid)",
         "config": {"workload": WORKLOAD, "orientations": S, "times": T, "dim": n,
                    "precision": "mixed", "l2": "flushed between timed steps (258 MB write)",
@@ -541,14 +552,14 @@ def run_gb300(args, world, rank, local):
             "traffic": TRAFFIC_PER_SNAPSHOT.get(dom, 0.0) * S or None,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
                               "scaled per snapshot",
-            "algorithmic": {"eigensolve": "36 n^3 per snapshot",
+            "algorithmic": {"eigensolve": ("19 n^3" if ql else "36 n^3") + " per snapshot",
                             "snapshots": "32 n^3 per snapshot",
                             "phase": "4 n^2 per sample", "reduce": "2 per sample"}[dom],
             "peak_source": src,
             "stages": rl_all,
         },
         "clocks": clk,
-        # double-word split of the system matrices, warp Jacobi, refinement,
+        # double-word split of the system matrices, eigensolve, refinement,
         # schedule, phase sum, reduction
         "gpu_launches": 6 * args.steps,
     }
@@ -770,12 +781,12 @@ def run_config3(args, world, rank, local):
                  "integrals/s", ms, args, world, f"mu_e_3H_dim32_alc_{Nf}_fields_{No}_orient",
                  {"fields": Nf, "orientations": No, "dim": 32, "tau_us": MU_TAU,
                   "l2": "inputs (96 MB of field/polarisation) resident; not flushed"},
-                 dtype="f32 Jacobi + double-word f32 refinement and integral sums",
+                 dtype="f32 Householder + QL + double-word f32 refinement and integral sums",
                  fp64={"value": sub * No / (ms64 * 1e-3), "unit": "integrals/s",
                        "ms_per_step": ms64, "sample": f"{sub} of {Nf} fields x {No} orientations"},
                  max_abs_dIntegral_mixed_vs_fp64=dP,
                  status_max=int(mixed.status[:units].max().item()),
-                 # double-word split, warp Jacobi, refinement + integrals,
+                 # double-word split, eigensolve, refinement + integrals,
                  # schedule, reduction
                  gpu_launches=5 * args.steps)
     if not args.no_cpu_baseline:
@@ -843,8 +854,8 @@ def run_config4(args, world, rank, local):
     return _line("heterogeneous-batch P(t) samples/s, mixed precision", samples / (ms * 1e-3),
                  "samples/s", ms, args, world,
                  f"{min(dims)}_to_{max(dims)}_dim_systems_{n_sys}x{n_or}_orient_{T}_t", cfg,
-                 dtype="f32 (Jacobi for n <= 64, Householder + QL for n > 64; double-word "
-                       "refinement; phase sum)",
+                 dtype="f32 (Jacobi for n <= 64, Householder + QL for n > 64 and for "
+                       "n <= 32 buckets of 4,096+ snapshots; double-word refinement; phase sum)",
                  fp64=({"value": samples / (out["fp64"][0] * 1e-3),
                         "ms_per_step": out["fp64"][0]} if "fp64" in out else None),
                  max_abs_dP_mixed_vs_fp64=dP, buckets=buckets)

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libmspgpu.so"
-SOURCES = ["msp_snap.cu", "msp_jacobi_warp.cu", "msp_phase.cu", "msp_api.cu", "msp_static.cu", "msp_adjoint.cu", "msp_large.cu",
+SOURCES = ["msp_snap.cu", "msp_jacobi_warp.cu", "msp_ql_warp.cu", "msp_phase.cu", "msp_api.cu", "msp_static.cu", "msp_adjoint.cu", "msp_large.cu",
            "msp_large_mixed.cu",
            "msp_multi.cu", "msp_orient.cu", "msp_assemble.cu",
            "msp_lindblad.cu", "msp_celio.cu"]

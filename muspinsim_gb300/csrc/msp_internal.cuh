@@ -153,6 +153,10 @@ cudaError_t launch_split_dw(const double *Hsys, size_t nh, const double *Z, size
 bool jacobi_warp_supported(int n);
 size_t snap_evec_bytes(int n, long long num_snap, int precision);
 cudaError_t launch_jacobi_warp(const SnapArgs &a, cudaStream_t st);
+// Householder + QL alternative to the warp Jacobi (msp_ql_warp.cu), same
+// inputs and eigenvector scratch
+bool ql_warp_supported(int n);
+cudaError_t launch_ql_warp(const SnapArgs &a, cudaStream_t st);
 cudaError_t launch_snapshots_refine(const SnapArgs &a, int mode, cudaStream_t st, int threads = 0,
                                     int grid = 0);
 cudaError_t launch_snapshots(const SnapArgs &a, int mode, int precision, cudaStream_t st,

@@ -396,7 +396,19 @@ bool jacobi_warp_supported(int n) {
     return m >= 4 && m <= 32;
 }
 
+// First stage of the two-stage MIXED snapshots.  Batches of 4,096 snapshots
+// or more take the Householder + QL form (msp_ql_warp.cu: at 10,000
+// snapshots of dimension 24 it takes 0.55 ms against the Jacobi's 0.86 ms,
+// and 20% less at dimension 32); smaller batches fill the GPU with too few
+// of its four-matrix warp tasks and keep the Jacobi (at 4,000 snapshots the
+// two tie).  MSP_EIGH_WARP = 0 or 2 pins one form.
+#ifndef MSP_EIGH_WARP
+#define MSP_EIGH_WARP 1
+#endif
 cudaError_t launch_jacobi_warp(const SnapArgs &a, cudaStream_t st) {
+    if (MSP_EIGH_WARP == 2 && ql_warp_supported(a.n)) return launch_ql_warp(a, st);
+    if (MSP_EIGH_WARP == 1 && ql_warp_supported(a.n) && a.num_snap >= 4096)
+        return launch_ql_warp(a, st);
     if (a.num_snap <= 0) return cudaSuccess;
     switch (a.n + (a.n & 1)) {
         case 4: return jw_launch<4>(a, st);
