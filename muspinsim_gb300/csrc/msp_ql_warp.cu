@@ -59,9 +59,11 @@ struct QwShape {
     static constexpr int BYTES = R_BYTES + G * DEV_BYTES + 16 * NM;
     static constexpr int LPM = 32 / G;              // lanes per matrix in the QL
     static constexpr int RPL = (NM + LPM - 1) / LPM;  // rows of Z per lane
-    // CTAs per SM that the shared memory allows (1 KB reserved per CTA)
+    // CTAs per SM that the shared memory allows (1 KB reserved per CTA),
+    // capped where registers would fall below ~96 a thread
     static constexpr int CTAS = (227 * 1024) / (QW_WARPS * BYTES + 1024);
-    static constexpr int MINB = CTAS < 1 ? 1 : (CTAS > 16 ? 16 : CTAS);
+    static constexpr int REG_CTAS = 65536 / (QW_WARPS * 32 * 96);
+    static constexpr int MINB = CTAS < 1 ? 1 : (CTAS > REG_CTAS ? REG_CTAS : CTAS);
     static_assert(NM % 8 == 0 && NM <= 32, "NM: a multiple of 8 up to 32");
     static_assert(G == 1 || G == 2 || G == 4 || G == 8, "G divides 32");
     static_assert(A_BYTES % 16 == 0 && BYTES % 16 == 0, "alignment");
