@@ -35,7 +35,7 @@ extern "C" {
 
 /* per-item status values written by the kernels */
 #define MSP_ITEM_OK 0
-#define MSP_ITEM_NOT_CONVERGED 1 /* Jacobi reached max_sweeps */
+#define MSP_ITEM_NOT_CONVERGED 1 /* Jacobi reached max_sweeps, or QL 60 steps on a level */
 #define MSP_ITEM_BAD_SLOT 2      /* slot index out of range / not sorted */
 #define MSP_ITEM_REFINE_LIMIT 4  /* MIXED: the last eigenvector refinement step
                                     allowed (max_refine) still corrected by more
@@ -252,7 +252,8 @@ typedef struct msp_powder_args {
     double tau;               /* INTEGRAL: decay time (us) */
     int mode;                 /* MSP_MODE_* */
     int precision;            /* MSP_PREC_* */
-    int max_sweeps;           /* Jacobi sweep cap, <= 0 selects 40 */
+    int max_sweeps;           /* Jacobi sweep cap, <= 0 selects 40 (the QL eigensolvers cap
+                                 their steps at 60 per level instead) */
     double *out;              /* num_slots*num_times (FAST/EVOLVE) or num_slots */
     int *status;              /* num_snap per-snapshot status (MSP_ITEM_*) */
     void *workspace;          /* caller scratch, >= msp_powder_workspace bytes,
@@ -329,7 +330,8 @@ typedef struct msp_multi_desc {
     int uniform;               /* 1: t_k = t0 + k dt */
     double t0, dt;
     int precision;             /* MSP_PREC_* */
-    int max_sweeps;            /* Jacobi sweep cap, <= 0 selects 40 */
+    int max_sweeps;            /* Jacobi sweep cap, <= 0 selects 40 (the QL eigensolvers cap
+                                  their steps at 60 per level instead) */
     long long max_pairs_per_chunk; /* pair records a bucket holds at once; larger
                                       buckets run in chunks (0: 2^26) */
     const msp_multi_tuning *tuning;
@@ -498,7 +500,8 @@ typedef struct msp_adjoint_args {
     double *grad_hsys;        /* out: n*n complex128, sum over snapshots of dL/dH_s */
     double *grad_field;       /* out, optional (NULL): num_snap*3 dL/dfield */
     int *status;              /* num_snap per-snapshot eigensolve status */
-    int max_sweeps;           /* Jacobi sweep cap, <= 0 selects 40 */
+    int max_sweeps;           /* Jacobi sweep cap, <= 0 selects 40 (the QL eigensolvers cap
+                                 their steps at 60 per level instead) */
     void *workspace;          /* >= msp_adjoint_workspace bytes, 256-byte aligned */
     size_t workspace_bytes;
     void *stream;             /* cudaStream_t */

@@ -1,7 +1,9 @@
 // FP32 cyclic Jacobi with one warp per Hamiltonian (n <= 32), the first
-// stage of the MIXED snapshot pipeline: replaces the FP32 sweeps of
-// Hermitian.diag's eigensolve (muspinsim/spinop.py:51-82) for the batched
-// snapshots of ExperimentRunner (muspinsim/experiment.py:332-341, 434-498).
+// stage of the MIXED snapshot pipeline for batches under 4,096 snapshots
+// (larger ones take msp_ql_warp.cu's Householder + QL): replaces the FP32
+// sweeps of Hermitian.diag's eigensolve (muspinsim/spinop.py:51-82) for the
+// batched snapshots of ExperimentRunner (muspinsim/experiment.py:332-341,
+// 434-498).
 // The second stage (msp_snap.cu, PRE variants) refines the eigenvectors
 // this kernel leaves in scratch.
 //
@@ -28,14 +30,16 @@
 //     row is permuted like the positions.
 // A step: each lane updates whole off-diagonal 2 x 2 blocks,
 // B' = G_k1^H B G_k2, and stores every element at its permuted place
-// (conjugated when it lands in the lower triangle); the elements that
+// (conjugated when it lands in the lower triangle: a store code is the
+// element's byte offset with the conjugation in bit 31, so a store is a
+// mask, an add and a sign-bit xor); the elements that
 // become next-step couplings land in the diagonal blocks.  After a
 // __syncwarp, lane X computes next-step pair X's rotation from its coupling
 // and the two diagonal entries (this step's rotated diagonal, moved), and
 // stores the zero left by this step's pair X at its new place.  The
-// rotation arithmetic uses the hardware reciprocal square root: a rotation
-// only has to stay unitary to FP32 rounding, and the refinement stage
-// restores full accuracy.  Convergence test and tolerances are those of
+// rotation arithmetic uses the hardware reciprocal and reciprocal square
+// root: a rotation only has to stay unitary to FP32 rounding, and the
+// refinement stage restores full accuracy.  Convergence test and tolerances are those of
 // msp_jacobi.cuh (FP32: off-diagonal norm <= 4e-7 of the total, or a
 // rounding floor of 2e-5 that a sweep no longer shrinks).
 #include "msp_internal.cuh"
@@ -97,7 +101,12 @@ __device__ __forceinline__ float4 jw_rotation(float app, float aqq, float2 apq, 
     if (!(mag2 > skip * skip)) return make_float4(1.f, 0.f, 0.f, 0.f);
     const float rinv = rsqrtf(mag2), mag = mag2 * rinv;
     const float zeta = 0.5f * (aqq - app) * rinv;
-    const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
+    // t = sign(zeta) / (|zeta| + sqrt(zeta^2 + 1)) from the hardware
+    // reciprocal and reciprocal square root: a rotated coupling above `skip`
+    // bounds |zeta| by ~5e7 (zeta^2 + 1 stays far from overflow), and an
+    // approximate t still gives an exactly-normalised rotation below
+    const float q1 = fmaf(zeta, zeta, 1.f);
+    const float t = copysignf(__fdividef(1.f, fabsf(zeta) + q1 * rsqrtf(q1)), zeta);
     const float c = rsqrtf(fmaf(t, t, 1.f));
     const float f = t * c * rinv;
     na = app - t * mag;
@@ -121,9 +130,10 @@ __host__ __device__ constexpr int jw_warp_floats() {
 
 template <int M>
 __host__ __device__ constexpr size_t jw_smem_bytes() {
-    // route table (uint2 codes + packed k1 | k2 << 8 per off-diagonal block,
-    // one code per diagonal block), then the warps' areas
-    return (size_t)JwShape<M>::NOFF * 12 + (size_t)JwShape<M>::H * 4 + 16 +
+    // route table (four 32-bit store codes + packed k1 | k2 << 8 per
+    // off-diagonal block, one 16-bit code per diagonal block), then the
+    // warps' areas
+    return (size_t)JwShape<M>::NOFF * 20 + (size_t)JwShape<M>::H * 4 + 16 +
            (size_t)JW_WARPS * jw_warp_floats<M>() * 4;
 }
 
@@ -145,11 +155,13 @@ __global__ void __launch_bounds__(JW_WARPS * 32, M <= 24 ? 5 : 4) msp_jacobi_war
     using S = JwShape<M>;
     constexpr int H = S::H, NB = S::NB, NOFF = S::NOFF;
     extern __shared__ __align__(16) char smem[];
-    uint2 *route = reinterpret_cast<uint2 *>(smem);                  // NOFF codes
+    // store codes of an off-diagonal block's four elements: byte offset in
+    // the H buffer, bit 31 set when the element lands conjugated
+    uint4 *route = reinterpret_cast<uint4 *>(smem);                  // NOFF codes
     unsigned *kk = reinterpret_cast<unsigned *>(route + NOFF);        // NOFF k1 | k2 << 8
     unsigned *zroute = kk + NOFF;                                     // H codes
     float *wbase = reinterpret_cast<float *>(
-        smem + (((size_t)NOFF * 12 + (size_t)H * 4 + 15) & ~(size_t)15));
+        smem + (((size_t)NOFF * 20 + (size_t)H * 4 + 15) & ~(size_t)15));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float *mine = wbase + (size_t)warp * jw_warp_floats<M>();
     // buffer b of each double-buffered table: base + b * stride
@@ -171,7 +183,9 @@ __global__ void __launch_bounds__(JW_WARPS * 32, M <= 24 ? 5 : 4) msp_jacobi_war
         unsigned c[4];
         for (int r = 0; r < 2; ++r)
             for (int q = 0; q < 2; ++q) c[r * 2 + q] = jw_route(2 * k1 + r, 2 * k2 + q, H);
-        route[o] = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+        unsigned b4[4];
+        for (int q = 0; q < 4; ++q) b4[q] = ((c[q] & 0x7fffu) * 8u) | ((c[q] & 0x8000u) << 16);
+        route[o] = make_uint4(b4[0], b4[1], b4[2], b4[3]);
         kk[o] = (unsigned)k1 | ((unsigned)k2 << 8);
     }
     for (int k = threadIdx.x; k < H; k += blockDim.x) zroute[k] = jw_route(2 * k, 2 * k + 1, H);
@@ -310,13 +324,14 @@ __global__ void __launch_bounds__(JW_WARPS * 32, M <= 24 ? 5 : 4) msp_jacobi_war
                     nv[1] = cadd(cmul(s2, t00), cscale(c2, t01));
                     nv[2] = cadd(cscale(c2, t10), cscale(-1.f, cmulc(s2, t11)));
                     nv[3] = cadd(cmul(s2, t10), cscale(c2, t11));
-                    const uint2 rt = route[o];
+                    const uint4 rt = route[o];
+                    const unsigned cq[4] = {rt.x, rt.y, rt.z, rt.w};
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const unsigned code = ((q < 2 ? rt.x : rt.y) >> (16 * (q & 1))) & 0xffffu;
-                        const float sg = (code & 0x8000u) ? -1.f : 1.f;
-                        Hn[code & 0x7fffu] = make_float2(nv[q].re, sg * nv[q].im);
-                    }
+                    for (int q = 0; q < 4; ++q)
+                        *reinterpret_cast<float2 *>(reinterpret_cast<char *>(Hn) +
+                                                    (cq[q] & 0x7fffffffu)) =
+                            make_float2(nv[q].re, __uint_as_float(__float_as_uint(nv[q].im) ^
+                                                                  (cq[q] & 0x80000000u)));
                 }
                 if (SPLIT && lane < 4 * LEFT) {
                     // element (r, cc) of B' = G1^H B G2 for block FULL + lane / 4
@@ -338,10 +353,9 @@ __global__ void __launch_bounds__(JW_WARPS * 32, M <= 24 ? 5 : 4) msp_jacobi_war
                                                 : cadd(cmulc(s1, b01), cscale(c1, b11));
                     const cx<float> v = cc == 0 ? cadd(cscale(c2, t0), cscale(-1.f, cmulc(s2, t1)))
                                                 : cadd(cmul(s2, t0), cscale(c2, t1));
-                    const uint2 rt = route[o];
-                    const unsigned code = ((q < 2 ? rt.x : rt.y) >> (16 * (q & 1))) & 0xffffu;
-                    const float sg = (code & 0x8000u) ? -1.f : 1.f;
-                    Hn[code & 0x7fffu] = make_float2(v.re, sg * v.im);
+                    const unsigned cq = reinterpret_cast<const unsigned *>(route + o)[q];
+                    *reinterpret_cast<float2 *>(reinterpret_cast<char *>(Hn) + (cq & 0x7fffffffu)) =
+                        make_float2(v.re, __uint_as_float(__float_as_uint(v.im) ^ (cq & 0x80000000u)));
                 }
                 __syncwarp();
                 // next-step rotations; this step's zeroed couplings moved
