@@ -10,14 +10,19 @@
 // The algorithm is msp_large.cuh's (LAPACK zhetd2 tridiagonalisation of the
 // lower triangle, EISPACK tql2 QL with the rotations accumulated into a real
 // Z, back-transformation U = Q Z).  A warp takes G matrices at a time:
-//   1. per matrix, one warp: A (full Hermitian, row-major, row stride NM + 1
-//      float2 so that column and row walks are both free of bank conflicts)
-//      in shared memory.  Step k: lane i holds x_i = A[k+1+i][k]; the
-//      reflector v_k (v_0 = 1) replaces column k of A, zero outside rows
-//      k+1 .. n-1, and is parked as row k of the snapshot's eigenvector
-//      scratch; p = tau A22 v and the rank-2 update A22 -= v w^H + w v^H are
-//      column-parallel (lane i owns column k+1+i; v_j, w_j are warp
-//      broadcasts).  d, e and tau stay in shared memory.
+//   1. two matrices at a time, one warp, their steps interleaved
+//      instruction by instruction (each step is a chain of warp reductions
+//      and shared-memory round trips; two independent chains fill each
+//      other's latency: 0.54 -> 0.52 ms on the headline): A (full
+//      Hermitian, row-major, row stride NM + 1 float2 so that column and
+//      row walks are both free of bank conflicts) in shared memory, both
+//      matrices side by side in the region the Z matrices later take.
+//      Step k: lane i holds x_i = A[k+1+i][k]; the reflector v_k (v_0 = 1)
+//      replaces column k of A, zero outside rows k+1 .. n-1, and is parked
+//      as row k of the snapshot's eigenvector scratch; p = tau A22 v and the
+//      rank-2 update A22 -= v w^H + w v^H are column-parallel (lane i owns
+//      column k+1+i; v_j, w_j are warp broadcasts).  d, e and tau stay in
+//      shared memory.
 //   2. the G QL runs side by side, 32 / G lanes per matrix: a QL step's
 //      shift and rotation chain are serial, so each lane group computes its
 //      own matrix's chain (its lanes redundantly) and applies every rotation
@@ -43,20 +48,22 @@ namespace {
 constexpr int QW_WARPS = 2;  // warps per CTA
 
 // Per-warp shared memory for a batch of G matrices up to NM x NM (NM a
-// multiple of 8): region R holds the working matrix A (NM x (NM + 1)
-// float2) while a matrix is tridiagonalised and the G matrices Z_g
+// multiple of 8): region R holds the two working matrices A (NM x (NM + 1)
+// float2 each) while matrices are tridiagonalised and the G matrices Z_g
 // (NM x (NM + 1) floats each) from the QL on; then per matrix d, e (NM
-// floats each) and tau (NM float2); then the v/w pairs (NM float4).
+// floats each) and tau (NM float2); then the two v/w pair buffers (NM
+// float4 each).
 template <int NM, int G>
 struct QwShape {
     static constexpr int LDA = NM + 1;  // float2
     static constexpr int LDZ = NM + 1;  // float
     static constexpr int A_BYTES = 8 * NM * LDA;
     static constexpr int Z_FLOATS = NM * LDZ;  // one matrix
+    static constexpr int A_F2 = NM * LDA;  // float2 of one working matrix
     static constexpr int R_BYTES =
-        (A_BYTES > 4 * G * Z_FLOATS ? A_BYTES : 4 * G * Z_FLOATS + 15) / 16 * 16;
+        (2 * A_BYTES > 4 * G * Z_FLOATS ? 2 * A_BYTES : 4 * G * Z_FLOATS + 15) / 16 * 16;
     static constexpr int DEV_BYTES = 16 * NM;  // d, e, tau of one matrix
-    static constexpr int BYTES = R_BYTES + G * DEV_BYTES + 16 * NM;
+    static constexpr int BYTES = R_BYTES + G * DEV_BYTES + 32 * NM;
     static constexpr int LPM = 32 / G;              // lanes per matrix in the QL
     static constexpr int RPL = (NM + LPM - 1) / LPM;  // rows of Z per lane
     // CTAs per SM that the shared memory allows (1 KB reserved per CTA),
@@ -68,12 +75,6 @@ struct QwShape {
     static_assert(G == 1 || G == 2 || G == 4 || G == 8, "G divides 32");
     static_assert(A_BYTES % 16 == 0 && BYTES % 16 == 0, "alignment");
 };
-
-__device__ __forceinline__ float qw_sum(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 }  // namespace
 
@@ -99,13 +100,30 @@ __global__ void __launch_bounds__(QW_WARPS * 32, QwShape<NM, G>::MINB)
         const int sn0 = task * G;
         const int cnt = min(G, a.num_snap - sn0);
 
-        // ---- 1. per matrix: H, tridiagonalisation
-        for (int q = 0; q < cnt; ++q) {
-            const int sn = sn0 + q;
-            const SnapSource src = snap_source(a, sn);
-            const double bx = a.field[3 * (size_t)src.g], by = a.field[3 * (size_t)src.g + 1],
-                         bz = a.field[3 * (size_t)src.g + 2];
-            const float bxf = (float)bx, byf = (float)by, bzf = (float)bz;
+        // ---- 1. two matrices at a time (their steps interleaved instruction
+        // by instruction): H, tridiagonalisation.  A missing second matrix
+        // (odd count) is zero: no reflections, nothing stored for it.
+        for (int q0 = 0; q0 < cnt; q0 += 2) {
+            const bool has1 = q0 + 1 < cnt;
+            float2 *Ap[2] = {A, A + S::A_F2};
+            float4 *vwp[2] = {vw, vw + NM};
+            float *dsp[2], *esp[2];
+            float2 *tp[2], *Vtp[2];
+            SnapSource src[2];
+            double bx[2], by[2], bz[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int q = q0 + u;
+                dsp[u] = dptr(q);
+                esp[u] = dsp[u] + NM;
+                tp[u] = reinterpret_cast<float2 *>(esp[u] + NM);
+                const int sn = (u == 0 || has1) ? sn0 + q : sn0 + q0;
+                Vtp[u] = evec + (size_t)sn * nn;
+                src[u] = snap_source(a, sn);
+                bx[u] = a.field[3 * (size_t)src[u].g];
+                by[u] = a.field[3 * (size_t)src[u].g + 1];
+                bz[u] = a.field[3 * (size_t)src[u].g + 2];
+            }
             // H = Hsys + b . Z in FP32 (from the double-word high parts when
             // the caller pre-split the matrices, else from FP64), upper
             // triangle mirrored; rows and columns n .. NM-1 zero
@@ -114,126 +132,172 @@ __global__ void __launch_bounds__(QW_WARPS * 32, QwShape<NM, G>::MINB)
                 while ((i + 1) * (i + 2) / 2 <= e) ++i;
                 while (i * (i + 1) / 2 > e) --i;
                 const int j = e - i * (i + 1) / 2;  // j <= i: element (j, i)
-                float hr = 0.f, hi = 0.f;
-                if (i < n) {
-                    const size_t o = (size_t)j * n + i;
-                    if (src.Hdw != nullptr) {
-                        const float4 hs = src.Hdw[o], z0 = src.Zdw[o], z1 = src.Zdw[nn + o],
-                                     z2 = src.Zdw[2 * (size_t)nn + o];
-                        hr = fmaf(bzf, z2.x, fmaf(byf, z1.x, fmaf(bxf, z0.x, hs.x)));
-                        hi = fmaf(bzf, z2.y, fmaf(byf, z1.y, fmaf(bxf, z0.y, hs.y)));
-                    } else {
-                        const cx<double> hs = src.Hsys[o], z0 = src.Z[o], z1 = src.Z[nn + o],
-                                         z2 = src.Z[2 * (size_t)nn + o];
-                        hr = (float)(hs.re + bx * z0.re + by * z1.re + bz * z2.re);
-                        hi = (float)(hs.im + bx * z0.im + by * z1.im + bz * z2.im);
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    float hr = 0.f, hi = 0.f;
+                    if (i < n && (u == 0 || has1)) {
+                        const size_t o = (size_t)j * n + i;
+                        if (src[u].Hdw != nullptr) {
+                            const float bxf = (float)bx[u], byf = (float)by[u], bzf = (float)bz[u];
+                            const float4 hs = src[u].Hdw[o], z0 = src[u].Zdw[o],
+                                         z1 = src[u].Zdw[nn + o], z2 = src[u].Zdw[2 * (size_t)nn + o];
+                            hr = fmaf(bzf, z2.x, fmaf(byf, z1.x, fmaf(bxf, z0.x, hs.x)));
+                            hi = fmaf(bzf, z2.y, fmaf(byf, z1.y, fmaf(bxf, z0.y, hs.y)));
+                        } else {
+                            const cx<double> hs = src[u].Hsys[o], z0 = src[u].Z[o],
+                                             z1 = src[u].Z[nn + o], z2 = src[u].Z[2 * (size_t)nn + o];
+                            hr = (float)(hs.re + bx[u] * z0.re + by[u] * z1.re + bz[u] * z2.re);
+                            hi = (float)(hs.im + bx[u] * z0.im + by[u] * z1.im + bz[u] * z2.im);
+                        }
                     }
-                }
-                if (i == j) {
-                    A[i * LDA + i] = make_float2(hr, 0.f);
-                } else {
-                    A[j * LDA + i] = make_float2(hr, hi);
-                    A[i * LDA + j] = make_float2(hr, -hi);
+                    if (i == j) {
+                        Ap[u][i * LDA + i] = make_float2(hr, 0.f);
+                    } else {
+                        Ap[u][j * LDA + i] = make_float2(hr, hi);
+                        Ap[u][i * LDA + j] = make_float2(hr, -hi);
+                    }
                 }
             }
             __syncwarp();
 
-            // d (diagonal), e (real off-diagonal, e[k] couples d[k] and
-            // d[k+1]), tau; reflector k into column k of A and row k of the
-            // eigenvector scratch
-            float *const ds = dptr(q);
-            float *const es = ds + NM;
-            float2 *const taus = reinterpret_cast<float2 *>(es + NM);
-            float2 *const Vt = evec + (size_t)sn * nn;
+            // d, e, tau; reflector k into column k of A and row k of the
+            // eigenvector scratch.  A step without a reflection (tau = 0)
+            // runs the updates too: they add exact zeros.
             for (int k = 0; k + 1 < n; ++k) {
                 const int m = n - k - 1;  // length of x
-                const float2 xi = lane < m ? A[(k + 1 + lane) * LDA + k] : make_float2(0.f, 0.f);
-                const float dk = A[k * LDA + k].x;
-                const float xn2 = qw_sum(lane >= 1 ? xi.x * xi.x + xi.y * xi.y : 0.f);
-                const float2 alpha = make_float2(__shfl_sync(0xffffffffu, xi.x, 0),
-                                                 __shfl_sync(0xffffffffu, xi.y, 0));
-                const bool reflect = !(xn2 == 0.f && alpha.y == 0.f);
-                float beta = alpha.x;
-                cx<float> tau = mk<float>(0.f, 0.f), vi = mk<float>(lane == 0 ? 1.f : 0.f, 0.f);
-                if (reflect) {
-                    beta = -copysignf(sqrtf(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
-                    tau = mk<float>((beta - alpha.x) / beta, -alpha.y / beta);
+                float2 xi[2];
+                float dk[2], xn2[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    xi[u] = lane < m ? Ap[u][(k + 1 + lane) * LDA + k] : make_float2(0.f, 0.f);
+                    dk[u] = Ap[u][k * LDA + k].x;
+                    xn2[u] = lane >= 1 ? xi[u].x * xi[u].x + xi[u].y * xi[u].y : 0.f;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) xn2[u] += __shfl_xor_sync(0xffffffffu, xn2[u], o);
+                }
+                float beta[2];
+                cx<float> tau[2], vi[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const float2 alpha = make_float2(__shfl_sync(0xffffffffu, xi[u].x, 0),
+                                                     __shfl_sync(0xffffffffu, xi[u].y, 0));
+                    const bool reflect = !(xn2[u] == 0.f && alpha.y == 0.f);
+                    const float br =
+                        -copysignf(sqrtf(alpha.x * alpha.x + alpha.y * alpha.y + xn2[u]), alpha.x);
+                    const cx<float> tr = mk<float>((br - alpha.x) / br, -alpha.y / br);
                     // v = x / (alpha - beta), v_0 = 1
-                    const float dr = alpha.x - beta, di = alpha.y;
+                    const float dr = alpha.x - br, di = alpha.y;
                     const float dd = 1.f / (dr * dr + di * di);
-                    const cx<float> sc = mk<float>(dr * dd, -di * dd);
-                    if (lane > 0) vi = cmul(mk<float>(xi.x, xi.y), sc);
+                    const cx<float> vr = cmul(mk<float>(xi[u].x, xi[u].y), mk<float>(dr * dd, -di * dd));
+                    beta[u] = reflect ? br : alpha.x;
+                    tau[u] = reflect ? tr : mk<float>(0.f, 0.f);
+                    vi[u] = lane == 0 ? mk<float>(1.f, 0.f)
+                                      : (reflect ? vr : mk<float>(0.f, 0.f));
                 }
                 __syncwarp();  // column k (x, A[k][k]) read by every lane
-                {
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
                     // column k <- v, zero outside rows k+1 .. n-1
                     const int src_lane = (lane - k - 1) & 31;
-                    const float vr = __shfl_sync(0xffffffffu, vi.re, src_lane);
-                    const float vim = __shfl_sync(0xffffffffu, vi.im, src_lane);
+                    const float vr = __shfl_sync(0xffffffffu, vi[u].re, src_lane);
+                    const float vim = __shfl_sync(0xffffffffu, vi[u].im, src_lane);
                     const float2 vv =
                         (lane > k && lane < n) ? make_float2(vr, vim) : make_float2(0.f, 0.f);
-                    if (lane < NM) A[lane * LDA + k] = vv;
-                    if (lane < n) Vt[(size_t)k * n + lane] = vv;
-                }
-                if (lane == 0) {
-                    ds[k] = dk;
-                    es[k] = beta;
-                    taus[k] = make_float2(tau.re, tau.im);
-                }
-                if (!reflect) {  // the same in every lane
-                    __syncwarp();
-                    continue;
+                    if (lane < NM) Ap[u][lane * LDA + k] = vv;
+                    if (lane < n && (u == 0 || has1)) Vtp[u][(size_t)k * n + lane] = vv;
+                    if (lane == 0) {
+                        dsp[u][k] = dk[u];
+                        esp[u][k] = beta[u];
+                        tp[u][k] = make_float2(tau[u].re, tau[u].im);
+                    }
                 }
                 __syncwarp();
                 // p_i = tau sum_j conj(A22[j][i]) v_j (A22 Hermitian), lane i
-                // owns column k+1+i; two accumulators per component
-                cx<float> pi = mk<float>(0.f, 0.f);
+                // owns column k+1+i
+                cx<float> pi[2] = {mk<float>(0.f, 0.f), mk<float>(0.f, 0.f)};
                 if (lane < m) {
-                    float r0 = 0.f, i0 = 0.f, r1 = 0.f, i1 = 0.f;
-                    const float2 *col = A + (k + 1) * LDA + (k + 1 + lane);
-                    const float2 *vk = A + (k + 1) * LDA + k;
+                    float r0[2] = {0.f, 0.f}, i0[2] = {0.f, 0.f}, r1[2] = {0.f, 0.f},
+                          i1[2] = {0.f, 0.f};
                     int j = 0;
                     for (; j + 1 < m; j += 2) {
-                        const float2 a0 = col[j * LDA], a1 = col[(j + 1) * LDA];
-                        const float2 v0 = vk[j * LDA], v1 = vk[(j + 1) * LDA];
-                        r0 += a0.x * v0.x + a0.y * v0.y;
-                        i0 += a0.x * v0.y - a0.y * v0.x;
-                        r1 += a1.x * v1.x + a1.y * v1.y;
-                        i1 += a1.x * v1.y - a1.y * v1.x;
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            const float2 *col = Ap[u] + (k + 1) * LDA + (k + 1 + lane);
+                            const float2 *vk = Ap[u] + (k + 1) * LDA + k;
+                            const float2 a0 = col[j * LDA], a1 = col[(j + 1) * LDA];
+                            const float2 v0 = vk[j * LDA], v1 = vk[(j + 1) * LDA];
+                            r0[u] += a0.x * v0.x + a0.y * v0.y;
+                            i0[u] += a0.x * v0.y - a0.y * v0.x;
+                            r1[u] += a1.x * v1.x + a1.y * v1.y;
+                            i1[u] += a1.x * v1.y - a1.y * v1.x;
+                        }
                     }
                     if (j < m) {
-                        const float2 a0 = col[j * LDA], v0 = vk[j * LDA];
-                        r0 += a0.x * v0.x + a0.y * v0.y;
-                        i0 += a0.x * v0.y - a0.y * v0.x;
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            const float2 a0 = Ap[u][(k + 1 + j) * LDA + (k + 1 + lane)];
+                            const float2 v0 = Ap[u][(k + 1 + j) * LDA + k];
+                            r0[u] += a0.x * v0.x + a0.y * v0.y;
+                            i0[u] += a0.x * v0.y - a0.y * v0.x;
+                        }
                     }
-                    pi = cmul(tau, mk<float>(r0 + r1, i0 + i1));
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+                        pi[u] = cmul(tau[u], mk<float>(r0[u] + r1[u], i0[u] + i1[u]));
                 }
                 // alpha2 = -1/2 tau (p^H v); w = p + alpha2 v
-                const cx<float> pv = lane < m ? cmulc(pi, vi) : mk<float>(0.f, 0.f);
-                const float hr = qw_sum(pv.re), hi = qw_sum(pv.im);
-                const cx<float> a2 = cscale(-0.5f, cmul(tau, mk<float>(hr, hi)));
-                const cx<float> wi = cadd(pi, cmul(a2, vi));
-                if (lane < m) vw[lane] = make_float4(vi.re, vi.im, wi.re, wi.im);
+                float hr[2], hi[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const cx<float> pv = lane < m ? cmulc(pi[u], vi[u]) : mk<float>(0.f, 0.f);
+                    hr[u] = pv.re;
+                    hi[u] = pv.im;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        hr[u] += __shfl_xor_sync(0xffffffffu, hr[u], o);
+                        hi[u] += __shfl_xor_sync(0xffffffffu, hi[u], o);
+                    }
+                }
+                cx<float> wi[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const cx<float> a2 = cscale(-0.5f, cmul(tau[u], mk<float>(hr[u], hi[u])));
+                    wi[u] = cadd(pi[u], cmul(a2, vi[u]));
+                    if (lane < m) vwp[u][lane] = make_float4(vi[u].re, vi[u].im, wi[u].re, wi[u].im);
+                }
                 __syncwarp();
                 // A22[j][i] -= v_j conj(w_i) + w_j conj(v_i), lane i owns column i
                 if (lane < m) {
-                    float2 *col = A + (k + 1) * LDA + (k + 1 + lane);
                     for (int j = 0; j < m; ++j) {
-                        const float4 qv = vw[j];
-                        const float2 x = col[j * LDA];
-                        // v_j conj(w_i) + w_j conj(v_i)
-                        const float tr = qv.x * wi.re + qv.y * wi.im + qv.z * vi.re + qv.w * vi.im;
-                        const float ti = qv.y * wi.re - qv.x * wi.im + qv.w * vi.re - qv.z * vi.im;
-                        col[j * LDA] = make_float2(x.x - tr, x.y - ti);
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            float2 *cp = Ap[u] + (k + 1 + j) * LDA + (k + 1 + lane);
+                            const float4 qv = vwp[u][j];
+                            const float2 x = *cp;
+                            const float tr = qv.x * wi[u].re + qv.y * wi[u].im + qv.z * vi[u].re +
+                                             qv.w * vi[u].im;
+                            const float ti = qv.y * wi[u].re - qv.x * wi[u].im + qv.w * vi[u].re -
+                                             qv.z * vi[u].im;
+                            *cp = make_float2(x.x - tr, x.y - ti);
+                        }
                     }
                 }
                 __syncwarp();
             }
             if (lane == 0) {
-                ds[n - 1] = A[(n - 1) * LDA + (n - 1)].x;
-                es[n - 1] = 0.f;
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    dsp[u][n - 1] = Ap[u][(n - 1) * LDA + (n - 1)].x;
+                    esp[u][n - 1] = 0.f;
+                }
             }
-            __syncwarp();  // A is reused by the next matrix, then by Z
+            __syncwarp();  // A is reused by the next pair, then by Z
         }
 
         // ---- 2. QL with implicit shifts (tql2) on the G matrices side by
