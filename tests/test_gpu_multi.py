@@ -149,3 +149,25 @@ def test_multi_with_dim192_systems(precision, tol):
     for k, (w, ref) in enumerate(zip(wls, refs)):
         err = np.abs(got[k] - ref).max()
         assert err <= tol, (k, w.name, err)
+
+
+def test_multi_buckets_through_the_ql_eigensolve():
+    """Buckets of 4,500 snapshots (three systems x 1,500 orientations each,
+    interleaved with the other bucket's systems in the input) take the
+    batched Householder + QL first stage, whose four-matrix warp tasks then
+    straddle segment boundaries: mixed rows against the FP64 rows."""
+    from muspinsim_gb300 import workloads
+    from muspinsim_gb300.multi import powder_average_multi
+    from muspinsim_gb300.orientations import zcw_gen
+
+    rng = np.random.default_rng(77)
+    orients = zcw_gen(1500)
+    times = np.linspace(0.0, 8.0, 32)
+    wls = [workloads.random_system_workload(rng, d, orients, times) for d in (8, 24, 8, 24, 8, 24)]
+    systems = [w.system() for w in wls]
+    kw = dict(field=wls[0].fields[0], polarization=wls[0].polarization, times=times)
+    fp64 = powder_average_multi(systems, orients, precision="fp64", **kw)
+    mixed = powder_average_multi(systems, orients, precision="mixed", **kw)
+    err = np.abs(mixed - fp64).max(axis=1)
+    print("QL buckets: per-system max|dP| mixed vs FP64:", err)
+    assert err.max() <= MIXED_TOL
